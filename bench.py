@@ -1,0 +1,540 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Levenshtein engine — one JSON line on stdout.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config 2] [--impl ours|reference]
+
+Default workload (the reference's headline search shape): cdist of 4096
+queries x 65536 choices, length 64 over uniform {A,C,G,T}, 1% planted
+mutants; exact distances, int32 output. A step is one full pass of that
+matrix. The metric is pairs/s (distances per second; GCUPS beside it).
+
+* value:   kernel-only throughput — inputs resident in HBM, results left in
+           HBM (the reference's "kernel-only" protocol, bench/baselines.py:
+           150-160), CUDA events on the library's stream around each step,
+           L2 flushed by a 256 MB memset between steps (outside the events).
+* e2e:     the same metric through the C-ABI one-call entry point with host
+           buffers: H2D of the packed inputs, kernels, D2H of the matrix.
+* roofline: the dominant kernel's algorithmic integer operations per launch
+           (15 per 32-bit word-step) over its event-timed
+           duration, against the integer-pipe peak measured on this GPU by
+           libblg_probe.so; plus its HBM figure.
+* cpu_baseline: the oracle's C restatement of the reference's CPU core on a
+           bounded sample, all host threads.
+* --impl reference: the reference's CPU path (here: the oracle port, since
+           the reference's sources are not on the GPU host) on the same
+           workload, all host threads.
+
+Under torchrun (N > 1) every rank runs its own replica of the workload on
+its own GPU (weak scaling, no data-path collective); rank 0 reports the
+aggregate over the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from editdist_bench_gb300 import _build, _lib, gpu, workloads as W  # noqa: E402
+
+H100_REF = {  # the reference's published kernel-only numbers (H100 SXM)
+    1: (4.65e9, "H100 pairs kernel-only dna L32 5% 1M int32 (results/gpu-NVIDIA-H100-80GB-HBM3/prior_art_20261107-075217.csv:26)"),
+    2: (6.1e9, "H100 search kernel-only dna L64 2000x2000 int32 (results/gpu-NVIDIA-H100-80GB-HBM3/prior_art_20261107-075006.csv:60)"),
+}
+L2_FLUSH_BYTES = 256 << 20
+OPS_PER_WORD32_STEP = 15
+
+
+# ------------------------------------------------------------------ ranks --
+class Ranks:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist      # plumbing only: barrier + max over ranks
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ----------------------------------------------------------------- clocks --
+class Clocks:
+    """nvidia-smi sampling during the timed region (SM MHz + throttle reasons)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self) -> dict:
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows),
+                "power_w_max": max((float(r[3]) for r in self.rows
+                                    if r[3].replace(".", "").isdigit()), default=None)}
+
+
+# ---------------------------------------------------------------- helpers --
+def device_timer(ctx):
+    lib = ctx.lib
+
+    def start():
+        ctx.check(lib.blg_timer_start(ctx.h))
+
+    def stop() -> float:
+        ms = ctypes.c_float()
+        ctx.check(lib.blg_timer_stop(ctx.h, ctypes.byref(ms)))
+        return float(ms.value)
+    return start, stop
+
+
+def flush_l2(ctx, buf):
+    ctx.check(ctx.lib.blg_memset(ctx.h, buf.ptr, 0x5a, ctypes.c_size_t(L2_FLUSH_BYTES)))
+
+
+def int_peak(device: int) -> dict:
+    lib = ctypes.CDLL(_build.build_probe())
+    lib.blg_probe_int_peak.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_double)]
+    a, b = ctypes.c_double(), ctypes.c_double()
+    rc = lib.blg_probe_int_peak(device, 4096, ctypes.byref(a), ctypes.byref(b))
+    if rc:
+        return {"gops": None}
+    return {"logic_gops": a.value / 1e9, "mixed_gops": b.value / 1e9,
+            "gops": max(a.value, b.value) / 1e9}
+
+
+def effective_cpus() -> int:
+    """min(affinity, cgroup quota) — the rule of bench/sysload.py:19-41."""
+    n = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    try:
+        q, period = open("/sys/fs/cgroup/cpu.max").read().split()[:2]
+        if q != "max":
+            n = min(n, max(1, int(int(q) / int(period))))
+    except (OSError, ValueError):
+        pass
+    return max(1, n)
+
+
+# -------------------------------------------------------------- workloads --
+class SearchBench:
+    kind = "cdist"
+
+    def __init__(self, w: W.SearchWork, runs):
+        self.w = w
+        self.runs = runs                  # [(max_dist, dtype), ...]; runs[0] is the headline
+        self.pairs = w.nq * w.nc
+        self.cells = W.cross_cells(w.q, w.c)
+        self.batch = gpu.SearchBatch(w.q, w.c)
+        self.outs = [self.batch.alloc(dt) for _, dt in runs]
+        self._host_out = {}
+
+    def step(self, i=0):
+        k, _ = self.runs[i]
+        self.batch.run(self.outs[i], max_dist=k)
+
+    def e2e_call(self, i=0):
+        k, dt = self.runs[i]
+        out = self._host_out.get(i)
+        if out is None:
+            out = self._host_out[i] = np.empty((self.w.nq, self.w.nc), dtype=dt)
+        ctx = _lib.context()
+        (bq, oq), (bc, oc) = self.w.q, self.w.c
+        ctx.check(ctx.lib.blg_cdist(ctx.h, bq.ctypes.data, oq.ctypes.data, self.w.nq, bc.ctypes.data,
+                                    oc.ctypes.data, self.w.nc, -1 if k is None else k,
+                                    {"int32": 0, "uint16": 1, "uint8": 2}[dt], out.ctypes.data, None))
+        return out
+
+    def io_bytes(self, i=0):
+        (bq, oq), (bc, oc) = self.w.q, self.w.c
+        h2d = int(oq[-1]) + oq.nbytes + int(oc[-1]) + oc.nbytes
+        return h2d, self.pairs * np.dtype(self.runs[i][1]).itemsize
+
+    def alg_ops(self, i=0, exit_cols_sum=None):
+        """15 x sum over pairs of ceil(m/32) x columns processed."""
+        words = np.sum((np.diff(self.w.q[1]) + 31) // 32).astype(np.float64)
+        if self.runs[i][0] is None:
+            return OPS_PER_WORD32_STEP * words * float(np.diff(self.w.c[1]).sum())
+        return None if exit_cols_sum is None else OPS_PER_WORD32_STEP * exit_cols_sum
+
+    def alg_bytes(self, i=0):
+        return self.pairs * np.dtype(self.runs[i][1]).itemsize + float(self.w.q[1][-1] + self.w.c[1][-1])
+
+    def describe(self):
+        return {"workload": f"{self.w.name} cdist {self.w.nq}x{self.w.nc}",
+                "nq": self.w.nq, "nc": self.w.nc, "runs": [
+                    {"max_dist": k, "dtype": dt} for k, dt in self.runs]}
+
+    def cpu_sample(self, threads: int, budget_s: float):
+        """Oracle on a bounded row sample; returns (pairs/s, sample text, rows, result)."""
+        import oracle
+        k, dt = self.runs[0]
+        rows = max(1, min(self.w.nq, 8))
+        while True:
+            sub = W.take(self.w.q, np.arange(rows))
+            t0 = time.perf_counter()
+            res = oracle.cross(sub, self.w.c, k, threads=threads)
+            dt_s = time.perf_counter() - t0
+            if dt_s > budget_s / 4 or rows >= self.w.nq:
+                break
+            rows = min(self.w.nq, max(rows + 1, int(rows * budget_s / 4 / max(dt_s, 1e-3))))
+        return rows * self.w.nc / dt_s, f"{rows} query rows x {self.w.nc} choices", rows, res
+
+    def gate(self, rows, res) -> bool:
+        got = self.outs[0].get()[:rows]
+        return bool(np.array_equal(got, res.astype(got.dtype)))
+
+
+class PairsBench:
+    kind = "pairwise"
+
+    def __init__(self, w: W.PairsWork):
+        self.w = w
+        self.runs = [(w.max_dist, w.dtype)]
+        self.pairs = w.n
+        self.cells = W.cells(w.a, w.b)
+        self.batch = gpu.PairsBatch(w.a, w.b)
+        self.outs = [self.batch.alloc(w.dtype)]
+        self._host = None
+
+    def step(self, i=0):
+        self.batch.run(self.outs[0], max_dist=self.w.max_dist)
+
+    def e2e_call(self, i=0):
+        if self._host is None:
+            self._host = np.empty(self.w.n, dtype=self.w.dtype)
+        ctx = _lib.context()
+        (ba, oa), (bb, ob) = self.w.a, self.w.b
+        k = self.w.max_dist
+        ctx.check(ctx.lib.blg_pairwise(ctx.h, ba.ctypes.data, oa.ctypes.data, bb.ctypes.data,
+                                       ob.ctypes.data, self.w.n, -1 if k is None else k,
+                                       {"int32": 0, "uint16": 1, "uint8": 2}[self.w.dtype],
+                                       self._host.ctypes.data, None))
+        return self._host
+
+    def io_bytes(self, i=0):
+        (ba, oa), (bb, ob) = self.w.a, self.w.b
+        return int(oa[-1]) + oa.nbytes + int(ob[-1]) + ob.nbytes, self.w.n * np.dtype(self.w.dtype).itemsize
+
+    def alg_ops(self, i=0, exit_cols_sum=None):
+        return None if exit_cols_sum is None else OPS_PER_WORD32_STEP * exit_cols_sum
+
+    def alg_bytes(self, i=0):
+        (ba, oa), (bb, ob) = self.w.a, self.w.b
+        return float(oa[-1] + ob[-1] + oa.nbytes + ob.nbytes + self.w.n * np.dtype(self.w.dtype).itemsize)
+
+    def describe(self):
+        return {"workload": f"{self.w.name} pairwise {self.w.n}", "n": self.w.n,
+                "runs": [{"max_dist": self.w.max_dist, "dtype": self.w.dtype}]}
+
+    def cpu_sample(self, threads: int, budget_s: float):
+        import oracle
+        n = min(self.w.n, 1 << 14)
+        while True:
+            sub_a = W.take(self.w.a, np.arange(n))
+            sub_b = W.take(self.w.b, np.arange(n))
+            t0 = time.perf_counter()
+            res = oracle.pairs(sub_a, sub_b, self.w.max_dist, threads=threads)
+            dt_s = time.perf_counter() - t0
+            if dt_s > budget_s / 4 or n >= self.w.n:
+                break
+            n = min(self.w.n, max(n + 1, int(n * budget_s / 4 / max(dt_s, 1e-3))))
+        return n / dt_s, f"first {n} pairs", n, res
+
+    def gate(self, n, res) -> bool:
+        got = self.outs[0].get()[:n]
+        import oracle
+        return bool(np.array_equal(got, oracle.saturate(res, self.w.dtype)))
+
+
+def exit_columns(bench, sample_rows_or_n):
+    """Oracle trace (columns processed under the reference's exit rule) on the
+    CPU sample, scaled to the full workload — algorithmic ops for max_dist runs."""
+    import oracle
+    if bench.kind == "cdist":
+        rows = sample_rows_or_n
+        sub = W.take(bench.w.q, np.arange(rows))
+        _, cols = oracle.cross_trace(sub, bench.w.c, bench.runs[0][0])
+        words = ((np.diff(sub[1]) + 31) // 32).astype(np.float64)
+        s = float((cols.astype(np.float64) * words[:, None]).sum())
+        return s * bench.w.nq / rows
+    n = sample_rows_or_n
+    sa, sb = W.take(bench.w.a, np.arange(n)), W.take(bench.w.b, np.arange(n))
+    _, m, _, cols = oracle.pairs_trace(sa, sb, bench.w.max_dist)
+    s = float((((m.astype(np.float64) + 31) // 32) * cols).sum())
+    return s * bench.w.n / n
+
+
+def make_bench(cfg: int):
+    if cfg == 1:
+        return PairsBench(W.config1())
+    if cfg == 2:
+        return SearchBench(W.config2(), [(None, "int32"), (2, "uint8")])
+    if cfg == 3:
+        return PairsBench(W.config3())
+    if cfg == 4:
+        return SearchBench(W.config4(), [(4, "uint8")])
+    raise SystemExit(f"unknown config {cfg}")
+
+
+def read_traffic(kernel: str, workload: str):
+    """dram bytes per launch from the committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.txt")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch="):
+                return float(line.split("=", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+# ------------------------------------------------------------------ arms --
+def run_ours(args, ranks: Ranks):
+    ctx = _lib.context()
+    bench = make_bench(args.config)
+    p = ctypes.c_void_p()
+    ctx.check(ctx.lib.blg_malloc(ctx.h, L2_FLUSH_BYTES, ctypes.byref(p)))
+    flush = gpu.DeviceArray(p.value, (L2_FLUSH_BYTES,), np.uint8, ctx)
+    start, stop = device_timer(ctx)
+
+    def timed(i, steps):
+        times = []
+        for _ in range(steps):
+            flush_l2(ctx, flush)
+            start()
+            bench.step(i)
+            times.append(stop())
+        return times
+
+    for i in range(len(bench.runs)):          # warm-up every run variant
+        for _ in range(args.warmup):
+            bench.step(i)
+    gpu.synchronize()
+
+    ranks.barrier()
+    clocks = Clocks(ranks.local)
+    clocks.start()
+    launches0 = ctx.lib.blg_launch_count(ctx.h)
+    wall0 = time.perf_counter()
+    times = timed(0, args.steps)
+    wall = time.perf_counter() - wall0
+    launches = ctx.lib.blg_launch_count(ctx.h) - launches0
+    gpu.synchronize()
+    clk = clocks.stop()
+    ranks.barrier()
+    total_ms = ranks.max(sum(times))
+    ms_per_step = total_ms / args.steps
+    value = bench.pairs * ranks.world / (ms_per_step / 1e3)
+
+    extra_runs = {}
+    for i in range(1, len(bench.runs)):
+        t = timed(i, max(3, args.steps // 2))
+        ms = statistics.median(t)
+        k, dt = bench.runs[i]
+        extra_runs[f"max_dist={k},{dt}"] = {"pairs_per_s": bench.pairs / (ms / 1e3), "ms_per_step": ms,
+                                            "gcups": bench.cells / (ms / 1e3) / 1e9}
+
+    # per-kernel event timing for the roofline (a separate, profiled pass)
+    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 1))
+    for _ in range(3):
+        flush_l2(ctx, flush)
+        bench.step(0)
+    buf = ctypes.create_string_buffer(4096)
+    ctx.check(ctx.lib.blg_profile_report(ctx.h, buf, 4096))
+    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 0))
+    kstats = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.split()
+        kstats[name] = {"launches": int(cnt), "total_ms": float(ms)}
+    top = max(kstats, key=lambda n: kstats[n]["total_ms"]) if kstats else None
+
+    # e2e through the C-ABI with host buffers
+    bench.e2e_call(0)
+    e2e_t = []
+    for _ in range(max(2, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        bench.e2e_call(0)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = ranks.max(statistics.median(e2e_t))
+    h2d, d2h = bench.io_bytes(0)
+
+    result = {
+        "metric": "pairs/s", "value": value, "unit": "pairs/s", "n_gpus": ranks.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": "synthetic (seeded numpy generator, workload shapes of the benchmark configuration)",
+        "config": dict(bench.describe(), l2="flushed between steps (256 MB memset outside the timed events)",
+                       parallelism="replicas" if ranks.world > 1 else "single GPU"),
+        "gcups": bench.cells * ranks.world / (ms_per_step / 1e3) / 1e9,
+        "e2e": {"value": bench.pairs * ranks.world / e2e_s, "unit": "pairs/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "blg_cdist/blg_pairwise C-ABI, pageable host buffers, wall clock"},
+        "gpu_launches": int(launches), "wall_s_timed_region": wall,
+        "clocks": clk, "runs": extra_runs, "kernels": kstats,
+    }
+    if args.config in H100_REF:
+        ref, src = H100_REF[args.config]
+        result["vs_baseline"] = value / ref
+        result["vs_baseline_ref"] = src
+
+    if ranks.rank == 0:
+        peak = int_peak(ranks.local)
+        exit_sum = None
+        cpu = None
+        if not args.no_cpu_baseline:
+            threads = effective_cpus()
+            v, sample, n_s, res = bench.cpu_sample(threads, args.cpu_budget)
+            v1, sample1, _, _ = bench.cpu_sample(1, args.cpu_budget / 3)
+            cpu = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": sample,
+                   "single_thread": {"value": v1, "sample": sample1},
+                   "gate": bench.gate(n_s, res)}
+            if bench.runs[0][0] is not None:
+                exit_sum = exit_columns(bench, n_s)
+        result["cpu_baseline"] = cpu
+        if top:
+            per_launch_ms = kstats[top]["total_ms"] / kstats[top]["launches"]
+            ops = bench.alg_ops(0, exit_sum)
+            launches_per_step = kstats[top]["launches"] / 3.0
+            rl = {"kernel": top, "bound": "int", "unit": "Gop/s", "ms_per_launch": per_launch_ms,
+                  "peak": peak.get("gops"), "peak_source": "measured: libblg_probe LOP3/IADD3 stream on this GPU",
+                  "peak_detail": peak,
+                  "traffic": read_traffic(top, bench.w.name)}
+            if ops is not None and peak.get("gops"):
+                rl["achieved"] = ops / launches_per_step / (per_launch_ms / 1e3) / 1e9
+                rl["frac"] = rl["achieved"] / peak["gops"]
+            hbm_bytes = bench.alg_bytes(0) / launches_per_step
+            rl["hbm"] = {"achieved": hbm_bytes / (per_launch_ms / 1e3) / 1e9, "peak": 6800.0, "unit": "GB/s",
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+            rl["hbm"]["frac"] = rl["hbm"]["achieved"] / rl["hbm"]["peak"]
+            result["roofline"] = rl
+        print(json.dumps(result), flush=True)
+
+
+def run_reference(args, ranks: Ranks):
+    """The reference's CPU path on the host cores (oracle port: the reference's
+    sources are not present on the GPU host), same workload and metric."""
+    if ranks.rank != 0:
+        return
+    import oracle
+    cfg = args.config
+    w = {1: W.config1, 2: W.config2, 3: W.config3, 4: W.config4}[cfg]()
+    threads = effective_cpus()
+    if isinstance(w, W.SearchWork):
+        k = w.max_dist
+        rows = max(1, min(w.nq, 16 * threads))
+        sub = W.take(w.q, np.arange(rows))
+        fn = lambda: oracle.cross(sub, w.c, k, threads=threads)  # noqa: E731
+        per = rows * w.nc
+        cells = W.cross_cells(sub, w.c)
+        sample = f"{rows} query rows x {w.nc} choices per step"
+    else:
+        n = min(w.n, 1 << 18)
+        sa, sb = W.take(w.a, np.arange(n)), W.take(w.b, np.arange(n))
+        fn = lambda: oracle.pairs(sa, sb, w.max_dist, threads=threads)  # noqa: E731
+        per = n
+        cells = W.cells(sa, sb)
+        sample = f"first {n} pairs per step"
+    for _ in range(args.warmup):
+        fn()
+    t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        fn()
+        t.append(time.perf_counter() - t0)
+    s = sum(t) / len(t)
+    value = per / s
+    print(json.dumps({
+        "impl": "reference", "metric": "pairs/s", "value": value, "unit": "pairs/s", "n_gpus": ranks.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": f"config {cfg}", "sample": sample},
+        "gcups": cells / s / 1e9,
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of oracle work per leg")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    ranks = Ranks()
+    if ranks.world > 1:
+        os.environ["BLG_DEVICE"] = str(ranks.local)
+    try:
+        if args.impl == "reference":
+            run_reference(args, ranks)
+        else:
+            run_ours(args, ranks)
+    finally:
+        ranks.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,641 @@
+// Host runtime of the C-ABI (include/bitlev_gb300.h).
+//
+// Replaces the CuPy driver of the reference (bitlev/gpu.py:54-138,
+// bench/cudamyers.py:83-174): packing stays with the caller, classification
+// of work by length happens here in C++ (queries) or on the device (pairs,
+// after trimming), kernels run on the context's stream, device memory comes
+// from the stream-ordered allocator (cudaMallocAsync) so repeated calls do
+// not synchronise on allocation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/bitlev_gb300.h"
+#include "blg_device.cuh"
+#include "blg_internal.h"
+
+namespace blg {
+cudaError_t launch_build_peq(cudaStream_t st, const DevStrings &Q, const int32_t *qidx, int nq, int nwc,
+                             uint64_t *peq, uint32_t *status);
+cudaError_t launch_search_seq(cudaStream_t st, int nw, bool hask, const DevStrings &C,
+                              const SearchClass &cls, int qpb, int k, int dtype, void *out,
+                              uint32_t *status);
+cudaError_t launch_search_lanes(cudaStream_t st, bool hask, const DevStrings &C, const SearchClass &cls,
+                                int nwc, int k, int dtype, void *out, uint32_t *status);
+cudaError_t launch_pairs_main(cudaStream_t st, int grid, bool hask, const DevStrings &A,
+                              const DevStrings &B, int k, int dtype, void *out, const LongQueue &q,
+                              uint32_t *status);
+cudaError_t launch_pairs_long(cudaStream_t st, int grid, bool hask, const LongQueue &q, int k,
+                              int dtype, void *out);
+}  // namespace blg
+
+using namespace blg;
+
+namespace {
+
+constexpr int kSeqMaxWords = 8;          // queries up to 512: sequential words per thread
+constexpr int kLaneMaxWords = 32;        // queries up to 2048: lane-spread
+
+struct ProfRec {
+    const char *name;
+    cudaEvent_t e0, e1;
+};
+
+struct OwnedStrings {
+    DevStrings d;
+    void *mem_buf = nullptr;   // allocation (d.buf - 16)
+    void *mem_off = nullptr;
+};
+
+}  // namespace
+
+struct blg_ctx {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t *d_status = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    std::mutex mu;
+    std::string err;
+    int64_t launches = 0;
+    bool prof = false;
+    std::vector<ProfRec> prof_recs;
+    std::map<std::string, std::pair<int64_t, double>> prof_acc;
+};
+
+struct blg_pairs {
+    OwnedStrings a, b;
+    int64_t n = 0;
+    int64_t cap[kLongClasses] = {0, 0, 0, 0, 0};
+    void *q_items = nullptr;      // all class regions, one allocation
+    int32_t *q_ctr = nullptr;     // counts[5], heads[5]
+};
+
+struct blg_search {
+    OwnedStrings q, c;
+    int64_t nq = 0, nc = 0;
+    struct Cls {
+        int nw;          // words (seq) or table stride (lanes)
+        bool lanes;
+        int nq;
+        int32_t *qidx, *qlen;
+        uint64_t *peq;
+    };
+    std::vector<Cls> cls;
+};
+
+// ------------------------------------------------------------ helpers --
+static int fail(blg_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+static int cuda_fail(blg_ctx *c, cudaError_t e, const char *what) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(c, BLG_ERR_ALLOC, std::string(what) + ": " + cudaGetErrorString(e));
+    return fail(c, BLG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+    } while (0)
+
+template <typename F>
+static cudaError_t launch(blg_ctx *c, const char *name, F &&fn) {
+    ProfRec r{name, nullptr, nullptr};
+    if (c->prof) {
+        cudaEventCreate(&r.e0);
+        cudaEventCreate(&r.e1);
+        cudaEventRecord(r.e0, c->stream);
+    }
+    cudaError_t e = fn();
+    c->launches++;
+    if (c->prof) {
+        cudaEventRecord(r.e1, c->stream);
+        c->prof_recs.push_back(r);
+    }
+    return e;
+}
+
+static cudaError_t dev_alloc(blg_ctx *c, void **p, size_t bytes) {
+    return cudaMallocAsync(p, bytes ? bytes : 16, c->stream);
+}
+
+static void dev_free(blg_ctx *c, void *p) {
+    if (p) cudaFreeAsync(p, c->stream);
+}
+
+static int check_offsets_host(blg_ctx *c, const int64_t *off, int64_t n) {
+    if (n < 0) return fail(c, BLG_ERR_ARG, "negative count");
+    if (n > 0 && !off) return fail(c, BLG_ERR_ARG, "null offsets");
+    if (n > 0 && (off[0] < 0 || off[n] < off[0]))
+        return fail(c, BLG_ERR_ARG, "offsets must start >= 0 and end >= start");
+    return BLG_OK;
+}
+
+// Copy a packed string set into HBM with 16 bytes of slack on both sides.
+static int upload_strings(blg_ctx *c, const uint8_t *buf, const int64_t *off, int64_t n,
+                          OwnedStrings &o) {
+    int rc = check_offsets_host(c, off, n);
+    if (rc) return rc;
+    const int64_t base = n > 0 ? off[0] : 0;
+    const int64_t bytes = n > 0 ? off[n] - off[0] : 0;
+    if (bytes > 0 && !buf) return fail(c, BLG_ERR_ARG, "null buffer");
+    CK(dev_alloc(c, &o.mem_buf, (size_t)bytes + 32), "cudaMallocAsync(strings)");
+    CK(cudaMemsetAsync(o.mem_buf, 0, (size_t)bytes + 32, c->stream), "cudaMemsetAsync(strings)");
+    uint8_t *dbuf = (uint8_t *)o.mem_buf + 16;
+    if (bytes > 0)
+        CK(cudaMemcpyAsync(dbuf, buf + base, (size_t)bytes, cudaMemcpyHostToDevice, c->stream),
+           "H2D strings");
+    CK(dev_alloc(c, &o.mem_off, sizeof(int64_t) * (size_t)(n + 1)), "cudaMallocAsync(offsets)");
+    if (n > 0)
+        CK(cudaMemcpyAsync(o.mem_off, off, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyHostToDevice,
+                           c->stream), "H2D offsets");
+    o.d.buf = dbuf;
+    o.d.off = (const int64_t *)o.mem_off;
+    o.d.n = n;
+    o.d.base = base;
+    o.d.bytes = bytes;
+    return BLG_OK;
+}
+
+static void free_strings(blg_ctx *c, OwnedStrings &o) {
+    dev_free(c, o.mem_buf);
+    dev_free(c, o.mem_off);
+    o = OwnedStrings();
+}
+
+static int status_to_rc(blg_ctx *c, uint32_t st) {
+    if (!st) return BLG_OK;
+    if (st & ST_QUEUE_TIMEOUT) return fail(c, BLG_ERR_TIMEOUT, "a bounded device wait timed out");
+    if (st & ST_BAD_OFFSETS) return fail(c, BLG_ERR_ARG, "corrupt offsets (not monotone or out of range)");
+    if (st & ST_TOO_LONG)
+        return fail(c, BLG_ERR_ARG, "a pattern is longer than 2048 bytes after trimming (unsupported)");
+    if (st & ST_QUEUE_OVERFLOW) return fail(c, BLG_ERR_CUDA, "internal work queue overflow");
+    return fail(c, BLG_ERR_CUDA, "device status " + std::to_string(st));
+}
+
+static int sync_and_status(blg_ctx *c) {
+    uint32_t st = 0;
+    CK(cudaMemcpyAsync(&st, c->d_status, sizeof(st), cudaMemcpyDeviceToHost, c->stream), "D2H status");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    if (st) {
+        CK(cudaMemsetAsync(c->d_status, 0, sizeof(uint32_t), c->stream), "reset status");
+        CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    }
+    return status_to_rc(c, st);
+}
+
+static size_t dtype_size(int dt) { return dt == BLG_UINT8 ? 1 : dt == BLG_UINT16 ? 2 : 4; }
+
+static bool dtype_ok(int dt) { return dt == BLG_INT32 || dt == BLG_UINT16 || dt == BLG_UINT8; }
+
+// ------------------------------------------------------------- pairs --
+static int pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uint8_t *bb,
+                        const int64_t *ob, int64_t n, blg_pairs *p) {
+    p->n = n;
+    int rc = upload_strings(c, ba, oa, n, p->a);
+    if (!rc) rc = upload_strings(c, bb, ob, n, p->b);
+    if (rc) return rc;
+    // Long-queue capacity per class: trimming only shortens a pattern, so a
+    // pair can land in class j only if its untrimmed shorter length reaches it.
+    int64_t hist[kLongClasses + 1] = {0, 0, 0, 0, 0, 0};
+    for (int64_t i = 0; i < n; i++) {
+        const int64_t la = oa[i + 1] - oa[i], lb = ob[i + 1] - ob[i];
+        const int64_t m = la < lb ? la : lb;
+        if (m <= 64) continue;
+        const int64_t W = (m + 63) >> 6;
+        const int cls = W <= 2 ? 0 : W <= 4 ? 1 : W <= 8 ? 2 : W <= 16 ? 3 : W <= 32 ? 4 : 5;
+        hist[cls]++;
+    }
+    int64_t total = 0, above = hist[kLongClasses];
+    for (int j = kLongClasses - 1; j >= 0; j--) {
+        above += hist[j];
+        p->cap[j] = above;
+        total += above;
+    }
+    if (total > 0) {
+        CK(dev_alloc(c, &p->q_items, sizeof(LongItem) * (size_t)total), "cudaMallocAsync(queue)");
+        CK(dev_alloc(c, (void **)&p->q_ctr, sizeof(int32_t) * 2 * kLongClasses), "cudaMallocAsync(ctr)");
+    }
+    return BLG_OK;
+}
+
+static int pairs_run(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out) {
+    if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
+    if (p->n == 0) return BLG_OK;
+    if (!d_out) return fail(c, BLG_ERR_ARG, "null output");
+    const bool hask = k >= 0;
+    LongQueue q{};
+    int64_t total = 0;
+    for (int j = 0; j < kLongClasses; j++) {
+        q.items[j] = (LongItem *)p->q_items + total;
+        q.cap[j] = p->cap[j];
+        total += p->cap[j];
+    }
+    q.counts = p->q_ctr;
+    q.heads = p->q_ctr ? p->q_ctr + kLongClasses : nullptr;
+    if (total > 0)
+        CK(cudaMemsetAsync(p->q_ctr, 0, sizeof(int32_t) * 2 * kLongClasses, c->stream), "reset queue");
+    // 64 KB of nibble tables per 256-thread CTA: 3 CTAs per SM.
+    const int64_t want = (p->n + 255) / 256;
+    const int grid = (int)std::min<int64_t>(want, (int64_t)c->sms * 3 * 16);
+    CK(launch(c, "pairs_main", [&] {
+           return launch_pairs_main(c->stream, grid, hask, p->a.d, p->b.d, k, dtype, d_out, q,
+                                    c->d_status);
+       }), "pairs_main");
+    if (total > 0)
+        CK(launch(c, "pairs_long", [&] {
+               return launch_pairs_long(c->stream, c->sms * 3, hask, q, k, dtype, d_out);
+           }), "pairs_long");
+    return BLG_OK;
+}
+
+static void pairs_release(blg_ctx *c, blg_pairs *p) {
+    free_strings(c, p->a);
+    free_strings(c, p->b);
+    dev_free(c, p->q_items);
+    dev_free(c, p->q_ctr);
+}
+
+// ------------------------------------------------------------ search --
+static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq,
+                         const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s) {
+    s->nq = nq;
+    s->nc = nc;
+    int rc = upload_strings(c, bq, oq, nq, s->q);
+    if (!rc) rc = upload_strings(c, bc, oc, nc, s->c);
+    if (rc) return rc;
+    // Query classes by word count (bitlev/gpu.py:116-118 uses 1,2,4,8 and the CPU
+    // above 512; here every length has a GPU class).
+    std::vector<std::vector<int32_t>> idx(kSeqMaxWords + 1), len(kSeqMaxWords + 1);
+    int lanes_nw = 0;
+    for (int64_t i = 0; i < nq; i++) {
+        const int64_t m = oq[i + 1] - oq[i];
+        int64_t W = (m + 63) >> 6;
+        if (W < 1) W = 1;
+        if (W > kLaneMaxWords)
+            return fail(c, BLG_ERR_ARG, "query longer than 2048 bytes is not supported");
+        const int slot = W <= kSeqMaxWords ? (int)W - 1 : kSeqMaxWords;
+        idx[slot].push_back((int32_t)i);
+        len[slot].push_back((int32_t)m);
+        if (slot == kSeqMaxWords) lanes_nw = std::max(lanes_nw, (int)W);
+    }
+    for (int slot = 0; slot <= kSeqMaxWords; slot++) {
+        if (idx[slot].empty()) continue;
+        blg_search::Cls k{};
+        k.lanes = slot == kSeqMaxWords;
+        k.nw = k.lanes ? lanes_nw : slot + 1;
+        k.nq = (int)idx[slot].size();
+        CK(dev_alloc(c, (void **)&k.qidx, sizeof(int32_t) * k.nq), "cudaMallocAsync(qidx)");
+        CK(dev_alloc(c, (void **)&k.qlen, sizeof(int32_t) * k.nq), "cudaMallocAsync(qlen)");
+        CK(dev_alloc(c, (void **)&k.peq, sizeof(uint64_t) * 256 * (size_t)k.nw * k.nq), "cudaMallocAsync(peq)");
+        CK(cudaMemcpyAsync(k.qidx, idx[slot].data(), sizeof(int32_t) * k.nq, cudaMemcpyHostToDevice, c->stream), "H2D qidx");
+        CK(cudaMemcpyAsync(k.qlen, len[slot].data(), sizeof(int32_t) * k.nq, cudaMemcpyHostToDevice, c->stream), "H2D qlen");
+        s->cls.push_back(k);
+    }
+    // the host vectors above are pageable: the copies completed before return
+    return BLG_OK;
+}
+
+static int pick_qpb(blg_ctx *c, int nq_cls, int64_t nc) {
+    const int64_t tiles = (nc + 1023) / 1024;
+    const int64_t target = (int64_t)c->sms * 8;
+    int64_t qpb = (int64_t)nq_cls * tiles / target;
+    if (qpb < 1) qpb = 1;
+    if (qpb > 16) qpb = 16;
+    return (int)qpb;
+}
+
+static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out) {
+    if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
+    if (s->nq == 0 || s->nc == 0) return BLG_OK;
+    if (!d_out) return fail(c, BLG_ERR_ARG, "null output");
+    const bool hask = k >= 0;
+    for (auto &k_ : s->cls)
+        CK(launch(c, "build_peq", [&] {
+               return launch_build_peq(c->stream, s->q.d, k_.qidx, k_.nq, k_.nw, k_.peq, c->d_status);
+           }), "build_peq");
+    for (auto &k_ : s->cls) {
+        SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
+        if (k_.lanes) {
+            CK(launch(c, "search_lanes", [&] {
+                   return launch_search_lanes(c->stream, hask, s->c.d, sc, k_.nw, k, dtype, d_out,
+                                              c->d_status);
+               }), "search_lanes");
+        } else {
+            const int qpb = pick_qpb(c, k_.nq, s->nc);
+            CK(launch(c, "search_seq", [&] {
+                   return launch_search_seq(c->stream, k_.nw, hask, s->c.d, sc, qpb, k, dtype, d_out,
+                                            c->d_status);
+               }), "search_seq");
+        }
+    }
+    return BLG_OK;
+}
+
+static void search_release(blg_ctx *c, blg_search *s) {
+    free_strings(c, s->q);
+    free_strings(c, s->c);
+    for (auto &k : s->cls) {
+        dev_free(c, k.qidx);
+        dev_free(c, k.qlen);
+        dev_free(c, k.peq);
+    }
+    s->cls.clear();
+}
+
+// ============================================================== C-ABI ==
+extern "C" {
+
+int blg_version(void) { return 100; }
+
+int blg_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int blg_init(int device, blg_ctx **out) {
+    if (!out) return BLG_ERR_ARG;
+    *out = nullptr;
+    int n = blg_device_count();
+    if (n <= 0) return BLG_ERR_NODEVICE;
+    if (device < 0 || device >= n) return BLG_ERR_ARG;
+    blg_ctx *c = new (std::nothrow) blg_ctx();
+    if (!c) return BLG_ERR_ALLOC;
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaEventCreate(&c->t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->t1);
+    if (e == cudaSuccess) {
+        // keep freed blocks in the stream-ordered pool instead of returning them
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    }
+    if (e != cudaSuccess) {
+        blg_destroy(c);
+        return e == cudaErrorMemoryAllocation ? BLG_ERR_ALLOC : BLG_ERR_CUDA;
+    }
+    *out = c;
+    return BLG_OK;
+}
+
+void blg_destroy(blg_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &r : c->prof_recs) {
+        cudaEventDestroy(r.e0);
+        cudaEventDestroy(r.e1);
+    }
+    if (c->d_status) cudaFree(c->d_status);
+    if (c->t0) cudaEventDestroy(c->t0);
+    if (c->t1) cudaEventDestroy(c->t1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char *blg_last_error(const blg_ctx *c) { return c ? c->err.c_str() : "no context"; }
+
+#define ENTER(c)                                      \
+    if (!(c)) return BLG_ERR_ARG;                     \
+    std::lock_guard<std::mutex> lock_((c)->mu);       \
+    (c)->err.clear();                                 \
+    if (cudaSetDevice((c)->device) != cudaSuccess) return fail((c), BLG_ERR_CUDA, "cudaSetDevice")
+
+int blg_pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uint8_t *bb,
+                     const int64_t *ob, int64_t n, blg_pairs **out) {
+    ENTER(c);
+    if (!out) return fail(c, BLG_ERR_ARG, "null out");
+    blg_pairs *p = new (std::nothrow) blg_pairs();
+    if (!p) return fail(c, BLG_ERR_ALLOC, "host allocation");
+    int rc = pairs_upload(c, ba, oa, bb, ob, n, p);
+    if (rc) {
+        pairs_release(c, p);
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return BLG_OK;
+}
+
+int blg_pairs_run(blg_ctx *c, blg_pairs *p, int32_t max_dist, int32_t dtype, void *d_out) {
+    ENTER(c);
+    if (!p) return fail(c, BLG_ERR_ARG, "null pairs");
+    return pairs_run(c, p, max_dist, dtype, d_out);
+}
+
+void blg_pairs_free(blg_ctx *c, blg_pairs *p) {
+    if (!c || !p) return;
+    std::lock_guard<std::mutex> lock_(c->mu);
+    cudaSetDevice(c->device);
+    pairs_release(c, p);
+    delete p;
+}
+
+int blg_search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq,
+                      const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search **out) {
+    ENTER(c);
+    if (!out) return fail(c, BLG_ERR_ARG, "null out");
+    blg_search *s = new (std::nothrow) blg_search();
+    if (!s) return fail(c, BLG_ERR_ALLOC, "host allocation");
+    int rc = search_upload(c, bq, oq, nq, bc, oc, nc, s);
+    if (rc) {
+        search_release(c, s);
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return BLG_OK;
+}
+
+int blg_search_run(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t dtype, void *d_out) {
+    ENTER(c);
+    if (!s) return fail(c, BLG_ERR_ARG, "null search");
+    return search_run(c, s, max_dist, dtype, d_out);
+}
+
+void blg_search_free(blg_ctx *c, blg_search *s) {
+    if (!c || !s) return;
+    std::lock_guard<std::mutex> lock_(c->mu);
+    cudaSetDevice(c->device);
+    search_release(c, s);
+    delete s;
+}
+
+int blg_pairwise(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uint8_t *bb,
+                 const int64_t *ob, int64_t n, int32_t max_dist, int32_t dtype, void *out_host,
+                 void **out_device) {
+    ENTER(c);
+    if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
+    if (n < 0) return fail(c, BLG_ERR_ARG, "negative count");
+    if (!out_device && n > 0 && !out_host) return fail(c, BLG_ERR_ARG, "null output");
+    const size_t obytes = dtype_size(dtype) * (size_t)n;
+    void *d_out = nullptr;
+    CK(dev_alloc(c, &d_out, obytes), "cudaMallocAsync(out)");
+    blg_pairs p;
+    int rc = pairs_upload(c, ba, oa, bb, ob, n, &p);
+    if (!rc) rc = pairs_run(c, &p, max_dist, dtype, d_out);
+    if (!rc && !out_device && n > 0) {
+        cudaError_t e = cudaMemcpyAsync(out_host, d_out, obytes, cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "D2H results");
+    }
+    pairs_release(c, &p);
+    if (rc || !out_device) dev_free(c, d_out);
+    const int rc2 = sync_and_status(c);
+    if (rc) return rc;
+    if (rc2) {
+        if (out_device) dev_free(c, d_out);
+        return rc2;
+    }
+    if (out_device) *out_device = d_out;
+    return BLG_OK;
+}
+
+int blg_cdist(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq, const uint8_t *bc,
+              const int64_t *oc, int64_t nc, int32_t max_dist, int32_t dtype, void *out_host,
+              void **out_device) {
+    ENTER(c);
+    if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
+    if (nq < 0 || nc < 0) return fail(c, BLG_ERR_ARG, "negative count");
+    const size_t obytes = dtype_size(dtype) * (size_t)nq * (size_t)nc;
+    if (!out_device && obytes > 0 && !out_host) return fail(c, BLG_ERR_ARG, "null output");
+    void *d_out = nullptr;
+    CK(dev_alloc(c, &d_out, obytes), "cudaMallocAsync(out)");
+    blg_search s;
+    int rc = BLG_OK;
+    if (nq > 0 && nc > 0) {
+        rc = search_upload(c, bq, oq, nq, bc, oc, nc, &s);
+        if (!rc) rc = search_run(c, &s, max_dist, dtype, d_out);
+        if (!rc && !out_device) {
+            cudaError_t e = cudaMemcpyAsync(out_host, d_out, obytes, cudaMemcpyDeviceToHost, c->stream);
+            if (e != cudaSuccess) rc = cuda_fail(c, e, "D2H results");
+        }
+        search_release(c, &s);
+    }
+    if (rc || !out_device) dev_free(c, d_out);
+    const int rc2 = sync_and_status(c);
+    if (rc) return rc;
+    if (rc2) {
+        if (out_device) dev_free(c, d_out);
+        return rc2;
+    }
+    if (out_device) *out_device = d_out;
+    return BLG_OK;
+}
+
+int blg_malloc(blg_ctx *c, size_t bytes, void **d_ptr) {
+    ENTER(c);
+    if (!d_ptr) return fail(c, BLG_ERR_ARG, "null out");
+    CK(dev_alloc(c, d_ptr, bytes), "cudaMallocAsync");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return BLG_OK;
+}
+
+int blg_free(blg_ctx *c, void *d_ptr) {
+    ENTER(c);
+    dev_free(c, d_ptr);
+    return BLG_OK;
+}
+
+int blg_memcpy_h2d(blg_ctx *c, void *d_dst, const void *h_src, size_t bytes) {
+    ENTER(c);
+    if (bytes == 0) return BLG_OK;
+    CK(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, c->stream), "H2D");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return BLG_OK;
+}
+
+int blg_memcpy_d2h(blg_ctx *c, void *h_dst, const void *d_src, size_t bytes) {
+    ENTER(c);
+    if (bytes == 0) return BLG_OK;
+    CK(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, c->stream), "D2H");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return BLG_OK;
+}
+
+int blg_memset(blg_ctx *c, void *d_dst, int value, size_t bytes) {
+    ENTER(c);
+    if (bytes == 0) return BLG_OK;
+    CK(cudaMemsetAsync(d_dst, value, bytes, c->stream), "memset");
+    return BLG_OK;
+}
+
+int blg_synchronize(blg_ctx *c) {
+    ENTER(c);
+    return sync_and_status(c);
+}
+
+int blg_timer_start(blg_ctx *c) {
+    ENTER(c);
+    CK(cudaEventRecord(c->t0, c->stream), "cudaEventRecord");
+    return BLG_OK;
+}
+
+int blg_timer_stop(blg_ctx *c, float *ms) {
+    ENTER(c);
+    CK(cudaEventRecord(c->t1, c->stream), "cudaEventRecord");
+    CK(cudaEventSynchronize(c->t1), "cudaEventSynchronize");
+    float v = 0.f;
+    CK(cudaEventElapsedTime(&v, c->t0, c->t1), "cudaEventElapsedTime");
+    if (ms) *ms = v;
+    return BLG_OK;
+}
+
+int64_t blg_launch_count(const blg_ctx *c) { return c ? c->launches : 0; }
+
+int blg_profile_enable(blg_ctx *c, int on) {
+    ENTER(c);
+    c->prof = on != 0;
+    return BLG_OK;
+}
+
+int blg_profile_report(blg_ctx *c, char *buf, size_t cap) {
+    ENTER(c);
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    for (auto &r : c->prof_recs) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.e0, r.e1);
+        auto &a = c->prof_acc[r.name];
+        a.first += 1;
+        a.second += ms;
+        cudaEventDestroy(r.e0);
+        cudaEventDestroy(r.e1);
+    }
+    c->prof_recs.clear();
+    std::string s;
+    for (auto &kv : c->prof_acc) {
+        char line[256];
+        snprintf(line, sizeof(line), "%s %lld %.6f\n", kv.first.c_str(), (long long)kv.second.first,
+                 kv.second.second);
+        s += line;
+    }
+    c->prof_acc.clear();
+    if (buf && cap) {
+        const size_t nb = std::min(cap - 1, s.size());
+        memcpy(buf, s.data(), nb);
+        buf[nb] = 0;
+    }
+    return BLG_OK;
+}
+
+}  // extern "C"

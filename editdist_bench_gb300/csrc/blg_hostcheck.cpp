@@ -1,0 +1,98 @@
+// Host build of the device primitives (blg_device.cuh) for the CPU tests.
+//
+// The same step/score/saturation functions the kernels call are compiled
+// here with g++ and driven two ways:
+//  * blg_host_distance: pattern = shorter trimmed string, words processed
+//    top to bottom in one column (the order k_search_seq uses);
+//  * blg_host_wavefront: the anti-diagonal lane schedule of the
+//    lane-spread kernels, emulated step by step: "lane" w handles column
+//    s - w at step s and reads the carry lane w-1 produced one step earlier
+//    (what __shfl_up_sync delivers on the GPU), with the max_dist exit
+//    decided by the last word's lane.
+// Both must equal the oracle for every input.
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "blg_device.cuh"
+
+using namespace blg;
+
+namespace {
+
+struct Pattern {
+    int m = 0, words = 0;
+    std::vector<uint64_t> peq;   // 256 x words
+    Pattern(const uint8_t *p, int m_) : m(m_), words(m_ > 0 ? (m_ + 63) / 64 : 1), peq(256 * (size_t)words, 0) {
+        for (int i = 0; i < m; i++) peq[(size_t)p[i] * words + i / 64] |= 1ull << (i % 64);
+    }
+    uint64_t eq(uint8_t c, int w) const { return peq[(size_t)c * words + w]; }
+};
+
+void normalise(const uint8_t *&a, int &la, const uint8_t *&b, int &lb, int trim) {
+    if (trim) trim_affixes(a, la, b, lb);
+    if (la > lb) {
+        const uint8_t *t = a; a = b; b = t;
+        int x = la; la = lb; lb = x;
+    }
+}
+
+}  // namespace
+
+extern "C" int blg_host_distance(const uint8_t *a, int la, const uint8_t *b, int lb, int trim, int k) {
+    normalise(a, la, b, lb, trim);
+    if (k >= 0 && lb - la > k) return k + 1;
+    if (la == 0) return lb;
+    Pattern P(a, la);
+    const int W = P.words, lastbit = (la - 1) % 64;
+    std::vector<uint64_t> pv(W, ~0ull), mv(W, 0);
+    int score = la;
+    for (int j = 0; j < lb; j++) {
+        uint64_t ph, mh;
+        step_top<uint64_t>(pv[0], mv[0], P.eq(b[j], 0), ph, mh);
+        int h = hdelta<uint64_t>(ph, mh, W == 1 ? lastbit : 63);
+        for (int w = 1; w < W; w++) {
+            step_mid<uint64_t>(pv[w], mv[w], P.eq(b[j], w), h, ph, mh);
+            h = hdelta<uint64_t>(ph, mh, w == W - 1 ? lastbit : 63);
+        }
+        score += h;
+        if (hopeless(score, j, lb, k)) return k + 1;
+    }
+    return cap_k(score, k);
+}
+
+extern "C" int blg_host_wavefront(const uint8_t *a, int la, const uint8_t *b, int lb, int trim, int k) {
+    normalise(a, la, b, lb, trim);
+    if (k >= 0 && lb - la > k) return k + 1;
+    if (la == 0) return lb;
+    Pattern P(a, la);
+    const int W = P.words, lastw = W - 1, lastbit = (la - 1) % 64;
+    std::vector<uint64_t> pv(W, ~0ull), mv(W, 0);
+    std::vector<int> carry(W, 0), next(W, 0);   // carry[w]: what lane w received last step
+    int score = la;
+    bool done = false;
+    for (int s = 0; s < lb + W - 1 && !done; s++) {
+        for (int w = 0; w < W; w++) {
+            const int j = s - w;
+            next[w] = 0;
+            if (j < 0 || j >= lb) continue;
+            uint64_t ph, mh;
+            step_mid<uint64_t>(pv[w], mv[w], P.eq(b[j], w), w == 0 ? 1 : carry[w], ph, mh);
+            const int hout = hdelta<uint64_t>(ph, mh, w == lastw ? lastbit : 63);
+            next[w] = hout;
+            if (w == lastw) {
+                score += hout;
+                if (hopeless(score, j, lb, k)) done = true;
+            }
+        }
+        for (int w = W - 1; w >= 1; w--) carry[w] = next[w - 1];   // shfl_up by one lane
+    }
+    if (done) return k + 1;
+    return cap_k(score, k);
+}
+
+extern "C" int blg_host_store(int d, int dtype) {
+    if (dtype == DT_UINT8) return (int)saturate_u8(d);
+    if (dtype == DT_UINT16) return (int)saturate_u16(d);
+    return d;
+}

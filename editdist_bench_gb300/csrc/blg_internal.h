@@ -1,0 +1,58 @@
+// Internal types shared by the kernels (blg_kernels.cu) and the host
+// runtime (blg_api.cu). Not part of the public C-ABI.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace blg {
+
+// A packed string set resident in HBM: bytes of string i are
+// buf[off[i] - base, off[i+1] - base). The byte buffer carries 16 bytes of
+// slack before and after the data so the kernels' aligned 4/16-byte window
+// loads never leave the allocation; `buf` points 16 bytes into it.
+struct DevStrings {
+    const uint8_t *buf = nullptr;
+    const int64_t *off = nullptr;
+    int64_t n = 0;
+    int64_t base = 0;       // off[0] on the host
+    int64_t bytes = 0;      // off[n] - off[0]
+};
+
+// Status bits raised by kernels (atomicOr into a device word).
+enum : uint32_t {
+    ST_BAD_OFFSETS = 1u << 0,   // offsets not monotone / out of range
+    ST_TOO_LONG = 1u << 1,      // pattern longer than the lane-spread limit
+    ST_QUEUE_TIMEOUT = 1u << 2, // a bounded device wait gave up
+    ST_QUEUE_OVERFLOW = 1u << 3,
+};
+
+// Long pairs (trimmed pattern longer than 64) are queued by the pairs kernel
+// and solved lane-spread: one 64-bit pattern word per lane, LANES lanes per
+// pair, classes LANES = 2, 4, 8, 16, 32.
+constexpr int kLongClasses = 5;
+constexpr int kMaxLanePattern = 64 * 32;
+
+struct LongItem {
+    const uint8_t *pat;
+    const uint8_t *txt;
+    int32_t m, n;
+    int64_t idx;
+};
+
+struct LongQueue {
+    LongItem *items[kLongClasses];   // one region per class
+    int64_t cap[kLongClasses];       // capacity of each region (pairs that may land there)
+    int32_t *counts;                 // kLongClasses producers' counters
+    int32_t *heads;                  // kLongClasses consumers' counters
+};
+
+// Per-query-class search launch description.
+struct SearchClass {
+    int nw;                 // pattern words (sequential kernels) or 0 for lane-spread
+    int nq;                 // queries in this class
+    const int32_t *qidx;    // device: query row per class entry
+    const int32_t *qlen;    // device: query length per class entry
+    const uint64_t *peq;    // device: [nq][256][nw] Peq tables
+};
+
+}  // namespace blg

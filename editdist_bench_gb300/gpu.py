@@ -1,0 +1,189 @@
+"""GB300 versions of ``pairwise`` and ``cdist`` — a drop-in for ``bitlev.gpu``.
+
+    from editdist_bench_gb300 import gpu
+    d = gpu.cdist(queries, choices, max_dist=2, dtype="uint8")
+
+Same signatures and results as bitlev/gpu.py:36-138: ``max_dist=k`` returns
+min(d, k+1); int32, uint16 or uint8 output with saturation;
+``return_device=True`` keeps the result in GPU memory (a ``DeviceArray``
+with ``__cuda_array_interface__``). Differences, all deliberate:
+
+* the work runs in ``libbitlev_gb300.so`` (C-ABI, ctypes), not CuPy/NVRTC;
+* every length runs on the GPU (the reference computes pairs whose shorter
+  string exceeds 256, and queries longer than 512, on the CPU);
+* uint16 saturation is fused into the kernels' stores.
+
+The packed entry points (``pairwise_packed``/``cdist_packed``) and the
+resident ``PairsBatch``/``SearchBatch`` mirror the reference benchmark's
+``PairsState``/``CrossState`` (bench/cudamyers.py:83-174).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._common import DTYPE_CODE, as_list, check_dtype, check_k, pack
+from .device_array import DeviceArray
+
+__all__ = ["available", "pairwise", "cdist", "pairwise_packed", "cdist_packed", "PairsBatch",
+           "SearchBatch", "pack"]
+
+
+def available() -> bool:
+    """True when the CUDA library is built and a GPU is visible."""
+    return _lib.device_count() > 0
+
+
+def _c(a: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(a)
+
+
+def _packed(p):
+    buf, off = p
+    return _c(np.asarray(buf, dtype=np.uint8)), _c(np.asarray(off, dtype=np.int64))
+
+
+def _empty(shape, dt, return_device, ctx=None):
+    if return_device:
+        return DeviceArray(0, shape, dt, ctx or _lib.context())
+    return np.empty(shape, dtype=dt)
+
+
+def pairwise_packed(pa, pb, max_dist=None, dtype=np.int32, return_device: bool = False):
+    """out[i] = d(a_i, b_i) for packed inputs ``(buf uint8, off int64[n+1])``."""
+    (ba, oa), (bb, ob) = _packed(pa), _packed(pb)
+    n = len(oa) - 1
+    if len(ob) - 1 != n:
+        raise ValueError(f"length mismatch: {n} vs {len(ob) - 1}")
+    k, dt = check_k(max_dist), check_dtype(dtype)
+    ctx = _lib.context()
+    if n == 0:
+        return _empty((0,), dt, return_device, ctx)
+    lib = ctx.lib
+    if return_device:
+        dptr = ctypes.c_void_p()
+        ctx.check(lib.blg_pairwise(ctx.h, ba.ctypes.data, oa.ctypes.data, bb.ctypes.data,
+                                   ob.ctypes.data, n, k, DTYPE_CODE[dt], None, ctypes.byref(dptr)),
+                  "pairwise")
+        return DeviceArray(dptr.value, (n,), dt, ctx)
+    out = np.empty(n, dtype=dt)
+    ctx.check(lib.blg_pairwise(ctx.h, ba.ctypes.data, oa.ctypes.data, bb.ctypes.data,
+                               ob.ctypes.data, n, k, DTYPE_CODE[dt], out.ctypes.data, None),
+              "pairwise")
+    return out
+
+
+def cdist_packed(pq, pc, max_dist=None, dtype=np.int32, return_device: bool = False):
+    """out[i, j] = d(q_i, c_j) for packed inputs."""
+    (bq, oq), (bc, oc) = _packed(pq), _packed(pc)
+    nq, nc = len(oq) - 1, len(oc) - 1
+    k, dt = check_k(max_dist), check_dtype(dtype)
+    ctx = _lib.context()
+    if nq == 0 or nc == 0:
+        return _empty((nq, nc), dt, return_device, ctx)
+    lib = ctx.lib
+    if return_device:
+        dptr = ctypes.c_void_p()
+        ctx.check(lib.blg_cdist(ctx.h, bq.ctypes.data, oq.ctypes.data, nq, bc.ctypes.data,
+                                oc.ctypes.data, nc, k, DTYPE_CODE[dt], None, ctypes.byref(dptr)),
+                  "cdist")
+        return DeviceArray(dptr.value, (nq, nc), dt, ctx)
+    out = np.empty((nq, nc), dtype=dt)
+    ctx.check(lib.blg_cdist(ctx.h, bq.ctypes.data, oq.ctypes.data, nq, bc.ctypes.data,
+                            oc.ctypes.data, nc, k, DTYPE_CODE[dt], out.ctypes.data, None),
+              "cdist")
+    return out
+
+
+def pairwise(a, b, max_dist=None, dtype=np.int32, return_device: bool = False):
+    """out[i] = d(a[i], b[i]) on the GPU (bitlev/gpu.py:71-103)."""
+    a, b = as_list(a), as_list(b)
+    if len(a) != len(b):
+        raise ValueError(f"length mismatch: {len(a)} vs {len(b)}")
+    k, dt = check_k(max_dist), check_dtype(dtype)
+    if len(a) == 0:
+        return _empty((0,), dt, return_device)
+    return pairwise_packed(pack(a), pack(b), k if k >= 0 else None, dt, return_device)
+
+
+def cdist(queries, choices, max_dist=None, dtype=np.int32, return_device: bool = False):
+    """out[i, j] = d(queries[i], choices[j]) on the GPU (bitlev/gpu.py:106-138)."""
+    q, c = as_list(queries), as_list(choices)
+    k, dt = check_k(max_dist), check_dtype(dtype)
+    if not q or not c:
+        return _empty((len(q), len(c)), dt, return_device)
+    return cdist_packed(pack(q), pack(c), k if k >= 0 else None, dt, return_device)
+
+
+class PairsBatch:
+    """Packed pairs resident in HBM (bench/cudamyers.py:83-114): upload once,
+    ``run`` many times into a device buffer (stream-ordered, no sync)."""
+
+    def __init__(self, pa, pb):
+        (ba, oa), (bb, ob) = _packed(pa), _packed(pb)
+        self.n = len(oa) - 1
+        if len(ob) - 1 != self.n:
+            raise ValueError(f"length mismatch: {self.n} vs {len(ob) - 1}")
+        self.ctx = _lib.context()
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.blg_pairs_upload(self.ctx.h, ba.ctypes.data, oa.ctypes.data,
+                                                     bb.ctypes.data, ob.ctypes.data, self.n,
+                                                     ctypes.byref(h)), "pairs_upload")
+        self.h = h
+
+    def alloc(self, dtype=np.int32) -> DeviceArray:
+        dt = check_dtype(dtype)
+        p = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.blg_malloc(self.ctx.h, max(1, self.n * dt.itemsize),
+                                               ctypes.byref(p)), "malloc")
+        return DeviceArray(p.value, (self.n,), dt, self.ctx)
+
+    def run(self, out: DeviceArray, max_dist=None):
+        k = check_k(max_dist)
+        self.ctx.check(self.ctx.lib.blg_pairs_run(self.ctx.h, self.h, k, DTYPE_CODE[out.dtype],
+                                                  out.ptr), "pairs_run")
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.ctx.lib.blg_pairs_free(self.ctx.h, self.h)
+            self.h = None
+
+
+class SearchBatch:
+    """Packed queries and choices resident in HBM (bench/cudamyers.py:139-174)."""
+
+    def __init__(self, pq, pc):
+        (bq, oq), (bc, oc) = _packed(pq), _packed(pc)
+        self.nq, self.nc = len(oq) - 1, len(oc) - 1
+        self.ctx = _lib.context()
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.blg_search_upload(self.ctx.h, bq.ctypes.data, oq.ctypes.data,
+                                                      self.nq, bc.ctypes.data, oc.ctypes.data,
+                                                      self.nc, ctypes.byref(h)), "search_upload")
+        self.h = h
+
+    def alloc(self, dtype=np.int32) -> DeviceArray:
+        dt = check_dtype(dtype)
+        p = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.blg_malloc(self.ctx.h, max(1, self.nq * self.nc * dt.itemsize),
+                                               ctypes.byref(p)), "malloc")
+        return DeviceArray(p.value, (self.nq, self.nc), dt, self.ctx)
+
+    def run(self, out: DeviceArray, max_dist=None):
+        k = check_k(max_dist)
+        self.ctx.check(self.ctx.lib.blg_search_run(self.ctx.h, self.h, k, DTYPE_CODE[out.dtype],
+                                                   out.ptr), "search_run")
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.ctx.lib.blg_search_free(self.ctx.h, self.h)
+            self.h = None
+
+
+def synchronize():
+    ctx = _lib.context()
+    ctx.check(ctx.lib.blg_synchronize(ctx.h), "synchronize")

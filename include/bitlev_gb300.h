@@ -1,0 +1,119 @@
+/*
+ * bitlev_gb300.h — C-ABI of the GB300 bit-parallel Levenshtein engine.
+ *
+ * Drop-in for the GPU path of karims/editdist-bench's `bitlev` library:
+ * bitlev.gpu.pairwise / bitlev.gpu.cdist (bitlev/gpu.py:71-138) and the
+ * resident-state launch helpers its benchmark uses (bench/cudamyers.py:
+ * 83-174). The library is loaded through ctypes by the Python layer
+ * (editdist_bench_gb300/gpu.py); plain pointers and sizes only.
+ *
+ * Inputs are bitlev's packed layout (csrc/edpy.c:200-224, `_edpy.pack`):
+ * one byte buffer and int64 offsets off[0..n], string i = buf[off[i] ..
+ * off[i+1]). Distances are exact unit-cost Levenshtein distances; with
+ * max_dist = k >= 0 the result is min(d, k + 1) (csrc/myers.c:101-143);
+ * max_dist < 0 means exact. Narrow dtypes saturate at their maximum
+ * (bitlev/_common.py:25-29). Every string length is computed on the GPU:
+ * there is no CPU fallback (the reference sends strings longer than
+ * 256/512 to its CPU path, bitlev/gpu.py:97-101,131-136).
+ *
+ * Return codes (bitlev raises the Python equivalents):
+ *   BLG_OK 0, BLG_ERR_ALLOC -1 (MemoryError), BLG_ERR_ARG -2 (ValueError),
+ *   BLG_ERR_CUDA -3, BLG_ERR_TIMEOUT -4, BLG_ERR_NODEVICE -5 (RuntimeError).
+ * blg_last_error() gives the message of the last failing call.
+ *
+ * Threading: one context per device and process is enough; calls on one
+ * context are serialised by a mutex; work runs on the context's stream.
+ */
+#ifndef BITLEV_GB300_H
+#define BITLEV_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BLG_OK 0
+#define BLG_ERR_ALLOC (-1)
+#define BLG_ERR_ARG (-2)
+#define BLG_ERR_CUDA (-3)
+#define BLG_ERR_TIMEOUT (-4)
+#define BLG_ERR_NODEVICE (-5)
+
+/* dtype codes: bitlev's DTYPES (bitlev/_common.py:7) */
+#define BLG_INT32 0
+#define BLG_UINT16 1
+#define BLG_UINT8 2
+
+typedef struct blg_ctx blg_ctx;
+typedef struct blg_pairs blg_pairs;   /* resident pairs  (bench/cudamyers.py:83-114 PairsState) */
+typedef struct blg_search blg_search; /* resident search (bench/cudamyers.py:139-152 CrossState) */
+
+/* Library ABI version (major*100 + minor). */
+int blg_version(void);
+
+/* Number of visible CUDA devices (0 when none). Replaces bitlev.gpu.available()'s
+ * CuPy device query (bitlev/gpu.py:36-41). */
+int blg_device_count(void);
+
+/* Create a context on `device` (own stream, status word, allocator pool).
+ * Replaces the lazily built CuPy RawModule (bitlev/gpu.py:44-51). */
+int blg_init(int device, blg_ctx **out);
+void blg_destroy(blg_ctx *ctx);
+const char *blg_last_error(const blg_ctx *ctx);
+
+/* out[i] = d(a_i, b_i) — bitlev.gpu.pairwise (bitlev/gpu.py:71-103).
+ * Host inputs; n >= 0. When out_device is NULL the results are written to
+ * out_host (n elements of `dtype`); otherwise a device buffer is allocated,
+ * filled and returned in *out_device (free with blg_free) — return_device. */
+int blg_pairwise(blg_ctx *ctx, const uint8_t *buf_a, const int64_t *off_a, const uint8_t *buf_b,
+                 const int64_t *off_b, int64_t n, int32_t max_dist, int32_t dtype, void *out_host,
+                 void **out_device);
+
+/* out[i*nc + j] = d(q_i, c_j) — bitlev.gpu.cdist (bitlev/gpu.py:106-138). */
+int blg_cdist(blg_ctx *ctx, const uint8_t *buf_q, const int64_t *off_q, int64_t nq,
+              const uint8_t *buf_c, const int64_t *off_c, int64_t nc, int32_t max_dist,
+              int32_t dtype, void *out_host, void **out_device);
+
+/* Resident pairs: upload once, run many times with results left in HBM —
+ * the "kernel-only" protocol of bench/cudamyers.py:83-136 (PairsState +
+ * pairs()). d_out must hold n elements of dtype (device memory). The run
+ * is stream-ordered and does not synchronise. */
+int blg_pairs_upload(blg_ctx *ctx, const uint8_t *buf_a, const int64_t *off_a, const uint8_t *buf_b,
+                     const int64_t *off_b, int64_t n, blg_pairs **out);
+int blg_pairs_run(blg_ctx *ctx, blg_pairs *p, int32_t max_dist, int32_t dtype, void *d_out);
+void blg_pairs_free(blg_ctx *ctx, blg_pairs *p);
+
+/* Resident search (bench/cudamyers.py:139-174, CrossState + cross()):
+ * d_out holds nq*nc elements of dtype, row-major. */
+int blg_search_upload(blg_ctx *ctx, const uint8_t *buf_q, const int64_t *off_q, int64_t nq,
+                      const uint8_t *buf_c, const int64_t *off_c, int64_t nc, blg_search **out);
+int blg_search_run(blg_ctx *ctx, blg_search *s, int32_t max_dist, int32_t dtype, void *d_out);
+void blg_search_free(blg_ctx *ctx, blg_search *s);
+
+/* Device memory and stream helpers (the parts of CuPy bitlev.gpu used:
+ * cp.empty / .get() / Device().synchronize(), bitlev/gpu.py:59-68,102). */
+int blg_malloc(blg_ctx *ctx, size_t bytes, void **d_ptr);
+int blg_free(blg_ctx *ctx, void *d_ptr);
+int blg_memcpy_h2d(blg_ctx *ctx, void *d_dst, const void *h_src, size_t bytes);
+int blg_memcpy_d2h(blg_ctx *ctx, void *h_dst, const void *d_src, size_t bytes);
+int blg_memset(blg_ctx *ctx, void *d_dst, int value, size_t bytes);
+/* Wait for the context's stream and report any status a kernel raised. */
+int blg_synchronize(blg_ctx *ctx);
+
+/* Timing on the context's stream with CUDA events (ms between start/stop). */
+int blg_timer_start(blg_ctx *ctx);
+int blg_timer_stop(blg_ctx *ctx, float *ms);
+/* Kernels launched by this context so far. */
+int64_t blg_launch_count(const blg_ctx *ctx);
+/* Per-kernel event timing of every launch while enabled (bench roofline). */
+int blg_profile_enable(blg_ctx *ctx, int on);
+/* Writes "name launches total_ms\n" lines (after synchronising) into buf. */
+int blg_profile_report(blg_ctx *ctx, char *buf, size_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BITLEV_GB300_H */

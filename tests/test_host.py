@@ -1,0 +1,171 @@
+"""Host-side logic without a GPU: bitlev's input semantics (checks, packing,
+errors), the host build of the device primitives against the oracle, the
+workload generators, and DeviceArray bookkeeping."""
+import ctypes
+import random
+
+import numpy as np
+import pytest
+
+import oracle
+from editdist_bench_gb300 import _build, workloads as W
+from editdist_bench_gb300._common import check_dtype, check_k, convert, pack
+from editdist_bench_gb300.device_array import DeviceArray
+
+
+# ---- bitlev/_common.py semantics ------------------------------------------
+def test_check_k_and_dtype():
+    assert check_k(None) == -1 and check_k(0) == 0 and check_k(7) == 7
+    assert check_k(2 ** 40) == 2 ** 30
+    with pytest.raises(ValueError):
+        check_k(-1)
+    for dt in (np.int32, "uint16", np.uint8, "int32"):
+        check_dtype(dt)
+    for dt in (np.float32, np.int64, "int8"):
+        with pytest.raises(ValueError):
+            check_dtype(dt)
+    np.testing.assert_array_equal(convert(np.array([0, 255, 256, 70000], np.int32), np.dtype(np.uint8)),
+                                  [0, 255, 255, 255])
+    np.testing.assert_array_equal(convert(np.array([0, 65535, 70000], np.int32), np.dtype(np.uint16)),
+                                  [0, 65535, 65535])
+
+
+# ---- packing (csrc/edpy.c:14-35, :200-224; tests/test_pack.py) -------------
+@pytest.mark.parametrize("S", [[], [""], ["", ""], ["ab", "", "xyz"], ["\xff\x00\x80"],
+                               ["q" * 1000] * 3, [b"by", "tes"], [b"x", b"", b"yz"]])
+def test_pack_matches_oracle_pack(S):
+    b1, o1 = pack(S)
+    b2, o2 = oracle.pack(S)
+    np.testing.assert_array_equal(o1, o2)
+    assert bytes(b1[:o1[-1]]) == bytes(b2[:o2[-1]])
+    assert len(b1) >= 1                       # never an empty buffer
+    assert b1.dtype == np.uint8 and o1.dtype == np.int64
+
+
+def test_pack_errors_and_generators():
+    with pytest.raises(ValueError):
+        pack(["ok", "ā"])                # above U+00FF
+    with pytest.raises(ValueError):
+        pack(["日本"])
+    with pytest.raises(TypeError):
+        pack(["ok", 3])
+    with pytest.raises(TypeError):
+        pack([1, "a"])
+    with pytest.raises(TypeError):
+        pack([b"a", bytearray(b"b")])        # bytes only, like PyBytes_Check
+    b, o = pack(x for x in ["caf\xe9", "\xff\x00"])
+    assert bytes(b[:o[-1]]) == b"caf\xe9\xff\x00" and o.tolist() == [0, 4, 6]
+
+
+# ---- host build of the device primitives -----------------------------------
+@pytest.fixture(scope="module")
+def hostcheck():
+    L = ctypes.CDLL(_build.build_hostcheck())
+    for f in (L.blg_host_distance, L.blg_host_wavefront):
+        f.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                      ctypes.c_int]
+        f.restype = ctypes.c_int
+    L.blg_host_store.argtypes = [ctypes.c_int, ctypes.c_int]
+    return L
+
+
+def _one(a, b, k):
+    return int(oracle.pairs(oracle.pack([a]), oracle.pack([b]), None if k < 0 else k)[0])
+
+
+def test_hostcheck_edge_cases(hostcheck, known):
+    for c in known["exact"]:
+        a, b = c["a"].encode("latin-1"), c["b"].encode("latin-1")
+        for trim in (0, 1):
+            for f in (hostcheck.blg_host_distance, hostcheck.blg_host_wavefront):
+                assert f(a, len(a), b, len(b), trim, -1) == c["d"]
+                assert f(b, len(b), a, len(a), trim, -1) == c["d"]
+
+
+@pytest.mark.parametrize("k", [-1, 0, 1, 2, 5, 8, 17, 100])
+def test_hostcheck_random_threshold(hostcheck, k):
+    rng = random.Random(1000 + k)
+    for _ in range(300):
+        m = rng.randrange(0, 700)
+        a = bytes(rng.choice(b"ACGT\x00") for _ in range(m))
+        b = bytearray(a)
+        for _ in range(rng.randrange(0, 25)):
+            i = rng.randrange(len(b) + 1)
+            op = rng.randrange(3)
+            if op == 0 and i < len(b): b[i] = rng.choice(b"ACGT")
+            elif op == 1: b.insert(i, rng.choice(b"ACGT"))
+            elif i < len(b): del b[i]
+        b = bytes(b)
+        want = _one(a, b, k)
+        for trim in (0, 1):
+            assert hostcheck.blg_host_distance(a, len(a), b, len(b), trim, k) == want
+            assert hostcheck.blg_host_wavefront(a, len(a), b, len(b), trim, k) == want
+
+
+@pytest.mark.parametrize("m", [1, 63, 64, 65, 127, 128, 129, 255, 256, 257, 511, 512, 513, 1000, 2048])
+def test_hostcheck_word_boundaries(hostcheck, m):
+    rng = random.Random(m)
+    for _ in range(6):
+        a = bytes(rng.randrange(256) for _ in range(m))
+        b = bytes(rng.randrange(256) for _ in range(rng.randrange(max(0, m - 30), m + 30)))
+        want = _one(a, b, -1)
+        assert hostcheck.blg_host_distance(a, len(a), b, len(b), 1, -1) == want
+        assert hostcheck.blg_host_wavefront(a, len(a), b, len(b), 0, -1) == want
+
+
+def test_hostcheck_store_saturation(hostcheck, known):
+    s = known["saturation"]["store8"]
+    assert [hostcheck.blg_host_store(d, 2) for d in s["in"]] == s["out"]
+    assert [hostcheck.blg_host_store(d, 1) for d in (0, 65535, 65536, 10 ** 6)] == [0, 65535, 65535, 65535]
+    assert hostcheck.blg_host_store(70000, 0) == 70000
+
+
+# ---- workloads ----------------------------------------------------------------
+def test_workloads_deterministic_and_shaped():
+    a1, a2 = W.config1(n=2000), W.config1(n=2000)
+    np.testing.assert_array_equal(a1.b[0], a2.b[0])
+    assert (np.diff(a1.a[1]) == 32).all()
+    w2 = W.config2(nq=64, nc=1000)
+    assert w2.nq == 64 and w2.nc == 1000 and (np.diff(w2.q[1]) == 64).all()
+    w3 = W.config3(n=3000)
+    la = np.diff(w3.a[1])
+    assert la.min() >= 8 and la.max() <= 256
+    assert set(np.unique(w3.a[0][:w3.a[1][-1]]).tolist()) <= set(b"ACGTN")
+    w4 = W.config4(nq=16, nc=2000)
+    lq = np.diff(w4.q[1])
+    assert lq.min() >= 100 and lq.max() <= 256
+    probs = W.config5(n_problems=8, scale=0.01)
+    assert len(probs) == 8 and all(0 <= p.max_dist <= 8 for p in probs)
+
+
+def test_mutation_rate_bounds_distance():
+    """At rate r each position edits with probability r, and every edit costs at
+    most 1, so the distance never exceeds the number of edited positions."""
+    rng = np.random.default_rng(5)
+    a = W.random_strings(rng, np.full(3000, 50))
+    b0 = W.mutate(np.random.default_rng(9), a, 0.0)
+    np.testing.assert_array_equal(a[0][:a[1][-1]], b0[0][:b0[1][-1]])
+    b = W.mutate(rng, a, 0.1)
+    d = oracle.pairs(a, b)
+    assert 3 <= d.mean() <= 7                  # ~ 50 * 0.1 edits, some cancel
+
+
+def test_take_and_concat_roundtrip():
+    S = [b"ab", b"", b"xyz", b"q" * 300]
+    p = oracle.pack(S)
+    assert W.unpack(W.take(p, [3, 0, 1])) == [S[3], S[0], S[1]]
+    assert W.unpack(W.concat(p, W.take(p, [2]))) == S + [S[2]]
+
+
+# ---- DeviceArray bookkeeping (no device memory touched) ----------------------
+def test_device_array_shapes():
+    d = DeviceArray(0, (6,), np.uint8, ctx=None)
+    assert d.size == 6 and d.ndim == 1 and d.nbytes == 6 and len(d) == 6
+    r = d.reshape(2, 3)
+    assert r.shape == (2, 3) and r.reshape(-1).shape == (6,)
+    cai = r.__cuda_array_interface__
+    assert cai["shape"] == (2, 3) and cai["typestr"] == "|u1" and cai["version"] == 3
+    with pytest.raises(ValueError):
+        d.reshape(4, 2)
+    e = DeviceArray(0, (0, 5), np.int32, ctx=None)
+    assert e.size == 0 and e.reshape(5, 0).shape == (5, 0)
