@@ -100,7 +100,7 @@ class Clocks:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -321,15 +321,19 @@ def exit_columns(bench, sample_rows_or_n):
     return s * bench.w.n / n
 
 
-def make_bench(cfg: int):
+def make_bench(cfg: int, args=None):
+    """Benchmark configuration `cfg`; --nq/--nc/--n shrink it (profiling runs)."""
+    nq = getattr(args, "nq", None)
+    nc = getattr(args, "nc", None)
+    n = getattr(args, "n", None)
     if cfg == 1:
-        return PairsBench(W.config1())
+        return PairsBench(W.config1(n=n or (1 << 20)))
     if cfg == 2:
-        return SearchBench(W.config2(), [(None, "int32"), (2, "uint8")])
+        return SearchBench(W.config2(nq=nq or 4096, nc=nc or 65536), [(None, "int32"), (2, "uint8")])
     if cfg == 3:
-        return PairsBench(W.config3())
+        return PairsBench(W.config3(n=n or (1 << 22)))
     if cfg == 4:
-        return SearchBench(W.config4(), [(4, "uint8")])
+        return SearchBench(W.config4(nq=nq or 1024, nc=nc or (1 << 20)), [(4, "uint8")])
     raise SystemExit(f"unknown config {cfg}")
 
 
@@ -348,7 +352,7 @@ def read_traffic(kernel: str, workload: str):
 # ------------------------------------------------------------------ arms --
 def run_ours(args, ranks: Ranks):
     ctx = _lib.context()
-    bench = make_bench(args.config)
+    bench = make_bench(args.config, args)
     p = ctypes.c_void_p()
     ctx.check(ctx.lib.blg_malloc(ctx.h, L2_FLUSH_BYTES, ctypes.byref(p)))
     flush = gpu.DeviceArray(p.value, (L2_FLUSH_BYTES,), np.uint8, ctx)
@@ -368,9 +372,12 @@ def run_ours(args, ranks: Ranks):
             bench.step(i)
     gpu.synchronize()
 
-    ranks.barrier()
     clocks = Clocks(ranks.local)
     clocks.start()
+    for _ in range(20):                       # let the sampler start; keep the GPU busy meanwhile
+        bench.step(0)
+    gpu.synchronize()
+    ranks.barrier()
     launches0 = ctx.lib.blg_launch_count(ctx.h)
     wall0 = time.perf_counter()
     times = timed(0, args.steps)
@@ -515,12 +522,15 @@ def run_reference(args, ranks: Ranks):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", type=int, default=2)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of oracle work per leg")
+    ap.add_argument("--nq", type=int, default=None, help="override the query count (profiling)")
+    ap.add_argument("--nc", type=int, default=None, help="override the choice count (profiling)")
+    ap.add_argument("--n", type=int, default=None, help="override the pair count (profiling)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -312,6 +312,8 @@ static int pick_qpb(blg_ctx *c, int nq_cls, int64_t nc) {
     int64_t qpb = (int64_t)nq_cls * tiles / target;
     if (qpb < 1) qpb = 1;
     if (qpb > 16) qpb = 16;
+    const int64_t min_qpb = ((int64_t)nq_cls + 65534) / 65535;   // grid.y limit
+    if (qpb < min_qpb) qpb = min_qpb;
     return (int)qpb;
 }
 

@@ -264,26 +264,28 @@ template <bool HASK>
 __global__ void __launch_bounds__(256) k_search_lanes(DevStrings C, SearchClass cls, int nwc, int L,
                                                       int k, int dtype, void *out, uint32_t *status) {
     extern __shared__ uint64_t s_peq[];
-    const int qi = blockIdx.y;
     const int words = 256 * nwc;
-    const uint64_t *src = cls.peq + (size_t)qi * words;
-    for (int x = threadIdx.x; x < words; x += blockDim.x) s_peq[x] = __ldg(src + x);
-    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int G = 32 / L, g = lane / L, w = lane & (L - 1);
     const int64_t c = ((int64_t)blockIdx.x * (blockDim.x >> 5) + warp) * G + g;
     const bool valid = c < C.n;
     int n = 0;
     const uint8_t *t = valid ? string_at(C, c, n, status) : C.buf;
-    const int m = cls.qlen[qi];
-    const int64_t row = cls.qidx[qi];
-    // gap exit and empty texts need no wavefront
-    bool quick = valid && HASK && (n > m ? n - m : m - n) > k;
-    bool is_last = false;
-    const int d = lane_wavefront<HASK>(valid && !quick, m, t, n, L, w, g, k,
-                                       [&](uint32_t ch) { return s_peq[ch * nwc + w]; }, is_last);
-    if (quick && w == 0) store1(out, dtype, row * C.n + c, k + 1);
-    else if (is_last) store1(out, dtype, row * C.n + c, d);
+    for (int qi = blockIdx.y; qi < cls.nq; qi += gridDim.y) {
+        __syncthreads();
+        const uint64_t *src = cls.peq + (size_t)qi * words;
+        for (int x = threadIdx.x; x < words; x += blockDim.x) s_peq[x] = __ldg(src + x);
+        __syncthreads();
+        const int m = cls.qlen[qi];
+        const int64_t row = cls.qidx[qi];
+        // a length gap beyond k needs no wavefront
+        const bool quick = valid && HASK && (n > m ? n - m : m - n) > k;
+        bool is_last = false;
+        const int d = lane_wavefront<HASK>(valid && !quick, m, t, n, L, w, g, k,
+                                           [&](uint32_t ch) { return s_peq[ch * nwc + w]; }, is_last);
+        if (quick && w == 0) store1(out, dtype, row * C.n + c, k + 1);
+        else if (is_last) store1(out, dtype, row * C.n + c, d);
+    }
 }
 
 // ------------------------------------------------------------ pairs: main --
@@ -523,7 +525,7 @@ cudaError_t launch_search_lanes(cudaStream_t st, bool hask, const DevStrings &C,
     while (L < nwc) L <<= 1;
     if (L > 32) return cudaErrorInvalidValue;
     const int per_cta = 8 * (32 / L);
-    dim3 grid((unsigned)((C.n + per_cta - 1) / per_cta), (unsigned)cls.nq);
+    dim3 grid((unsigned)((C.n + per_cta - 1) / per_cta), (unsigned)min(cls.nq, 65535));
     const size_t smem = (size_t)256 * nwc * sizeof(uint64_t);
     if (hask) {
         cudaFuncSetAttribute(k_search_lanes<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
