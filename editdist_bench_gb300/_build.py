@@ -23,7 +23,7 @@ HOSTCHECK = os.path.join(HERE, "libblg_hostcheck.so")
 PROBE = os.path.join(HERE, "libblg_probe.so")
 
 CU_SOURCES = ["blg_api.cu", "blg_kernels.cu"]
-HEADERS = ["blg_device.cuh", "blg_internal.h"]
+HEADERS = ["blg_device.cuh", "blg_internal.h", "blg_kernels.cuh", "blg_context.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/bitlev_gb300.h"
+#include "blg_context.h"
 #include "blg_device.cuh"
 #include "blg_internal.h"
 
@@ -42,11 +43,6 @@ namespace {
 constexpr int kSeqMaxWords = 8;          // queries up to 512: sequential words per thread
 constexpr int kLaneMaxWords = 32;        // queries up to 2048: lane-spread
 
-struct ProfRec {
-    const char *name;
-    cudaEvent_t e0, e1;
-};
-
 struct OwnedStrings {
     DevStrings d;
     void *mem_buf = nullptr;   // allocation (d.buf - 16)
@@ -55,19 +51,6 @@ struct OwnedStrings {
 
 }  // namespace
 
-struct blg_ctx {
-    int device = 0;
-    int sms = 0;
-    cudaStream_t stream = nullptr;
-    uint32_t *d_status = nullptr;
-    cudaEvent_t t0 = nullptr, t1 = nullptr;
-    std::mutex mu;
-    std::string err;
-    int64_t launches = 0;
-    bool prof = false;
-    std::vector<ProfRec> prof_recs;
-    std::map<std::string, std::pair<int64_t, double>> prof_acc;
-};
 
 struct blg_pairs {
     OwnedStrings a, b;
@@ -91,12 +74,12 @@ struct blg_search {
 };
 
 // ------------------------------------------------------------ helpers --
-static int fail(blg_ctx *c, int code, const std::string &msg) {
+int fail(blg_ctx *c, int code, const std::string &msg) {
     if (c) c->err = msg;
     return code;
 }
 
-static int cuda_fail(blg_ctx *c, cudaError_t e, const char *what) {
+int cuda_fail(blg_ctx *c, cudaError_t e, const char *what) {
     if (e == cudaErrorMemoryAllocation)
         return fail(c, BLG_ERR_ALLOC, std::string(what) + ": " + cudaGetErrorString(e));
     return fail(c, BLG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -110,7 +93,7 @@ static int cuda_fail(blg_ctx *c, cudaError_t e, const char *what) {
 
 template <typename F>
 static cudaError_t launch(blg_ctx *c, const char *name, F &&fn) {
-    ProfRec r{name, nullptr, nullptr};
+    blg_ctx::ProfRec r{name, nullptr, nullptr};
     if (c->prof) {
         cudaEventCreate(&r.e0);
         cudaEventCreate(&r.e1);
@@ -183,7 +166,7 @@ static int status_to_rc(blg_ctx *c, uint32_t st) {
     return fail(c, BLG_ERR_CUDA, "device status " + std::to_string(st));
 }
 
-static int sync_and_status(blg_ctx *c) {
+int sync_and_status(blg_ctx *c) {
     uint32_t st = 0;
     CK(cudaMemcpyAsync(&st, c->d_status, sizeof(st), cudaMemcpyDeviceToHost, c->stream), "D2H status");
     CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");

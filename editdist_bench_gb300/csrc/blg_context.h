@@ -1,0 +1,33 @@
+// The library context shared by the host translation units of the C-ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+struct blg_ctx {
+    struct ProfRec {
+        const char *name;
+        cudaEvent_t e0, e1;
+    };
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t *d_status = nullptr;      // status bits raised by kernels (blg::ST_*)
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    std::mutex mu;                     // serialises calls on one context
+    std::string err;
+    int64_t launches = 0;
+    bool prof = false;
+    std::vector<ProfRec> prof_recs;
+    std::map<std::string, std::pair<int64_t, double>> prof_acc;
+};
+
+// Record an error message and return `code`.
+int fail(blg_ctx *c, int code, const std::string &msg);
+// Map a CUDA error to BLG_ERR_ALLOC / BLG_ERR_CUDA with a message.
+int cuda_fail(blg_ctx *c, cudaError_t e, const char *what);
+// Synchronise the context stream, read and clear the kernels' status word.
+int sync_and_status(blg_ctx *c);

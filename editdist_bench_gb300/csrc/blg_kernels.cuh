@@ -1,0 +1,313 @@
+// Device-side building blocks shared by the kernel translation units:
+// string access, stores, the per-query Peq column loop (search), the
+// lane-spread wavefront and the pair-solving helpers (trimming, per-lane
+// nibble Peq tables). Device code only; the host-testable primitives live in
+// blg_device.cuh.
+#pragma once
+#include "blg_device.cuh"
+#include "blg_internal.h"
+
+namespace blg {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------- loads --
+// Four bytes starting at an arbitrary address: two aligned 32-bit loads and
+// a funnel shift. Callers keep 16 bytes of slack around every string buffer
+// so the aligned words never leave the allocation.
+__device__ __forceinline__ uint32_t load4(const uint8_t *p) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~uintptr_t(3));
+    return __funnelshift_r(__ldg(w), __ldg(w + 1), (uint32_t)(a & 3) * 8u);
+}
+
+// Sequential reader: 4 characters per call, one aligned load per call.
+struct TextScan {
+    const uint32_t *w;
+    uint32_t lo, sh;
+    __device__ __forceinline__ void init(const uint8_t *p) {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+        w = reinterpret_cast<const uint32_t *>(a & ~uintptr_t(3));
+        sh = (uint32_t)(a & 3) * 8u;
+        lo = __ldg(w);
+    }
+    __device__ __forceinline__ uint32_t next4() {
+        const uint32_t hi = __ldg(++w);
+        const uint32_t r = __funnelshift_r(lo, hi, sh);
+        lo = hi;
+        return r;
+    }
+};
+
+// Validated string view; a corrupt offset pair raises ST_BAD_OFFSETS and
+// yields an empty string instead of an out-of-range read.
+__device__ __forceinline__ const uint8_t *string_at(const DevStrings &S, int64_t i, int &len,
+                                                    uint32_t *status) {
+    const int64_t o0 = S.off[i], o1 = S.off[i + 1];
+    if (o0 < S.base || o1 < o0 || o1 - S.base > S.bytes || o1 - o0 > 0x7fffffff) {
+        atomicOr(status, ST_BAD_OFFSETS);
+        len = 0;
+        return S.buf;
+    }
+    len = (int)(o1 - o0);
+    return S.buf + (o0 - S.base);
+}
+
+// --------------------------------------------------------------- stores --
+__device__ __forceinline__ void store1(void *out, int dtype, int64_t i, int d) {
+    if (dtype == DT_UINT8) reinterpret_cast<uint8_t *>(out)[i] = (uint8_t)saturate_u8(d);
+    else if (dtype == DT_UINT16) reinterpret_cast<uint16_t *>(out)[i] = (uint16_t)saturate_u16(d);
+    else reinterpret_cast<int32_t *>(out)[i] = d;
+}
+
+// cnt (1..4) consecutive results from element i; one vector store when the
+// four land on an aligned group (uint8: 4 B, uint16: 8 B, int32: 16 B).
+__device__ __forceinline__ void store4(void *out, int dtype, int64_t i, int cnt, int d0, int d1,
+                                       int d2, int d3) {
+    if (cnt == 4 && (i & 3) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
+        if (dtype == DT_UINT8) {
+            const uint32_t v = saturate_u8(d0) | (saturate_u8(d1) << 8) | (saturate_u8(d2) << 16) |
+                               (saturate_u8(d3) << 24);
+            reinterpret_cast<uint32_t *>(out)[i >> 2] = v;
+        } else if (dtype == DT_UINT16) {
+            uint2 v;
+            v.x = saturate_u16(d0) | (saturate_u16(d1) << 16);
+            v.y = saturate_u16(d2) | (saturate_u16(d3) << 16);
+            reinterpret_cast<uint2 *>(out)[i >> 2] = v;
+        } else {
+            reinterpret_cast<int4 *>(out)[i >> 2] = make_int4(d0, d1, d2, d3);
+        }
+        return;
+    }
+    store1(out, dtype, i, d0);
+    if (cnt > 1) store1(out, dtype, i + 1, d1);
+    if (cnt > 2) store1(out, dtype, i + 2, d2);
+    if (cnt > 3) store1(out, dtype, i + 3, d3);
+}
+
+// --------------------------------------------------- search, NW <= 8 words --
+// One text column through NW pattern words (word 0 takes the +1 top-row carry).
+template <int NW, bool TOP63>
+__device__ __forceinline__ void column_seq(uint64_t (&pv)[NW], uint64_t (&mv)[NW],
+                                           const uint64_t *row, int lastbit, int &score) {
+    uint64_t ph, mh;
+    step_top<uint64_t>(pv[0], mv[0], row[0], ph, mh);
+    if (NW == 1) {
+        score += TOP63 ? hdelta<uint64_t>(ph, mh, 63) : hdelta<uint64_t>(ph, mh, lastbit);
+        return;
+    }
+    int h = hdelta<uint64_t>(ph, mh, 63);
+#pragma unroll
+    for (int w = 1; w < NW - 1; w++) {
+        step_mid<uint64_t>(pv[w], mv[w], row[w], h, ph, mh);
+        h = hdelta<uint64_t>(ph, mh, 63);
+    }
+    step_mid<uint64_t>(pv[NW - 1], mv[NW - 1], row[NW - 1], h, ph, mh);
+    score += TOP63 ? hdelta<uint64_t>(ph, mh, 63) : hdelta<uint64_t>(ph, mh, lastbit);
+}
+
+// d(query, t) with the query's Peq table in shared memory (NW = ceil(m/64)).
+template <int NW, bool HASK, bool TOP63>
+__device__ __forceinline__ int dist_seq(const uint64_t *peq, int m, const uint8_t *t, int n, int k) {
+    if (m == 0) return cap_k(n, k);                    // csrc/gpu_kernels.cu:53
+    if (HASK && (n > m ? n - m : m - n) > k) return k + 1;
+    uint64_t pv[NW], mv[NW];
+#pragma unroll
+    for (int w = 0; w < NW; w++) { pv[w] = ~0ull; mv[w] = 0; }
+    const int lastbit = (m - 1) & 63;
+    int score = m;
+    TextScan ts;
+    ts.init(t);
+    int j = 0;
+    for (; j + 4 <= n; j += 4) {
+        const uint32_t w4 = ts.next4();
+#pragma unroll
+        for (int b = 0; b < 4; b++)
+            column_seq<NW, TOP63>(pv, mv, peq + ((w4 >> (8 * b)) & 0xffu) * NW, lastbit, score);
+        // the exit test is monotone in j, so testing every 4th column is exact
+        if (HASK && hopeless(score, j + 3, n, k)) return k + 1;
+    }
+    if (j < n) {
+        uint32_t w4 = ts.next4();
+        for (; j < n; j++, w4 >>= 8) column_seq<NW, TOP63>(pv, mv, peq + (w4 & 0xffu) * NW, lastbit, score);
+    }
+    return HASK ? cap_k(score, k) : score;
+}
+
+template <int NW, bool HASK>
+__device__ __forceinline__ int dist_seq_any(const uint64_t *peq, int m, const uint8_t *t, int n, int k) {
+    // the last pattern bit is bit 63 for full words: cheaper score extraction
+    if (((m - 1) & 63) == 63) return dist_seq<NW, HASK, true>(peq, m, t, n, k);
+    return dist_seq<NW, HASK, false>(peq, m, t, n, k);
+}
+
+// ------------------------------------------------ lane-spread core (L lanes) --
+// One pair per group of L lanes; lane w owns pattern word w and processes
+// text column j = s - w at wavefront step s. The horizontal delta leaving a
+// word's bottom row is the only coupling between words (csrc/myers.c:24-27):
+// it reaches lane w+1 one step later through __shfl_up_sync. The lane of
+// the last word keeps the score and decides the max_dist exit, which the
+// group learns through __ballot_sync.
+template <bool HASK, typename EqFn>
+__device__ __forceinline__ int lane_wavefront(bool valid, int m, const uint8_t *txt, int n, int L,
+                                              int w, int g, int k, EqFn eqfn, bool &is_last) {
+    const int W = valid ? (m + 63) >> 6 : 0;
+    const bool own = valid && w < W;
+    const int lastw = W - 1;
+    is_last = valid && w == lastw;
+    const int ob = is_last ? ((m - 1) & 63) : 63;
+    uint64_t pv = ~0ull, mv = 0;
+    int score = m;
+    const int steps = valid ? n + W - 1 : 0;
+    const int maxsteps = __reduce_max_sync(kFull, steps);
+    int hrecv = 0;
+    bool done = false;
+    TextScan ts;
+    uint32_t win = 0;
+    if (own) ts.init(txt);
+    for (int s = 0; s < maxsteps; s++) {
+        const int j = s - w;
+        const bool act = own && !done && j >= 0 && j < n;
+        int hout = 0;
+        if (act) {
+            if ((j & 3) == 0) win = ts.next4();
+            const uint32_t c = (win >> (8 * (j & 3))) & 0xffu;
+            uint64_t ph, mh;
+            step_mid<uint64_t>(pv, mv, eqfn(c), w == 0 ? 1 : hrecv, ph, mh);
+            hout = hdelta<uint64_t>(ph, mh, ob);
+            if (is_last) score += hout;
+        }
+        hrecv = __shfl_up_sync(kFull, hout, 1, L);
+        if (HASK) {
+            const bool ex = act && is_last && hopeless(score, j, n, k);
+            const unsigned bal = __ballot_sync(kFull, ex);
+            if (valid && ((bal >> (g * L + lastw)) & 1u)) done = true;
+        }
+    }
+    if (done) return k + 1;
+    return HASK ? cap_k(score, k) : score;
+}
+
+// ------------------------------------------------------------ pairs: main --
+// Trim the common prefix and suffix with 4-byte window compares (exact:
+// d(xPy, xQy) = d(P, Q), csrc/myers.c:80-87).
+__device__ __forceinline__ void trim_windows(const uint8_t *&a, int &la, const uint8_t *&b, int &lb) {
+    const int lim = la < lb ? la : lb;
+    int p = 0;
+    while (p < lim) {
+        const uint32_t x = load4(a + p) ^ load4(b + p);
+        int q = x ? (__ffs(x) - 1) >> 3 : 4;               // equal leading bytes
+        if (q > lim - p) q = lim - p;
+        p += q;
+        if (q < 4) break;
+    }
+    const int lim2 = lim - p;
+    int s = 0;
+    while (s < lim2) {
+        const uint32_t x = load4(a + la - s - 4) ^ load4(b + lb - s - 4);
+        int q = x ? __clz(x) >> 3 : 4;                     // equal trailing bytes
+        if (q > lim2 - s) q = lim2 - s;
+        s += q;
+        if (q < 4) break;
+    }
+    a += p; b += p;
+    la -= p + s; lb -= p + s;
+}
+
+// Per-lane nibble Peq tables: rows 0..15 hold the positions whose high
+// nibble is r, rows 16..31 those whose low nibble is r; Eq(c) is the AND of
+// the two rows. Layout [row][lane] (stride 32 words) keeps every access
+// bank-conflict free. `tc` points at this lane's column.
+__device__ __forceinline__ uint64_t nib_eq(const uint64_t *tc, uint32_t c) {
+    return tc[(c >> 4) * 32] & tc[(16 + (c & 15)) * 32];
+}
+
+__device__ __forceinline__ void nib_build(uint64_t *tc, const uint8_t *p, int m) {
+    TextScan ps;
+    ps.init(p);
+    for (int i = 0; i < m; i += 4) {
+        const uint32_t w4 = ps.next4();
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            if (i + b < m) {
+                const uint32_t c = (w4 >> (8 * b)) & 0xffu;
+                const uint64_t bit = 1ull << (i + b);
+                tc[(c >> 4) * 32] |= bit;
+                tc[(16 + (c & 15)) * 32] |= bit;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void nib_clear(uint64_t *tc, const uint8_t *p, int m) {
+    TextScan ps;
+    ps.init(p);
+    for (int i = 0; i < m; i += 4) {
+        const uint32_t w4 = ps.next4();
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            if (i + b < m) {
+                const uint32_t c = (w4 >> (8 * b)) & 0xffu;
+                tc[(c >> 4) * 32] = 0;
+                tc[(16 + (c & 15)) * 32] = 0;
+            }
+        }
+    }
+}
+
+// Single-word pair (1 <= m <= 64, m <= n): pattern p, text t.
+template <bool HASK>
+__device__ __forceinline__ int solve_word(uint64_t *tc, const uint8_t *p, int m, const uint8_t *t,
+                                          int n, int k) {
+    nib_build(tc, p, m);
+    uint64_t pv = ~0ull, mv = 0;
+    const int lastbit = m - 1;
+    int score = m;
+    bool dead = false;
+    TextScan ts;
+    ts.init(t);
+    int j = 0;
+    for (; j + 4 <= n; j += 4) {
+        const uint32_t w4 = ts.next4();
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            uint64_t ph, mh;
+            step_top<uint64_t>(pv, mv, nib_eq(tc, (w4 >> (8 * b)) & 0xffu), ph, mh);
+            score += hdelta<uint64_t>(ph, mh, lastbit);
+        }
+        if (HASK && hopeless(score, j + 3, n, k)) { dead = true; break; }
+    }
+    if (!dead && j < n) {
+        uint32_t w4 = ts.next4();
+        for (; j < n; j++, w4 >>= 8) {
+            uint64_t ph, mh;
+            step_top<uint64_t>(pv, mv, nib_eq(tc, w4 & 0xffu), ph, mh);
+            score += hdelta<uint64_t>(ph, mh, lastbit);
+        }
+    }
+    nib_clear(tc, p, m);
+    if (dead) return k + 1;
+    return HASK ? cap_k(score, k) : score;
+}
+
+__device__ __forceinline__ int long_class(int m) {
+    const int W = (m + 63) >> 6;
+    return W <= 2 ? 0 : W <= 4 ? 1 : W <= 8 ? 2 : W <= 16 ? 3 : W <= 32 ? 4 : -1;
+}
+
+// Build the Peq table of one query into shared memory `tab` (256 x nwc
+// words) and copy it to `dst`: one block, shared-memory atomics.
+__device__ __forceinline__ void build_peq_block(const uint8_t *p, int m, int nwc, uint64_t *tab,
+                                                uint64_t *dst) {
+    const int words = 256 * nwc;
+    for (int x = threadIdx.x; x < words; x += blockDim.x) tab[x] = 0;
+    __syncthreads();
+    if (m > 64 * nwc) m = 64 * nwc;   // callers guarantee m <= 64*nwc; keep the write in range
+    for (int i = threadIdx.x; i < m; i += blockDim.x)
+        atomicOr(reinterpret_cast<unsigned long long *>(&tab[(int)p[i] * nwc + (i >> 6)]),
+                 1ull << (i & 63));
+    __syncthreads();
+    for (int x = threadIdx.x; x < words; x += blockDim.x) dst[x] = tab[x];
+}
+
+}  // namespace blg
