@@ -34,6 +34,7 @@ SIGNATURES = [
     ("blg_search_upload", ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _I64, ctypes.POINTER(_P)]),
     ("blg_search_run", ctypes.c_int, [_P, _P, _I32, _I32, _P]),
     ("blg_search_free", None, [_P, _P]),
+    ("blg_cdist_noalloc", ctypes.c_int, [_P, _P, _SZ, _P, _I64, _P, _SZ, _P, _I64, _I32, _I32, _P]),
     ("blg_malloc", ctypes.c_int, [_P, _SZ, ctypes.POINTER(_P)]),
     ("blg_free", ctypes.c_int, [_P, _P]),
     ("blg_memcpy_h2d", ctypes.c_int, [_P, _P, _P, _SZ]),

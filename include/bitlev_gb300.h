@@ -92,6 +92,24 @@ int blg_search_upload(blg_ctx *ctx, const uint8_t *buf_q, const int64_t *off_q, 
 int blg_search_run(blg_ctx *ctx, blg_search *s, int32_t max_dist, int32_t dtype, void *d_out);
 void blg_search_free(blg_ctx *ctx, blg_search *s);
 
+/* cdist with every buffer already in device memory and NO device allocation:
+ * no counterpart in the reference (bitlev.gpu always allocates through CuPy).
+ * For callers that cannot call cudaMalloc — plugins of an engine that owns
+ * the GPU's memory, or request paths that must not block on or fail in an
+ * allocation. The only scratch (per-query Peq tables) is a fixed 2 MiB
+ * array inside the library, per device, for the life of the process.
+ * Limits: every query at most 256 bytes (longer -> BLG_ERR_ARG after the
+ * call; that row is not written); buffers 16-byte aligned; offsets relative
+ * to each buffer's start; q_bytes/c_bytes are the readable sizes of the byte
+ * buffers and must leave 16 bytes after the last string. The first call on a
+ * device looks up the scratch address (do it before any stream capture).
+ * All calls share the scratch: calls whose work overlaps on the GPU (other
+ * contexts or threads on the same device) race; calls on one context are
+ * ordered. Returns after the results are complete (synchronises). */
+int blg_cdist_noalloc(blg_ctx *ctx, const uint8_t *d_buf_q, size_t q_bytes, const int64_t *d_off_q,
+                      int64_t nq, const uint8_t *d_buf_c, size_t c_bytes, const int64_t *d_off_c,
+                      int64_t nc, int32_t max_dist, int32_t dtype, void *d_out);
+
 /* Device memory and stream helpers (the parts of CuPy bitlev.gpu used:
  * cp.empty / .get() / Device().synchronize(), bitlev/gpu.py:59-68,102). */
 int blg_malloc(blg_ctx *ctx, size_t bytes, void **d_ptr);

@@ -1,0 +1,96 @@
+"""blg_cdist_noalloc: the cdist entry point for callers that cannot allocate
+device memory (an engine that owns the GPU's memory and forbids its plugins
+to call cudaMalloc, or a request path that must not block on or fail in an
+allocation). The test owns the device buffers, as such a caller would, and
+checks the results against the allocating entry point (blg_cdist) bit for
+bit on two calls in a row — the second call reuses the fixed scratch that
+the first one left behind. Kept in its own file, collected last."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from editdist_bench_gb300 import _lib, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+_DT = {"int32": 0, "uint16": 1, "uint8": 2}
+
+
+class DevBuf:
+    """A device buffer the caller owns (allocated through the library's helper)."""
+
+    def __init__(self, ctx, host: np.ndarray, extra: int = 0):
+        self.ctx = ctx
+        self.nbytes = host.nbytes + extra
+        p = ctypes.c_void_p()
+        ctx.check(ctx.lib.blg_malloc(ctx.h, max(16, self.nbytes), ctypes.byref(p)))
+        self.ptr = p.value
+        ctx.check(ctx.lib.blg_memset(ctx.h, self.ptr, 0, max(16, self.nbytes)))
+        if host.nbytes:
+            ctx.check(ctx.lib.blg_memcpy_h2d(ctx.h, self.ptr, host.ctypes.data, host.nbytes))
+
+    def free(self):
+        self.ctx.check(self.ctx.lib.blg_free(self.ctx.h, self.ptr))
+
+
+def _noalloc(ctx, pq, pc, k, dt):
+    (bq, oq), (bc, oc) = pq, pc
+    nq, nc = len(oq) - 1, len(oc) - 1
+    bufs = [DevBuf(ctx, np.ascontiguousarray(bq[:oq[-1]]), 16), DevBuf(ctx, oq),
+            DevBuf(ctx, np.ascontiguousarray(bc[:oc[-1]]), 16), DevBuf(ctx, oc),
+            DevBuf(ctx, np.zeros(nq * nc, dtype=dt))]
+    q, qo, c, co, out = bufs
+    rc = ctx.lib.blg_cdist_noalloc(ctx.h, q.ptr, q.nbytes, qo.ptr, nq, c.ptr, c.nbytes, co.ptr, nc,
+                                   -1 if k is None else k, _DT[dt], out.ptr)
+    msg = ctx.lib.blg_last_error(ctx.h)          # read before the next call clears it
+    got = np.empty((nq, nc), dtype=dt)
+    if rc == 0:
+        ctx.check(ctx.lib.blg_memcpy_d2h(ctx.h, got.ctypes.data, out.ptr, got.nbytes))
+    for b in bufs:
+        b.free()
+    return rc, got, msg
+
+
+def _alloc_entry(ctx, pq, pc, k, dt):
+    (bq, oq), (bc, oc) = pq, pc
+    nq, nc = len(oq) - 1, len(oc) - 1
+    out = np.empty((nq, nc), dtype=dt)
+    ctx.check(ctx.lib.blg_cdist(ctx.h, bq.ctypes.data, oq.ctypes.data, nq, bc.ctypes.data,
+                                oc.ctypes.data, nc, -1 if k is None else k, _DT[dt],
+                                out.ctypes.data, None))
+    return out
+
+
+def test_noalloc_matches_allocating_entry_point_twice(gpu):
+    ctx = _lib.context()
+    rng = np.random.default_rng(2026)
+    # call 1: 300 queries of every length 0..256 (more than one 256-query chunk)
+    q1 = W.random_strings(rng, rng.integers(0, 257, 300))
+    c1 = W.concat(W.mutate(rng, W.take(q1, rng.integers(0, 300, 200)), 0.05),
+                  W.random_strings(rng, rng.integers(0, 300, 900)))
+    # call 2: fewer, shorter queries, thresholded, narrow output
+    q2 = W.random_strings(rng, rng.integers(0, 70, 37))
+    c2 = W.concat(W.mutate(rng, q2, 0.1), W.random_strings(rng, rng.integers(0, 90, 500)))
+    for pq, pc, k, dt in ((q1, c1, None, "int32"), (q2, c2, 3, "uint8")):
+        rc, got, msg = _noalloc(ctx, pq, pc, k, dt)
+        assert rc == 0, msg
+        want = _alloc_entry(ctx, pq, pc, k, dt)
+        np.testing.assert_array_equal(got, want)
+    # and both against the oracle on the second call
+    np.testing.assert_array_equal(got, oracle.saturate(oracle.cross(q2, c2, 3), "uint8"))
+
+
+def test_noalloc_rejects_queries_beyond_its_scratch(gpu):
+    ctx = _lib.context()
+    rng = np.random.default_rng(5)
+    q = W.random_strings(rng, [10, 257, 40])
+    c = W.random_strings(rng, rng.integers(0, 80, 64))
+    rc, _, msg = _noalloc(ctx, q, c, None, "int32")
+    assert rc == _lib.ERR_ARG
+    assert b"256 bytes" in msg
+    # the context and the scratch stay usable
+    rc, got, msg = _noalloc(ctx, W.take(q, [0, 2]), c, 2, "uint16")
+    assert rc == 0, msg
+    np.testing.assert_array_equal(got, _alloc_entry(ctx, W.take(q, [0, 2]), c, 2, "uint16"))
