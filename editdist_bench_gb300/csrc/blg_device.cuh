@@ -76,6 +76,89 @@ BLG_HD int hdelta(W ph, W mh, int b) {
 // column, so score - (n - 1 - j) > k already proves d > k.
 BLG_HD bool hopeless(int score, int j, int n, int k) { return k >= 0 && score - (n - 1 - j) > k; }
 
+// ---- pipe-balanced step on 32-bit halves --------------------------------
+// A 64-bit Myers step is ~25 32-bit instructions; written plainly they all
+// land on the ALU pipe, which then limits throughput while the FMA pipe
+// (IMAD) idles. The forms below move the 64-bit add, the low-half shifts
+// and the score bits onto IMAD, keeping only the genuinely bitwise work on
+// the ALU. Multipliers come from run-time values (`Units`, loaded from a
+// kernel parameter) so the compiler cannot turn the multiply-adds back into
+// shifts. On the host the same functions are plain integer arithmetic.
+struct Units {
+    uint32_t one, two;
+};
+
+BLG_HD uint32_t imad_lo(uint32_t a, uint32_t b, uint32_t c) {
+#if defined(__CUDA_ARCH__)
+    uint32_t r;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+    return r;
+#else
+    return a * b + c;
+#endif
+}
+
+// high 32 bits of a*b, plus c
+BLG_HD uint32_t imad_hi(uint32_t a, uint32_t b, uint32_t c) {
+#if defined(__CUDA_ARCH__)
+    uint32_t r;
+    asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+    return r;
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32) + c;
+#endif
+}
+
+BLG_HD uint64_t imad_wide(uint32_t a, uint32_t b, uint64_t c) {
+#if defined(__CUDA_ARCH__)
+    uint64_t r;
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(r) : "r"(a), "r"(b), "l"(c));
+    return r;
+#else
+    return (uint64_t)a * b + c;
+#endif
+}
+
+// (hi:lo) << 1, high half
+BLG_HD uint32_t shl1_hi(uint32_t lo, uint32_t hi) {
+#if defined(__CUDA_ARCH__)
+    return __funnelshift_l(lo, hi, 1);
+#else
+    return (hi << 1) | (lo >> 31);
+#endif
+}
+
+// A pattern word as halves plus its vertical-delta state.
+struct Word2 {
+    uint32_t pl, ph, ml, mh;   // Pv, Mv
+};
+
+// One column on one word. cin_p / cin_m are the +1 / -1 carry-in bits
+// (top word: cin_p = 1, cin_m = 0). Returns the pre-shift Ph/Mh halves so
+// the caller reads the horizontal delta at its output bit.
+BLG_HD void step_h(Word2 &s, uint32_t el, uint32_t eh, uint32_t cin_p, uint32_t cin_m, Units u,
+                   uint32_t &Phl, uint32_t &Phh, uint32_t &Mhl, uint32_t &Mhh) {
+    const uint32_t vl = el | s.ml, vh = eh | s.mh;            // Xv = Eq | Mv
+    const uint32_t el2 = el | cin_m;                           // a -1 carry acts as a match
+    // sum = (Eq & Pv) + Pv as one 64-bit IMAD.WIDE plus one IMAD for the high half
+    const uint64_t w = imad_wide(el2 & s.pl, u.one, ((uint64_t)s.ph << 32) | s.pl);
+    const uint32_t sl = (uint32_t)w, sh = imad_lo(eh & s.ph, u.one, (uint32_t)(w >> 32));
+    const uint32_t xl = (sl ^ s.pl) | el2, xh = (sh ^ s.ph) | eh;   // Xh
+    Phl = s.ml | ~(xl | s.pl);
+    Phh = s.mh | ~(xh | s.ph);
+    Mhl = s.pl & xl;
+    Mhh = s.ph & xh;
+    const uint32_t psl = imad_lo(Phl, u.two, cin_p), psh = shl1_hi(Phl, Phh);   // Ph << 1 | cin_p
+    const uint32_t msl = imad_lo(Mhl, u.two, cin_m), msh = shl1_hi(Mhl, Mhh);   // Mh << 1 | cin_m
+    s.pl = msl | ~(vl | psl);
+    s.ph = msh | ~(vh | psh);
+    s.ml = psl & vl;
+    s.mh = psh & vh;
+}
+
+// Bit 31 of x as 0/1, on the FMA pipe: hi32(x * 2).
+BLG_HD uint32_t top_bit(uint32_t x, Units u) { return imad_hi(x, u.two, 0); }
+
 // ---- host-side reference of the per-pair device logic ------------------
 // pair_distance_plain: trimming + pattern = shorter string + gap exit +
 // single/multi-word run with per-character Eq from a 256-row table.  The

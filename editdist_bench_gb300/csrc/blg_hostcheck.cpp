@@ -91,6 +91,40 @@ extern "C" int blg_host_wavefront(const uint8_t *a, int la, const uint8_t *b, in
     return cap_k(score, k);
 }
 
+// The pipe-balanced form the search kernels use: 32-bit halves, IMAD-style
+// add/shift/score (plain arithmetic on the host), score kept as +1/-1 counts
+// of the last word's output bit, words chained top to bottom in a column.
+extern "C" int blg_host_distance_halves(const uint8_t *a, int la, const uint8_t *b, int lb, int trim, int k) {
+    normalise(a, la, b, lb, trim);
+    if (k >= 0 && lb - la > k) return k + 1;
+    if (la == 0) return lb;
+    Pattern P(a, la);
+    const int W = P.words, lastbit = (la - 1) % 64;
+    const Units u{1u, 2u};
+    const uint32_t mult = u.one << (31 - (lastbit & 31));
+    std::vector<Word2> st(W);
+    for (auto &x : st) { x.pl = x.ph = ~0u; x.ml = x.mh = 0; }
+    uint32_t accP = 0, accM = 0;
+    for (int j = 0; j < lb; j++) {
+        uint32_t Phl = 0, Phh = 0, Mhl = 0, Mhh = 0, cp = u.one, cm = 0;
+        for (int w = 0; w < W; w++) {
+            const uint64_t e = P.eq(b[j], w);
+            step_h(st[w], (uint32_t)e, (uint32_t)(e >> 32), cp, cm, u, Phl, Phh, Mhl, Mhh);
+            cp = top_bit(Phh, u);
+            cm = top_bit(Mhh, u);
+        }
+        if (lastbit >= 32) {
+            accP = imad_hi(imad_lo(Phh, mult, 0), u.two, accP);
+            accM = imad_hi(imad_lo(Mhh, mult, 0), u.two, accM);
+        } else {
+            accP = imad_hi(imad_lo(Phl, mult, 0), u.two, accP);
+            accM = imad_hi(imad_lo(Mhl, mult, 0), u.two, accM);
+        }
+        if (hopeless(la + (int)accP - (int)accM, j, lb, k)) return k + 1;
+    }
+    return cap_k(la + (int)accP - (int)accM, k);
+}
+
 extern "C" int blg_host_store(int d, int dtype) {
     if (dtype == DT_UINT8) return (int)saturate_u8(d);
     if (dtype == DT_UINT16) return (int)saturate_u16(d);

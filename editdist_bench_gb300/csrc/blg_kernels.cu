@@ -39,8 +39,11 @@ __global__ void __launch_bounds__(256) k_build_peq(DevStrings Q, const int32_t *
 // grid: x = candidate tiles of 4*blockDim.x, y = query chunks of `qpb`.
 template <int NW, bool HASK>
 __global__ void __launch_bounds__(256) k_search_seq(DevStrings C, SearchClass cls, int qpb, int k,
-                                                    int dtype, void *out, uint32_t *status) {
+                                                    int dtype, void *out, uint32_t *status, uint32_t unit) {
     extern __shared__ uint64_t s_peq[];
+    const Units u{unit, unit + unit};
+    RowAddr<NW> ra;
+    ra.init(u);
     const int64_t nc = C.n;
     const int64_t c0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
     const uint8_t *tp0 = C.buf, *tp1 = C.buf, *tp2 = C.buf, *tp3 = C.buf;
@@ -61,10 +64,10 @@ __global__ void __launch_bounds__(256) k_search_seq(DevStrings C, SearchClass cl
         if (cnt == 0) continue;
         const int m = cls.qlen[qi];
         const int64_t row = cls.qidx[qi];
-        const int d0 = dist_seq_any<NW, HASK>(s_peq, m, tp0, tn0, k);
-        const int d1 = cnt > 1 ? dist_seq_any<NW, HASK>(s_peq, m, tp1, tn1, k) : 0;
-        const int d2 = cnt > 2 ? dist_seq_any<NW, HASK>(s_peq, m, tp2, tn2, k) : 0;
-        const int d3 = cnt > 3 ? dist_seq_any<NW, HASK>(s_peq, m, tp3, tn3, k) : 0;
+        const int d0 = dist_seq_any<NW, HASK>(s_peq, m, tp0, tn0, k, u, ra);
+        const int d1 = cnt > 1 ? dist_seq_any<NW, HASK>(s_peq, m, tp1, tn1, k, u, ra) : 0;
+        const int d2 = cnt > 2 ? dist_seq_any<NW, HASK>(s_peq, m, tp2, tn2, k, u, ra) : 0;
+        const int d3 = cnt > 3 ? dist_seq_any<NW, HASK>(s_peq, m, tp3, tn3, k, u, ra) : 0;
         store4(out, dtype, row * nc + c0, cnt, d0, d1, d2, d3);
     }
 }
@@ -185,10 +188,10 @@ static cudaError_t launch_seq(bool hask, dim3 grid, size_t smem, cudaStream_t st
                               uint32_t *status) {
     if (hask) {
         cudaFuncSetAttribute(k_search_seq<NW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_search_seq<NW, true><<<grid, 256, smem, st>>>(C, cls, qpb, k, dtype, out, status);
+        k_search_seq<NW, true><<<grid, 256, smem, st>>>(C, cls, qpb, k, dtype, out, status, 1u);
     } else {
         cudaFuncSetAttribute(k_search_seq<NW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_search_seq<NW, false><<<grid, 256, smem, st>>>(C, cls, qpb, k, dtype, out, status);
+        k_search_seq<NW, false><<<grid, 256, smem, st>>>(C, cls, qpb, k, dtype, out, status, 1u);
     }
     return cudaGetLastError();
 }

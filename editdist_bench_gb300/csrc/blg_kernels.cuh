@@ -86,59 +86,109 @@ __device__ __forceinline__ void store4(void *out, int dtype, int64_t i, int cnt,
 }
 
 // --------------------------------------------------- search, NW <= 8 words --
-// One text column through NW pattern words (word 0 takes the +1 top-row carry).
-template <int NW, bool TOP63>
-__device__ __forceinline__ void column_seq(uint64_t (&pv)[NW], uint64_t (&mv)[NW],
-                                           const uint64_t *row, int lastbit, int &score) {
-    uint64_t ph, mh;
-    step_top<uint64_t>(pv[0], mv[0], row[0], ph, mh);
-    if (NW == 1) {
-        score += TOP63 ? hdelta<uint64_t>(ph, mh, 63) : hdelta<uint64_t>(ph, mh, lastbit);
-        return;
+// Address arithmetic for the Peq row of text byte b (0..3) of a 4-byte
+// window: byte offset = c * 8 * NW. For power-of-two NW the byte is shifted
+// straight into place by one IMAD (hi or lo) and masked; otherwise it is
+// extracted and scaled by IMAD. Multipliers are run-time values.
+template <int NW>
+struct RowAddr {
+    static constexpr bool kPow2 = (NW & (NW - 1)) == 0;
+    static constexpr int kSh = 3 + (NW >= 8 ? 3 : NW >= 4 ? 2 : NW >= 2 ? 1 : 0);
+    uint32_t mul[4], mask, stride, ext[4];
+    __device__ __forceinline__ void init(Units u) {
+        if (kPow2) {
+            mul[0] = u.one << kSh;
+            mul[1] = u.one << (24 + kSh);
+            mul[2] = u.one << (16 + kSh);
+            mul[3] = u.one << (8 + kSh);
+            mask = 0xffu << kSh;
+        }
+        ext[1] = u.one << 24;
+        ext[2] = u.one << 16;
+        ext[3] = u.one << 8;
+        stride = imad_lo(u.one, 8u * NW, 0);
     }
-    int h = hdelta<uint64_t>(ph, mh, 63);
+    template <int B>
+    __device__ __forceinline__ uint32_t off(uint32_t w4) const {
+        if (kPow2) return (B == 0 ? imad_lo(w4, mul[0], 0) : imad_hi(w4, mul[B], 0)) & mask;
+        const uint32_t c = B == 0 ? (w4 & 0xffu) : B == 3 ? imad_hi(w4, ext[3], 0)
+                                                          : (imad_hi(w4, ext[B], 0) & 0xffu);
+        return imad_lo(c, stride, 0);
+    }
+};
+
+// One text column through the NW words of the query (word 0 takes the +1
+// top-row carry); the last word's horizontal delta is accumulated as +1/-1
+// counts. LAST: 0 = score bit is bit 63, 1 = bit (lastbit-32) of the high
+// half, 2 = bit lastbit of the low half (`mult` = 2^(31 - that bit)).
+template <int NW, int LAST>
+__device__ __forceinline__ void column_h(Word2 (&st)[NW], const uint64_t *row, Units u, uint32_t mult,
+                                         uint32_t &accP, uint32_t &accM) {
+    uint32_t Phl, Phh, Mhl, Mhh;
+    uint32_t cp = u.one, cm = 0;
 #pragma unroll
-    for (int w = 1; w < NW - 1; w++) {
-        step_mid<uint64_t>(pv[w], mv[w], row[w], h, ph, mh);
-        h = hdelta<uint64_t>(ph, mh, 63);
+    for (int w = 0; w < NW; w++) {
+        const uint64_t e = row[w];
+        step_h(st[w], (uint32_t)e, (uint32_t)(e >> 32), cp, cm, u, Phl, Phh, Mhl, Mhh);
+        if (w < NW - 1) {
+            cp = top_bit(Phh, u);
+            cm = top_bit(Mhh, u);
+        }
     }
-    step_mid<uint64_t>(pv[NW - 1], mv[NW - 1], row[NW - 1], h, ph, mh);
-    score += TOP63 ? hdelta<uint64_t>(ph, mh, 63) : hdelta<uint64_t>(ph, mh, lastbit);
+    if (LAST == 0) {
+        accP = imad_hi(Phh, u.two, accP);
+        accM = imad_hi(Mhh, u.two, accM);
+    } else if (LAST == 1) {
+        accP = imad_hi(imad_lo(Phh, mult, 0), u.two, accP);
+        accM = imad_hi(imad_lo(Mhh, mult, 0), u.two, accM);
+    } else {
+        accP = imad_hi(imad_lo(Phl, mult, 0), u.two, accP);
+        accM = imad_hi(imad_lo(Mhl, mult, 0), u.two, accM);
+    }
 }
 
 // d(query, t) with the query's Peq table in shared memory (NW = ceil(m/64)).
-template <int NW, bool HASK, bool TOP63>
-__device__ __forceinline__ int dist_seq(const uint64_t *peq, int m, const uint8_t *t, int n, int k) {
+template <int NW, bool HASK, int LAST>
+__device__ __forceinline__ int dist_seq(const uint64_t *peq, int m, const uint8_t *t, int n, int k,
+                                        Units u, const RowAddr<NW> &ra) {
     if (m == 0) return cap_k(n, k);                    // csrc/gpu_kernels.cu:53
     if (HASK && (n > m ? n - m : m - n) > k) return k + 1;
-    uint64_t pv[NW], mv[NW];
+    Word2 st[NW];
 #pragma unroll
-    for (int w = 0; w < NW; w++) { pv[w] = ~0ull; mv[w] = 0; }
+    for (int w = 0; w < NW; w++) { st[w].pl = st[w].ph = ~0u; st[w].ml = st[w].mh = 0; }
     const int lastbit = (m - 1) & 63;
-    int score = m;
+    const uint32_t mult = u.one << (31 - (lastbit & 31));
+    uint32_t accP = 0, accM = 0;                        // score = m + accP - accM
+    const char *base = reinterpret_cast<const char *>(peq);
     TextScan ts;
     ts.init(t);
     int j = 0;
     for (; j + 4 <= n; j += 4) {
         const uint32_t w4 = ts.next4();
-#pragma unroll
-        for (int b = 0; b < 4; b++)
-            column_seq<NW, TOP63>(pv, mv, peq + ((w4 >> (8 * b)) & 0xffu) * NW, lastbit, score);
+        column_h<NW, LAST>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<0>(w4)), u, mult, accP, accM);
+        column_h<NW, LAST>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<1>(w4)), u, mult, accP, accM);
+        column_h<NW, LAST>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<2>(w4)), u, mult, accP, accM);
+        column_h<NW, LAST>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<3>(w4)), u, mult, accP, accM);
         // the exit test is monotone in j, so testing every 4th column is exact
-        if (HASK && hopeless(score, j + 3, n, k)) return k + 1;
+        if (HASK && hopeless(m + (int)accP - (int)accM, j + 3, n, k)) return k + 1;
     }
     if (j < n) {
         uint32_t w4 = ts.next4();
-        for (; j < n; j++, w4 >>= 8) column_seq<NW, TOP63>(pv, mv, peq + (w4 & 0xffu) * NW, lastbit, score);
+        for (; j < n; j++, w4 >>= 8)
+            column_h<NW, LAST>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<0>(w4)), u, mult,
+                               accP, accM);
     }
+    const int score = m + (int)accP - (int)accM;
     return HASK ? cap_k(score, k) : score;
 }
 
 template <int NW, bool HASK>
-__device__ __forceinline__ int dist_seq_any(const uint64_t *peq, int m, const uint8_t *t, int n, int k) {
-    // the last pattern bit is bit 63 for full words: cheaper score extraction
-    if (((m - 1) & 63) == 63) return dist_seq<NW, HASK, true>(peq, m, t, n, k);
-    return dist_seq<NW, HASK, false>(peq, m, t, n, k);
+__device__ __forceinline__ int dist_seq_any(const uint64_t *peq, int m, const uint8_t *t, int n, int k,
+                                            Units u, const RowAddr<NW> &ra) {
+    const int lastbit = (m - 1) & 63;
+    if (m > 0 && lastbit == 63) return dist_seq<NW, HASK, 0>(peq, m, t, n, k, u, ra);
+    if (lastbit >= 32) return dist_seq<NW, HASK, 1>(peq, m, t, n, k, u, ra);
+    return dist_seq<NW, HASK, 2>(peq, m, t, n, k, u, ra);
 }
 
 // ------------------------------------------------ lane-spread core (L lanes) --

@@ -57,12 +57,13 @@ __global__ void __launch_bounds__(256) k_na_build(DevStrings Q, int64_t q0, uint
 }
 
 template <bool HASK>
-__device__ __forceinline__ int na_dist(int nw, const uint64_t *peq, int m, const uint8_t *t, int n, int k) {
+__device__ __forceinline__ int na_dist(int nw, const uint64_t *peq, int m, const uint8_t *t, int n, int k,
+                                       Units u) {
     switch (nw) {
-    case 1: return dist_seq_any<1, HASK>(peq, m, t, n, k);
-    case 2: return dist_seq_any<2, HASK>(peq, m, t, n, k);
-    case 3: return dist_seq_any<3, HASK>(peq, m, t, n, k);
-    default: return dist_seq_any<4, HASK>(peq, m, t, n, k);
+    case 1: { RowAddr<1> ra; ra.init(u); return dist_seq_any<1, HASK>(peq, m, t, n, k, u, ra); }
+    case 2: { RowAddr<2> ra; ra.init(u); return dist_seq_any<2, HASK>(peq, m, t, n, k, u, ra); }
+    case 3: { RowAddr<3> ra; ra.init(u); return dist_seq_any<3, HASK>(peq, m, t, n, k, u, ra); }
+    default: { RowAddr<4> ra; ra.init(u); return dist_seq_any<4, HASK>(peq, m, t, n, k, u, ra); }
     }
 }
 
@@ -70,8 +71,9 @@ __device__ __forceinline__ int na_dist(int nw, const uint64_t *peq, int m, const
 template <bool HASK>
 __global__ void __launch_bounds__(256) k_na_search(DevStrings C, DevStrings Q, int64_t q0, int cnt,
                                                    int qpb, const uint64_t *scratch, int k, int dtype,
-                                                   void *out, uint32_t *status) {
+                                                   void *out, uint32_t *status, uint32_t unit) {
     extern __shared__ uint64_t s_peq[];
+    const Units u{unit, unit + unit};
     const int64_t nc = C.n;
     const int64_t c0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
     const int ccnt = (int)(c0 >= nc ? 0 : (nc - c0 < 4 ? nc - c0 : 4));
@@ -94,10 +96,10 @@ __global__ void __launch_bounds__(256) k_na_search(DevStrings C, DevStrings Q, i
             s_peq[x] = src[(x / nw) * kNoAllocWords + (x % nw)];
         __syncthreads();
         if (ccnt == 0) continue;
-        const int d0 = na_dist<HASK>(nw, s_peq, m, tp0, tn0, k);
-        const int d1 = ccnt > 1 ? na_dist<HASK>(nw, s_peq, m, tp1, tn1, k) : 0;
-        const int d2 = ccnt > 2 ? na_dist<HASK>(nw, s_peq, m, tp2, tn2, k) : 0;
-        const int d3 = ccnt > 3 ? na_dist<HASK>(nw, s_peq, m, tp3, tn3, k) : 0;
+        const int d0 = na_dist<HASK>(nw, s_peq, m, tp0, tn0, k, u);
+        const int d1 = ccnt > 1 ? na_dist<HASK>(nw, s_peq, m, tp1, tn1, k, u) : 0;
+        const int d2 = ccnt > 2 ? na_dist<HASK>(nw, s_peq, m, tp2, tn2, k, u) : 0;
+        const int d3 = ccnt > 3 ? na_dist<HASK>(nw, s_peq, m, tp3, tn3, k, u) : 0;
         store4(out, dtype, (q0 + i) * nc + c0, ccnt, d0, d1, d2, d3);
     }
 }
@@ -156,10 +158,10 @@ extern "C" int blg_cdist_noalloc(blg_ctx *c, const uint8_t *d_buf_q, size_t q_by
         const dim3 grid((unsigned)tiles, (unsigned)((cnt + qpb - 1) / qpb));
         if (hask)
             k_na_search<true><<<grid, 256, smem, c->stream>>>(C, Q, q0, cnt, qpb, scratch, max_dist,
-                                                              dtype, d_out, c->d_status);
+                                                              dtype, d_out, c->d_status, 1u);
         else
             k_na_search<false><<<grid, 256, smem, c->stream>>>(C, Q, q0, cnt, qpb, scratch, max_dist,
-                                                               dtype, d_out, c->d_status);
+                                                               dtype, d_out, c->d_status, 1u);
         c->launches += 2;
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_fail(c, e, "blg_cdist_noalloc launch");

@@ -61,7 +61,7 @@ def test_pack_errors_and_generators():
 @pytest.fixture(scope="module")
 def hostcheck():
     L = ctypes.CDLL(_build.build_hostcheck())
-    for f in (L.blg_host_distance, L.blg_host_wavefront):
+    for f in (L.blg_host_distance, L.blg_host_wavefront, L.blg_host_distance_halves):
         f.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
                       ctypes.c_int]
         f.restype = ctypes.c_int
@@ -77,7 +77,8 @@ def test_hostcheck_edge_cases(hostcheck, known):
     for c in known["exact"]:
         a, b = c["a"].encode("latin-1"), c["b"].encode("latin-1")
         for trim in (0, 1):
-            for f in (hostcheck.blg_host_distance, hostcheck.blg_host_wavefront):
+            for f in (hostcheck.blg_host_distance, hostcheck.blg_host_wavefront,
+                      hostcheck.blg_host_distance_halves):
                 assert f(a, len(a), b, len(b), trim, -1) == c["d"]
                 assert f(b, len(b), a, len(a), trim, -1) == c["d"]
 
@@ -100,6 +101,7 @@ def test_hostcheck_random_threshold(hostcheck, k):
         for trim in (0, 1):
             assert hostcheck.blg_host_distance(a, len(a), b, len(b), trim, k) == want
             assert hostcheck.blg_host_wavefront(a, len(a), b, len(b), trim, k) == want
+            assert hostcheck.blg_host_distance_halves(a, len(a), b, len(b), trim, k) == want
 
 
 @pytest.mark.parametrize("m", [1, 63, 64, 65, 127, 128, 129, 255, 256, 257, 511, 512, 513, 1000, 2048])
@@ -111,6 +113,7 @@ def test_hostcheck_word_boundaries(hostcheck, m):
         want = _one(a, b, -1)
         assert hostcheck.blg_host_distance(a, len(a), b, len(b), 1, -1) == want
         assert hostcheck.blg_host_wavefront(a, len(a), b, len(b), 0, -1) == want
+        assert hostcheck.blg_host_distance_halves(a, len(a), b, len(b), 0, -1) == want
 
 
 def test_hostcheck_store_saturation(hostcheck, known):
