@@ -15,6 +15,7 @@ import numpy as np
 from . import _build
 
 OK, ERR_ALLOC, ERR_ARG, ERR_CUDA, ERR_TIMEOUT, ERR_NODEVICE = 0, -1, -2, -3, -4, -5
+SCHED_AUTO, SCHED_PLAIN, SCHED_LEARNED, SCHED_LENSORT = 0, 1, 2, 3
 
 _P = ctypes.c_void_p
 _I32, _I64, _SZ = ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t
@@ -44,6 +45,7 @@ SIGNATURES = [
     ("blg_timer_start", ctypes.c_int, [_P]),
     ("blg_timer_stop", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float)]),
     ("blg_launch_count", ctypes.c_int64, [_P]),
+    ("blg_set_schedule", ctypes.c_int, [_P, ctypes.c_int]),
     ("blg_profile_enable", ctypes.c_int, [_P, ctypes.c_int]),
     ("blg_profile_report", ctypes.c_int, [_P, ctypes.c_char_p, _SZ]),
 ]

@@ -34,6 +34,16 @@ cudaError_t launch_pairs_main(cudaStream_t st, int grid, bool hask, const DevStr
                               uint32_t *status);
 cudaError_t launch_pairs_long(cudaStream_t st, int grid, bool hask, const LongQueue &q, int k,
                               int dtype, void *out);
+cudaError_t launch_fill(cudaStream_t st, int sms, void *out, int64_t n, int dtype, uint32_t v);
+cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &src, const int32_t *perm,
+                                  const int64_t *dst_off, uint8_t *dst, int64_t n, uint32_t *status);
+cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
+                             int64_t min_len, int64_t n_len, int k, int32_t *lo, int32_t *hi,
+                             int64_t *tile_start, int32_t *work);
+cudaError_t launch_search_surv(cudaStream_t st, int sms, int nw, const DevStrings &CS, const int32_t *perm,
+                               const SearchClass &cls, const int32_t *lo, const int32_t *hi,
+                               const int64_t *tile_start, int32_t *work, int k, int dtype, void *out,
+                               int64_t nc, uint32_t *status);
 }  // namespace blg
 
 using namespace blg;
@@ -67,10 +77,20 @@ struct blg_search {
         int nw;          // words (seq) or table stride (lanes)
         bool lanes;
         int nq;
-        int32_t *qidx, *qlen;
+        int32_t *qidx, *qlen;      // queries of the class, sorted by length
         uint64_t *peq;
+        int32_t *lo, *hi, *work;   // survivor plan (thresholded runs)
+        int64_t *tile_start;
     };
     std::vector<Cls> cls;
+    // choices sorted by length (thresholded runs): cs = sorted copy,
+    // perm[i] = original index of sorted choice i, lstart[L - min_len] =
+    // first sorted index of length L (n_len + 1 entries)
+    bool lsorted = false;
+    OwnedStrings cs;
+    int32_t *perm = nullptr;
+    int64_t *lstart = nullptr;
+    int64_t min_len = 0, n_len = 0;
 };
 
 // ------------------------------------------------------------ helpers --
@@ -274,6 +294,14 @@ static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64
     }
     for (int slot = 0; slot <= kSeqMaxWords; slot++) {
         if (idx[slot].empty()) continue;
+        // queries by length: consecutive survivor tiles then share choices in L2
+        std::vector<size_t> ord(idx[slot].size());
+        for (size_t i = 0; i < ord.size(); i++) ord[i] = i;
+        std::stable_sort(ord.begin(), ord.end(), [&](size_t x, size_t y) { return len[slot][x] < len[slot][y]; });
+        std::vector<int32_t> si(ord.size()), sl(ord.size());
+        for (size_t i = 0; i < ord.size(); i++) { si[i] = idx[slot][ord[i]]; sl[i] = len[slot][ord[i]]; }
+        idx[slot].swap(si);
+        len[slot].swap(sl);
         blg_search::Cls k{};
         k.lanes = slot == kSeqMaxWords;
         k.nw = k.lanes ? lanes_nw : slot + 1;
@@ -283,7 +311,54 @@ static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64
         CK(dev_alloc(c, (void **)&k.peq, sizeof(uint64_t) * 256 * (size_t)k.nw * k.nq), "cudaMallocAsync(peq)");
         CK(cudaMemcpyAsync(k.qidx, idx[slot].data(), sizeof(int32_t) * k.nq, cudaMemcpyHostToDevice, c->stream), "H2D qidx");
         CK(cudaMemcpyAsync(k.qlen, len[slot].data(), sizeof(int32_t) * k.nq, cudaMemcpyHostToDevice, c->stream), "H2D qlen");
+        CK(dev_alloc(c, (void **)&k.lo, sizeof(int32_t) * k.nq), "cudaMallocAsync(lo)");
+        CK(dev_alloc(c, (void **)&k.hi, sizeof(int32_t) * k.nq), "cudaMallocAsync(hi)");
+        CK(dev_alloc(c, (void **)&k.tile_start, sizeof(int64_t) * (k.nq + 1)), "cudaMallocAsync(tiles)");
+        CK(dev_alloc(c, (void **)&k.work, sizeof(int32_t)), "cudaMallocAsync(work)");
         s->cls.push_back(k);
+    }
+    // Choices sorted by length (counting sort on the host, byte gather on the
+    // device), when the length range is moderate.
+    if (nc > 0) {
+        int64_t mn = INT64_MAX, mx = 0;
+        for (int64_t i = 0; i < nc; i++) {
+            const int64_t l = oc[i + 1] - oc[i];
+            mn = std::min(mn, l);
+            mx = std::max(mx, l);
+        }
+        if (mx - mn < (1 << 22) && nc < INT32_MAX) {
+            const int64_t n_len = mx - mn + 1;
+            std::vector<int64_t> lstart(n_len + 1, 0);
+            for (int64_t i = 0; i < nc; i++) lstart[oc[i + 1] - oc[i] - mn + 1]++;
+            for (int64_t r = 0; r < n_len; r++) lstart[r + 1] += lstart[r];
+            std::vector<int64_t> fillp(lstart.begin(), lstart.end() - 1);
+            std::vector<int32_t> perm(nc);
+            for (int64_t i = 0; i < nc; i++) perm[fillp[oc[i + 1] - oc[i] - mn]++] = (int32_t)i;
+            std::vector<int64_t> soff(nc + 1, 0);
+            for (int64_t i = 0; i < nc; i++) soff[i + 1] = soff[i] + (oc[perm[i] + 1] - oc[perm[i]]);
+            const int64_t bytes = soff[nc];
+            OwnedStrings &cs = s->cs;
+            CK(dev_alloc(c, &cs.mem_buf, (size_t)bytes + 32), "cudaMallocAsync(sorted choices)");
+            CK(cudaMemsetAsync(cs.mem_buf, 0, (size_t)bytes + 32, c->stream), "memset sorted choices");
+            CK(dev_alloc(c, &cs.mem_off, sizeof(int64_t) * (size_t)(nc + 1)), "cudaMallocAsync(sorted offsets)");
+            CK(cudaMemcpyAsync(cs.mem_off, soff.data(), sizeof(int64_t) * (nc + 1), cudaMemcpyHostToDevice, c->stream), "H2D soff");
+            CK(dev_alloc(c, (void **)&s->perm, sizeof(int32_t) * nc), "cudaMallocAsync(perm)");
+            CK(cudaMemcpyAsync(s->perm, perm.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice, c->stream), "H2D perm");
+            CK(dev_alloc(c, (void **)&s->lstart, sizeof(int64_t) * (n_len + 1)), "cudaMallocAsync(lstart)");
+            CK(cudaMemcpyAsync(s->lstart, lstart.data(), sizeof(int64_t) * (n_len + 1), cudaMemcpyHostToDevice, c->stream), "H2D lstart");
+            cs.d.buf = (uint8_t *)cs.mem_buf + 16;
+            cs.d.off = (const int64_t *)cs.mem_off;
+            cs.d.n = nc;
+            cs.d.base = 0;
+            cs.d.bytes = bytes;
+            CK(launch(c, "gather_strings", [&] {
+                   return launch_gather_strings(c->stream, c->sms, s->c.d, s->perm, cs.d.off,
+                                                (uint8_t *)cs.d.buf, nc, c->d_status);
+               }), "gather_strings");
+            s->min_len = mn;
+            s->n_len = n_len;
+            s->lsorted = true;
+        }
     }
     // the host vectors above are pageable: the copies completed before return
     return BLG_OK;
@@ -305,12 +380,31 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out) 
     if (s->nq == 0 || s->nc == 0) return BLG_OK;
     if (!d_out) return fail(c, BLG_ERR_ARG, "null output");
     const bool hask = k >= 0;
+    const bool surv = hask && s->lsorted && c->sched != BLG_SCHED_PLAIN;
+    if (surv) {
+        const uint32_t fillv = (uint32_t)(dtype == BLG_UINT8 ? std::min(k + 1, 255)
+                                          : dtype == BLG_UINT16 ? std::min(k + 1, 65535) : k + 1);
+        CK(launch(c, "fill", [&] {
+               return launch_fill(c->stream, c->sms, d_out, s->nq * s->nc, dtype, fillv);
+           }), "fill");
+    }
     for (auto &k_ : s->cls)
         CK(launch(c, "build_peq", [&] {
                return launch_build_peq(c->stream, s->q.d, k_.qidx, k_.nq, k_.nw, k_.peq, c->d_status);
            }), "build_peq");
     for (auto &k_ : s->cls) {
         SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
+        if (surv && !k_.lanes) {
+            CK(launch(c, "surv_plan", [&] {
+                   return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, k, k_.lo,
+                                           k_.hi, k_.tile_start, k_.work);
+               }), "surv_plan");
+            CK(launch(c, "search_surv", [&] {
+                   return launch_search_surv(c->stream, c->sms, k_.nw, s->cs.d, s->perm, sc, k_.lo, k_.hi,
+                                             k_.tile_start, k_.work, k, dtype, d_out, s->nc, c->d_status);
+               }), "search_surv");
+            continue;
+        }
         if (k_.lanes) {
             CK(launch(c, "search_lanes", [&] {
                    return launch_search_lanes(c->stream, hask, s->c.d, sc, k_.nw, k, dtype, d_out,
@@ -330,10 +424,20 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out) 
 static void search_release(blg_ctx *c, blg_search *s) {
     free_strings(c, s->q);
     free_strings(c, s->c);
+    free_strings(c, s->cs);
+    dev_free(c, s->perm);
+    dev_free(c, s->lstart);
+    s->perm = nullptr;
+    s->lstart = nullptr;
+    s->lsorted = false;
     for (auto &k : s->cls) {
         dev_free(c, k.qidx);
         dev_free(c, k.qlen);
         dev_free(c, k.peq);
+        dev_free(c, k.lo);
+        dev_free(c, k.hi);
+        dev_free(c, k.tile_start);
+        dev_free(c, k.work);
     }
     s->cls.clear();
 }
@@ -587,6 +691,13 @@ int blg_timer_stop(blg_ctx *c, float *ms) {
 }
 
 int64_t blg_launch_count(const blg_ctx *c) { return c ? c->launches : 0; }
+
+int blg_set_schedule(blg_ctx *c, int mode) {
+    ENTER(c);
+    if (mode < BLG_SCHED_AUTO || mode > BLG_SCHED_LENSORT) return fail(c, BLG_ERR_ARG, "unknown schedule");
+    c->sched = mode;
+    return BLG_OK;
+}
 
 int blg_profile_enable(blg_ctx *c, int on) {
     ENTER(c);

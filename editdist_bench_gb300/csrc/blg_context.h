@@ -20,6 +20,7 @@ struct blg_ctx {
     std::mutex mu;                     // serialises calls on one context
     std::string err;
     int64_t launches = 0;
+    int sched = 0;                     // BLG_SCHED_* (work order of thresholded runs)
     bool prof = false;
     std::vector<ProfRec> prof_recs;
     std::map<std::string, std::pair<int64_t, double>> prof_acc;

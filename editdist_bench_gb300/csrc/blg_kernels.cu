@@ -181,6 +181,145 @@ __global__ void __launch_bounds__(256) k_pairs_long(LongQueue q, int k, int dtyp
     }
 }
 
+// ------------------------------------------- thresholded search: survivors --
+// With max_dist = k, a (query, choice) pair whose lengths differ by more than
+// k is decided by the lengths alone (csrc/myers.c:101-106): its result is
+// k+1. Choices are kept in a length-sorted copy, so the pairs that need the
+// column loop ("survivors") of a query of length m are one contiguous range
+// of that copy: lengths m-k .. m+k. The output is first filled with k+1;
+// survivors are computed in tiles of 1024 and only results <= k are written.
+
+// out[0..n) = v (dtype-sized), 16-byte stores for the aligned middle.
+__global__ void __launch_bounds__(256) k_fill(void *out, int64_t n, int dtype, uint32_t v) {
+    const int es = dtype == DT_UINT8 ? 1 : dtype == DT_UINT16 ? 2 : 4;
+    uint32_t word = v;
+    if (es == 1) word = v * 0x01010101u;
+    else if (es == 2) word = v | (v << 16);
+    const int64_t bytes = n * es;
+    uint8_t *b = reinterpret_cast<uint8_t *>(out);
+    const int64_t head = (16 - (reinterpret_cast<uintptr_t>(b) & 15)) & 15;
+    const int64_t nvec = bytes > head ? (bytes - head) / 16 : 0;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    uint4 *vp = reinterpret_cast<uint4 *>(b + head);
+    const uint4 vv = make_uint4(word, word, word, word);
+    for (int64_t i = tid; i < nvec; i += stride) vp[i] = vv;
+    // unaligned head and tail, one element at a time (out is element-aligned,
+    // so the head is a whole number of elements)
+    const int64_t tail0 = head + nvec * 16;
+    for (int64_t r = tid * es; r < head + (bytes - tail0); r += stride * es) {
+        const int64_t x = r < head ? r : tail0 + (r - head);
+        if (x >= bytes) break;
+        if (es == 1) b[x] = (uint8_t)v;
+        else if (es == 2) *reinterpret_cast<uint16_t *>(b + x) = (uint16_t)v;
+        else *reinterpret_cast<uint32_t *>(b + x) = v;
+    }
+}
+
+// dst string i = src string perm[i]; one warp per string, byte-wise copy.
+__global__ void __launch_bounds__(256) k_gather_strings(DevStrings src, const int32_t *perm,
+                                                        const int64_t *dst_off, uint8_t *dst, int64_t n,
+                                                        uint32_t *status) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = warp; i < n; i += nwarps) {
+        int len;
+        const uint8_t *p = string_at(src, perm[i], len, status);
+        uint8_t *q = dst + dst_off[i];
+        const int64_t cap = dst_off[i + 1] - dst_off[i];
+        if (len > cap) len = (int)cap;
+        for (int x = lane; x < len; x += 32) q[x] = p[x];
+    }
+}
+
+// Per class: survivor range [lo, hi) of every query (queries sorted by
+// length), tile counts, and their exclusive prefix tile_start[0..nq]. One
+// block; the scan walks the queries 1024 at a time.
+__global__ void __launch_bounds__(1024) k_surv_plan(SearchClass cls, const int64_t *lstart, int64_t min_len,
+                                                    int64_t n_len, int k, int32_t *lo, int32_t *hi,
+                                                    int64_t *tile_start, int32_t *work) {
+    __shared__ int64_t s_sum[1024];
+    __shared__ int64_t s_carry;
+    if (threadIdx.x == 0) { s_carry = 0; *work = 0; }
+    __syncthreads();
+    for (int base = 0; base < cls.nq; base += 1024) {
+        const int qi = base + threadIdx.x;
+        int64_t tiles = 0;
+        if (qi < cls.nq) {
+            const int64_t m = cls.qlen[qi];
+            int64_t a = m - k - min_len, b = m + k - min_len + 1;   // length window, index space
+            a = a < 0 ? 0 : (a > n_len ? n_len : a);
+            b = b < 0 ? 0 : (b > n_len ? n_len : b);
+            const int64_t l = lstart[a], h = b > a ? lstart[b] : l;
+            lo[qi] = (int32_t)l;
+            hi[qi] = (int32_t)h;
+            tiles = (h - l + 1023) / 1024;
+        }
+        s_sum[threadIdx.x] = tiles;
+        __syncthreads();
+        for (int off = 1; off < 1024; off <<= 1) {                     // inclusive scan
+            const int64_t v = threadIdx.x >= off ? s_sum[threadIdx.x - off] : 0;
+            __syncthreads();
+            s_sum[threadIdx.x] += v;
+            __syncthreads();
+        }
+        if (qi < cls.nq) tile_start[qi] = s_carry + s_sum[threadIdx.x] - tiles;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += s_sum[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tile_start[cls.nq] = s_carry;
+}
+
+// Persistent: every CTA pulls tiles from the device work counter until the
+// plan is exhausted (the counter only grows, so the loop always ends).
+template <int NW>
+__global__ void __launch_bounds__(256) k_search_surv(DevStrings CS, const int32_t *perm, SearchClass cls,
+                                                     const int32_t *lo, const int32_t *hi,
+                                                     const int64_t *tile_start, int32_t *work, int k,
+                                                     int dtype, void *out, int64_t nc, uint32_t *status,
+                                                     uint32_t unit) {
+    extern __shared__ uint64_t s_peq[];
+    __shared__ int s_tile;
+    const Units u{unit, unit + unit};
+    RowAddr<NW> ra;
+    ra.init(u);
+    const int64_t total = tile_start[cls.nq];
+    int cur = -1;
+    while (true) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(work, 1);
+        __syncthreads();
+        const int64_t tile = s_tile;
+        if (tile >= total) break;
+        int a = 0, b = cls.nq;                        // tile_start[a] <= tile < tile_start[b]
+        while (b - a > 1) {
+            const int mid = (a + b) >> 1;
+            if (tile_start[mid] <= tile) a = mid; else b = mid;
+        }
+        const int qi = a;
+        if (qi != cur) {
+            const uint64_t *src = cls.peq + (size_t)qi * 256 * NW;
+            for (int x = threadIdx.x; x < 256 * NW; x += blockDim.x) s_peq[x] = __ldg(src + x);
+            cur = qi;
+        }
+        __syncthreads();
+        const int m = cls.qlen[qi];
+        const int64_t row = cls.qidx[qi];
+        const int64_t s_end = hi[qi];
+        const int64_t s0 = lo[qi] + (tile - tile_start[qi]) * 1024 + threadIdx.x * 4;
+#pragma unroll 1
+        for (int t = 0; t < 4; t++) {
+            const int64_t sidx = s0 + t;
+            if (sidx >= s_end) break;
+            int n;
+            const uint8_t *tp = string_at(CS, sidx, n, status);
+            const int d = dist_seq_any<NW, true>(s_peq, m, tp, n, k, u, ra);
+            if (d <= k) store1(out, dtype, row * nc + perm[sidx], d);
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------- launchers --
 template <int NW>
 static cudaError_t launch_seq(bool hask, dim3 grid, size_t smem, cudaStream_t st, const DevStrings &C,
@@ -269,6 +408,63 @@ cudaError_t launch_pairs_long(cudaStream_t st, int grid, bool hask, const LongQu
         k_pairs_long<false><<<grid, 256, smem, st>>>(q, k, dtype, out);
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_fill(cudaStream_t st, int sms, void *out, int64_t n, int dtype, uint32_t v) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t es = dtype == DT_UINT8 ? 1 : dtype == DT_UINT16 ? 2 : 4;
+    int64_t blocks = (n * es / 16 + 255) / 256;
+    blocks = blocks < 1 ? 1 : (blocks > (int64_t)sms * 16 ? (int64_t)sms * 16 : blocks);
+    k_fill<<<(unsigned)blocks, 256, 0, st>>>(out, n, dtype, v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &src, const int32_t *perm,
+                                  const int64_t *dst_off, uint8_t *dst, int64_t n, uint32_t *status) {
+    if (n <= 0) return cudaSuccess;
+    int64_t blocks = (n + 7) / 8;
+    blocks = blocks > (int64_t)sms * 32 ? (int64_t)sms * 32 : blocks;
+    k_gather_strings<<<(unsigned)blocks, 256, 0, st>>>(src, perm, dst_off, dst, n, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
+                             int64_t min_len, int64_t n_len, int k, int32_t *lo, int32_t *hi,
+                             int64_t *tile_start, int32_t *work) {
+    if (cls.nq <= 0) return cudaSuccess;
+    k_surv_plan<<<1, 1024, 0, st>>>(cls, lstart, min_len, n_len, k, lo, hi, tile_start, work);
+    return cudaGetLastError();
+}
+
+template <int NW>
+static cudaError_t launch_surv_nw(cudaStream_t st, int grid, const DevStrings &CS, const int32_t *perm,
+                                  const SearchClass &cls, const int32_t *lo, const int32_t *hi,
+                                  const int64_t *tile_start, int32_t *work, int k, int dtype, void *out,
+                                  int64_t nc, uint32_t *status) {
+    const size_t smem = (size_t)256 * NW * sizeof(uint64_t);
+    cudaFuncSetAttribute(k_search_surv<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_search_surv<NW><<<grid, 256, smem, st>>>(CS, perm, cls, lo, hi, tile_start, work, k, dtype, out, nc,
+                                                status, 1u);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_search_surv(cudaStream_t st, int sms, int nw, const DevStrings &CS, const int32_t *perm,
+                               const SearchClass &cls, const int32_t *lo, const int32_t *hi,
+                               const int64_t *tile_start, int32_t *work, int k, int dtype, void *out,
+                               int64_t nc, uint32_t *status) {
+    if (cls.nq <= 0) return cudaSuccess;
+    const int grid = sms * 4;
+    switch (nw) {
+    case 1: return launch_surv_nw<1>(st, grid, CS, perm, cls, lo, hi, tile_start, work, k, dtype, out, nc, status);
+    case 2: return launch_surv_nw<2>(st, grid, CS, perm, cls, lo, hi, tile_start, work, k, dtype, out, nc, status);
+    case 3: return launch_surv_nw<3>(st, grid, CS, perm, cls, lo, hi, tile_start, work, k, dtype, out, nc, status);
+    case 4: return launch_surv_nw<4>(st, grid, CS, perm, cls, lo, hi, tile_start, work, k, dtype, out, nc, status);
+    case 5: return launch_surv_nw<5>(st, grid, CS, perm, cls, lo, hi, tile_start, work, k, dtype, out, nc, status);
+    case 6: return launch_surv_nw<6>(st, grid, CS, perm, cls, lo, hi, tile_start, work, k, dtype, out, nc, status);
+    case 7: return launch_surv_nw<7>(st, grid, CS, perm, cls, lo, hi, tile_start, work, k, dtype, out, nc, status);
+    case 8: return launch_surv_nw<8>(st, grid, CS, perm, cls, lo, hi, tile_start, work, k, dtype, out, nc, status);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace blg

@@ -28,7 +28,7 @@ from ._common import DTYPE_CODE, as_list, check_dtype, check_k, pack
 from .device_array import DeviceArray
 
 __all__ = ["available", "pairwise", "cdist", "pairwise_packed", "cdist_packed", "PairsBatch",
-           "SearchBatch", "pack"]
+           "SearchBatch", "pack", "set_schedule", "synchronize"]
 
 
 def available() -> bool:
@@ -182,6 +182,19 @@ class SearchBatch:
         if getattr(self, "h", None) and self.h.value:
             self.ctx.lib.blg_search_free(self.ctx.h, self.h)
             self.h = None
+
+
+_SCHEDULES = {"auto": _lib.SCHED_AUTO, "plain": _lib.SCHED_PLAIN, "learned": _lib.SCHED_LEARNED,
+              "lensort": _lib.SCHED_LENSORT}
+
+
+def set_schedule(name: str):
+    """Work order of max_dist runs: "auto" (survivor compaction), "plain" (one
+    thread per pair in natural order, the reference's schedule), "learned"
+    (compaction + the scheduler network's predicted exit order) or
+    "lensort" (compaction + length-difference order). Results never change."""
+    ctx = _lib.context()
+    ctx.check(ctx.lib.blg_set_schedule(ctx.h, _SCHEDULES[name]), "set_schedule")
 
 
 def synchronize():

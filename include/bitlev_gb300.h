@@ -110,6 +110,21 @@ int blg_cdist_noalloc(blg_ctx *ctx, const uint8_t *d_buf_q, size_t q_bytes, cons
                       int64_t nq, const uint8_t *d_buf_c, size_t c_bytes, const int64_t *d_off_c,
                       int64_t nc, int32_t max_dist, int32_t dtype, void *d_out);
 
+/* Work order of thresholded (max_dist >= 0) runs. Results never depend on it.
+ *  AUTO    — survivor compaction: choices kept length-sorted, only pairs whose
+ *            lengths are within max_dist run the column loop, the rest of the
+ *            output is filled with max_dist+1;
+ *  PLAIN   — every (query, choice) / pair in natural order, one thread each
+ *            (the reference's schedule, csrc/gpu_kernels.cu:6-69);
+ *  LEARNED — AUTO plus survivors ordered by the scheduler network's
+ *            predicted exit column;
+ *  LENSORT — AUTO plus survivors ordered by length difference (ablation). */
+#define BLG_SCHED_AUTO 0
+#define BLG_SCHED_PLAIN 1
+#define BLG_SCHED_LEARNED 2
+#define BLG_SCHED_LENSORT 3
+int blg_set_schedule(blg_ctx *ctx, int mode);
+
 /* Device memory and stream helpers (the parts of CuPy bitlev.gpu used:
  * cp.empty / .get() / Device().synchronize(), bitlev/gpu.py:59-68,102). */
 int blg_malloc(blg_ctx *ctx, size_t bytes, void **d_ptr);

@@ -222,3 +222,37 @@ def test_symmetry_property(gpu):
     d = gpu.cdist_packed(q, q)
     np.testing.assert_array_equal(d, d.T)
     assert (np.diag(d) == 0).all()
+
+
+# ---- work order: every schedule gives identical results ----------------------
+@pytest.mark.parametrize("sched", ["auto", "plain"])
+def test_thresholded_search_schedules(gpu, sched):
+    rng = np.random.default_rng(31)
+    # wide and narrow length spreads, empty strings, planted near-copies
+    q = W.concat(W.random_strings(rng, rng.integers(0, 300, 60)), W.random_strings(rng, [0, 1, 64, 65, 512]))
+    c = W.concat(W.mutate(rng, W.take(q, rng.integers(0, 65, 300)), 0.05),
+                 W.random_strings(rng, rng.integers(0, 320, 1500)), W.random_strings(rng, [0, 0, 7]))
+    gpu.set_schedule(sched)
+    try:
+        for k, dt in ((0, "int32"), (2, "uint8"), (7, "uint16"), (40, "uint8"), (300, "int32"), (1000, "uint8")):
+            got = gpu.cdist_packed(q, c, max_dist=k, dtype=dt)
+            want = oracle.saturate(oracle.cross(q, c, k), dt)
+            np.testing.assert_array_equal(got, want, err_msg=f"{sched} k={k} {dt}")
+        # odd output sizes exercise the fill's unaligned head and tail
+        q3, c3 = W.take(q, [1, 2, 3]), W.take(c, np.arange(997))
+        np.testing.assert_array_equal(gpu.cdist_packed(q3, c3, 3, "uint8"),
+                                      oracle.saturate(oracle.cross(q3, c3, 3), "uint8"))
+    finally:
+        gpu.set_schedule("auto")
+
+
+def test_thresholded_search_resident_repeat(gpu):
+    """The survivor plan is rebuilt per run: different k on one resident batch."""
+    rng = np.random.default_rng(8)
+    q = W.random_strings(rng, rng.integers(90, 130, 40))
+    c = W.concat(W.mutate(rng, W.take(q, rng.integers(0, 40, 100)), 0.04),
+                 W.random_strings(rng, rng.integers(80, 140, 2000)))
+    s = gpu.SearchBatch(q, c)
+    for k, dt in ((4, "uint8"), (0, "uint8"), (12, "int32"), (4, "uint8")):
+        out = s.run(s.alloc(dt), max_dist=k).get()
+        np.testing.assert_array_equal(out, oracle.saturate(oracle.cross(q, c, k), dt))
