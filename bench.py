@@ -352,6 +352,7 @@ def read_traffic(kernel: str, workload: str):
 # ------------------------------------------------------------------ arms --
 def run_ours(args, ranks: Ranks):
     ctx = _lib.context()
+    gpu.set_schedule(args.schedule)
     bench = make_bench(args.config, args)
     p = ctypes.c_void_p()
     ctx.check(ctx.lib.blg_malloc(ctx.h, L2_FLUSH_BYTES, ctypes.byref(p)))
@@ -428,7 +429,7 @@ def run_ours(args, ranks: Ranks):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u64", "data": "synthetic (seeded numpy generator, workload shapes of the benchmark configuration)",
         "config": dict(bench.describe(), l2="flushed between steps (256 MB memset outside the timed events)",
-                       parallelism="replicas" if ranks.world > 1 else "single GPU"),
+                       parallelism="replicas" if ranks.world > 1 else "single GPU", schedule=args.schedule),
         "gcups": bench.cells * ranks.world / (ms_per_step / 1e3) / 1e9,
         "e2e": {"value": bench.pairs * ranks.world / e2e_s, "unit": "pairs/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -531,6 +532,8 @@ def main():
     ap.add_argument("--nq", type=int, default=None, help="override the query count (profiling)")
     ap.add_argument("--nc", type=int, default=None, help="override the choice count (profiling)")
     ap.add_argument("--n", type=int, default=None, help="override the pair count (profiling)")
+    ap.add_argument("--schedule", default="auto", choices=["auto", "plain", "learned", "lensort"],
+                    help="work order of max_dist runs (results are identical)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
