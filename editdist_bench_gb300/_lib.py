@@ -32,6 +32,7 @@ SIGNATURES = [
     ("blg_pairs_upload", ctypes.c_int, [_P, _P, _P, _P, _P, _I64, ctypes.POINTER(_P)]),
     ("blg_pairs_run", ctypes.c_int, [_P, _P, _I32, _I32, _P]),
     ("blg_pairs_free", None, [_P, _P]),
+    ("blg_pairs_run_logged", ctypes.c_int, [_P, _P, _I32, _I32, _P, _P]),
     ("blg_search_upload", ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _I64, ctypes.POINTER(_P)]),
     ("blg_search_run", ctypes.c_int, [_P, _P, _I32, _I32, _P]),
     ("blg_search_free", None, [_P, _P]),

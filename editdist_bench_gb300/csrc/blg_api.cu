@@ -20,6 +20,7 @@
 #include "blg_context.h"
 #include "blg_device.cuh"
 #include "blg_internal.h"
+#include "blg_sched.h"
 
 namespace blg {
 cudaError_t launch_build_peq(cudaStream_t st, const DevStrings &Q, const int32_t *qidx, int nq, int nwc,
@@ -35,6 +36,12 @@ cudaError_t launch_pairs_main(cudaStream_t st, int grid, bool hask, const DevStr
 cudaError_t launch_pairs_long(cudaStream_t st, int grid, bool hask, const LongQueue &q, int k,
                               int dtype, void *out);
 cudaError_t launch_fill(cudaStream_t st, int sms, void *out, int64_t n, int dtype, uint32_t v);
+cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, const DevStrings &A,
+                              const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
+                              uint32_t *status);
+cudaError_t launch_order(cudaStream_t st, int sms, bool need_hist, const PairsPlan &plan);
+cudaError_t launch_solve(cudaStream_t st, int sms, bool hask, const PairsPlan &plan, int k, int dtype,
+                         void *out, int32_t *exit_log, bool any_long);
 cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &src, const int32_t *perm,
                                   const int64_t *dst_off, uint8_t *dst, int64_t n, uint32_t *status);
 cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
@@ -68,6 +75,11 @@ struct blg_pairs {
     int64_t cap[kLongClasses] = {0, 0, 0, 0, 0};
     void *q_items = nullptr;      // all class regions, one allocation
     int32_t *q_ctr = nullptr;     // counts[5], heads[5]
+    // scheduled path (prep -> order -> solve), allocated on first use
+    int64_t pcap[kPairClasses] = {0, 0, 0, 0, 0, 0};
+    void *plan_mem = nullptr;     // raw + sorted records, keys
+    half *feat_mem = nullptr;     // feature rows (learned schedule)
+    int32_t *plan_ctr = nullptr;  // count, head, hist, cursor
 };
 
 struct blg_search {
@@ -225,6 +237,9 @@ static int pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const 
         p->cap[j] = above;
         total += above;
     }
+    // scheduled classes: 0 = one word (any pair), 1..5 = the lane classes
+    p->pcap[0] = n;
+    for (int j = 0; j < kLongClasses; j++) p->pcap[j + 1] = p->cap[j];
     if (total > 0) {
         CK(dev_alloc(c, &p->q_items, sizeof(LongItem) * (size_t)total), "cudaMallocAsync(queue)");
         CK(dev_alloc(c, (void **)&p->q_ctr, sizeof(int32_t) * 2 * kLongClasses), "cudaMallocAsync(ctr)");
@@ -232,10 +247,70 @@ static int pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const 
     return BLG_OK;
 }
 
-static int pairs_run(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out) {
+constexpr size_t kPlanCounters = 2 * kPairClasses + 2 * kPairClasses * kCostBuckets;
+
+static int plan_alloc(blg_ctx *c, blg_pairs *p, bool feat) {
+    int64_t slots = 0;
+    for (int j = 0; j < kPairClasses; j++) slots += p->pcap[j];
+    if (!p->plan_mem) {
+        CK(dev_alloc(c, &p->plan_mem, (size_t)slots * (2 * sizeof(LongItem) + 1) + 64), "cudaMallocAsync(plan)");
+        CK(dev_alloc(c, (void **)&p->plan_ctr, sizeof(int32_t) * kPlanCounters), "cudaMallocAsync(plan ctr)");
+    }
+    if (feat && !p->feat_mem)
+        CK(dev_alloc(c, (void **)&p->feat_mem, sizeof(half) * kFeatures * (size_t)slots + 16), "cudaMallocAsync(features)");
+    return BLG_OK;
+}
+
+static PairsPlan plan_view(blg_pairs *p) {
+    PairsPlan pl{};
+    int64_t slots = 0;
+    for (int j = 0; j < kPairClasses; j++) slots += p->pcap[j];
+    LongItem *raw = (LongItem *)p->plan_mem, *sorted = raw + slots;
+    uint8_t *key = (uint8_t *)(sorted + slots);
+    int64_t off = 0;
+    for (int j = 0; j < kPairClasses; j++) {
+        pl.raw[j] = raw + off;
+        pl.sorted[j] = sorted + off;
+        pl.key[j] = key + off;
+        pl.feat[j] = p->feat_mem ? p->feat_mem + off * kFeatures : nullptr;
+        pl.cap[j] = p->pcap[j];
+        off += p->pcap[j];
+    }
+    pl.count = p->plan_ctr;
+    pl.head = p->plan_ctr + kPairClasses;
+    pl.hist = p->plan_ctr + 2 * kPairClasses;
+    pl.cursor = pl.hist + kPairClasses * kCostBuckets;
+    return pl;
+}
+
+// prep -> order -> solve (every schedule but PLAIN). exit_log (optional,
+// device int32[n]) receives the columns each pair's column loop processed.
+static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, int32_t *exit_log) {
+    const bool hask = k >= 0;
+    int rc = plan_alloc(c, p, false);
+    if (rc) return rc;
+    const PairsPlan plan = plan_view(p);
+    CK(cudaMemsetAsync(p->plan_ctr, 0, sizeof(int32_t) * kPlanCounters, c->stream), "reset plan");
+    if (exit_log) CK(cudaMemsetAsync(exit_log, 0, sizeof(int32_t) * (size_t)p->n, c->stream), "reset log");
+    const int grid = (int)std::min<int64_t>((p->n + 255) / 256, (int64_t)c->sms * 8);
+    CK(launch(c, "pairs_prep", [&] {
+           return launch_pairs_prep(c->stream, grid, hask, false, p->a.d, p->b.d, k, dtype, d_out, plan,
+                                    c->d_status);
+       }), "pairs_prep");
+    CK(launch(c, "pairs_order", [&] { return launch_order(c->stream, c->sms, false, plan); }), "pairs_order");
+    bool any_long = false;
+    for (int j = 1; j < kPairClasses; j++) any_long |= p->pcap[j] > 0;
+    CK(launch(c, "pairs_solve", [&] {
+           return launch_solve(c->stream, c->sms, hask, plan, k, dtype, d_out, exit_log, any_long);
+       }), "pairs_solve");
+    return BLG_OK;
+}
+
+static int pairs_run(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, int32_t *exit_log = nullptr) {
     if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
     if (p->n == 0) return BLG_OK;
     if (!d_out) return fail(c, BLG_ERR_ARG, "null output");
+    if (c->sched != BLG_SCHED_PLAIN || exit_log) return pairs_run_scheduled(c, p, k, dtype, d_out, exit_log);
     const bool hask = k >= 0;
     LongQueue q{};
     int64_t total = 0;
@@ -267,6 +342,12 @@ static void pairs_release(blg_ctx *c, blg_pairs *p) {
     free_strings(c, p->b);
     dev_free(c, p->q_items);
     dev_free(c, p->q_ctr);
+    dev_free(c, p->plan_mem);
+    dev_free(c, p->plan_ctr);
+    dev_free(c, p->feat_mem);
+    p->plan_mem = nullptr;
+    p->plan_ctr = nullptr;
+    p->feat_mem = nullptr;
 }
 
 // ------------------------------------------------------------ search --
@@ -531,6 +612,13 @@ int blg_pairs_run(blg_ctx *c, blg_pairs *p, int32_t max_dist, int32_t dtype, voi
     ENTER(c);
     if (!p) return fail(c, BLG_ERR_ARG, "null pairs");
     return pairs_run(c, p, max_dist, dtype, d_out);
+}
+
+int blg_pairs_run_logged(blg_ctx *c, blg_pairs *p, int32_t max_dist, int32_t dtype, void *d_out,
+                         int32_t *d_exit_cols) {
+    ENTER(c);
+    if (!p || !d_exit_cols) return fail(c, BLG_ERR_ARG, "null pairs or log");
+    return pairs_run(c, p, max_dist, dtype, d_out, d_exit_cols);
 }
 
 void blg_pairs_free(blg_ctx *c, blg_pairs *p) {

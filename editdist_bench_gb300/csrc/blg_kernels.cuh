@@ -200,7 +200,8 @@ __device__ __forceinline__ int dist_seq_any(const uint64_t *peq, int m, const ui
 // group learns through __ballot_sync.
 template <bool HASK, typename EqFn>
 __device__ __forceinline__ int lane_wavefront(bool valid, int m, const uint8_t *txt, int n, int L,
-                                              int w, int g, int k, EqFn eqfn, bool &is_last) {
+                                              int w, int g, int k, EqFn eqfn, bool &is_last,
+                                              int *cols_out = nullptr) {
     const int W = valid ? (m + 63) >> 6 : 0;
     const bool own = valid && w < W;
     const int lastw = W - 1;
@@ -231,10 +232,14 @@ __device__ __forceinline__ int lane_wavefront(bool valid, int m, const uint8_t *
         if (HASK) {
             const bool ex = act && is_last && hopeless(score, j, n, k);
             const unsigned bal = __ballot_sync(kFull, ex);
-            if (valid && ((bal >> (g * L + lastw)) & 1u)) done = true;
+            if (valid && ((bal >> (g * L + lastw)) & 1u)) {
+                if (!done && cols_out) *cols_out = s - lastw + 1;   // columns the last word processed
+                done = true;
+            }
         }
     }
     if (done) return k + 1;
+    if (cols_out) *cols_out = n;
     return HASK ? cap_k(score, k) : score;
 }
 
@@ -308,7 +313,7 @@ __device__ __forceinline__ void nib_clear(uint64_t *tc, const uint8_t *p, int m)
 // Single-word pair (1 <= m <= 64, m <= n): pattern p, text t.
 template <bool HASK>
 __device__ __forceinline__ int solve_word(uint64_t *tc, const uint8_t *p, int m, const uint8_t *t,
-                                          int n, int k) {
+                                          int n, int k, int *cols_out = nullptr) {
     nib_build(tc, p, m);
     uint64_t pv = ~0ull, mv = 0;
     const int lastbit = m - 1;
@@ -325,7 +330,11 @@ __device__ __forceinline__ int solve_word(uint64_t *tc, const uint8_t *p, int m,
             step_top<uint64_t>(pv, mv, nib_eq(tc, (w4 >> (8 * b)) & 0xffu), ph, mh);
             score += hdelta<uint64_t>(ph, mh, lastbit);
         }
-        if (HASK && hopeless(score, j + 3, n, k)) { dead = true; break; }
+        if (HASK && hopeless(score, j + 3, n, k)) {
+            dead = true;
+            if (cols_out) *cols_out = j + 4;
+            break;
+        }
     }
     if (!dead && j < n) {
         uint32_t w4 = ts.next4();
@@ -337,6 +346,7 @@ __device__ __forceinline__ int solve_word(uint64_t *tc, const uint8_t *p, int m,
     }
     nib_clear(tc, p, m);
     if (dead) return k + 1;
+    if (cols_out) *cols_out = n;
     return HASK ? cap_k(score, k) : score;
 }
 

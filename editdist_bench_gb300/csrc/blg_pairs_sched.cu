@@ -1,0 +1,288 @@
+// Scheduled pairwise path: prep -> order -> solve.
+//
+// One thread per pair in natural order (the reference's schedule,
+// csrc/gpu_kernels.cu:6-32) leaves most lanes of a warp idle: after exact
+// trimming the remaining work of neighbouring pairs differs by an order of
+// magnitude (trimmed lengths, max_dist exits). Here
+//   1. k_pairs_prep trims every pair, finishes the trivial ones (length gap
+//      beyond k, empty pattern) and writes the rest as 32-byte work records
+//      into per-class regions (class 0: pattern <= 64, one thread; classes
+//      1..5: 2..32 lanes), each with a cost key and, for the learned
+//      schedule, a feature row;
+//   2. k_order_hist / k_order_scan / k_order_scatter counting-sort every
+//      class by cost key, largest cost first;
+//   3. k_solve_word / k_solve_lanes consume the sorted records from device
+//      work counters, so a warp takes pairs of similar cost.
+// Which pairs are computed and their values never change: only the order.
+#include "blg_kernels.cuh"
+#include "blg_sched.h"
+
+namespace blg {
+
+// Cost bucket of an estimated work amount (columns x words), log-spaced so
+// 256 buckets cover 1 .. 2^32.
+__device__ __forceinline__ int cost_bucket(float work) {
+    if (work < 1.f) return 0;
+    const int b = (int)(__log2f(work) * 8.f) + 1;
+    return b > kCostBuckets - 1 ? kCostBuckets - 1 : b;
+}
+
+// Features of one trimmed pair (pattern p of m, text t of n; la, lb
+// untrimmed): lengths, trimmed lengths, length gap, k, and the q-gram lower
+// bound sum|h_p - h_t| / (2q) over 4-grams hashed into 32 bins (each edit
+// changes at most 4 4-grams of each string, so the bound holds for any
+// binning). `hist` is this thread's 32-byte scratch in shared memory.
+__device__ __forceinline__ float qgram_bound(const uint8_t *p, int m, const uint8_t *t, int n, int8_t *hist) {
+#pragma unroll
+    for (int i = 0; i < 32; i++) hist[i] = 0;
+    int overflow = 0;
+    uint32_t h = 0;
+    for (int i = 0; i < m; i++) {
+        h = (h << 8) | p[i];
+        if (i >= 3) {
+            const int bin = (int)((h * 0x9E3779B1u) >> 27);
+            const int v = hist[bin] + 1;
+            if (v > 127) overflow = 1; else hist[bin] = (int8_t)v;
+        }
+    }
+    h = 0;
+    for (int i = 0; i < n; i++) {
+        h = (h << 8) | t[i];
+        if (i >= 3) {
+            const int bin = (int)((h * 0x9E3779B1u) >> 27);
+            const int v = hist[bin] - 1;
+            if (v < -127) overflow = 1; else hist[bin] = (int8_t)v;
+        }
+    }
+    int l1 = 0;
+#pragma unroll
+    for (int i = 0; i < 32; i++) l1 += hist[i] < 0 ? -hist[i] : hist[i];
+    if (overflow) return 0.f;              // saturated counters: report no bound
+    return l1 * 0.125f;
+}
+
+template <bool HASK, bool FEAT>
+__global__ void __launch_bounds__(256) k_pairs_prep(DevStrings A, DevStrings B, int k, int dtype, void *out,
+                                                    PairsPlan plan, uint32_t *status) {
+    __shared__ int s_hist[kPairClasses * kCostBuckets];
+    __shared__ int8_t s_qg[FEAT ? 256 * 32 : 1];
+    for (int x = threadIdx.x; x < kPairClasses * kCostBuckets; x += blockDim.x) s_hist[x] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t n = A.n;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // whole warps iterate together so the slot claim below can be warp-aggregated
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+        const int64_t i = base + lane;
+        int cls = -1, la = 0, lb = 0, la0 = 0, lb0 = 0;
+        const uint8_t *a = nullptr, *b = nullptr;
+        if (i < n) {
+            a = string_at(A, i, la, status);
+            b = string_at(B, i, lb, status);
+            la0 = la;
+            lb0 = lb;
+            trim_windows(a, la, b, lb);
+            if (la > lb) {
+                const uint8_t *t = a; a = b; b = t;
+                const int x = la; la = lb; lb = x;
+            }
+            const int W = (la + 63) >> 6;
+            if (HASK && lb - la > k) store1(out, dtype, i, k + 1);          // length gap alone exceeds k
+            else if (la == 0) store1(out, dtype, i, lb);
+            else if (W > 32) { atomicOr(status, ST_TOO_LONG); store1(out, dtype, i, -1); }
+            else cls = W <= 1 ? 0 : W <= 2 ? 1 : W <= 4 ? 2 : W <= 8 ? 3 : W <= 16 ? 4 : 5;
+        }
+        // claim record slots: one atomic per class present in the warp
+        const unsigned peers = __match_any_sync(kFull, cls);
+        const int leader = __ffs(peers) - 1;
+        int pos = 0;
+        if (cls >= 0 && lane == leader) pos = atomicAdd(&plan.count[cls], __popc(peers));
+        pos = __shfl_sync(kFull, pos, leader) + __popc(peers & ((1u << lane) - 1));
+        if (cls < 0) continue;
+        if (pos >= plan.cap[cls]) { atomicOr(status, ST_QUEUE_OVERFLOW); store1(out, dtype, i, -1); continue; }
+        LongItem it;
+        it.pat = a; it.txt = b; it.m = la; it.n = lb; it.idx = i;
+        plan.raw[cls][pos] = it;
+        int key = cost_bucket((float)lb * (float)((la + 63) >> 6));
+        if (FEAT) {
+            const float qb = qgram_bound(a, la, b, lb, s_qg + threadIdx.x * 32);
+            half *f = plan.feat[cls] + (size_t)pos * kFeatures;
+            f[0] = __float2half((float)la * (1.f / 256.f));
+            f[1] = __float2half((float)lb * (1.f / 256.f));
+            f[2] = __float2half((float)la0 * (1.f / 256.f));
+            f[3] = __float2half((float)lb0 * (1.f / 256.f));
+            f[4] = __float2half((float)(lb - la) * (1.f / 16.f));
+            f[5] = __float2half(qb * (1.f / 16.f));
+            f[6] = __float2half(HASK ? (float)k * (1.f / 16.f) : 16.f);
+            key = 0;                       // the network's prediction sets the key later
+        }
+        plan.key[cls][pos] = (uint8_t)key;
+        if (!FEAT) atomicAdd(&s_hist[cls * kCostBuckets + key], 1);
+    }
+    __syncthreads();
+    if (!FEAT)
+        for (int x = threadIdx.x; x < kPairClasses * kCostBuckets; x += blockDim.x)
+            if (s_hist[x]) atomicAdd(&plan.hist[x], s_hist[x]);
+}
+
+// Histogram of keys already written (learned schedule: keys come from the network).
+__global__ void __launch_bounds__(256) k_order_hist(PairsPlan plan) {
+    __shared__ int s_hist[kCostBuckets];
+    for (int cls = 0; cls < kPairClasses; cls++) {
+        for (int x = threadIdx.x; x < kCostBuckets; x += blockDim.x) s_hist[x] = 0;
+        __syncthreads();
+        const int cnt = min(plan.count[cls], (int)plan.cap[cls]);
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+            atomicAdd(&s_hist[plan.key[cls][i]], 1);
+        __syncthreads();
+        for (int x = threadIdx.x; x < kCostBuckets; x += blockDim.x)
+            if (s_hist[x]) atomicAdd(&plan.hist[cls * kCostBuckets + x], s_hist[x]);
+        __syncthreads();
+    }
+}
+
+// Bucket starts, largest key first: start[cls][b] = sum of counts of keys > b.
+__global__ void __launch_bounds__(kCostBuckets) k_order_scan(PairsPlan plan) {
+    __shared__ int s[kCostBuckets];
+    for (int cls = 0; cls < kPairClasses; cls++) {
+        const int b = threadIdx.x;
+        s[kCostBuckets - 1 - b] = plan.hist[cls * kCostBuckets + b];     // reversed
+        __syncthreads();
+        for (int off = 1; off < kCostBuckets; off <<= 1) {
+            const int v = b >= off ? s[b - off] : 0;
+            __syncthreads();
+            s[b] += v;
+            __syncthreads();
+        }
+        // inclusive scan over reversed buckets; exclusive start of bucket b:
+        const int r = kCostBuckets - 1 - b;
+        plan.cursor[cls * kCostBuckets + b] = s[r] - plan.hist[cls * kCostBuckets + b];
+        __syncthreads();
+    }
+}
+
+// Scatter records to their sorted slots (order inside a bucket is free).
+// Lanes with equal keys share one atomic (warp-aggregated).
+__global__ void __launch_bounds__(256) k_order_scatter(PairsPlan plan) {
+    const int lane = threadIdx.x & 31;
+    for (int cls = 0; cls < kPairClasses; cls++) {
+        const int cnt = min(plan.count[cls], (int)plan.cap[cls]);
+        const int stride = gridDim.x * blockDim.x;
+        for (int base = blockIdx.x * blockDim.x; base < cnt; base += stride) {
+            const int i = base + threadIdx.x;
+            const bool valid = i < cnt;
+            const int key = valid ? plan.key[cls][i] : -1 - lane;          // distinct for idle lanes
+            const unsigned peers = __match_any_sync(kFull, key);
+            const int leader = __ffs(peers) - 1;
+            const int rank = __popc(peers & ((1u << lane) - 1));
+            int start = 0;
+            if (valid && lane == leader) start = atomicAdd(&plan.cursor[cls * kCostBuckets + key], __popc(peers));
+            start = __shfl_sync(kFull, start, leader);
+            if (valid) plan.sorted[cls][start + rank] = plan.raw[cls][i];
+        }
+    }
+}
+
+// Class 0: one thread per record (pattern <= 64), records in sorted order.
+template <bool HASK>
+__global__ void __launch_bounds__(256) k_solve_word(PairsPlan plan, int k, int dtype, void *out,
+                                                    int32_t *exit_log) {
+    extern __shared__ uint64_t s_tab[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t *tc = s_tab + warp * 1024 + lane;
+#pragma unroll
+    for (int r = 0; r < 32; r++) tc[r * 32] = 0;
+    const int cnt = min(plan.count[0], (int)plan.cap[0]);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+        const LongItem it = plan.sorted[0][i];
+        int cols = 0;
+        const int d = solve_word<HASK>(tc, it.pat, it.m, it.txt, it.n, k, exit_log ? &cols : nullptr);
+        store1(out, dtype, it.idx, d);
+        if (exit_log) exit_log[it.idx] = cols;
+    }
+}
+
+// Classes 1..5: lane-spread, pulling 32/L records at a time from the class's counter.
+template <bool HASK>
+__global__ void __launch_bounds__(256) k_solve_lanes(PairsPlan plan, int k, int dtype, void *out,
+                                                     int32_t *exit_log) {
+    extern __shared__ uint64_t s_tab[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t *tc = s_tab + warp * 1024 + lane;
+#pragma unroll
+    for (int r = 0; r < 32; r++) tc[r * 32] = 0;
+    for (int cls = 1; cls < kPairClasses; cls++) {
+        const int L = 1 << cls, G = 32 / L, g = lane / L, w = lane & (L - 1);
+        const int count = min(plan.count[cls], (int)plan.cap[cls]);
+        if (count == 0) continue;
+        while (true) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&plan.head[cls], G);
+            base = __shfl_sync(kFull, base, 0);
+            if (base >= count) break;
+            const int it_i = base + g;
+            const bool valid = it_i < count;
+            LongItem it;
+            if (valid) it = plan.sorted[cls][it_i];
+            else { it.pat = nullptr; it.txt = nullptr; it.m = 0; it.n = 0; it.idx = 0; }
+            const bool own = valid && w < ((it.m + 63) >> 6);
+            const uint8_t *pw = own ? it.pat + 64 * w : nullptr;
+            const int plen = own ? min(64, it.m - 64 * w) : 0;
+            if (own) nib_build(tc, pw, plen);
+            bool is_last = false;
+            int cols = 0;
+            const int d = lane_wavefront<HASK>(valid, it.m, it.txt, it.n, L, w, g, k,
+                                               [&](uint32_t ch) { return nib_eq(tc, ch); }, is_last,
+                                               exit_log ? &cols : nullptr);
+            if (own) nib_clear(tc, pw, plen);
+            if (is_last) {
+                store1(out, dtype, it.idx, d);
+                if (exit_log) exit_log[it.idx] = cols;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------- launchers --
+cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, const DevStrings &A,
+                              const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
+                              uint32_t *status) {
+    if (hask) {
+        if (feat) k_pairs_prep<true, true><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, status);
+        else k_pairs_prep<true, false><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, status);
+    } else {
+        if (feat) k_pairs_prep<false, true><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, status);
+        else k_pairs_prep<false, false><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, status);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_order(cudaStream_t st, int sms, bool need_hist, const PairsPlan &plan) {
+    if (need_hist) k_order_hist<<<sms * 2, 256, 0, st>>>(plan);
+    k_order_scan<<<1, kCostBuckets, 0, st>>>(plan);
+    k_order_scatter<<<sms * 4, 256, 0, st>>>(plan);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve(cudaStream_t st, int sms, bool hask, const PairsPlan &plan, int k, int dtype,
+                         void *out, int32_t *exit_log, bool any_long) {
+    const size_t smem = 8 * 1024 * sizeof(uint64_t);
+    if (hask) {
+        cudaFuncSetAttribute(k_solve_word<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_solve_word<true><<<sms * 3 * 4, 256, smem, st>>>(plan, k, dtype, out, exit_log);
+        if (any_long) {
+            cudaFuncSetAttribute(k_solve_lanes<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_solve_lanes<true><<<sms * 3, 256, smem, st>>>(plan, k, dtype, out, exit_log);
+        }
+    } else {
+        cudaFuncSetAttribute(k_solve_word<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_solve_word<false><<<sms * 3 * 4, 256, smem, st>>>(plan, k, dtype, out, exit_log);
+        if (any_long) {
+            cudaFuncSetAttribute(k_solve_lanes<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_solve_lanes<false><<<sms * 3, 256, smem, st>>>(plan, k, dtype, out, exit_log);
+        }
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace blg

@@ -84,6 +84,12 @@ int blg_pairs_upload(blg_ctx *ctx, const uint8_t *buf_a, const int64_t *off_a, c
                      const int64_t *off_b, int64_t n, blg_pairs **out);
 int blg_pairs_run(blg_ctx *ctx, blg_pairs *p, int32_t max_dist, int32_t dtype, void *d_out);
 void blg_pairs_free(blg_ctx *ctx, blg_pairs *p);
+/* blg_pairs_run that also records, per pair, how many text columns its
+ * column loop processed before the max_dist exit fired (0 for pairs settled
+ * by the length gap or an empty pattern; the text length when no exit) —
+ * the labels the work-order scheduler is trained on. d_exit_cols: int32[n]. */
+int blg_pairs_run_logged(blg_ctx *ctx, blg_pairs *p, int32_t max_dist, int32_t dtype, void *d_out,
+                         int32_t *d_exit_cols);
 
 /* Resident search (bench/cudamyers.py:139-174, CrossState + cross()):
  * d_out holds nq*nc elements of dtype, row-major. */

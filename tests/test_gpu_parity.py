@@ -256,3 +256,44 @@ def test_thresholded_search_resident_repeat(gpu):
     for k, dt in ((4, "uint8"), (0, "uint8"), (12, "int32"), (4, "uint8")):
         out = s.run(s.alloc(dt), max_dist=k).get()
         np.testing.assert_array_equal(out, oracle.saturate(oracle.cross(q, c, k), dt))
+
+
+@pytest.mark.parametrize("sched", ["auto", "plain"])
+def test_pairs_schedules(gpu, sched):
+    rng = np.random.default_rng(77)
+    alph = np.frombuffer(b"ACGTN", dtype=np.uint8)
+    a = W.concat(W.random_strings(rng, rng.integers(0, 400, 6000), alph),
+                 W.random_strings(rng, [0, 1, 64, 65, 128, 129, 2048], alph))
+    b = W.mutate(rng, a, rng.uniform(0, 0.3, len(a[1]) - 1), alph)
+    gpu.set_schedule(sched)
+    try:
+        for k, dt in ((None, "int32"), (0, "uint8"), (8, "uint8"), (30, "uint16"), (500, "int32")):
+            got = gpu.pairwise_packed(a, b, max_dist=k, dtype=dt)
+            np.testing.assert_array_equal(got, oracle.saturate(oracle.pairs(a, b, k), dt),
+                                          err_msg=f"{sched} k={k}")
+    finally:
+        gpu.set_schedule("auto")
+
+
+def test_pairs_exit_column_log(gpu):
+    """The logged column counts: 0 for pairs settled by the length gap or an
+    empty pattern, the trimmed text length without an exit, and never fewer
+    columns than the reference's exit rule needs."""
+    import ctypes
+    from editdist_bench_gb300 import _lib
+    rng = np.random.default_rng(5)
+    a = W.random_strings(rng, rng.integers(0, 300, 4000))
+    b = W.mutate(rng, a, rng.uniform(0, 0.3, 4000))
+    batch = gpu.PairsBatch(a, b)
+    ctx = _lib.context()
+    for k in (None, 6):
+        out = batch.alloc("int32")
+        log = batch.alloc("int32")
+        ctx.check(ctx.lib.blg_pairs_run_logged(ctx.h, batch.h, -1 if k is None else k, 0, out.ptr, log.ptr))
+        cols = log.get()
+        d, m_, n_, ocols = oracle.pairs_trace(a, b, k)
+        np.testing.assert_array_equal(out.get(), d)
+        assert (cols <= n_).all() and (cols >= ocols).all()
+        assert (cols[ocols == 0] == 0).all() or k is None
+        if k is None:
+            np.testing.assert_array_equal(cols[m_ > 0], n_[m_ > 0])
