@@ -349,6 +349,25 @@ def read_traffic(kernel: str, workload: str):
     return None
 
 
+def train_scheduler(ctx, args) -> dict:
+    """Train the work-order network on 2^20 pairs of the same workload shape
+    drawn with a different seed (2000 + config), outside the timed region."""
+    gen = {1: W.config1, 3: W.config3}.get(args.config)
+    if gen is None:
+        return {"trained": False, "why": "the learned order applies to pairwise workloads"}
+    t0 = time.perf_counter()
+    w = gen(n=1 << 20, seed=2000 + args.config)
+    batch = gpu.PairsBatch(w.a, w.b)
+    t1 = time.perf_counter()
+    loss = ctypes.c_float()
+    k = -1 if w.max_dist is None else w.max_dist
+    ctx.check(ctx.lib.blg_sched_train(ctx.h, batch.h, k, args.epochs, ctypes.c_float(args.lr), 1 << 20,
+                                      ctypes.byref(loss)))
+    t2 = time.perf_counter()
+    return {"trained": True, "rows_max": 1 << 20, "seed": 2000 + args.config, "epochs": args.epochs,
+            "lr": args.lr, "final_mse": loss.value, "train_s": t2 - t1, "data_s": t1 - t0}
+
+
 # ------------------------------------------------------------------ arms --
 def run_ours(args, ranks: Ranks):
     ctx = _lib.context()
@@ -368,6 +387,9 @@ def run_ours(args, ranks: Ranks):
             times.append(stop())
         return times
 
+    sched_info = None
+    if args.schedule == "learned":
+        sched_info = train_scheduler(ctx, args)
     for i in range(len(bench.runs)):          # warm-up every run variant
         for _ in range(args.warmup):
             bench.step(i)
@@ -434,7 +456,7 @@ def run_ours(args, ranks: Ranks):
         "e2e": {"value": bench.pairs * ranks.world / e2e_s, "unit": "pairs/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "blg_cdist/blg_pairwise C-ABI, pageable host buffers, wall clock"},
-        "gpu_launches": int(launches), "wall_s_timed_region": wall,
+        "gpu_launches": int(launches), "wall_s_timed_region": wall, "scheduler": sched_info,
         "clocks": clk, "runs": extra_runs, "kernels": kstats,
     }
     if args.config in H100_REF:
@@ -534,6 +556,8 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="override the pair count (profiling)")
     ap.add_argument("--schedule", default="auto", choices=["auto", "plain", "learned", "lensort"],
                     help="work order of max_dist runs (results are identical)")
+    ap.add_argument("--epochs", type=int, default=10, help="scheduler training epochs (learned)")
+    ap.add_argument("--lr", type=float, default=0.02, help="scheduler learning rate (learned)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

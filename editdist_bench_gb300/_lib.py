@@ -37,6 +37,13 @@ SIGNATURES = [
     ("blg_search_run", ctypes.c_int, [_P, _P, _I32, _I32, _P]),
     ("blg_search_free", None, [_P, _P]),
     ("blg_cdist_noalloc", ctypes.c_int, [_P, _P, _SZ, _P, _I64, _P, _SZ, _P, _I64, _I32, _I32, _P]),
+    ("blg_sched_train", ctypes.c_int, [_P, _P, _I32, _I32, ctypes.c_float, _I64, ctypes.POINTER(ctypes.c_float)]),
+    ("blg_sched_set_weights", ctypes.c_int, [_P, _P, ctypes.c_int]),
+    ("blg_sched_get_weights", ctypes.c_int, [_P, _P, ctypes.c_int]),
+    ("blg_sched_gradient", ctypes.c_int, [_P, _P, _P, ctypes.c_int, _P, ctypes.POINTER(ctypes.c_float)]),
+    ("blg_sched_predict", ctypes.c_int, [_P, _P, _I64, _P]),
+    ("blg_sched_save", ctypes.c_int, [_P, ctypes.c_char_p]),
+    ("blg_sched_load", ctypes.c_int, [_P, ctypes.c_char_p]),
     ("blg_malloc", ctypes.c_int, [_P, _SZ, ctypes.POINTER(_P)]),
     ("blg_free", ctypes.c_int, [_P, _P]),
     ("blg_memcpy_h2d", ctypes.c_int, [_P, _P, _P, _SZ]),

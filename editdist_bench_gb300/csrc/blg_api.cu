@@ -42,6 +42,15 @@ cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, c
 cudaError_t launch_order(cudaStream_t st, int sms, bool need_hist, const PairsPlan &plan);
 cudaError_t launch_solve(cudaStream_t st, int sms, bool hask, const PairsPlan &plan, int k, int dtype,
                          void *out, int32_t *exit_log, bool any_long);
+}  // namespace blg
+int sched_model_ensure(blg_ctx *c, blg_sched_model **out);
+cudaError_t launch_mlp_keys(cudaStream_t st, int sms, const blg_sched_model *m, const blg::PairsPlan &plan);
+cudaError_t launch_collect_rows(cudaStream_t st, int sms, const blg::PairsPlan &plan, const int32_t *cols,
+                                int64_t stride, int64_t max_rows, half *x, float *y, int64_t *n_rows);
+int sched_train_rows(blg_ctx *c, blg_sched_model *m, half *x, float *y, const int64_t *d_rows, int64_t rows,
+                     int epochs, float lr, int batch, float *loss_out);
+bool sched_model_trained(const blg_sched_model *m);
+namespace blg {
 cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &src, const int32_t *perm,
                                   const int64_t *dst_off, uint8_t *dst, int64_t n, uint32_t *status);
 cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
@@ -117,11 +126,6 @@ int cuda_fail(blg_ctx *c, cudaError_t e, const char *what) {
     return fail(c, BLG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define CK(call, what)                                   \
-    do {                                                 \
-        cudaError_t e_ = (call);                         \
-        if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
-    } while (0)
 
 template <typename F>
 static cudaError_t launch(blg_ctx *c, const char *name, F &&fn) {
@@ -285,19 +289,24 @@ static PairsPlan plan_view(blg_pairs *p) {
 
 // prep -> order -> solve (every schedule but PLAIN). exit_log (optional,
 // device int32[n]) receives the columns each pair's column loop processed.
-static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, int32_t *exit_log) {
+static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, int32_t *exit_log,
+                               bool want_features = false) {
     const bool hask = k >= 0;
-    int rc = plan_alloc(c, p, false);
+    // the learned order needs a trained network; otherwise cost buckets order the work
+    const bool learned = want_features || (c->sched == BLG_SCHED_LEARNED && c->model && sched_model_trained(c->model));
+    int rc = plan_alloc(c, p, learned);
     if (rc) return rc;
     const PairsPlan plan = plan_view(p);
     CK(cudaMemsetAsync(p->plan_ctr, 0, sizeof(int32_t) * kPlanCounters, c->stream), "reset plan");
     if (exit_log) CK(cudaMemsetAsync(exit_log, 0, sizeof(int32_t) * (size_t)p->n, c->stream), "reset log");
     const int grid = (int)std::min<int64_t>((p->n + 255) / 256, (int64_t)c->sms * 8);
     CK(launch(c, "pairs_prep", [&] {
-           return launch_pairs_prep(c->stream, grid, hask, false, p->a.d, p->b.d, k, dtype, d_out, plan,
+           return launch_pairs_prep(c->stream, grid, hask, learned, p->a.d, p->b.d, k, dtype, d_out, plan,
                                     c->d_status);
        }), "pairs_prep");
-    CK(launch(c, "pairs_order", [&] { return launch_order(c->stream, c->sms, false, plan); }), "pairs_order");
+    if (learned && !want_features)
+        CK(launch(c, "sched_keys", [&] { return launch_mlp_keys(c->stream, c->sms, c->model, plan); }), "sched_keys");
+    CK(launch(c, "pairs_order", [&] { return launch_order(c->stream, c->sms, learned, plan); }), "pairs_order");
     bool any_long = false;
     for (int j = 1; j < kPairClasses; j++) any_long |= p->pcap[j] > 0;
     CK(launch(c, "pairs_solve", [&] {
@@ -577,6 +586,8 @@ void blg_destroy(blg_ctx *c) {
         cudaEventDestroy(r.e0);
         cudaEventDestroy(r.e1);
     }
+    sched_model_free(c->model);
+    c->model = nullptr;
     if (c->d_status) cudaFree(c->d_status);
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
@@ -619,6 +630,53 @@ int blg_pairs_run_logged(blg_ctx *c, blg_pairs *p, int32_t max_dist, int32_t dty
     ENTER(c);
     if (!p || !d_exit_cols) return fail(c, BLG_ERR_ARG, "null pairs or log");
     return pairs_run(c, p, max_dist, dtype, d_out, d_exit_cols);
+}
+
+int blg_sched_train(blg_ctx *c, blg_pairs *p, int32_t max_dist, int32_t epochs, float lr, int64_t max_rows,
+                    float *loss_out) {
+    ENTER(c);
+    if (!p || p->n == 0) return fail(c, BLG_ERR_ARG, "empty training batch");
+    if (epochs < 0 || max_rows <= 0 || !(lr > 0.f)) return fail(c, BLG_ERR_ARG, "bad training arguments");
+    blg_sched_model *m = nullptr;
+    int rc = sched_model_ensure(c, &m);
+    if (rc) return rc;
+    // 1. a logged run with features: labels = columns each pair's loop processed
+    void *out = nullptr, *cols = nullptr, *x = nullptr, *y = nullptr, *nrows = nullptr;
+    CK(dev_alloc(c, &out, sizeof(int32_t) * (size_t)p->n), "alloc");
+    CK(dev_alloc(c, &cols, sizeof(int32_t) * (size_t)p->n), "alloc");
+    rc = pairs_run_scheduled(c, p, max_dist, BLG_INT32, out, (int32_t *)cols, true);
+    if (rc) return rc;
+    // 2. rows (subsampled to at most max_rows)
+    int64_t records = 0;
+    for (int j = 0; j < kPairClasses; j++) records += p->pcap[j];
+    int32_t counts[kPairClasses];
+    CK(cudaMemcpyAsync(counts, p->plan_ctr, sizeof(counts), cudaMemcpyDeviceToHost, c->stream), "D2H counts");
+    CK(cudaStreamSynchronize(c->stream), "sync");
+    records = 0;
+    for (int j = 0; j < kPairClasses; j++) records += std::min<int64_t>(counts[j], p->pcap[j]);
+    const int64_t stride = std::max<int64_t>(1, (records + max_rows - 1) / max_rows);
+    CK(dev_alloc(c, &x, sizeof(half) * kFeatures * (size_t)max_rows + 16), "alloc");
+    CK(dev_alloc(c, &y, sizeof(float) * (size_t)max_rows + 16), "alloc");
+    CK(dev_alloc(c, &nrows, sizeof(int64_t)), "alloc");
+    const PairsPlan plan = plan_view(p);
+    CK(launch(c, "collect_rows", [&] {
+           return launch_collect_rows(c->stream, c->sms, plan, (const int32_t *)cols, stride, max_rows, (half *)x,
+                                      (float *)y, (int64_t *)nrows);
+       }), "collect_rows");
+    int64_t rows = 0;
+    CK(cudaMemcpyAsync(&rows, nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream), "D2H rows");
+    CK(cudaStreamSynchronize(c->stream), "sync");
+    // 3. train
+    rc = rows > 0 ? sched_train_rows(c, m, (half *)x, (float *)y, (const int64_t *)nrows, rows, epochs, lr, 4096,
+                                     loss_out)
+                  : fail(c, BLG_ERR_ARG, "no non-trivial pairs to learn from");
+    dev_free(c, out);
+    dev_free(c, cols);
+    dev_free(c, x);
+    dev_free(c, y);
+    dev_free(c, nrows);
+    const int rc2 = sync_and_status(c);
+    return rc ? rc : rc2;
 }
 
 void blg_pairs_free(blg_ctx *c, blg_pairs *p) {

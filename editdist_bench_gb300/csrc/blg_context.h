@@ -7,6 +7,8 @@
 #include <string>
 #include <vector>
 
+struct blg_sched_model;   // the work-order scheduler network (blg_mlp.cu)
+
 struct blg_ctx {
     struct ProfRec {
         const char *name;
@@ -21,6 +23,7 @@ struct blg_ctx {
     std::string err;
     int64_t launches = 0;
     int sched = 0;                     // BLG_SCHED_* (work order of thresholded runs)
+    blg_sched_model *model = nullptr;  // trained/loaded scheduler network, if any
     bool prof = false;
     std::vector<ProfRec> prof_recs;
     std::map<std::string, std::pair<int64_t, double>> prof_acc;
@@ -32,3 +35,11 @@ int fail(blg_ctx *c, int code, const std::string &msg);
 int cuda_fail(blg_ctx *c, cudaError_t e, const char *what);
 // Synchronise the context stream, read and clear the kernels' status word.
 int sync_and_status(blg_ctx *c);
+void sched_model_free(blg_sched_model *m);
+
+// Return the mapped error from the enclosing function (its context is `c`).
+#define CK(call, what)                                        \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+    } while (0)

@@ -131,6 +131,29 @@ int blg_cdist_noalloc(blg_ctx *ctx, const uint8_t *d_buf_q, size_t q_bytes, cons
 #define BLG_SCHED_LENSORT 3
 int blg_set_schedule(blg_ctx *ctx, int mode);
 
+/* The work-order scheduler (BLG_SCHED_LEARNED): a 7 -> 32 -> 32 -> 1 MLP
+ * (FP16 weights, FP32 sums) that predicts the fraction of a pair's text its
+ * column loop processes before the max_dist exit. No counterpart in the
+ * reference. blg_sched_train runs a logged pass over the batch (features:
+ * trimmed and untrimmed lengths, length gap, max_dist, 4-gram lower bound;
+ * label: logged exit column / text length), keeps at most max_rows rows and
+ * trains the context's network for `epochs` epochs on the GPU (momentum
+ * SGD, minibatches of 4096, one epoch captured as a CUDA graph); *loss_out
+ * = last epoch's mean squared error. */
+int blg_sched_train(blg_ctx *ctx, blg_pairs *p, int32_t max_dist, int32_t epochs, float lr,
+                    int64_t max_rows, float *loss_out);
+/* 1345 FP32 master weights: W1[32][7], b1[32], W2[32][32], b2[32], W3[32], b3. */
+int blg_sched_set_weights(blg_ctx *ctx, const float *w, int n);
+int blg_sched_get_weights(blg_ctx *ctx, float *w, int n);
+/* Mean-squared-error gradient at the current weights over host rows
+ * (x: rows x 7 IEEE halves, y: targets) without updating the weights. */
+int blg_sched_gradient(blg_ctx *ctx, const uint16_t *x_half, const float *y, int rows, float *grad_out,
+                       float *loss_out);
+int blg_sched_predict(blg_ctx *ctx, const uint16_t *x_half, int64_t rows, float *out);
+/* Versioned checkpoint ("BLGMLP01", count, FP32 weights). */
+int blg_sched_save(blg_ctx *ctx, const char *path);
+int blg_sched_load(blg_ctx *ctx, const char *path);
+
 /* Device memory and stream helpers (the parts of CuPy bitlev.gpu used:
  * cp.empty / .get() / Device().synchronize(), bitlev/gpu.py:59-68,102). */
 int blg_malloc(blg_ctx *ctx, size_t bytes, void **d_ptr);

@@ -1,0 +1,110 @@
+"""The work-order scheduler network: its GPU gradient against a float64 CPU
+restatement, training on logged exit columns, and the learned schedule's
+results (identical to the oracle: the network only reorders work)."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from editdist_bench_gb300 import _lib, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+F, H = 7, 32
+P = H * F + H + H * H + H + H + 1     # 1345
+
+
+def _unpack(w):
+    o = 0
+    W1 = w[o:o + H * F].reshape(H, F); o += H * F
+    b1 = w[o:o + H]; o += H
+    W2 = w[o:o + H * H].reshape(H, H); o += H * H
+    b2 = w[o:o + H]; o += H
+    W3 = w[o:o + H]; o += H
+    b3 = w[o]
+    return W1, b1, W2, b2, W3, b3
+
+
+def cpu_grad(w16, x, y):
+    """Mean-squared-error gradient of the 7-32-32-1 ReLU MLP in float64, with
+    the FP16-rounded weights the GPU forward pass uses."""
+    W1, b1, W2, b2, W3, b3 = _unpack(w16.astype(np.float64))
+    x = x.astype(np.float64)
+    z1 = x @ W1.T + b1
+    h1 = np.maximum(z1, 0)
+    z2 = h1 @ W2.T + b2
+    h2 = np.maximum(z2, 0)
+    out = h2 @ W3 + b3
+    e = out - y
+    B = len(y)
+    d = 2 * e / B
+    dh2 = (d[:, None] * W3[None, :]) * (z2 > 0)
+    dh1 = (dh2 @ W2) * (z1 > 0)
+    g = np.concatenate([(dh1.T @ x).ravel(), dh1.sum(0), (dh2.T @ h1).ravel(), dh2.sum(0),
+                        (d[:, None] * h2).sum(0), [d.sum()]])
+    return g, float((e ** 2).mean())
+
+
+def _set(ctx, w):
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    ctx.check(ctx.lib.blg_sched_set_weights(ctx.h, w.ctypes.data, P))
+
+
+def test_gradient_matches_cpu(gpu):
+    ctx = _lib.context()
+    rng = np.random.default_rng(0)
+    w = (rng.standard_normal(P) * 0.3).astype(np.float32)
+    _set(ctx, w)
+    for rows in (1, 77, 128, 1000):
+        x = rng.uniform(0, 1.5, (rows, F)).astype(np.float16)
+        y = rng.uniform(0, 1, rows).astype(np.float32)
+        g = np.empty(P, dtype=np.float32)
+        loss = ctypes.c_float()
+        ctx.check(ctx.lib.blg_sched_gradient(ctx.h, x.ctypes.data, y.ctypes.data, rows, g.ctypes.data,
+                                             ctypes.byref(loss)))
+        want, wl = cpu_grad(w.astype(np.float16), x, y)
+        np.testing.assert_allclose(g, want, rtol=2e-3, atol=2e-5)
+        assert abs(loss.value - wl) <= 1e-3 * max(1.0, wl)
+    # predictions use the same FP16 weights
+    x = rng.uniform(0, 1, (513, F)).astype(np.float16)
+    pred = np.empty(513, dtype=np.float32)
+    ctx.check(ctx.lib.blg_sched_predict(ctx.h, x.ctypes.data, 513, pred.ctypes.data))
+    W1, b1, W2, b2, W3, b3 = _unpack(w.astype(np.float16).astype(np.float64))
+    ref = np.maximum(np.maximum(x.astype(np.float64) @ W1.T + b1, 0) @ W2.T + b2, 0) @ W3 + b3
+    np.testing.assert_allclose(pred, ref, rtol=1e-3, atol=1e-4)
+
+
+def test_training_learns_and_learned_schedule_is_exact(gpu, tmp_path):
+    ctx = _lib.context()
+    train = W.config3(n=1 << 16, seed=2003)
+    batch = gpu.PairsBatch(train.a, train.b)
+    losses = []
+    for epochs in (1, 8):
+        loss = ctypes.c_float()
+        ctx.check(ctx.lib.blg_sched_train(ctx.h, batch.h, 8, epochs, ctypes.c_float(0.02), 1 << 16,
+                                          ctypes.byref(loss)))
+        losses.append(loss.value)
+    assert np.isfinite(losses).all() and losses[1] < losses[0]
+    # checkpoint round trip
+    path = os.path.join(str(tmp_path), "sched.bin").encode()
+    w0 = np.empty(P, dtype=np.float32)
+    ctx.check(ctx.lib.blg_sched_get_weights(ctx.h, w0.ctypes.data, P))
+    ctx.check(ctx.lib.blg_sched_save(ctx.h, path))
+    _set(ctx, np.zeros(P, dtype=np.float32))
+    ctx.check(ctx.lib.blg_sched_load(ctx.h, path))
+    w1 = np.empty(P, dtype=np.float32)
+    ctx.check(ctx.lib.blg_sched_get_weights(ctx.h, w1.ctypes.data, P))
+    np.testing.assert_array_equal(w0, w1)
+    # the learned order computes exactly the same values
+    test = W.config3(n=20000, seed=1003)
+    gpu.set_schedule("learned")
+    try:
+        got = gpu.pairwise_packed(test.a, test.b, max_dist=8, dtype="uint8")
+        for k in (None, 0, 3):
+            np.testing.assert_array_equal(gpu.pairwise_packed(test.a, test.b, max_dist=k),
+                                          oracle.pairs(test.a, test.b, k))
+    finally:
+        gpu.set_schedule("auto")
+    np.testing.assert_array_equal(got, oracle.saturate(oracle.pairs(test.a, test.b, 8), "uint8"))
