@@ -303,6 +303,67 @@ class PairsBench:
         return bool(np.array_equal(got, oracle.saturate(res, self.w.dtype)))
 
 
+class BatchBench:
+    """The mixed many-problem batch: one step = one replay of the batch's graph."""
+    kind = "batch"
+
+    def __init__(self, probs):
+        self.probs = probs
+        self.runs = [("mixed", "mixed")]
+        self.batch = gpu.ProblemBatch([(p.q, p.c, p.max_dist, p.dtype) for p in probs])
+        self.pairs = self.batch.pairs
+        self.cells = sum(W.cross_cells(p.q, p.c) for p in probs)
+        self.outs = self.batch.outputs
+        self.w = type("Batch", (), {"name": "cdist-batch-256-mixed"})()
+        self._structs = None
+
+    def step(self, i=0):
+        self.batch.run()
+
+    def e2e_call(self, i=0):
+        """Host inputs -> one-call C-ABI (upload, graph, sync) into the device outputs."""
+        ctx = _lib.context()
+        if self._structs is None:
+            s = [_lib.Problem(p.q[0].ctypes.data, p.q[1].ctypes.data, p.nq, p.c[0].ctypes.data, p.c[1].ctypes.data,
+                              p.nc, -1 if p.max_dist is None else p.max_dist,
+                              {"int32": 0, "uint16": 1, "uint8": 2}[p.dtype], o.ptr)
+                 for p, o in zip(self.probs, self.outs)]
+            self._structs = (_lib.Problem * len(s))(*s)
+        ctx.check(ctx.lib.blg_cdist_batch(ctx.h, self._structs, len(self.probs)))
+
+    def io_bytes(self, i=0):
+        h2d = sum(int(p.q[1][-1]) + p.q[1].nbytes + int(p.c[1][-1]) + p.c[1].nbytes for p in self.probs)
+        return h2d, 4          # results stay on the device (return_device); the status word comes back
+
+    def alg_ops(self, i=0, exit_cols_sum=None):
+        return None if exit_cols_sum is None else OPS_PER_WORD32_STEP * exit_cols_sum
+
+    def alg_bytes(self, i=0):
+        return float(sum(p.nq * p.nc * np.dtype(p.dtype).itemsize + p.q[1][-1] + p.c[1][-1] for p in self.probs))
+
+    def describe(self):
+        return {"workload": f"cdist batch of {len(self.probs)} problems", "problems": len(self.probs),
+                "pairs": self.pairs, "runs": [{"max_dist": "mixed 0..8", "dtype": "mixed int32/uint16/uint8"}]}
+
+    def cpu_sample(self, threads: int, budget_s: float):
+        import oracle
+        done, t0, res = 0, time.perf_counter(), None
+        for p in self.probs:                       # smallest problems first, until the budget is spent
+            rows = max(1, min(p.nq, 4))
+            sub = W.take(p.q, np.arange(rows))
+            oracle.cross(sub, p.c, p.max_dist, threads=threads)
+            done += rows * p.nc
+            if time.perf_counter() - t0 > budget_s / 4:
+                break
+        dt_s = time.perf_counter() - t0
+        return done / dt_s, f"up to 4 query rows of each problem, {done} pairs", 0, res
+
+    def gate(self, n, res) -> bool:
+        import oracle
+        p, o = self.probs[0], self.outs[0]
+        return bool(np.array_equal(o.get(), oracle.saturate(oracle.cross(p.q, p.c, p.max_dist), p.dtype)))
+
+
 def exit_columns(bench, sample_rows_or_n):
     """Oracle trace (columns processed under the reference's exit rule) on the
     CPU sample, scaled to the full workload — algorithmic ops for max_dist runs."""
@@ -334,6 +395,8 @@ def make_bench(cfg: int, args=None):
         return PairsBench(W.config3(n=n or (1 << 22)))
     if cfg == 4:
         return SearchBench(W.config4(nq=nq or 1024, nc=nc or (1 << 20)), [(4, "uint8")])
+    if cfg == 5:
+        return BatchBench(W.config5(scale=getattr(args, "scale", 1.0) or 1.0))
     raise SystemExit(f"unknown config {cfg}")
 
 
@@ -475,7 +538,7 @@ def run_ours(args, ranks: Ranks):
             cpu = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": sample,
                    "single_thread": {"value": v1, "sample": sample1},
                    "gate": bench.gate(n_s, res)}
-            if bench.runs[0][0] is not None:
+            if bench.runs[0][0] is not None and bench.kind != "batch":
                 exit_sum = exit_columns(bench, n_s)
         result["cpu_baseline"] = cpu
         if top:
@@ -554,6 +617,7 @@ def main():
     ap.add_argument("--nq", type=int, default=None, help="override the query count (profiling)")
     ap.add_argument("--nc", type=int, default=None, help="override the choice count (profiling)")
     ap.add_argument("--n", type=int, default=None, help="override the pair count (profiling)")
+    ap.add_argument("--scale", type=float, default=None, help="shrink the batch's choice counts (config 5)")
     ap.add_argument("--schedule", default="auto", choices=["auto", "plain", "learned", "lensort"],
                     help="work order of max_dist runs (results are identical)")
     ap.add_argument("--epochs", type=int, default=10, help="scheduler training epochs (learned)")

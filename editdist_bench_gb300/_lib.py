@@ -36,6 +36,11 @@ SIGNATURES = [
     ("blg_search_upload", ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _I64, ctypes.POINTER(_P)]),
     ("blg_search_run", ctypes.c_int, [_P, _P, _I32, _I32, _P]),
     ("blg_search_free", None, [_P, _P]),
+    ("blg_batch_upload", ctypes.c_int, [_P, _P, _I32, ctypes.POINTER(_P)]),
+    ("blg_batch_run", ctypes.c_int, [_P, _P]),
+    ("blg_batch_pairs", _I64, [_P]),
+    ("blg_batch_free", None, [_P, _P]),
+    ("blg_cdist_batch", ctypes.c_int, [_P, _P, _I32]),
     ("blg_cdist_noalloc", ctypes.c_int, [_P, _P, _SZ, _P, _I64, _P, _SZ, _P, _I64, _I32, _I32, _P]),
     ("blg_sched_train", ctypes.c_int, [_P, _P, _I32, _I32, ctypes.c_float, _I64, ctypes.POINTER(ctypes.c_float)]),
     ("blg_sched_set_weights", ctypes.c_int, [_P, _P, ctypes.c_int]),
@@ -57,6 +62,12 @@ SIGNATURES = [
     ("blg_profile_enable", ctypes.c_int, [_P, ctypes.c_int]),
     ("blg_profile_report", ctypes.c_int, [_P, ctypes.c_char_p, _SZ]),
 ]
+
+class Problem(ctypes.Structure):
+    """blg_problem (include/bitlev_gb300.h)."""
+    _fields_ = [("buf_q", _P), ("off_q", _P), ("nq", _I64), ("buf_c", _P), ("off_c", _P), ("nc", _I64),
+                ("max_dist", _I32), ("dtype", _I32), ("d_out", _P)]
+
 
 _lib = None
 _ctx = None

@@ -19,6 +19,7 @@
 #include "../../include/bitlev_gb300.h"
 #include "blg_context.h"
 #include "blg_device.cuh"
+#include "blg_batch.h"
 #include "blg_internal.h"
 #include "blg_sched.h"
 
@@ -532,6 +533,149 @@ static void search_release(blg_ctx *c, blg_search *s) {
     s->cls.clear();
 }
 
+// ------------------------------------------------------------ batches --
+struct blg_batch {
+    std::vector<blg_search *> probs;
+    std::vector<int> kk, dt;
+    std::vector<void *> outs;
+    std::vector<int> regular;         // problems outside the persistent kernel (long queries)
+    BatchJob *d_jobs = nullptr;
+    int njobs = 0;
+    int64_t *d_qprefix = nullptr, *d_job_tiles = nullptr, *d_tile_base = nullptr;
+    int32_t *d_work = nullptr;
+    BatchFill *d_fills = nullptr;
+    int nfill = 0;
+    int64_t max_fill = 0, total_queries = 0, pairs = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t graph_kernels = 0;
+};
+
+static void batch_release(blg_ctx *c, blg_batch *b) {
+    for (auto *s : b->probs) {
+        if (!s) continue;
+        search_release(c, s);
+        delete s;
+    }
+    b->probs.clear();
+    dev_free(c, b->d_jobs);
+    dev_free(c, b->d_qprefix);
+    dev_free(c, b->d_job_tiles);
+    dev_free(c, b->d_tile_base);
+    dev_free(c, b->d_work);
+    dev_free(c, b->d_fills);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch *b) {
+    if (nprob < 0 || (nprob > 0 && !pr)) return fail(c, BLG_ERR_ARG, "bad problem list");
+    std::vector<BatchJob> jobs;
+    std::vector<BatchFill> fills;
+    std::vector<int64_t> qprefix(1, 0);
+    for (int i = 0; i < nprob; i++) {
+        const blg_problem &p = pr[i];
+        if (!dtype_ok(p.dtype)) return fail(c, BLG_ERR_ARG, "problem " + std::to_string(i) + ": bad dtype");
+        if (p.nq < 0 || p.nc < 0) return fail(c, BLG_ERR_ARG, "problem " + std::to_string(i) + ": negative count");
+        if (p.nq > 0 && p.nc > 0 && !p.d_out)
+            return fail(c, BLG_ERR_ARG, "problem " + std::to_string(i) + ": null device output");
+        const int k = p.max_dist < 0 ? -1 : p.max_dist;
+        blg_search *s = new (std::nothrow) blg_search();
+        if (!s) return fail(c, BLG_ERR_ALLOC, "host allocation");
+        b->probs.push_back(s);
+        b->kk.push_back(k);
+        b->dt.push_back(p.dtype);
+        b->outs.push_back(p.d_out);
+        if (p.nq == 0 || p.nc == 0) continue;
+        int rc = search_upload(c, p.buf_q, p.off_q, p.nq, p.buf_c, p.off_c, p.nc, s);
+        if (rc) return rc;
+        b->pairs += p.nq * p.nc;
+        bool eligible = s->lsorted;
+        for (auto &cl : s->cls) eligible &= !cl.lanes && cl.nw <= kBatchMaxWords;
+        if (!eligible) {
+            b->regular.push_back(i);
+            continue;
+        }
+        for (auto &cl : s->cls) {
+            BatchJob j{};
+            j.Q = s->q.d;
+            j.CS = s->cs.d;
+            j.perm = s->perm;
+            j.lstart = s->lstart;
+            j.min_len = s->min_len;
+            j.n_len = s->n_len;
+            j.cls = SearchClass{cl.nw, cl.nq, cl.qidx, cl.qlen, cl.peq};
+            j.lo = cl.lo;
+            j.hi = cl.hi;
+            j.tile_start = cl.tile_start;
+            j.nc = p.nc;
+            j.k = k;
+            j.dtype = p.dtype;
+            j.nw = cl.nw;
+            j.out = p.d_out;
+            jobs.push_back(j);
+            qprefix.push_back(qprefix.back() + cl.nq);
+        }
+        if (k >= 0) {
+            const uint32_t v = (uint32_t)(p.dtype == BLG_UINT8 ? std::min(k + 1, 255)
+                                          : p.dtype == BLG_UINT16 ? std::min(k + 1, 65535) : k + 1);
+            fills.push_back(BatchFill{p.d_out, p.nq * p.nc, p.dtype, v});
+            b->max_fill = std::max(b->max_fill, p.nq * p.nc * (int64_t)dtype_size(p.dtype));
+        }
+    }
+    b->njobs = (int)jobs.size();
+    b->nfill = (int)fills.size();
+    b->total_queries = qprefix.back();
+    if (b->njobs > 0) {
+        CK(dev_alloc(c, (void **)&b->d_jobs, sizeof(BatchJob) * jobs.size()), "alloc jobs");
+        CK(cudaMemcpyAsync(b->d_jobs, jobs.data(), sizeof(BatchJob) * jobs.size(), cudaMemcpyHostToDevice, c->stream), "H2D jobs");
+        CK(dev_alloc(c, (void **)&b->d_qprefix, sizeof(int64_t) * qprefix.size()), "alloc qprefix");
+        CK(cudaMemcpyAsync(b->d_qprefix, qprefix.data(), sizeof(int64_t) * qprefix.size(), cudaMemcpyHostToDevice, c->stream), "H2D qprefix");
+        CK(dev_alloc(c, (void **)&b->d_job_tiles, sizeof(int64_t) * jobs.size()), "alloc job tiles");
+        CK(dev_alloc(c, (void **)&b->d_tile_base, sizeof(int64_t) * (jobs.size() + 1)), "alloc tile base");
+        CK(dev_alloc(c, (void **)&b->d_work, sizeof(int32_t)), "alloc work");
+    }
+    if (b->nfill > 0) {
+        CK(dev_alloc(c, (void **)&b->d_fills, sizeof(BatchFill) * fills.size()), "alloc fills");
+        CK(cudaMemcpyAsync(b->d_fills, fills.data(), sizeof(BatchFill) * fills.size(), cudaMemcpyHostToDevice, c->stream), "H2D fills");
+    }
+    CK(batch_set_attributes(), "kernel attributes");
+    CK(cudaStreamSynchronize(c->stream), "sync upload");
+    return BLG_OK;
+}
+
+// First run: capture the batch's launches into one CUDA graph; every run
+// then replays it on the context's stream.
+static int batch_run(blg_ctx *c, blg_batch *b) {
+    if (!b->exec) {
+        const bool prof = c->prof;
+        c->prof = false;                      // no per-launch events inside a capture
+        const int64_t before = c->launches;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "begin capture");
+        BatchPlan plan{b->d_jobs, b->njobs, b->d_qprefix, b->d_job_tiles, b->d_tile_base, b->d_work};
+        cudaError_t e = launch_batch(c->stream, c->sms, plan, b->d_fills, b->nfill, b->max_fill, b->total_queries,
+                                     c->d_status);
+        int rc = e == cudaSuccess ? BLG_OK : cuda_fail(c, e, "batch launch");
+        for (int i : b->regular)
+            if (!rc) rc = search_run(c, b->probs[i], b->kk[i], b->dt[i], b->outs[i]);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(c->stream, &g);
+        c->prof = prof;
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_fail(c, e, "graph instantiate"); }
+        b->graph = g;
+        b->graph_kernels = (b->nfill > 0 ? 1 : 0) + (b->njobs > 0 ? 4 : 0) + (c->launches - before);
+        c->launches = before;
+    }
+    CK(launch(c, "batch_graph", [&] { return cudaGraphLaunch(b->exec, c->stream); }), "graph launch");
+    c->launches += b->graph_kernels - 1;
+    return BLG_OK;
+}
+
 // ============================================================== C-ABI ==
 extern "C" {
 
@@ -776,6 +920,47 @@ int blg_cdist(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq, cons
     }
     if (out_device) *out_device = d_out;
     return BLG_OK;
+}
+
+int blg_batch_upload(blg_ctx *c, const blg_problem *probs, int32_t nprob, blg_batch **out) {
+    ENTER(c);
+    if (!out) return fail(c, BLG_ERR_ARG, "null out");
+    blg_batch *b = new (std::nothrow) blg_batch();
+    if (!b) return fail(c, BLG_ERR_ALLOC, "host allocation");
+    int rc = batch_upload(c, probs, nprob, b);
+    if (rc) {
+        batch_release(c, b);
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return BLG_OK;
+}
+
+int blg_batch_run(blg_ctx *c, blg_batch *b) {
+    ENTER(c);
+    if (!b) return fail(c, BLG_ERR_ARG, "null batch");
+    return batch_run(c, b);
+}
+
+int64_t blg_batch_pairs(const blg_batch *b) { return b ? b->pairs : 0; }
+
+void blg_batch_free(blg_ctx *c, blg_batch *b) {
+    if (!c || !b) return;
+    std::lock_guard<std::mutex> lock_(c->mu);
+    cudaSetDevice(c->device);
+    batch_release(c, b);
+    delete b;
+}
+
+int blg_cdist_batch(blg_ctx *c, const blg_problem *probs, int32_t nprob) {
+    blg_batch *b = nullptr;
+    int rc = blg_batch_upload(c, probs, nprob, &b);
+    if (rc) return rc;
+    rc = blg_batch_run(c, b);
+    if (!rc) rc = blg_synchronize(c);
+    blg_batch_free(c, b);
+    return rc;
 }
 
 int blg_malloc(blg_ctx *c, size_t bytes, void **d_ptr) {

@@ -1,0 +1,218 @@
+// Many independent cdist problems in one persistent launch.
+//
+// A batch is a set of problems, each with its own queries, choices, max_dist,
+// output dtype and device output. Every problem keeps the layout of a
+// resident search (length-sorted choices, per-query Peq tables); a "job" is
+// one (problem, query word-class). Five kernels run the whole batch:
+//   k_batch_fill    max_dist+1 into every thresholded problem's output
+//   k_batch_peq     one CTA per (job, query): the query's Peq table
+//   k_batch_plan    one block per job: survivor ranges and tile prefix
+//   k_batch_scan    job tile prefix (the global tile space)
+//   k_batch_search  persistent: every CTA pulls (job, query, 1024-survivor)
+//                   tiles from one device counter until the space is done
+// The host captures them once into a CUDA graph and replays it per run.
+#include "blg_batch.h"
+#include "blg_kernels.cuh"
+
+namespace blg {
+
+// out[0..n) = v (dtype-sized) by this thread's share (tid of stride).
+__device__ __forceinline__ void fill_share(void *out, int64_t n, int dtype, uint32_t v, int64_t tid,
+                                           int64_t stride) {
+    const int es = dtype == DT_UINT8 ? 1 : dtype == DT_UINT16 ? 2 : 4;
+    uint32_t word = v;
+    if (es == 1) word = v * 0x01010101u;
+    else if (es == 2) word = v | (v << 16);
+    const int64_t bytes = n * es;
+    uint8_t *b = reinterpret_cast<uint8_t *>(out);
+    const int64_t head = (16 - (reinterpret_cast<uintptr_t>(b) & 15)) & 15;
+    const int64_t nvec = bytes > head ? (bytes - head) / 16 : 0;
+    uint4 *vp = reinterpret_cast<uint4 *>(b + head);
+    const uint4 vv = make_uint4(word, word, word, word);
+    for (int64_t i = tid; i < nvec; i += stride) vp[i] = vv;
+    const int64_t tail0 = head + nvec * 16;
+    for (int64_t r = tid * es; r < head + (bytes - tail0); r += stride * es) {
+        const int64_t x = r < head ? r : tail0 + (r - head);
+        if (x >= bytes) break;
+        if (es == 1) b[x] = (uint8_t)v;
+        else if (es == 2) *reinterpret_cast<uint16_t *>(b + x) = (uint16_t)v;
+        else *reinterpret_cast<uint32_t *>(b + x) = v;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_batch_fill(const BatchFill *fills) {
+    const BatchFill f = fills[blockIdx.y];
+    fill_share(f.out, f.n, f.dtype, f.value, (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+               (int64_t)gridDim.x * blockDim.x);
+}
+
+// largest j in [0, n) with pre[j] <= x (pre non-decreasing, pre[0] <= x)
+__device__ __forceinline__ int upper_index(const int64_t *pre, int n, int64_t x) {
+    int a = 0, b = n;
+    while (b - a > 1) {
+        const int mid = (a + b) >> 1;
+        if (pre[mid] <= x) a = mid; else b = mid;
+    }
+    return a;
+}
+
+__global__ void __launch_bounds__(256) k_batch_peq(BatchPlan plan, uint32_t *status) {
+    extern __shared__ uint64_t tab[];
+    const int j = upper_index(plan.q_prefix, plan.njobs, blockIdx.x);
+    const BatchJob &job = plan.jobs[j];
+    const int qi = (int)(blockIdx.x - plan.q_prefix[j]);
+    int m;
+    const uint8_t *p = string_at(job.Q, job.cls.qidx[qi], m, status);
+    build_peq_block(p, m, job.nw, tab, const_cast<uint64_t *>(job.cls.peq) + (size_t)qi * 256 * job.nw);
+}
+
+// One block per job: survivor range of every query (all choices for exact
+// problems), tile counts and their prefix, the job's tile total.
+__global__ void __launch_bounds__(1024) k_batch_plan(BatchPlan plan) {
+    __shared__ int64_t s_sum[1024];
+    __shared__ int64_t s_carry;
+    const BatchJob &job = plan.jobs[blockIdx.x];
+    const SearchClass &cls = job.cls;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (int base = 0; base < cls.nq; base += 1024) {
+        const int qi = base + threadIdx.x;
+        int64_t tiles = 0;
+        if (qi < cls.nq) {
+            int64_t a = 0, b = job.n_len;
+            if (job.k >= 0) {
+                const int64_t m = cls.qlen[qi];
+                a = m - job.k - job.min_len;
+                b = m + job.k - job.min_len + 1;
+                a = a < 0 ? 0 : (a > job.n_len ? job.n_len : a);
+                b = b < 0 ? 0 : (b > job.n_len ? job.n_len : b);
+            }
+            const int64_t l = job.lstart[a], h = b > a ? job.lstart[b] : l;
+            job.lo[qi] = (int32_t)l;
+            job.hi[qi] = (int32_t)h;
+            tiles = (h - l + 1023) / 1024;
+        }
+        s_sum[threadIdx.x] = tiles;
+        __syncthreads();
+        for (int off = 1; off < 1024; off <<= 1) {
+            const int64_t v = threadIdx.x >= off ? s_sum[threadIdx.x - off] : 0;
+            __syncthreads();
+            s_sum[threadIdx.x] += v;
+            __syncthreads();
+        }
+        if (qi < cls.nq) job.tile_start[qi] = s_carry + s_sum[threadIdx.x] - tiles;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += s_sum[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        job.tile_start[cls.nq] = s_carry;
+        plan.job_tiles[blockIdx.x] = s_carry;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_batch_scan(BatchPlan plan) {
+    __shared__ int64_t s_sum[1024];
+    __shared__ int64_t s_carry;
+    if (threadIdx.x == 0) { s_carry = 0; *plan.work = 0; }
+    __syncthreads();
+    for (int base = 0; base < plan.njobs; base += 1024) {
+        const int j = base + threadIdx.x;
+        const int64_t t = j < plan.njobs ? plan.job_tiles[j] : 0;
+        s_sum[threadIdx.x] = t;
+        __syncthreads();
+        for (int off = 1; off < 1024; off <<= 1) {
+            const int64_t v = threadIdx.x >= off ? s_sum[threadIdx.x - off] : 0;
+            __syncthreads();
+            s_sum[threadIdx.x] += v;
+            __syncthreads();
+        }
+        if (j < plan.njobs) plan.tile_base[j] = s_carry + s_sum[threadIdx.x] - t;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += s_sum[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) plan.tile_base[plan.njobs] = s_carry;
+}
+
+template <int NW>
+__device__ __forceinline__ void batch_tile(const BatchJob &job, const uint64_t *s_peq, int qi, int64_t s0, Units u,
+                                           uint32_t *status) {
+    RowAddr<NW> ra;
+    ra.init(u);
+    const int m = job.cls.qlen[qi];
+    const int64_t row = job.cls.qidx[qi];
+    const int64_t s_end = job.hi[qi];
+    const int k = job.k >= 0 ? job.k : 0x3fffffff;    // exact problems: no exit can fire
+#pragma unroll 1
+    for (int t = 0; t < 4; t++) {
+        const int64_t sidx = s0 + t;
+        if (sidx >= s_end) break;
+        int n;
+        const uint8_t *tp = string_at(job.CS, sidx, n, status);
+        const int d = dist_seq_any<NW, true>(s_peq, m, tp, n, k, u, ra);
+        if (d <= k) store1(job.out, job.dtype, row * job.nc + job.perm[sidx], d);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_batch_search(BatchPlan plan, uint32_t *status, uint32_t unit) {
+    extern __shared__ uint64_t s_peq[];
+    __shared__ int s_tile;
+    const Units u{unit, unit + unit};
+    const int64_t total = plan.tile_base[plan.njobs];
+    int cur_j = -1, cur_q = -1;
+    while (true) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(plan.work, 1);
+        __syncthreads();
+        const int64_t tile = s_tile;
+        if (tile >= total) break;
+        const int j = upper_index(plan.tile_base, plan.njobs, tile);
+        const BatchJob &job = plan.jobs[j];
+        const int64_t lt = tile - plan.tile_base[j];
+        const int qi = upper_index(job.tile_start, job.cls.nq, lt);
+        const int nw = job.nw;
+        if (j != cur_j || qi != cur_q) {
+            const uint64_t *src = job.cls.peq + (size_t)qi * 256 * nw;
+            for (int x = threadIdx.x; x < 256 * nw; x += blockDim.x) s_peq[x] = __ldg(src + x);
+            cur_j = j;
+            cur_q = qi;
+        }
+        __syncthreads();
+        const int64_t s0 = job.lo[qi] + (lt - job.tile_start[qi]) * 1024 + threadIdx.x * 4;
+        switch (nw) {
+        case 1: batch_tile<1>(job, s_peq, qi, s0, u, status); break;
+        case 2: batch_tile<2>(job, s_peq, qi, s0, u, status); break;
+        case 3: batch_tile<3>(job, s_peq, qi, s0, u, status); break;
+        default: batch_tile<4>(job, s_peq, qi, s0, u, status); break;
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t batch_set_attributes() {
+    cudaError_t e = cudaFuncSetAttribute(k_batch_peq, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         256 * kBatchMaxWords * 8);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch_search, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * kBatchMaxWords * 8);
+    return e;
+}
+
+// The five launches of one batch run, on `st` (capturable: no allocation,
+// no attribute change, no synchronisation).
+cudaError_t launch_batch(cudaStream_t st, int sms, const BatchPlan &plan, const BatchFill *fills, int nfill,
+                         int64_t max_fill, int64_t total_queries, uint32_t *status) {
+    if (nfill > 0) {
+        int64_t bx = (max_fill / 16 + 255) / 256;
+        bx = bx < 1 ? 1 : (bx > 1024 ? 1024 : bx);
+        k_batch_fill<<<dim3((unsigned)bx, (unsigned)nfill), 256, 0, st>>>(fills);
+    }
+    if (plan.njobs > 0) {
+        k_batch_peq<<<(unsigned)total_queries, 256, 256 * kBatchMaxWords * 8, st>>>(plan, status);
+        k_batch_plan<<<plan.njobs, 1024, 0, st>>>(plan);
+        k_batch_scan<<<1, 1024, 0, st>>>(plan);
+        k_batch_search<<<sms * 4, 256, 256 * kBatchMaxWords * 8, st>>>(plan, status, 1u);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace blg

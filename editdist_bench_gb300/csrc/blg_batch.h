@@ -1,0 +1,47 @@
+// Descriptors of a multi-problem batch (shared by kernels and host runtime).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "blg_internal.h"
+
+namespace blg {
+
+constexpr int kBatchMaxWords = 4;   // batched queries up to 256 bytes; longer ones run per problem
+
+// One (problem, query word-class): everything the persistent kernel needs.
+struct BatchJob {
+    DevStrings Q;              // the problem's queries
+    DevStrings CS;             // its choices, length-sorted
+    const int32_t *perm;       // sorted -> original choice index
+    const int64_t *lstart;     // first sorted index per length
+    int64_t min_len, n_len;
+    SearchClass cls;           // the class's queries and Peq tables
+    int32_t *lo, *hi;          // survivor range per query
+    int64_t *tile_start;       // tile prefix per query (nq + 1)
+    int64_t nc;
+    int k, dtype, nw;
+    void *out;
+};
+
+struct BatchFill {
+    void *out;
+    int64_t n;
+    int dtype;
+    uint32_t value;
+};
+
+struct BatchPlan {
+    const BatchJob *jobs;      // device array
+    int njobs;
+    const int64_t *q_prefix;   // [njobs + 1] queries before each job (Peq build CTAs)
+    int64_t *job_tiles;        // [njobs]
+    int64_t *tile_base;        // [njobs + 1]
+    int32_t *work;             // persistent-kernel tile counter
+};
+
+cudaError_t batch_set_attributes();
+cudaError_t launch_batch(cudaStream_t st, int sms, const BatchPlan &plan, const BatchFill *fills, int nfill,
+                         int64_t max_fill, int64_t total_queries, uint32_t *status);
+
+}  // namespace blg

@@ -28,7 +28,7 @@ from ._common import DTYPE_CODE, as_list, check_dtype, check_k, pack
 from .device_array import DeviceArray
 
 __all__ = ["available", "pairwise", "cdist", "pairwise_packed", "cdist_packed", "PairsBatch",
-           "SearchBatch", "pack", "set_schedule", "synchronize"]
+           "SearchBatch", "ProblemBatch", "cdist_batch", "pack", "set_schedule", "synchronize"]
 
 
 def available() -> bool:
@@ -182,6 +182,53 @@ class SearchBatch:
         if getattr(self, "h", None) and self.h.value:
             self.ctx.lib.blg_search_free(self.ctx.h, self.h)
             self.h = None
+
+
+class ProblemBatch:
+    """Many independent cdist problems ``(queries, choices, max_dist, dtype)``
+    (packed inputs) resident in HBM, with device outputs (``outputs``, one
+    DeviceArray each). ``run()`` launches the whole batch as one CUDA graph
+    around a persistent kernel (stream-ordered, no sync)."""
+
+    def __init__(self, problems):
+        self.ctx = _lib.context()
+        self.outputs = []
+        structs = []
+        keep = []
+        for pq, pc, max_dist, dtype in problems:
+            (bq, oq), (bc, oc) = _packed(pq), _packed(pc)
+            k, dt = check_k(max_dist), check_dtype(dtype)
+            nq, nc = len(oq) - 1, len(oc) - 1
+            p = ctypes.c_void_p()
+            self.ctx.check(self.ctx.lib.blg_malloc(self.ctx.h, max(16, nq * nc * dt.itemsize), ctypes.byref(p)),
+                           "malloc")
+            out = DeviceArray(p.value, (nq, nc), dt, self.ctx)
+            self.outputs.append(out)
+            keep += [bq, oq, bc, oc]
+            structs.append(_lib.Problem(bq.ctypes.data, oq.ctypes.data, nq, bc.ctypes.data, oc.ctypes.data, nc,
+                                        k, DTYPE_CODE[dt], out.ptr))
+        arr = (_lib.Problem * max(1, len(structs)))(*structs)
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.blg_batch_upload(self.ctx.h, arr, len(structs), ctypes.byref(h)), "batch_upload")
+        self.h = h
+        self.pairs = int(self.ctx.lib.blg_batch_pairs(h))
+
+    def run(self):
+        self.ctx.check(self.ctx.lib.blg_batch_run(self.ctx.h, self.h), "batch_run")
+        return self.outputs
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.ctx.lib.blg_batch_free(self.ctx.h, self.h)
+            self.h = None
+
+
+def cdist_batch(problems, return_device: bool = True):
+    """[cdist(q, c, k, dtype) for each problem] in one batched launch."""
+    b = ProblemBatch(problems)
+    b.run()
+    synchronize()
+    return b.outputs if return_device else [o.get() for o in b.outputs]
 
 
 _SCHEDULES = {"auto": _lib.SCHED_AUTO, "plain": _lib.SCHED_PLAIN, "learned": _lib.SCHED_LEARNED,

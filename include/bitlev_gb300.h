@@ -98,6 +98,31 @@ int blg_search_upload(blg_ctx *ctx, const uint8_t *buf_q, const int64_t *off_q, 
 int blg_search_run(blg_ctx *ctx, blg_search *s, int32_t max_dist, int32_t dtype, void *d_out);
 void blg_search_free(blg_ctx *ctx, blg_search *s);
 
+/* Many independent cdist problems (host inputs, device outputs — the
+ * return_device form), run by one persistent kernel that pulls
+ * (problem, query, 1024-choice) tiles from a device work counter; the batch's
+ * launches are captured into one CUDA graph on the first run and replayed.
+ * No counterpart in the reference (one bitlev.gpu.cdist call per problem,
+ * bitlev/gpu.py:106-138). d_out: nq*nc elements of dtype, row-major. */
+typedef struct {
+    const uint8_t *buf_q;
+    const int64_t *off_q;
+    int64_t nq;
+    const uint8_t *buf_c;
+    const int64_t *off_c;
+    int64_t nc;
+    int32_t max_dist;   /* < 0: exact */
+    int32_t dtype;
+    void *d_out;
+} blg_problem;
+typedef struct blg_batch blg_batch;
+int blg_batch_upload(blg_ctx *ctx, const blg_problem *probs, int32_t nprob, blg_batch **out);
+int blg_batch_run(blg_ctx *ctx, blg_batch *b);         /* stream-ordered, no sync */
+int64_t blg_batch_pairs(const blg_batch *b);          /* sum of nq*nc */
+void blg_batch_free(blg_ctx *ctx, blg_batch *b);
+/* upload + run + synchronise + free */
+int blg_cdist_batch(blg_ctx *ctx, const blg_problem *probs, int32_t nprob);
+
 /* cdist with every buffer already in device memory and NO device allocation:
  * no counterpart in the reference (bitlev.gpu always allocates through CuPy).
  * For callers that cannot call cudaMalloc — plugins of an engine that owns

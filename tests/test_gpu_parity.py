@@ -297,3 +297,24 @@ def test_pairs_exit_column_log(gpu):
         assert (cols[ocols == 0] == 0).all() or k is None
         if k is None:
             np.testing.assert_array_equal(cols[m_ > 0], n_[m_ > 0])
+
+
+def test_problem_batch_graph(gpu):
+    """Many cdist problems in one persistent launch, replayed from a CUDA graph:
+    thresholded and exact problems, every dtype, empty problems, and a problem
+    with queries longer than 256 (run per problem inside the same graph)."""
+    rng = np.random.default_rng(55)
+    probs = [(p.q, p.c, p.max_dist, p.dtype) for p in W.config5(n_problems=10, scale=1 / 128, seed=9)]
+    probs.append((W.random_strings(rng, rng.integers(0, 200, 7)), W.random_strings(rng, rng.integers(0, 220, 900)),
+                  None, "int32"))
+    probs.append((W.random_strings(rng, [300, 20]), W.random_strings(rng, rng.integers(250, 330, 400)), 6, "uint8"))
+    probs.append((W.random_strings(rng, []), W.random_strings(rng, [3, 4]), 2, "uint8"))
+    batch = gpu.ProblemBatch(probs)
+    for _ in range(2):                                   # capture, then replay
+        outs = batch.run()
+        gpu.synchronize()
+        for (pq, pc, k, dt), o in zip(probs, outs):
+            np.testing.assert_array_equal(o.get(), oracle.saturate(oracle.cross(pq, pc, k), dt))
+    got = gpu.cdist_batch(probs[:3], return_device=False)
+    for (pq, pc, k, dt), o in zip(probs[:3], got):
+        np.testing.assert_array_equal(o, oracle.saturate(oracle.cross(pq, pc, k), dt))
