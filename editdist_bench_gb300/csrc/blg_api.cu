@@ -43,6 +43,8 @@ cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, c
 cudaError_t launch_order(cudaStream_t st, int sms, bool need_hist, const PairsPlan &plan);
 cudaError_t launch_solve(cudaStream_t st, int sms, bool hask, const PairsPlan &plan, int k, int dtype,
                          void *out, int32_t *exit_log, bool any_long);
+cudaError_t launch_solve_band(cudaStream_t st, int sms, const PairsPlan &plan, int k, int dtype, void *out,
+                              int32_t *exit_log);
 }  // namespace blg
 int sched_model_ensure(blg_ctx *c, blg_sched_model **out);
 cudaError_t launch_mlp_keys(cudaStream_t st, int sms, const blg_sched_model *m, const blg::PairsPlan &plan);
@@ -310,9 +312,14 @@ static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, int k, int dtype, void 
     CK(launch(c, "pairs_order", [&] { return launch_order(c->stream, c->sms, learned, plan); }), "pairs_order");
     bool any_long = false;
     for (int j = 1; j < kPairClasses; j++) any_long |= p->pcap[j] > 0;
-    CK(launch(c, "pairs_solve", [&] {
-           return launch_solve(c->stream, c->sms, hask, plan, k, dtype, d_out, exit_log, any_long);
-       }), "pairs_solve");
+    if (hask && k <= 31 && !c->no_band)
+        CK(launch(c, "pairs_band", [&] {
+               return launch_solve_band(c->stream, c->sms, plan, k, dtype, d_out, exit_log);
+           }), "pairs_band");
+    else
+        CK(launch(c, "pairs_solve", [&] {
+               return launch_solve(c->stream, c->sms, hask, plan, k, dtype, d_out, exit_log, any_long);
+           }), "pairs_solve");
     return BLG_OK;
 }
 

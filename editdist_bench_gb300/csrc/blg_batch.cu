@@ -16,6 +16,11 @@
 
 namespace blg {
 
+// Peq staging of the persistent kernel: [256][NW] u64, or the banded padded
+// halves [256][2*NW + 6] u32, whichever is larger for NW = kBatchMaxWords.
+constexpr int kBatchSearchSmem = 256 * (2 * kBatchMaxWords + 6) * 4 > 256 * kBatchMaxWords * 8
+                                     ? 256 * (2 * kBatchMaxWords + 6) * 4 : 256 * kBatchMaxWords * 8;
+
 // out[0..n) = v (dtype-sized) by this thread's share (tid of stride).
 __device__ __forceinline__ void fill_share(void *out, int64_t n, int dtype, uint32_t v, int64_t tid,
                                            int64_t stride) {
@@ -144,13 +149,21 @@ __device__ __forceinline__ void batch_tile(const BatchJob &job, const uint64_t *
     const int64_t row = job.cls.qidx[qi];
     const int64_t s_end = job.hi[qi];
     const int k = job.k >= 0 ? job.k : 0x3fffffff;    // exact problems: no exit can fire
+    const bool banded = job.k >= 0 && job.k <= 31;
+    const uint32_t *rows32 = reinterpret_cast<const uint32_t *>(s_peq);
+    constexpr int kStride = 2 * NW + 6;
 #pragma unroll 1
     for (int t = 0; t < 4; t++) {
         const int64_t sidx = s0 + t;
         if (sidx >= s_end) break;
         int n;
         const uint8_t *tp = string_at(job.CS, sidx, n, status);
-        const int d = dist_seq_any<NW, true>(s_peq, m, tp, n, k, u, ra);
+        int d;
+        if (!banded) d = dist_seq_any<NW, true>(s_peq, m, tp, n, k, u, ra);
+        else if (m == 0) d = cap_k(n, k);
+        else if ((n > m ? n - m : m - n) > k) d = k + 1;
+        else d = band_distance(m, tp, n, k,
+                               [&](uint32_t c, int p0) { return band_row_bits(rows32 + c * kStride, p0); }, u);
         if (d <= k) store1(job.out, job.dtype, row * job.nc + job.perm[sidx], d);
     }
 }
@@ -173,7 +186,8 @@ __global__ void __launch_bounds__(256) k_batch_search(BatchPlan plan, uint32_t *
         const int nw = job.nw;
         if (j != cur_j || qi != cur_q) {
             const uint64_t *src = job.cls.peq + (size_t)qi * 256 * nw;
-            for (int x = threadIdx.x; x < 256 * nw; x += blockDim.x) s_peq[x] = __ldg(src + x);
+            if (job.k >= 0 && job.k <= 31) stage_band_rows(src, nw, reinterpret_cast<uint32_t *>(s_peq));
+            else for (int x = threadIdx.x; x < 256 * nw; x += blockDim.x) s_peq[x] = __ldg(src + x);
             cur_j = j;
             cur_q = qi;
         }
@@ -193,7 +207,7 @@ cudaError_t batch_set_attributes() {
     cudaError_t e = cudaFuncSetAttribute(k_batch_peq, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          256 * kBatchMaxWords * 8);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch_search, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * kBatchMaxWords * 8);
+        e = cudaFuncSetAttribute(k_batch_search, cudaFuncAttributeMaxDynamicSharedMemorySize, kBatchSearchSmem);
     return e;
 }
 
@@ -210,7 +224,7 @@ cudaError_t launch_batch(cudaStream_t st, int sms, const BatchPlan &plan, const 
         k_batch_peq<<<(unsigned)total_queries, 256, 256 * kBatchMaxWords * 8, st>>>(plan, status);
         k_batch_plan<<<plan.njobs, 1024, 0, st>>>(plan);
         k_batch_scan<<<1, 1024, 0, st>>>(plan);
-        k_batch_search<<<sms * 4, 256, 256 * kBatchMaxWords * 8, st>>>(plan, status, 1u);
+        k_batch_search<<<sms * 4, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
     }
     return cudaGetLastError();
 }

@@ -24,6 +24,7 @@ struct blg_ctx {
     int64_t launches = 0;
     int sched = 0;                     // BLG_SCHED_* (work order of thresholded runs)
     blg_sched_model *model = nullptr;  // trained/loaded scheduler network, if any
+    bool no_band = false;              // force the full-word loops even for max_dist <= 31
     bool prof = false;
     std::vector<ProfRec> prof_recs;
     std::map<std::string, std::pair<int64_t, double>> prof_acc;

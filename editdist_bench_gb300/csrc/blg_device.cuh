@@ -159,6 +159,85 @@ BLG_HD void step_h(Word2 &s, uint32_t el, uint32_t eh, uint32_t cin_p, uint32_t 
 // Bit 31 of x as 0/1, on the FMA pipe: hi32(x * 2).
 BLG_HD uint32_t top_bit(uint32_t x, Units u) { return imad_hi(x, u.two, 0); }
 
+// ---- banded column loop (max_dist k <= 31) --------------------------------
+// Every alignment path of cost <= k keeps its diagonal delta = j - i within
+// |delta| + |g - delta| <= k (g = n - m): at most k+1 diagonals [dlo, dhi].
+// A 32-row window sliding down one row per text column (rows j - dhi ..
+// j - dhi + 31) holds them all, so one 32-bit Myers step per column suffices
+// whatever the pattern length. Boundaries: rows <= 0 are virtual rows with
+// D[i][j] = j - i (exact under the recurrence since they never match); the
+// row leaving the window top is taken to grow by +1 per column and the row
+// entering at the bottom gets vertical delta +1. Both are upper bounds of
+// the true values and the recurrence is monotone, while the cells of an
+// optimal in-band path are computed exactly; so min(D'[m][n], k+1) =
+// min(d, k+1). The exit fires once a lower bound of every band cell of the
+// current column exceeds k (a path of cost <= k crosses every column inside
+// the band, through exactly computed cells).
+struct BandGeom {
+    int dhi, g, s;          // top diagonal, n - m, window bit of row m at column n
+    uint32_t band;          // window bits 1 .. B-1 (B = band width <= k + 1)
+};
+
+BLG_HD BandGeom band_geom(int m, int n, int k) {
+    BandGeom bg;
+    bg.g = n - m;
+    const int ag = bg.g < 0 ? -bg.g : bg.g;
+    const int half = (k - ag) >> 1;
+    bg.dhi = (bg.g > 0 ? bg.g : 0) + half;
+    const int dlo = (bg.g < 0 ? bg.g : 0) - half;
+    const int B = bg.dhi - dlo + 1;
+    bg.band = (B >= 32 ? 0xffffffffu : ((1u << B) - 1u)) & ~1u;
+    bg.s = bg.dhi - bg.g;
+    return bg;
+}
+
+BLG_HD int popc32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+    return __popc(x);
+#else
+    return __builtin_popcount(x);
+#endif
+}
+
+// text(j) returns text byte j (0-based, called once per j in order);
+// eqw(c, p0) returns the window's match bits for byte c, where p0 is the
+// 0-based pattern index of window bit 0 (positions < 0 or >= m give no
+// bits). Caller guarantees 1 <= m, |n - m| <= k <= 31. Returns min(d, k+1);
+// *cols_out = text columns processed.
+template <typename TextFn, typename EqW>
+BLG_HD int band_core(int m, int n, int k, TextFn text, EqW eqw, Units u, int *cols_out) {
+    const BandGeom bg = band_geom(m, n, k);
+    const int nv = bg.dhi + 1;                               // virtual rows -dhi .. 0 at column 0
+    uint32_t mv = nv >= 32 ? 0xffffffffu : ((1u << nv) - 1u);
+    uint32_t pv = ~mv;
+    int A = bg.dhi;                                          // D'[top window row][current column]
+    const uint32_t half_top = u.one << 31;
+    for (int j = 0; j < n; j++) {
+        if ((j & 3) == 0 && j > 0 && A - popc32(mv & bg.band) > k) {   // every band cell > k
+            if (cols_out) *cols_out = j;
+            return k + 1;
+        }
+        const uint32_t c = text(j);
+        // column j's deltas re-indexed one row down; the new bottom row enters with +1
+        pv = imad_hi(pv, half_top, half_top);
+        mv = imad_hi(mv, half_top, 0);
+        const uint32_t eq = eqw(c, j - bg.dhi);
+        const uint32_t xv = eq | mv;
+        const uint32_t sum = imad_lo(eq & pv, u.one, pv);
+        const uint32_t xh = (sum ^ pv) | eq;
+        const uint32_t ph = mv | ~(xh | pv);
+        const uint32_t mh = pv & xh;
+        const uint32_t phs = imad_lo(ph, u.two, u.one), mhs = imad_lo(mh, u.two, 0);
+        pv = mhs | ~(xv | phs);
+        mv = phs & xv;
+        A += 1 + (int)(pv & 1u) - (int)(mv & 1u);
+    }
+    if (cols_out) *cols_out = n;
+    const uint32_t ms = (bg.s >= 31 ? 0xffffffffu : ((2u << bg.s) - 1u)) & ~1u;   // bits 1..s
+    const int d = A + popc32(pv & ms) - popc32(mv & ms);
+    return cap_k(d, k);
+}
+
 // ---- host-side reference of the per-pair device logic ------------------
 // pair_distance_plain: trimming + pattern = shorter string + gap exit +
 // single/multi-word run with per-character Eq from a 256-row table.  The

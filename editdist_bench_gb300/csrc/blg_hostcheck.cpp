@@ -125,6 +125,46 @@ extern "C" int blg_host_distance_halves(const uint8_t *a, int la, const uint8_t 
     return cap_k(la + (int)accP - (int)accM, k);
 }
 
+// The banded loop (k <= 31) with the window bits read from a full Peq table.
+extern "C" int blg_host_band(const uint8_t *a, int la, const uint8_t *b, int lb, int trim, int k) {
+    normalise(a, la, b, lb, trim);
+    if (k < 0 || k > 31) return -1;
+    if (lb - la > k) return k + 1;
+    if (la == 0) return lb;
+    Pattern P(a, la);
+    const Units u{1u, 2u};
+    auto text = [&](int j) -> uint32_t { return b[j]; };
+    auto eqw = [&](uint32_t c, int p0) -> uint32_t {
+        uint32_t v = 0;
+        for (int q = 0; q < 32; q++) {
+            const int p = p0 + q;
+            if (p >= 0 && p < la && ((P.eq((uint8_t)c, p / 64) >> (p % 64)) & 1u)) v |= 1u << q;
+        }
+        return v;
+    };
+    return band_core(la, lb, k, text, eqw, u, nullptr);
+}
+
+// Same, with the pattern as the LONGER string (the search kernels' case:
+// the query is the pattern whatever the choice's length), no trimming.
+extern "C" int blg_host_band_query(const uint8_t *q, int m, const uint8_t *t, int n, int k) {
+    if (k < 0 || k > 31) return -1;
+    if (m == 0) return cap_k(n, k);
+    if ((n > m ? n - m : m - n) > k) return k + 1;
+    Pattern P(q, m);
+    const Units u{1u, 2u};
+    auto text = [&](int j) -> uint32_t { return t[j]; };
+    auto eqw = [&](uint32_t c, int p0) -> uint32_t {
+        uint32_t v = 0;
+        for (int qq = 0; qq < 32; qq++) {
+            const int p = p0 + qq;
+            if (p >= 0 && p < m && ((P.eq((uint8_t)c, p / 64) >> (p % 64)) & 1u)) v |= 1u << qq;
+        }
+        return v;
+    };
+    return band_core(m, n, k, text, eqw, u, nullptr);
+}
+
 extern "C" int blg_host_store(int d, int dtype) {
     if (dtype == DT_UINT8) return (int)saturate_u8(d);
     if (dtype == DT_UINT16) return (int)saturate_u16(d);

@@ -20,6 +20,8 @@
 //  * k_pairs_long       persistent consumer of that queue, lane-spread.
 //
 // All arithmetic is integer bit logic on the ALU/FMA pipes; no tensor cores.
+#include <algorithm>
+
 #include "blg_kernels.cuh"
 
 namespace blg {
@@ -297,9 +299,11 @@ __global__ void __launch_bounds__(256) k_search_surv(DevStrings CS, const int32_
             if (tile_start[mid] <= tile) a = mid; else b = mid;
         }
         const int qi = a;
+        const bool banded = k <= 31;                  // uniform: one band word holds every path <= k
         if (qi != cur) {
             const uint64_t *src = cls.peq + (size_t)qi * 256 * NW;
-            for (int x = threadIdx.x; x < 256 * NW; x += blockDim.x) s_peq[x] = __ldg(src + x);
+            if (banded) stage_band_rows(src, NW, reinterpret_cast<uint32_t *>(s_peq));
+            else for (int x = threadIdx.x; x < 256 * NW; x += blockDim.x) s_peq[x] = __ldg(src + x);
             cur = qi;
         }
         __syncthreads();
@@ -307,13 +311,20 @@ __global__ void __launch_bounds__(256) k_search_surv(DevStrings CS, const int32_
         const int64_t row = cls.qidx[qi];
         const int64_t s_end = hi[qi];
         const int64_t s0 = lo[qi] + (tile - tile_start[qi]) * 1024 + threadIdx.x * 4;
+        const uint32_t *rows32 = reinterpret_cast<const uint32_t *>(s_peq);
+        constexpr int kStride = 2 * NW + 6;
 #pragma unroll 1
         for (int t = 0; t < 4; t++) {
             const int64_t sidx = s0 + t;
             if (sidx >= s_end) break;
             int n;
             const uint8_t *tp = string_at(CS, sidx, n, status);
-            const int d = dist_seq_any<NW, true>(s_peq, m, tp, n, k, u, ra);
+            int d;
+            if (!banded) d = dist_seq_any<NW, true>(s_peq, m, tp, n, k, u, ra);
+            else if (m == 0) d = cap_k(n, k);
+            else if ((n > m ? n - m : m - n) > k) d = k + 1;
+            else d = band_distance(m, tp, n, k,
+                                   [&](uint32_t c, int p0) { return band_row_bits(rows32 + c * kStride, p0); }, u);
             if (d <= k) store1(out, dtype, row * nc + perm[sidx], d);
         }
         __syncthreads();
@@ -441,7 +452,7 @@ static cudaError_t launch_surv_nw(cudaStream_t st, int grid, const DevStrings &C
                                   const SearchClass &cls, const int32_t *lo, const int32_t *hi,
                                   const int64_t *tile_start, int32_t *work, int k, int dtype, void *out,
                                   int64_t nc, uint32_t *status) {
-    const size_t smem = (size_t)256 * NW * sizeof(uint64_t);
+    const size_t smem = std::max((size_t)256 * NW * sizeof(uint64_t), (size_t)256 * (2 * NW + 6) * sizeof(uint32_t));
     cudaFuncSetAttribute(k_search_surv<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_search_surv<NW><<<grid, 256, smem, st>>>(CS, perm, cls, lo, hi, tile_start, work, k, dtype, out, nc,
                                                 status, 1u);

@@ -355,6 +355,44 @@ __device__ __forceinline__ int long_class(int m) {
     return W <= 2 ? 0 : W <= 4 ? 1 : W <= 8 ? 2 : W <= 16 ? 3 : W <= 32 ? 4 : -1;
 }
 
+// Banded column loop (blg_device.cuh: band_core) reading the text with 4-byte loads.
+template <typename EqW>
+__device__ __forceinline__ int band_distance(int m, const uint8_t *t, int n, int k, EqW eqw, Units u,
+                                             int *cols_out = nullptr) {
+    TextScan ts;
+    ts.init(t);
+    uint32_t w4 = 0;
+    auto text = [&](int j) -> uint32_t {
+        if ((j & 3) == 0) w4 = ts.next4();
+        const uint32_t c = w4 & 0xffu;
+        w4 >>= 8;
+        return c;
+    };
+    return band_core(m, n, k, text, eqw, u, cols_out);
+}
+
+// Query Peq rows as 32-bit halves with zero padding (2 halves before, 4
+// after): row stride 2*NW + 6 halves. Window bits at pattern index p0:
+// halves around p0 + 64, one funnel shift.
+__device__ __forceinline__ uint32_t band_row_bits(const uint32_t *row, int p0) {
+    const int P = p0 + 64;
+    return __funnelshift_r(row[P >> 5], row[(P >> 5) + 1], (uint32_t)(P & 31));
+}
+
+// Stage a [256][nw] u64 Peq table as padded halves (stride 2*nw + 6).
+__device__ __forceinline__ void stage_band_rows(const uint64_t *src, int nw, uint32_t *dst) {
+    const int stride = 2 * nw + 6;
+    for (int x = threadIdx.x; x < 256 * stride; x += blockDim.x) {
+        const int r = x / stride, h = x - r * stride - 2;
+        uint32_t v = 0;
+        if (h >= 0 && h < 2 * nw) {
+            const uint64_t wd = src[r * nw + (h >> 1)];
+            v = (h & 1) ? (uint32_t)(wd >> 32) : (uint32_t)wd;
+        }
+        dst[x] = v;
+    }
+}
+
 // Build the Peq table of one query into shared memory `tab` (256 x nwc
 // words) and copy it to `dst`: one block, shared-memory atomics.
 __device__ __forceinline__ void build_peq_block(const uint8_t *p, int m, int nwc, uint64_t *tab,

@@ -243,6 +243,74 @@ __global__ void __launch_bounds__(256) k_solve_lanes(PairsPlan plan, int k, int 
     }
 }
 
+// max_dist <= 31: every record (any pattern length) solved by the banded
+// loop, one thread per record. The window's match bits come from a 32-slot
+// ring per thread: rows 0..15 / 16..31 of a [row][thread] u32 table hold,
+// for each high / low nibble value, the ring slots whose pattern byte has
+// it; slot (p & 31) holds pattern position p. Each column the position
+// leaving the window top and the one entering at its bottom share a slot:
+// the leaving byte (kept in a per-thread byte ring) is cleared, the entering
+// one set, and the slot order is rotated into window order. Both tables are
+// laid out [row or slot][thread], so every access is bank-conflict free.
+template <bool LOG>
+__global__ void __launch_bounds__(256) k_solve_band(PairsPlan plan, int k, int dtype, void *out,
+                                                    int32_t *exit_log, uint32_t unit) {
+    __shared__ uint32_t s_tab[32 * 256];
+    __shared__ uint8_t s_ring[256 * 32];
+    const Units u{unit, unit + unit};
+    uint32_t *tc = s_tab + threadIdx.x;                     // row r at tc[r * 256]
+    uint8_t *ring = s_ring + threadIdx.x;                  // slot q at ring[q * 256] (conflict-free)
+    const int lane = threadIdx.x & 31;
+    for (int cls = kPairClasses - 1; cls >= 0; cls--) {
+        const int count = min(plan.count[cls], (int)plan.cap[cls]);
+        while (true) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&plan.head[cls], 32);
+            base = __shfl_sync(kFull, base, 0);
+            if (base >= count) break;
+            const int ri = base + lane;
+            if (ri >= count) continue;
+            const LongItem it = plan.sorted[cls][ri];
+            const int m = it.m, n = it.n;
+            const uint8_t *pat = it.pat;
+            int d, cols = 0;
+            if (n - m > k || m - n > k) d = k + 1;
+            else {
+                const BandGeom bg = band_geom(m, n, k);
+#pragma unroll
+                for (int r = 0; r < 32; r++) tc[r * 256] = 0;
+                // window of column 1 holds positions -dhi .. 30 - dhi; real ones first
+                for (int p = 0; p <= 30 - bg.dhi && p < m; p++) {
+                    const uint32_t c = pat[p], bit = 1u << (p & 31);
+                    tc[(c >> 4) * 256] |= bit;
+                    tc[(16 + (c & 15)) * 256] |= bit;
+                    ring[(p & 31) * 256] = (uint8_t)c;
+                }
+                auto eqw = [&](uint32_t c, int p0) -> uint32_t {
+                    const int pin = p0 + 31, pout = p0 - 1;   // same ring slot
+                    const uint32_t bit = 1u << (pin & 31);
+                    if (pout >= 0 && pout < m) {
+                        const uint32_t co = ring[(pin & 31) * 256];
+                        tc[(co >> 4) * 256] &= ~bit;
+                        tc[(16 + (co & 15)) * 256] &= ~bit;
+                    }
+                    if (pin >= 0 && pin < m) {
+                        const uint32_t cn = pat[pin];
+                        tc[(cn >> 4) * 256] |= bit;
+                        tc[(16 + (cn & 15)) * 256] |= bit;
+                        ring[(pin & 31) * 256] = (uint8_t)cn;
+                    }
+                    const uint32_t x = tc[(c >> 4) * 256] & tc[(16 + (c & 15)) * 256];
+                    return __funnelshift_r(x, x, (uint32_t)(p0 & 31));
+                };
+                d = band_distance(m, it.txt, n, k, eqw, u, LOG ? &cols : nullptr);
+            }
+            store1(out, dtype, it.idx, d);
+            if (LOG) exit_log[it.idx] = cols;
+        }
+    }
+}
+
 // ------------------------------------------------------------- launchers --
 cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, const DevStrings &A,
                               const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
@@ -261,6 +329,13 @@ cudaError_t launch_order(cudaStream_t st, int sms, bool need_hist, const PairsPl
     if (need_hist) k_order_hist<<<sms * 2, 256, 0, st>>>(plan);
     k_order_scan<<<1, kCostBuckets, 0, st>>>(plan);
     k_order_scatter<<<sms * 4, 256, 0, st>>>(plan);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve_band(cudaStream_t st, int sms, const PairsPlan &plan, int k, int dtype, void *out,
+                              int32_t *exit_log) {
+    if (exit_log) k_solve_band<true><<<sms * 3, 256, 0, st>>>(plan, k, dtype, out, exit_log, 1u);
+    else k_solve_band<false><<<sms * 3, 256, 0, st>>>(plan, k, dtype, out, nullptr, 1u);
     return cudaGetLastError();
 }
 

@@ -66,6 +66,9 @@ def hostcheck():
                       ctypes.c_int]
         f.restype = ctypes.c_int
     L.blg_host_store.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.blg_host_band.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int]
+    L.blg_host_band_query.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
     return L
 
 
@@ -172,3 +175,27 @@ def test_device_array_shapes():
         d.reshape(4, 2)
     e = DeviceArray(0, (0, 5), np.int32, ctx=None)
     assert e.size == 0 and e.reshape(5, 0).shape == (5, 0)
+
+
+# ---- the banded loop (max_dist <= 31): exact min(d, k+1) for any lengths -----
+@pytest.mark.parametrize("k", [0, 1, 2, 3, 5, 8, 13, 20, 31])
+def test_band_matches_oracle(hostcheck, k):
+    rng = random.Random(500 + k)
+    for _ in range(400):
+        m = rng.randrange(0, 420)
+        al = rng.choice([b"AC", b"ACGT", b"ACGT\x00", bytes(range(256))])
+        a = bytes(rng.choice(al) for _ in range(m))
+        b = bytearray(a)
+        for _ in range(rng.randrange(0, 3 * k + 4)):
+            i = rng.randrange(len(b) + 1)
+            op = rng.randrange(3)
+            if op == 0 and i < len(b): b[i] = rng.choice(al)
+            elif op == 1: b.insert(i, rng.choice(al))
+            elif i < len(b): del b[i]
+        b = bytes(b)
+        if rng.random() < 0.5:
+            a, b = b, a
+        want = _one(a, b, k)
+        assert hostcheck.blg_host_band(a, len(a), b, len(b), 1, k) == want
+        assert hostcheck.blg_host_band(a, len(a), b, len(b), 0, k) == want
+        assert hostcheck.blg_host_band_query(a, len(a), b, len(b), k) == want
