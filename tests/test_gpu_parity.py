@@ -277,8 +277,9 @@ def test_pairs_schedules(gpu, sched):
 
 def test_pairs_exit_column_log(gpu):
     """The logged column counts: 0 for pairs settled by the length gap or an
-    empty pattern, the trimmed text length without an exit, and never fewer
-    columns than the reference's exit rule needs."""
+    empty pattern, the trimmed text length without max_dist, at most the
+    text length otherwise (the banded loop's exit may fire before the
+    reference's bottom-row rule; only the values must agree)."""
     import ctypes
     from editdist_bench_gb300 import _lib
     rng = np.random.default_rng(5)
@@ -293,8 +294,9 @@ def test_pairs_exit_column_log(gpu):
         cols = log.get()
         d, m_, n_, ocols = oracle.pairs_trace(a, b, k)
         np.testing.assert_array_equal(out.get(), d)
-        assert (cols <= n_).all() and (cols >= ocols).all()
-        assert (cols[ocols == 0] == 0).all() or k is None
+        assert (cols <= n_).all()
+        settled = (m_ == 0) | (np.abs(n_ - m_) > (k if k is not None else 1 << 30))
+        assert (cols[settled] == 0).all()
         if k is None:
             np.testing.assert_array_equal(cols[m_ > 0], n_[m_ > 0])
 
