@@ -286,22 +286,38 @@ __global__ void __launch_bounds__(256) k_solve_band(PairsPlan plan, int k, int d
                     tc[(16 + (c & 15)) * 256] |= bit;
                     ring[(p & 31) * 256] = (uint8_t)c;
                 }
+                // entering positions p0 + 31 = 31 - dhi + j advance one per column:
+                // a 4-byte cursor keeps the pattern loads off the column chain
+                const int pin0 = 31 - bg.dhi;
+                TextScan ps;
+                if (pin0 < m) ps.init(pat + pin0);
+                uint32_t pw = 0;
                 auto eqw = [&](uint32_t c, int p0) -> uint32_t {
                     const int pin = p0 + 31, pout = p0 - 1;   // same ring slot
-                    const uint32_t bit = 1u << (pin & 31);
-                    if (pout >= 0 && pout < m) {
-                        const uint32_t co = ring[(pin & 31) * 256];
+                    const uint32_t slot = (uint32_t)pin & 31u, bit = 1u << slot;
+                    // match bits from the table before this column's update; window
+                    // bit 31 (the entering position) from a register compare instead
+                    const uint32_t x = tc[(c >> 4) * 256] & tc[(16 + (c & 15)) * 256];
+                    uint32_t eq = __funnelshift_r(x, x, (uint32_t)(p0 & 31)) & 0x7fffffffu;
+                    if (pin < m) {
+                        if (((pin - pin0) & 3) == 0) pw = ps.next4();
+                        const uint32_t cn = pw & 0xffu;
+                        pw >>= 8;
+                        if (cn == c) eq |= 0x80000000u;
+                        if (pout >= 0) {
+                            const uint32_t co = ring[slot * 256];
+                            tc[(co >> 4) * 256] &= ~bit;
+                            tc[(16 + (co & 15)) * 256] &= ~bit;
+                        }
+                        tc[(cn >> 4) * 256] |= bit;
+                        tc[(16 + (cn & 15)) * 256] |= bit;
+                        ring[slot * 256] = (uint8_t)cn;
+                    } else if (pout >= 0 && pout < m) {
+                        const uint32_t co = ring[slot * 256];
                         tc[(co >> 4) * 256] &= ~bit;
                         tc[(16 + (co & 15)) * 256] &= ~bit;
                     }
-                    if (pin >= 0 && pin < m) {
-                        const uint32_t cn = pat[pin];
-                        tc[(cn >> 4) * 256] |= bit;
-                        tc[(16 + (cn & 15)) * 256] |= bit;
-                        ring[(pin & 31) * 256] = (uint8_t)cn;
-                    }
-                    const uint32_t x = tc[(c >> 4) * 256] & tc[(16 + (c & 15)) * 256];
-                    return __funnelshift_r(x, x, (uint32_t)(p0 & 31));
+                    return eq;
                 };
                 d = band_distance(m, it.txt, n, k, eqw, u, LOG ? &cols : nullptr);
             }
