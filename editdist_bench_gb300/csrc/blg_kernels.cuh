@@ -21,20 +21,23 @@ __device__ __forceinline__ uint32_t load4(const uint8_t *p) {
     return __funnelshift_r(__ldg(w), __ldg(w + 1), (uint32_t)(a & 3) * 8u);
 }
 
-// Sequential reader: 4 characters per call, one aligned load per call.
+// Sequential reader: 4 characters per call, one aligned load per call,
+// issued one call ahead so its latency overlaps the caller's columns. Reads
+// at most 12 bytes past the last character returned (the 16-byte slack).
 struct TextScan {
     const uint32_t *w;
-    uint32_t lo, sh;
+    uint32_t lo, hi, sh;
     __device__ __forceinline__ void init(const uint8_t *p) {
         const uintptr_t a = reinterpret_cast<uintptr_t>(p);
         w = reinterpret_cast<const uint32_t *>(a & ~uintptr_t(3));
         sh = (uint32_t)(a & 3) * 8u;
         lo = __ldg(w);
+        hi = __ldg(++w);
     }
     __device__ __forceinline__ uint32_t next4() {
-        const uint32_t hi = __ldg(++w);
         const uint32_t r = __funnelshift_r(lo, hi, sh);
         lo = hi;
+        hi = __ldg(++w);
         return r;
     }
 };

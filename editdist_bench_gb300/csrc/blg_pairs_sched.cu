@@ -280,11 +280,19 @@ __global__ void __launch_bounds__(256) k_solve_band(PairsPlan plan, int k, int d
 #pragma unroll
                 for (int r = 0; r < 32; r++) tc[r * 256] = 0;
                 // window of column 1 holds positions -dhi .. 30 - dhi; real ones first
-                for (int p = 0; p <= 30 - bg.dhi && p < m; p++) {
-                    const uint32_t c = pat[p], bit = 1u << (p & 31);
-                    tc[(c >> 4) * 256] |= bit;
-                    tc[(16 + (c & 15)) * 256] |= bit;
-                    ring[(p & 31) * 256] = (uint8_t)c;
+                {
+                    const int fill = min(31 - bg.dhi, m);
+                    TextScan fs;
+                    fs.init(pat);
+                    uint32_t f4 = 0;
+                    for (int p = 0; p < fill; p++) {
+                        if ((p & 3) == 0) f4 = fs.next4();
+                        const uint32_t c = f4 & 0xffu, bit = 1u << p;
+                        f4 >>= 8;
+                        tc[(c >> 4) * 256] |= bit;
+                        tc[(16 + (c & 15)) * 256] |= bit;
+                        ring[p * 256] = (uint8_t)c;
+                    }
                 }
                 // entering positions p0 + 31 = 31 - dhi + j advance one per column:
                 // a 4-byte cursor keeps the pattern loads off the column chain
@@ -350,8 +358,9 @@ cudaError_t launch_order(cudaStream_t st, int sms, bool need_hist, const PairsPl
 
 cudaError_t launch_solve_band(cudaStream_t st, int sms, const PairsPlan &plan, int k, int dtype, void *out,
                               int32_t *exit_log) {
-    if (exit_log) k_solve_band<true><<<sms * 3, 256, 0, st>>>(plan, k, dtype, out, exit_log, 1u);
-    else k_solve_band<false><<<sms * 3, 256, 0, st>>>(plan, k, dtype, out, nullptr, 1u);
+    // 40 KB of ring tables per CTA: five CTAs per SM
+    if (exit_log) k_solve_band<true><<<sms * 5, 256, 0, st>>>(plan, k, dtype, out, exit_log, 1u);
+    else k_solve_band<false><<<sms * 5, 256, 0, st>>>(plan, k, dtype, out, nullptr, 1u);
     return cudaGetLastError();
 }
 
