@@ -42,6 +42,25 @@ struct TextScan {
     }
 };
 
+// Non-prefetching variant for register-bound loops (the full-word search
+// loop), where the extra live word costs more than the load latency saves.
+struct TextScanLean {
+    const uint32_t *w;
+    uint32_t lo, sh;
+    __device__ __forceinline__ void init(const uint8_t *p) {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+        w = reinterpret_cast<const uint32_t *>(a & ~uintptr_t(3));
+        sh = (uint32_t)(a & 3) * 8u;
+        lo = __ldg(w);
+    }
+    __device__ __forceinline__ uint32_t next4() {
+        const uint32_t hi = __ldg(++w);
+        const uint32_t r = __funnelshift_r(lo, hi, sh);
+        lo = hi;
+        return r;
+    }
+};
+
 // Validated string view; a corrupt offset pair raises ST_BAD_OFFSETS and
 // yields an empty string instead of an out-of-range read.
 __device__ __forceinline__ const uint8_t *string_at(const DevStrings &S, int64_t i, int &len,
@@ -163,7 +182,7 @@ __device__ __forceinline__ int dist_seq(const uint64_t *peq, int m, const uint8_
     const uint32_t mult = u.one << (31 - (lastbit & 31));
     uint32_t accP = 0, accM = 0;                        // score = m + accP - accM
     const char *base = reinterpret_cast<const char *>(peq);
-    TextScan ts;
+    TextScanLean ts;
     ts.init(t);
     int j = 0;
     for (; j + 4 <= n; j += 4) {
