@@ -36,6 +36,8 @@ cudaError_t launch_pairs_main(cudaStream_t st, int grid, bool hask, const DevStr
                               uint32_t *status);
 cudaError_t launch_pairs_long(cudaStream_t st, int grid, bool hask, const LongQueue &q, int k,
                               int dtype, void *out);
+cudaError_t launch_pairs_staged(cudaStream_t st, int sms, bool hask, const DevStrings &A, const DevStrings &B,
+                                int k, int dtype, void *out, const LongQueue &q, uint32_t *status);
 cudaError_t launch_fill(cudaStream_t st, int sms, void *out, int64_t n, int dtype, uint32_t v);
 cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, const DevStrings &A,
                               const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
@@ -343,10 +345,10 @@ static int pairs_run(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, in
     // 64 KB of nibble tables per 256-thread CTA: 3 CTAs per SM.
     const int64_t want = (p->n + 255) / 256;
     const int grid = (int)std::min<int64_t>(want, (int64_t)c->sms * 3 * 16);
-    CK(launch(c, "pairs_main", [&] {
-           return launch_pairs_main(c->stream, grid, hask, p->a.d, p->b.d, k, dtype, d_out, q,
-                                    c->d_status);
-       }), "pairs_main");
+    CK(launch(c, "pairs_staged", [&] {
+           return launch_pairs_staged(c->stream, c->sms, hask, p->a.d, p->b.d, k, dtype, d_out, q, c->d_status);
+       }), "pairs_staged");
+    (void)grid;
     if (total > 0)
         CK(launch(c, "pairs_long", [&] {
                return launch_pairs_long(c->stream, c->sms * 3, hask, q, k, dtype, d_out);

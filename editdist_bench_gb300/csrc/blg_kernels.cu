@@ -147,6 +147,100 @@ __global__ void __launch_bounds__(256) k_pairs_main(DevStrings A, DevStrings B, 
     }
 }
 
+// Staged variant of k_pairs_main: each warp takes 32 consecutive pairs,
+// copies the byte spans of their a and b strings into shared memory with
+// coalesced 16-byte loads (one round trip instead of a chain of dependent
+// global reads per pair), then trims and solves from shared memory. Groups
+// whose span does not fit read global memory directly; long patterns are
+// queued with their global addresses. 128 threads: per warp 8 KB of nibble
+// tables and two staging buffers.
+constexpr int kStageSpan = 1536;
+constexpr int kStageBuf = kStageSpan + 48;      // 16 bytes before, 32 after the span
+
+__device__ __forceinline__ int64_t warp_min64(int64_t v) {
+    for (int o = 16; o; o >>= 1) { const int64_t w = __shfl_xor_sync(kFull, v, o); v = w < v ? w : v; }
+    return v;
+}
+__device__ __forceinline__ int64_t warp_max64(int64_t v) {
+    for (int o = 16; o; o >>= 1) { const int64_t w = __shfl_xor_sync(kFull, v, o); v = w > v ? w : v; }
+    return v;
+}
+
+// Copy bytes [lo, hi) of a 16-byte-aligned buffer into stage + 16 (lo, hi
+// rounded out to 16 bytes; the buffer's 16-byte slack covers the rounding).
+__device__ __forceinline__ void stage_span(uint8_t *stage, const uint8_t *buf, int64_t lo16, int64_t hi16, int lane) {
+    for (int64_t x = (int64_t)lane * 16; x < hi16 - lo16; x += 32 * 16)
+        *reinterpret_cast<uint4 *>(stage + 16 + x) = __ldg(reinterpret_cast<const uint4 *>(buf + lo16 + x));
+}
+
+template <bool HASK>
+__global__ void __launch_bounds__(128) k_pairs_staged(DevStrings A, DevStrings B, int k, int dtype, void *out,
+                                                      LongQueue q, uint32_t *status) {
+    extern __shared__ uint64_t s_mem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t *tc = s_mem + warp * 1024 + lane;
+    uint8_t *sa = reinterpret_cast<uint8_t *>(s_mem + 4 * 1024) + warp * 2 * kStageBuf;
+    uint8_t *sb = sa + kStageBuf;
+#pragma unroll
+    for (int r = 0; r < 32; r++) tc[r * 32] = 0;
+    const int64_t n = A.n;
+    const int64_t nwarps = (int64_t)gridDim.x * 4;
+    for (int64_t grp = (int64_t)blockIdx.x * 4 + warp; grp * 32 < n; grp += nwarps) {
+        const int64_t i = grp * 32 + lane;
+        const bool valid = i < n;
+        int la = 0, lb = 0;
+        const uint8_t *ga = valid ? string_at(A, i, la, status) : A.buf;
+        const uint8_t *gb = valid ? string_at(B, i, lb, status) : B.buf;
+        const int64_t a0 = ga - A.buf, b0 = gb - B.buf;
+        const int64_t alo = warp_min64(valid ? a0 : INT64_MAX) & ~int64_t(15);
+        const int64_t ahi = (warp_max64(valid ? a0 + la : 0) + 15) & ~int64_t(15);
+        const int64_t blo = warp_min64(valid ? b0 : INT64_MAX) & ~int64_t(15);
+        const int64_t bhi = (warp_max64(valid ? b0 + lb : 0) + 15) & ~int64_t(15);
+        const bool staged = ahi - alo <= kStageSpan && bhi - blo <= kStageSpan;
+        if (staged) {
+            stage_span(sa, A.buf, alo, ahi, lane);
+            stage_span(sb, B.buf, blo, bhi, lane);
+        }
+        __syncwarp();
+        if (valid) {
+            const uint8_t *a = staged ? sa + 16 + (a0 - alo) : ga;
+            const uint8_t *b = staged ? sb + 16 + (b0 - blo) : gb;
+            const uint8_t *a_start = a;
+            trim_windows<GenericLoad>(a, la, b, lb);
+            const int64_t pre = a - a_start;                 // common prefix removed
+            const uint8_t *gta = ga + pre, *gtb = gb + pre;  // the same trimmed strings in global memory
+            if (la > lb) {
+                const uint8_t *t = a; a = b; b = t;
+                t = gta; gta = gtb; gtb = t;
+                const int x = la; la = lb; lb = x;
+            }
+            int d;
+            bool queued = false;
+            if (HASK && lb - la > k) d = k + 1;
+            else if (la == 0) d = lb;
+            else if (la <= 64) d = solve_word<HASK, GenericLoad>(tc, a, la, b, lb, k);
+            else {
+                const int cls = long_class(la);
+                d = -1;
+                if (cls < 0) atomicOr(status, ST_TOO_LONG);
+                else {
+                    const int pos = atomicAdd(&q.counts[cls], 1);
+                    if (pos < q.cap[cls]) {
+                        LongItem it;
+                        it.pat = gta; it.txt = gtb; it.m = la; it.n = lb; it.idx = i;
+                        q.items[cls][pos] = it;
+                        queued = true;
+                    } else {
+                        atomicOr(status, ST_QUEUE_OVERFLOW);
+                    }
+                }
+            }
+            if (!queued) store1(out, dtype, i, d);
+        }
+        __syncwarp();                                        // staging reused by the next group
+    }
+}
+
 // Persistent consumer of the long-pair queues: each warp takes 32/L pairs
 // of one class at a time until every class queue is drained.
 template <bool HASK>
@@ -390,6 +484,21 @@ cudaError_t launch_search_lanes(cudaStream_t st, bool hask, const DevStrings &C,
     } else {
         cudaFuncSetAttribute(k_search_lanes<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_search_lanes<false><<<grid, 256, smem, st>>>(C, cls, nwc, L, k, dtype, out, status);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pairs_staged(cudaStream_t st, int sms, bool hask, const DevStrings &A, const DevStrings &B,
+                                int k, int dtype, void *out, const LongQueue &q, uint32_t *status) {
+    const size_t smem = 4 * 1024 * sizeof(uint64_t) + 4 * 2 * kStageBuf;
+    const int64_t want = (A.n + 127) / 128;
+    const int grid = (int)std::min<int64_t>(want, (int64_t)sms * 5 * 8);
+    if (hask) {
+        cudaFuncSetAttribute(k_pairs_staged<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_pairs_staged<true><<<grid, 128, smem, st>>>(A, B, k, dtype, out, q, status);
+    } else {
+        cudaFuncSetAttribute(k_pairs_staged<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_pairs_staged<false><<<grid, 128, smem, st>>>(A, B, k, dtype, out, q, status);
     }
     return cudaGetLastError();
 }

@@ -12,35 +12,47 @@ namespace blg {
 constexpr unsigned kFull = 0xffffffffu;
 
 // ---------------------------------------------------------------- loads --
+// Load policies: strings in global memory go through the read-only cache;
+// strings staged in shared memory are read with generic loads.
+struct LdgLoad {
+    static __device__ __forceinline__ uint32_t ld(const uint32_t *p) { return __ldg(p); }
+};
+struct GenericLoad {
+    static __device__ __forceinline__ uint32_t ld(const uint32_t *p) { return *p; }
+};
+
 // Four bytes starting at an arbitrary address: two aligned 32-bit loads and
 // a funnel shift. Callers keep 16 bytes of slack around every string buffer
 // so the aligned words never leave the allocation.
+template <typename L = LdgLoad>
 __device__ __forceinline__ uint32_t load4(const uint8_t *p) {
     const uintptr_t a = reinterpret_cast<uintptr_t>(p);
     const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~uintptr_t(3));
-    return __funnelshift_r(__ldg(w), __ldg(w + 1), (uint32_t)(a & 3) * 8u);
+    return __funnelshift_r(L::ld(w), L::ld(w + 1), (uint32_t)(a & 3) * 8u);
 }
 
 // Sequential reader: 4 characters per call, one aligned load per call,
 // issued one call ahead so its latency overlaps the caller's columns. Reads
 // at most 12 bytes past the last character returned (the 16-byte slack).
-struct TextScan {
+template <typename L = LdgLoad>
+struct TextScanT {
     const uint32_t *w;
     uint32_t lo, hi, sh;
     __device__ __forceinline__ void init(const uint8_t *p) {
         const uintptr_t a = reinterpret_cast<uintptr_t>(p);
         w = reinterpret_cast<const uint32_t *>(a & ~uintptr_t(3));
         sh = (uint32_t)(a & 3) * 8u;
-        lo = __ldg(w);
-        hi = __ldg(++w);
+        lo = L::ld(w);
+        hi = L::ld(++w);
     }
     __device__ __forceinline__ uint32_t next4() {
         const uint32_t r = __funnelshift_r(lo, hi, sh);
         lo = hi;
-        hi = __ldg(++w);
+        hi = L::ld(++w);
         return r;
     }
 };
+using TextScan = TextScanT<LdgLoad>;
 
 // Non-prefetching variant for register-bound loops (the full-word search
 // loop), where the extra live word costs more than the load latency saves.
@@ -268,11 +280,12 @@ __device__ __forceinline__ int lane_wavefront(bool valid, int m, const uint8_t *
 // ------------------------------------------------------------ pairs: main --
 // Trim the common prefix and suffix with 4-byte window compares (exact:
 // d(xPy, xQy) = d(P, Q), csrc/myers.c:80-87).
+template <typename L = LdgLoad>
 __device__ __forceinline__ void trim_windows(const uint8_t *&a, int &la, const uint8_t *&b, int &lb) {
     const int lim = la < lb ? la : lb;
     int p = 0;
     while (p < lim) {
-        const uint32_t x = load4(a + p) ^ load4(b + p);
+        const uint32_t x = load4<L>(a + p) ^ load4<L>(b + p);
         int q = x ? (__ffs(x) - 1) >> 3 : 4;               // equal leading bytes
         if (q > lim - p) q = lim - p;
         p += q;
@@ -281,7 +294,7 @@ __device__ __forceinline__ void trim_windows(const uint8_t *&a, int &la, const u
     const int lim2 = lim - p;
     int s = 0;
     while (s < lim2) {
-        const uint32_t x = load4(a + la - s - 4) ^ load4(b + lb - s - 4);
+        const uint32_t x = load4<L>(a + la - s - 4) ^ load4<L>(b + lb - s - 4);
         int q = x ? __clz(x) >> 3 : 4;                     // equal trailing bytes
         if (q > lim2 - s) q = lim2 - s;
         s += q;
@@ -299,8 +312,9 @@ __device__ __forceinline__ uint64_t nib_eq(const uint64_t *tc, uint32_t c) {
     return tc[(c >> 4) * 32] & tc[(16 + (c & 15)) * 32];
 }
 
+template <typename L = LdgLoad>
 __device__ __forceinline__ void nib_build(uint64_t *tc, const uint8_t *p, int m) {
-    TextScan ps;
+    TextScanT<L> ps;
     ps.init(p);
     for (int i = 0; i < m; i += 4) {
         const uint32_t w4 = ps.next4();
@@ -316,8 +330,9 @@ __device__ __forceinline__ void nib_build(uint64_t *tc, const uint8_t *p, int m)
     }
 }
 
+template <typename L = LdgLoad>
 __device__ __forceinline__ void nib_clear(uint64_t *tc, const uint8_t *p, int m) {
-    TextScan ps;
+    TextScanT<L> ps;
     ps.init(p);
     for (int i = 0; i < m; i += 4) {
         const uint32_t w4 = ps.next4();
@@ -333,15 +348,15 @@ __device__ __forceinline__ void nib_clear(uint64_t *tc, const uint8_t *p, int m)
 }
 
 // Single-word pair (1 <= m <= 64, m <= n): pattern p, text t.
-template <bool HASK>
+template <bool HASK, typename L = LdgLoad>
 __device__ __forceinline__ int solve_word(uint64_t *tc, const uint8_t *p, int m, const uint8_t *t,
                                           int n, int k, int *cols_out = nullptr) {
-    nib_build(tc, p, m);
+    nib_build<L>(tc, p, m);
     uint64_t pv = ~0ull, mv = 0;
     const int lastbit = m - 1;
     int score = m;
     bool dead = false;
-    TextScan ts;
+    TextScanT<L> ts;
     ts.init(t);
     int j = 0;
     for (; j + 4 <= n; j += 4) {
@@ -366,7 +381,7 @@ __device__ __forceinline__ int solve_word(uint64_t *tc, const uint8_t *p, int m,
             score += hdelta<uint64_t>(ph, mh, lastbit);
         }
     }
-    nib_clear(tc, p, m);
+    nib_clear<L>(tc, p, m);
     if (dead) return k + 1;
     if (cols_out) *cols_out = n;
     return HASK ? cap_k(score, k) : score;
