@@ -39,6 +39,8 @@ cudaError_t launch_pairs_long(cudaStream_t st, int grid, bool hask, const LongQu
 cudaError_t launch_pairs_staged(cudaStream_t st, int sms, bool hask, const DevStrings &A, const DevStrings &B,
                                 int k, int dtype, void *out, const LongQueue &q, uint32_t *status);
 cudaError_t launch_fill(cudaStream_t st, int sms, void *out, int64_t n, int dtype, uint32_t v);
+cudaError_t launch_pairs_tile(cudaStream_t st, int sms, bool hask, const DevStrings &A, const DevStrings &B,
+                              int tile_pairs, int k, int dtype, void *out, const LongQueue &q, uint32_t *status);
 cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, const DevStrings &A,
                               const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
                               uint32_t *status);
@@ -87,6 +89,8 @@ struct blg_pairs {
     OwnedStrings a, b;
     int64_t n = 0;
     int64_t cap[kLongClasses] = {0, 0, 0, 0, 0};
+    int64_t short_pairs = 0;      // pairs whose shorter string is at most 32 bytes
+    int64_t len_max_side = 0;     // total bytes of the larger side (a or b)
     void *q_items = nullptr;      // all class regions, one allocation
     int32_t *q_ctr = nullptr;     // counts[5], heads[5]
     // scheduled path (prep -> order -> solve), allocated on first use
@@ -231,11 +235,18 @@ static int pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const 
     if (rc) return rc;
     // Long-queue capacity per class: trimming only shortens a pattern, so a
     // pair can land in class j only if its untrimmed shorter length reaches it.
+    // The tile kernel queues every pattern longer than 32 (32 < m <= 64 goes
+    // to class 0 too); the other pairs kernels queue patterns longer than 64.
     int64_t hist[kLongClasses + 1] = {0, 0, 0, 0, 0, 0};
+    p->short_pairs = 0;
+    p->len_max_side = n > 0 ? std::max(oa[n] - oa[0], ob[n] - ob[0]) : 0;
     for (int64_t i = 0; i < n; i++) {
         const int64_t la = oa[i + 1] - oa[i], lb = ob[i + 1] - ob[i];
         const int64_t m = la < lb ? la : lb;
-        if (m <= 64) continue;
+        if (m <= 32) {
+            p->short_pairs++;
+            continue;
+        }
         const int64_t W = (m + 63) >> 6;
         const int cls = W <= 2 ? 0 : W <= 4 ? 1 : W <= 8 ? 2 : W <= 16 ? 3 : W <= 32 ? 4 : 5;
         hist[cls]++;
@@ -329,7 +340,13 @@ static int pairs_run(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, in
     if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
     if (p->n == 0) return BLG_OK;
     if (!d_out) return fail(c, BLG_ERR_ARG, "null output");
-    if (c->sched != BLG_SCHED_PLAIN || exit_log) return pairs_run_scheduled(c, p, k, dtype, d_out, exit_log);
+    // Short pairs (the shorter string <= 32 bytes for at least 3 in 4 pairs)
+    // run in the tile kernel under the automatic schedule: trimming, the
+    // in-CTA work sort and the 32-bit solve need no global work plan.
+    const bool use_tile = c->sched == BLG_SCHED_AUTO && !exit_log &&
+                          4 * p->short_pairs >= 3 * p->n;
+    if (!use_tile && (c->sched != BLG_SCHED_PLAIN || exit_log))
+        return pairs_run_scheduled(c, p, k, dtype, d_out, exit_log);
     const bool hask = k >= 0;
     LongQueue q{};
     int64_t total = 0;
@@ -342,13 +359,21 @@ static int pairs_run(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, in
     q.heads = p->q_ctr ? p->q_ctr + kLongClasses : nullptr;
     if (total > 0)
         CK(cudaMemsetAsync(p->q_ctr, 0, sizeof(int32_t) * 2 * kLongClasses, c->stream), "reset queue");
-    // 64 KB of nibble tables per 256-thread CTA: 3 CTAs per SM.
-    const int64_t want = (p->n + 255) / 256;
-    const int grid = (int)std::min<int64_t>(want, (int64_t)c->sms * 3 * 16);
-    CK(launch(c, "pairs_staged", [&] {
-           return launch_pairs_staged(c->stream, c->sms, hask, p->a.d, p->b.d, k, dtype, d_out, q, c->d_status);
-       }), "pairs_staged");
-    (void)grid;
+    if (use_tile) {
+        // 512 pairs per tile while each side averages <= 33 bytes; longer
+        // strings get smaller tiles so a tile's span still fits the stage
+        const double avg = (double)p->len_max_side / (double)p->n;
+        const int tile = avg <= 33.0 ? 512 : std::max(32, (int)(17000.0 / avg) & ~31);
+        CK(launch(c, "pairs_tile", [&] {
+               return launch_pairs_tile(c->stream, c->sms, hask, p->a.d, p->b.d, tile, k, dtype, d_out, q,
+                                        c->d_status);
+           }), "pairs_tile");
+    } else {
+        CK(launch(c, "pairs_staged", [&] {
+               return launch_pairs_staged(c->stream, c->sms, hask, p->a.d, p->b.d, k, dtype, d_out, q,
+                                          c->d_status);
+           }), "pairs_staged");
+    }
     if (total > 0)
         CK(launch(c, "pairs_long", [&] {
                return launch_pairs_long(c->stream, c->sms * 3, hask, q, k, dtype, d_out);
