@@ -29,6 +29,10 @@ cudaError_t launch_build_peq(cudaStream_t st, const DevStrings &Q, const int32_t
 cudaError_t launch_search_seq(cudaStream_t st, int nw, bool hask, const DevStrings &C,
                               const SearchClass &cls, int qpb, int k, int dtype, void *out,
                               uint32_t *status);
+cudaError_t launch_search_tt(cudaStream_t st, int nw, bool hask, const TransposedChoices &T,
+                             const SearchClass &cls, int qpb, int k, int dtype, void *out);
+cudaError_t launch_transpose_choices(cudaStream_t st, int sms, const DevStrings &C, const int64_t *base,
+                                     uint32_t *words, int32_t *len, uint32_t *status);
 cudaError_t launch_search_lanes(cudaStream_t st, bool hask, const DevStrings &C, const SearchClass &cls,
                                 int nwc, int k, int dtype, void *out, uint32_t *status);
 cudaError_t launch_pairs_main(cudaStream_t st, int grid, bool hask, const DevStrings &A,
@@ -121,6 +125,12 @@ struct blg_search {
     int32_t *perm = nullptr;
     int64_t *lstart = nullptr;
     int64_t min_len = 0, n_len = 0;
+    // choices in tile-transposed form (exact and unsorted runs), when the
+    // padding to each tile's longest choice stays small
+    bool tt = false;
+    uint32_t *tt_words = nullptr;
+    int64_t *tt_base = nullptr;
+    int32_t *tt_len = nullptr;
 };
 
 // ------------------------------------------------------------ helpers --
@@ -485,6 +495,32 @@ static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64
             s->lsorted = true;
         }
     }
+    // Tile-transposed choices: padded size = sum over tiles of kTileCands x
+    // the tile's longest choice; kept when at most twice the packed bytes
+    // (plus 64 MiB), so a few long choices cannot blow up the copy.
+    if (nc > 0) {
+        const int64_t tiles = (nc + kTileCands - 1) / kTileCands;
+        std::vector<int64_t> base(tiles + 1, 0);
+        for (int64_t t = 0; t < tiles; t++) {
+            int64_t mx = 0;
+            const int64_t e = std::min(nc, (t + 1) * kTileCands);
+            for (int64_t i = t * kTileCands; i < e; i++) mx = std::max(mx, oc[i + 1] - oc[i]);
+            base[t + 1] = base[t] + kTileCands * ((mx + 3) / 4);
+        }
+        const int64_t bytes = oc[nc] - oc[0];
+        if (base[tiles] * 4 <= 2 * bytes + (64ll << 20)) {
+            CK(dev_alloc(c, (void **)&s->tt_words, sizeof(uint32_t) * (size_t)base[tiles] + 16), "cudaMallocAsync(tt)");
+            CK(dev_alloc(c, (void **)&s->tt_base, sizeof(int64_t) * (size_t)(tiles + 1)), "cudaMallocAsync(tt base)");
+            CK(dev_alloc(c, (void **)&s->tt_len, sizeof(int32_t) * (size_t)nc), "cudaMallocAsync(tt len)");
+            CK(cudaMemcpyAsync(s->tt_base, base.data(), sizeof(int64_t) * (tiles + 1), cudaMemcpyHostToDevice,
+                               c->stream), "H2D tt base");
+            CK(launch(c, "transpose_choices", [&] {
+                   return launch_transpose_choices(c->stream, c->sms, s->c.d, s->tt_base, s->tt_words, s->tt_len,
+                                                   c->d_status);
+               }), "transpose_choices");
+            s->tt = true;
+        }
+    }
     // the host vectors above are pageable: the copies completed before return
     return BLG_OK;
 }
@@ -537,10 +573,17 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out) 
                }), "search_lanes");
         } else {
             const int qpb = pick_qpb(c, k_.nq, s->nc);
-            CK(launch(c, "search_seq", [&] {
-                   return launch_search_seq(c->stream, k_.nw, hask, s->c.d, sc, qpb, k, dtype, d_out,
-                                            c->d_status);
-               }), "search_seq");
+            if (s->tt) {
+                const TransposedChoices T{s->tt_words, s->tt_base, s->tt_len, s->nc};
+                CK(launch(c, "search_tt", [&] {
+                       return launch_search_tt(c->stream, k_.nw, hask, T, sc, qpb, k, dtype, d_out);
+                   }), "search_tt");
+            } else {
+                CK(launch(c, "search_seq", [&] {
+                       return launch_search_seq(c->stream, k_.nw, hask, s->c.d, sc, qpb, k, dtype, d_out,
+                                                c->d_status);
+                   }), "search_seq");
+            }
         }
     }
     return BLG_OK;
@@ -555,6 +598,13 @@ static void search_release(blg_ctx *c, blg_search *s) {
     s->perm = nullptr;
     s->lstart = nullptr;
     s->lsorted = false;
+    dev_free(c, s->tt_words);
+    dev_free(c, s->tt_base);
+    dev_free(c, s->tt_len);
+    s->tt_words = nullptr;
+    s->tt_base = nullptr;
+    s->tt_len = nullptr;
+    s->tt = false;
     for (auto &k : s->cls) {
         dev_free(c, k.qidx);
         dev_free(c, k.qlen);

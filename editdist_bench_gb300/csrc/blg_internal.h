@@ -46,6 +46,20 @@ struct LongQueue {
     int32_t *heads;                  // kLongClasses consumers' counters
 };
 
+// Choices in tile-transposed form (exact search): tiles of kTileCands
+// consecutive choices; word w (bytes 4w..4w+3) of choice c of tile T sits at
+// words[base[T] + w * kTileCands + (c - T * kTileCands)], so the 32 lanes of
+// a warp reading their choices' word w touch one 128-byte line. base[T+1] -
+// base[T] = kTileCands * ceil(longest choice of T / 4); len[c] = length.
+constexpr int kTileCands = 1024;
+
+struct TransposedChoices {
+    const uint32_t *words = nullptr;
+    const int64_t *base = nullptr;    // [tiles + 1]
+    const int32_t *len = nullptr;     // [n]
+    int64_t n = 0;
+};
+
 // Per-query-class search launch description.
 struct SearchClass {
     int nw;                 // pattern words (sequential kernels) or 0 for lane-spread

@@ -74,6 +74,68 @@ __global__ void __launch_bounds__(256) k_search_seq(DevStrings C, SearchClass cl
     }
 }
 
+// Exact-capable search over tile-transposed choices: grid x = choice tiles
+// of kTileCands, y = query chunks of `qpb`. Thread t owns choices t, t+256,
+// t+512, t+768 of the tile, so a warp's text loads and its result stores are
+// each one contiguous line.
+template <int NW, bool HASK>
+__global__ void __launch_bounds__(256) k_search_tt(TransposedChoices T, SearchClass cls, int qpb, int k,
+                                                   int dtype, void *out, uint32_t unit) {
+    extern __shared__ uint64_t s_peq[];
+    const Units u{unit, unit + unit};
+    RowAddr<NW> ra;
+    ra.init(u);
+    const int64_t nc = T.n;
+    const int64_t tile = blockIdx.x;
+    const int64_t c0 = tile * kTileCands + threadIdx.x;
+    const uint32_t *tw = T.words + T.base[tile] + threadIdx.x;
+    const int q_begin = blockIdx.y * qpb;
+    const int q_end = min(q_begin + qpb, cls.nq);
+    constexpr int kWords = 256 * NW;
+    for (int qi = q_begin; qi < q_end; qi++) {
+        __syncthreads();
+        const uint64_t *src = cls.peq + (size_t)qi * kWords;
+        for (int x = threadIdx.x; x < kWords; x += blockDim.x) s_peq[x] = __ldg(src + x);
+        __syncthreads();
+        const int m = cls.qlen[qi];
+        const int64_t row = cls.qidx[qi] * nc;
+#pragma unroll 1
+        for (int t = 0; t < 4; t++) {
+            const int64_t c = c0 + 256 * t;
+            if (c >= nc) break;
+            const int d = dist_tt<NW, HASK>(s_peq, m, tw + 256 * t, __ldg(T.len + c), k, u, ra);
+            store1(out, dtype, row + c, d);
+        }
+    }
+}
+
+// Transpose choices into tiles (see TransposedChoices); one thread per
+// (choice, word), bytes past a choice's end are zero.
+__global__ void __launch_bounds__(256) k_transpose_choices(DevStrings C, const int64_t *base, uint32_t *words,
+                                                           int32_t *len, uint32_t *status) {
+    const int64_t nc = C.n;
+    const int64_t tiles = (nc + kTileCands - 1) / kTileCands;
+    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int64_t b0 = base[tile];
+        const int nwords = (int)((base[tile + 1] - b0) / kTileCands);
+        for (int cl = threadIdx.x; cl < kTileCands; cl += blockDim.x) {
+            const int64_t c = tile * kTileCands + cl;
+            int n = 0;
+            const uint8_t *p = c < nc ? string_at(C, c, n, status) : C.buf;
+            if (c < nc) len[c] = n;
+            for (int w = 0; w < nwords; w++) {
+                uint32_t v = 0;
+                const int rem = n - 4 * w;
+                if (rem > 0) {
+                    v = load4(p + 4 * w);
+                    if (rem < 4) v &= (1u << (8 * rem)) - 1u;
+                }
+                words[b0 + (int64_t)w * kTileCands + cl] = v;
+            }
+        }
+    }
+}
+
 // ----------------------------------------------- search, long queries (lanes) --
 // grid: x = candidate tiles of (warps * 32/L), y = queries of the class.
 template <bool HASK>
@@ -467,6 +529,47 @@ cudaError_t launch_search_seq(cudaStream_t st, int nw, bool hask, const DevStrin
     case 8: return launch_seq<8>(hask, grid, smem, st, C, cls, qpb, k, dtype, out, status);
     default: return cudaErrorInvalidValue;
     }
+}
+
+template <int NW>
+static cudaError_t launch_tt(bool hask, dim3 grid, size_t smem, cudaStream_t st, const TransposedChoices &T,
+                             const SearchClass &cls, int qpb, int k, int dtype, void *out) {
+    if (hask) {
+        cudaFuncSetAttribute(k_search_tt<NW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_search_tt<NW, true><<<grid, 256, smem, st>>>(T, cls, qpb, k, dtype, out, 1u);
+    } else {
+        cudaFuncSetAttribute(k_search_tt<NW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_search_tt<NW, false><<<grid, 256, smem, st>>>(T, cls, qpb, k, dtype, out, 1u);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_search_tt(cudaStream_t st, int nw, bool hask, const TransposedChoices &T,
+                             const SearchClass &cls, int qpb, int k, int dtype, void *out) {
+    if (cls.nq <= 0 || T.n <= 0) return cudaSuccess;
+    const int64_t tiles = (T.n + kTileCands - 1) / kTileCands;
+    dim3 grid((unsigned)tiles, (unsigned)((cls.nq + qpb - 1) / qpb));
+    const size_t smem = (size_t)256 * nw * sizeof(uint64_t);
+    switch (nw) {
+    case 1: return launch_tt<1>(hask, grid, smem, st, T, cls, qpb, k, dtype, out);
+    case 2: return launch_tt<2>(hask, grid, smem, st, T, cls, qpb, k, dtype, out);
+    case 3: return launch_tt<3>(hask, grid, smem, st, T, cls, qpb, k, dtype, out);
+    case 4: return launch_tt<4>(hask, grid, smem, st, T, cls, qpb, k, dtype, out);
+    case 5: return launch_tt<5>(hask, grid, smem, st, T, cls, qpb, k, dtype, out);
+    case 6: return launch_tt<6>(hask, grid, smem, st, T, cls, qpb, k, dtype, out);
+    case 7: return launch_tt<7>(hask, grid, smem, st, T, cls, qpb, k, dtype, out);
+    case 8: return launch_tt<8>(hask, grid, smem, st, T, cls, qpb, k, dtype, out);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_transpose_choices(cudaStream_t st, int sms, const DevStrings &C, const int64_t *base,
+                                     uint32_t *words, int32_t *len, uint32_t *status) {
+    if (C.n <= 0) return cudaSuccess;
+    const int64_t tiles = (C.n + kTileCands - 1) / kTileCands;
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)sms * 8);
+    k_transpose_choices<<<grid, 256, 0, st>>>(C, base, words, len, status);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_search_lanes(cudaStream_t st, bool hask, const DevStrings &C, const SearchClass &cls,

@@ -216,6 +216,68 @@ __device__ __forceinline__ int dist_seq(const uint64_t *peq, int m, const uint8_
     return HASK ? cap_k(score, k) : score;
 }
 
+// One text column through the NW words of the query without the score
+// (the score is read from the vertical deltas when needed).
+template <int NW>
+__device__ __forceinline__ void column_v(Word2 (&st)[NW], const uint64_t *row, Units u) {
+    uint32_t Phl, Phh, Mhl, Mhh;
+    uint32_t cp = u.one, cm = 0;
+#pragma unroll
+    for (int w = 0; w < NW; w++) {
+        const uint64_t e = row[w];
+        step_h(st[w], (uint32_t)e, (uint32_t)(e >> 32), cp, cm, u, Phl, Phh, Mhl, Mhh);
+        if (w < NW - 1) {
+            cp = top_bit(Phh, u);
+            cm = top_bit(Mhh, u);
+        }
+    }
+}
+
+// Sum of the vertical deltas of the pattern rows (the last word masked to
+// its `lastbits` = m - 64 (NW - 1) rows): D[m][j] = j + this, after j columns.
+template <int NW>
+__device__ __forceinline__ int vsum(const Word2 (&st)[NW], uint32_t ml, uint32_t mh) {
+    int s = 0;
+#pragma unroll
+    for (int w = 0; w < NW - 1; w++)
+        s += popc32(st[w].pl) + popc32(st[w].ph) - popc32(st[w].ml) - popc32(st[w].mh);
+    s += popc32(st[NW - 1].pl & ml) + popc32(st[NW - 1].ph & mh) - popc32(st[NW - 1].ml & ml) -
+         popc32(st[NW - 1].mh & mh);
+    return s;
+}
+
+// d(query, choice) with the choice in tile-transposed form: word w of the
+// text at txt[w * kTileCands] (one coalesced line per warp).
+template <int NW, bool HASK>
+__device__ __forceinline__ int dist_tt(const uint64_t *peq, int m, const uint32_t *txt, int n, int k, Units u,
+                                       const RowAddr<NW> &ra) {
+    if (m == 0) return cap_k(n, k);                    // csrc/gpu_kernels.cu:53
+    if (HASK && (n > m ? n - m : m - n) > k) return k + 1;
+    Word2 st[NW];
+#pragma unroll
+    for (int w = 0; w < NW; w++) { st[w].pl = st[w].ph = ~0u; st[w].ml = st[w].mh = 0; }
+    const int lb = m - 64 * (NW - 1);                  // rows of the last word, 1..64
+    const uint32_t ml = lb >= 32 ? ~0u : ((1u << lb) - 1u);
+    const uint32_t mh = lb >= 64 ? ~0u : (lb <= 32 ? 0u : ((1u << (lb - 32)) - 1u));
+    const char *base = reinterpret_cast<const char *>(peq);
+    int j = 0;
+    uint32_t nxt = n > 0 ? __ldg(txt) : 0u;            // one word ahead
+    for (; j + 4 <= n; j += 4) {
+        const uint32_t w4 = nxt;
+        if (j + 4 < n) nxt = __ldg(txt + ((j >> 2) + 1) * kTileCands);
+        column_v<NW>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<0>(w4)), u);
+        column_v<NW>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<1>(w4)), u);
+        column_v<NW>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<2>(w4)), u);
+        column_v<NW>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<3>(w4)), u);
+        // the exit test is monotone in j, so testing every 4th column is exact
+        if (HASK && hopeless(j + 4 + vsum<NW>(st, ml, mh), j + 3, n, k)) return k + 1;
+    }
+    for (uint32_t w4 = nxt; j < n; j++, w4 >>= 8)
+        column_v<NW>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<0>(w4)), u);
+    const int d = n + vsum<NW>(st, ml, mh);
+    return HASK ? cap_k(d, k) : d;
+}
+
 template <int NW, bool HASK>
 __device__ __forceinline__ int dist_seq_any(const uint64_t *peq, int m, const uint8_t *t, int n, int k,
                                             Units u, const RowAddr<NW> &ra) {
