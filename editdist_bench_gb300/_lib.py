@@ -51,6 +51,8 @@ SIGNATURES = [
     ("blg_sched_load", ctypes.c_int, [_P, ctypes.c_char_p]),
     ("blg_malloc", ctypes.c_int, [_P, _SZ, ctypes.POINTER(_P)]),
     ("blg_free", ctypes.c_int, [_P, _P]),
+    ("blg_host_alloc", ctypes.c_int, [_P, _SZ, ctypes.POINTER(_P)]),
+    ("blg_host_free", ctypes.c_int, [_P, _P]),
     ("blg_memcpy_h2d", ctypes.c_int, [_P, _P, _P, _SZ]),
     ("blg_memcpy_d2h", ctypes.c_int, [_P, _P, _P, _SZ]),
     ("blg_memset", ctypes.c_int, [_P, _P, ctypes.c_int, _SZ]),

@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -179,30 +181,48 @@ static int check_offsets_host(blg_ctx *c, const int64_t *off, int64_t n) {
     return BLG_OK;
 }
 
-// Copy a packed string set into HBM with 16 bytes of slack on both sides.
-static int upload_strings(blg_ctx *c, const uint8_t *buf, const int64_t *off, int64_t n,
-                          OwnedStrings &o) {
+// Device storage for a packed string set: the bytes with 16 bytes of
+// (zeroed) slack on both sides, and the offsets. Nothing is copied yet.
+static int alloc_strings(blg_ctx *c, const uint8_t *buf, const int64_t *off, int64_t n, OwnedStrings &o) {
     int rc = check_offsets_host(c, off, n);
     if (rc) return rc;
     const int64_t base = n > 0 ? off[0] : 0;
     const int64_t bytes = n > 0 ? off[n] - off[0] : 0;
     if (bytes > 0 && !buf) return fail(c, BLG_ERR_ARG, "null buffer");
     CK(dev_alloc(c, &o.mem_buf, (size_t)bytes + 32), "cudaMallocAsync(strings)");
-    CK(cudaMemsetAsync(o.mem_buf, 0, (size_t)bytes + 32, c->stream), "cudaMemsetAsync(strings)");
     uint8_t *dbuf = (uint8_t *)o.mem_buf + 16;
-    if (bytes > 0)
-        CK(cudaMemcpyAsync(dbuf, buf + base, (size_t)bytes, cudaMemcpyHostToDevice, c->stream),
-           "H2D strings");
+    // only the 16-byte slack on either side needs defined contents
+    CK(cudaMemsetAsync(o.mem_buf, 0, 16, c->stream), "cudaMemsetAsync(slack)");
+    CK(cudaMemsetAsync(dbuf + bytes, 0, 16, c->stream), "cudaMemsetAsync(slack)");
     CK(dev_alloc(c, &o.mem_off, sizeof(int64_t) * (size_t)(n + 1)), "cudaMallocAsync(offsets)");
-    if (n > 0)
-        CK(cudaMemcpyAsync(o.mem_off, off, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyHostToDevice,
-                           c->stream), "H2D offsets");
     o.d.buf = dbuf;
     o.d.off = (const int64_t *)o.mem_off;
     o.d.n = n;
     o.d.base = base;
     o.d.bytes = bytes;
     return BLG_OK;
+}
+
+// Copy strings [i0, i1) of a packed set (and offsets i0..i1) into storage
+// made by alloc_strings, on stream `st`.
+static int copy_strings(blg_ctx *c, const uint8_t *buf, const int64_t *off, int64_t i0, int64_t i1,
+                        OwnedStrings &o, cudaStream_t st) {
+    if (i1 <= i0) return BLG_OK;
+    const int64_t b0 = off[i0] - o.d.base, b1 = off[i1] - o.d.base;
+    if (b1 > b0)
+        CK(cudaMemcpyAsync((uint8_t *)o.d.buf + b0, buf + off[i0], (size_t)(b1 - b0), cudaMemcpyHostToDevice, st),
+           "H2D strings");
+    CK(cudaMemcpyAsync((int64_t *)o.mem_off + i0, off + i0, sizeof(int64_t) * (size_t)(i1 - i0 + 1),
+                       cudaMemcpyHostToDevice, st), "H2D offsets");
+    return BLG_OK;
+}
+
+// Copy a packed string set into HBM with 16 bytes of slack on both sides.
+static int upload_strings(blg_ctx *c, const uint8_t *buf, const int64_t *off, int64_t n,
+                          OwnedStrings &o) {
+    int rc = alloc_strings(c, buf, off, n, o);
+    if (!rc) rc = copy_strings(c, buf, off, 0, n, o, c->stream);
+    return rc;
 }
 
 static void free_strings(blg_ctx *c, OwnedStrings &o) {
@@ -237,29 +257,55 @@ static size_t dtype_size(int dt) { return dt == BLG_UINT8 ? 1 : dt == BLG_UINT16
 static bool dtype_ok(int dt) { return dt == BLG_INT32 || dt == BLG_UINT16 || dt == BLG_UINT8; }
 
 // ------------------------------------------------------------- pairs --
-static int pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uint8_t *bb,
-                        const int64_t *ob, int64_t n, blg_pairs *p) {
-    p->n = n;
-    int rc = upload_strings(c, ba, oa, n, p->a);
-    if (!rc) rc = upload_strings(c, bb, ob, n, p->b);
+// Host pass over the offsets: how many pairs are short (shorter string <= 32
+// bytes) and the long-queue capacity per class. Trimming only shortens a
+// pattern, so a pair can land in class j only if its untrimmed shorter
+// length reaches it. The tile kernel queues every pattern longer than 32
+// (32 < m <= 64 goes to class 0 too); the other pairs kernels queue
+// patterns longer than 64.
+static int pairs_classify(blg_ctx *c, const int64_t *oa, const int64_t *ob, int64_t n, blg_pairs *p) {
+    int rc = check_offsets_host(c, oa, n);
+    if (!rc) rc = check_offsets_host(c, ob, n);
     if (rc) return rc;
-    // Long-queue capacity per class: trimming only shortens a pattern, so a
-    // pair can land in class j only if its untrimmed shorter length reaches it.
-    // The tile kernel queues every pattern longer than 32 (32 < m <= 64 goes
-    // to class 0 too); the other pairs kernels queue patterns longer than 64.
     int64_t hist[kLongClasses + 1] = {0, 0, 0, 0, 0, 0};
-    p->short_pairs = 0;
+    p->n = n;
     p->len_max_side = n > 0 ? std::max(oa[n] - oa[0], ob[n] - ob[0]) : 0;
-    for (int64_t i = 0; i < n; i++) {
-        const int64_t la = oa[i + 1] - oa[i], lb = ob[i + 1] - ob[i];
-        const int64_t m = la < lb ? la : lb;
-        if (m <= 32) {
-            p->short_pairs++;
-            continue;
+    // the pass reads 16 bytes of offsets per pair: large sets are split
+    // over host threads
+    const int nt = n >= (1 << 20) ? (int)std::min<unsigned>(8, std::max(1u, std::thread::hardware_concurrency())) : 1;
+    std::vector<std::array<int64_t, kLongClasses + 2>> part(nt);
+    auto work = [&](int t) {
+        std::array<int64_t, kLongClasses + 2> h{};
+        const int64_t i0 = n * t / nt, i1 = n * (t + 1) / nt;
+        int64_t shorts = 0;
+        for (int64_t i = i0; i < i1; i++) {                  // branch-free, vectorisable
+            const int64_t la = oa[i + 1] - oa[i], lb = ob[i + 1] - ob[i];
+            shorts += (la <= 32) | (lb <= 32);
         }
-        const int64_t W = (m + 63) >> 6;
-        const int cls = W <= 2 ? 0 : W <= 4 ? 1 : W <= 8 ? 2 : W <= 16 ? 3 : W <= 32 ? 4 : 5;
-        hist[cls]++;
+        if (shorts < i1 - i0) {
+            for (int64_t i = i0; i < i1; i++) {
+                const int64_t la = oa[i + 1] - oa[i], lb = ob[i + 1] - ob[i];
+                const int64_t m = la < lb ? la : lb;
+                if (m <= 32) continue;
+                const int64_t W = (m + 63) >> 6;
+                h[W <= 2 ? 0 : W <= 4 ? 1 : W <= 8 ? 2 : W <= 16 ? 3 : W <= 32 ? 4 : 5]++;
+            }
+        }
+        h[kLongClasses + 1] = shorts;
+        part[t] = h;
+    };
+    if (nt == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 1; t < nt; t++) th.emplace_back(work, t);
+        work(0);
+        for (auto &x : th) x.join();
+    }
+    p->short_pairs = 0;
+    for (int t = 0; t < nt; t++) {
+        for (int j = 0; j <= kLongClasses; j++) hist[j] += part[t][j];
+        p->short_pairs += part[t][kLongClasses + 1];
     }
     int64_t total = 0, above = hist[kLongClasses];
     for (int j = kLongClasses - 1; j >= 0; j--) {
@@ -275,6 +321,14 @@ static int pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const 
         CK(dev_alloc(c, (void **)&p->q_ctr, sizeof(int32_t) * 2 * kLongClasses), "cudaMallocAsync(ctr)");
     }
     return BLG_OK;
+}
+
+static int pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uint8_t *bb,
+                        const int64_t *ob, int64_t n, blg_pairs *p) {
+    int rc = upload_strings(c, ba, oa, n, p->a);
+    if (!rc) rc = upload_strings(c, bb, ob, n, p->b);
+    if (!rc) rc = pairs_classify(c, oa, ob, n, p);
+    return rc;
 }
 
 constexpr size_t kPlanCounters = 2 * kPairClasses + 2 * kPairClasses * kCostBuckets;
@@ -315,8 +369,8 @@ static PairsPlan plan_view(blg_pairs *p) {
 
 // prep -> order -> solve (every schedule but PLAIN). exit_log (optional,
 // device int32[n]) receives the columns each pair's column loop processed.
-static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, int32_t *exit_log,
-                               bool want_features = false) {
+static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, const DevStrings &A, const DevStrings &B, int k,
+                               int dtype, void *d_out, int32_t *exit_log, bool want_features = false) {
     const bool hask = k >= 0;
     // the learned order needs a trained network; otherwise cost buckets order the work
     const bool learned = want_features || (c->sched == BLG_SCHED_LEARNED && c->model && sched_model_trained(c->model));
@@ -324,11 +378,10 @@ static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, int k, int dtype, void 
     if (rc) return rc;
     const PairsPlan plan = plan_view(p);
     CK(cudaMemsetAsync(p->plan_ctr, 0, sizeof(int32_t) * kPlanCounters, c->stream), "reset plan");
-    if (exit_log) CK(cudaMemsetAsync(exit_log, 0, sizeof(int32_t) * (size_t)p->n, c->stream), "reset log");
-    const int grid = (int)std::min<int64_t>((p->n + 255) / 256, (int64_t)c->sms * 8);
+    if (exit_log) CK(cudaMemsetAsync(exit_log, 0, sizeof(int32_t) * (size_t)A.n, c->stream), "reset log");
+    const int grid = (int)std::min<int64_t>((A.n + 255) / 256, (int64_t)c->sms * 8);
     CK(launch(c, "pairs_prep", [&] {
-           return launch_pairs_prep(c->stream, grid, hask, learned, p->a.d, p->b.d, k, dtype, d_out, plan,
-                                    c->d_status);
+           return launch_pairs_prep(c->stream, grid, hask, learned, A, B, k, dtype, d_out, plan, c->d_status);
        }), "pairs_prep");
     if (learned && !want_features)
         CK(launch(c, "sched_keys", [&] { return launch_mlp_keys(c->stream, c->sms, c->model, plan); }), "sched_keys");
@@ -346,17 +399,17 @@ static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, int k, int dtype, void 
     return BLG_OK;
 }
 
-static int pairs_run(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, int32_t *exit_log = nullptr) {
-    if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
-    if (p->n == 0) return BLG_OK;
-    if (!d_out) return fail(c, BLG_ERR_ARG, "null output");
-    // Short pairs (the shorter string <= 32 bytes for at least 3 in 4 pairs)
-    // run in the tile kernel under the automatic schedule: trimming, the
-    // in-CTA work sort and the 32-bit solve need no global work plan.
-    const bool use_tile = c->sched == BLG_SCHED_AUTO && !exit_log &&
-                          4 * p->short_pairs >= 3 * p->n;
-    if (!use_tile && (c->sched != BLG_SCHED_PLAIN || exit_log))
-        return pairs_run_scheduled(c, p, k, dtype, d_out, exit_log);
+// Short pairs (the shorter string <= 32 bytes for at least 3 in 4 pairs)
+// run in the tile kernel under the automatic schedule: trimming, the
+// in-CTA work sort and the 32-bit solve need no global work plan.
+static bool pairs_use_tile(const blg_ctx *c, const blg_pairs *p) {
+    return c->sched == BLG_SCHED_AUTO && 4 * p->short_pairs >= 3 * p->n;
+}
+
+// One launch of the direct pairs path (tile or staged kernel + the long-pair
+// consumer) over strings A, B (a range of the pair set), results at d_out.
+static int pairs_run_direct(blg_ctx *c, blg_pairs *p, const DevStrings &A, const DevStrings &B, bool use_tile,
+                            int k, int dtype, void *d_out) {
     const bool hask = k >= 0;
     LongQueue q{};
     int64_t total = 0;
@@ -375,13 +428,11 @@ static int pairs_run(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, in
         const double avg = (double)p->len_max_side / (double)p->n;
         const int tile = avg <= 33.0 ? 512 : std::max(32, (int)(17000.0 / avg) & ~31);
         CK(launch(c, "pairs_tile", [&] {
-               return launch_pairs_tile(c->stream, c->sms, hask, p->a.d, p->b.d, tile, k, dtype, d_out, q,
-                                        c->d_status);
+               return launch_pairs_tile(c->stream, c->sms, hask, A, B, tile, k, dtype, d_out, q, c->d_status);
            }), "pairs_tile");
     } else {
         CK(launch(c, "pairs_staged", [&] {
-               return launch_pairs_staged(c->stream, c->sms, hask, p->a.d, p->b.d, k, dtype, d_out, q,
-                                          c->d_status);
+               return launch_pairs_staged(c->stream, c->sms, hask, A, B, k, dtype, d_out, q, c->d_status);
            }), "pairs_staged");
     }
     if (total > 0)
@@ -389,6 +440,93 @@ static int pairs_run(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, in
                return launch_pairs_long(c->stream, c->sms * 3, hask, q, k, dtype, d_out);
            }), "pairs_long");
     return BLG_OK;
+}
+
+// Pairs A, B (the whole uploaded set or a range of it) by the context's
+// schedule: the tile kernel, the prep -> order -> solve plan, or the
+// reference's natural order.
+static int pairs_run_range(blg_ctx *c, blg_pairs *p, const DevStrings &A, const DevStrings &B, int k, int dtype,
+                           void *d_out, int32_t *exit_log) {
+    if (A.n == 0) return BLG_OK;
+    const bool use_tile = !exit_log && pairs_use_tile(c, p);
+    if (!use_tile && (c->sched != BLG_SCHED_PLAIN || exit_log))
+        return pairs_run_scheduled(c, p, A, B, k, dtype, d_out, exit_log);
+    return pairs_run_direct(c, p, A, B, use_tile, k, dtype, d_out);
+}
+
+static int pairs_run(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_out, int32_t *exit_log = nullptr) {
+    if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
+    if (p->n == 0) return BLG_OK;
+    if (!d_out) return fail(c, BLG_ERR_ARG, "null output");
+    return pairs_run_range(c, p, p->a.d, p->b.d, k, dtype, d_out, exit_log);
+}
+
+// Strings [i0, i1) of an uploaded set, as their own set (offsets are shared).
+static DevStrings sub_strings(const DevStrings &S, int64_t i0, int64_t i1) {
+    DevStrings r = S;
+    r.off = S.off + i0;
+    r.n = i1 - i0;
+    return r;
+}
+
+// Pipeline of the one-call pairwise with host results: the pair set is cut
+// into chunks; every chunk's copy to the device is issued first (stream
+// `up`), the host's pass over the offsets (path choice, queue capacities)
+// runs while they are in flight, then each chunk's kernels (context stream,
+// any schedule, ordered within the chunk) start as soon as its bytes have
+// landed and its results go back on stream `down` while later chunks
+// compute. Pinned buffers overlap fully; pageable ones block the host on
+// each copy and overlap less.
+static int pairwise_pipelined(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uint8_t *bb,
+                              const int64_t *ob, int64_t n, int k, int dtype, void *out_host, void *d_out,
+                              blg_pairs *p) {
+    const size_t es = dtype_size(dtype);
+    const int nch = (int)std::min<int64_t>(4, std::max<int64_t>(1, n / (1 << 17)));
+    std::vector<cudaEvent_t> ev(2 * nch + 2, nullptr);
+    int rc = BLG_OK;
+    for (auto &e : ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = BLG_ERR_CUDA;
+    auto fin = [&](int r) {
+        cudaStreamSynchronize(c->up);
+        cudaStreamSynchronize(c->down);
+        cudaStreamSynchronize(c->stream);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+        return r;
+    };
+    if (rc) return fin(fail(c, rc, "cudaEventCreate"));
+    // storage was allocated on the context stream: order both copy streams after it
+    if (cudaEventRecord(ev[0], c->stream) != cudaSuccess || cudaStreamWaitEvent(c->up, ev[0], 0) != cudaSuccess ||
+        cudaStreamWaitEvent(c->down, ev[0], 0) != cudaSuccess)
+        return fin(fail(c, BLG_ERR_CUDA, "stream ordering"));
+    for (int ch = 0; ch < nch && !rc; ch++) {
+        const int64_t i0 = n * ch / nch, i1 = n * (ch + 1) / nch;
+        rc = copy_strings(c, ba, oa, i0, i1, p->a, c->up);
+        if (!rc) rc = copy_strings(c, bb, ob, i0, i1, p->b, c->up);
+        if (!rc && cudaEventRecord(ev[1 + ch], c->up) != cudaSuccess) rc = fail(c, BLG_ERR_CUDA, "event");
+    }
+    if (!rc) rc = pairs_classify(c, oa, ob, n, p);          // overlaps the copies
+    for (int ch = 0; ch <= nch && !rc; ch++) {
+        if (ch < nch) {
+            const int64_t i0 = n * ch / nch, i1 = n * (ch + 1) / nch;
+            if (cudaStreamWaitEvent(c->stream, ev[1 + ch], 0) != cudaSuccess) { rc = fail(c, BLG_ERR_CUDA, "wait"); break; }
+            rc = pairs_run_range(c, p, sub_strings(p->a.d, i0, i1), sub_strings(p->b.d, i0, i1), k, dtype,
+                                 (uint8_t *)d_out + i0 * es, nullptr);
+            if (rc) break;
+            if (cudaEventRecord(ev[1 + nch + ch], c->stream) != cudaSuccess) { rc = fail(c, BLG_ERR_CUDA, "event"); break; }
+        }
+        // the results of the previous chunk go back while this one computes
+        if (ch >= 1) {
+            const int64_t i0 = n * (ch - 1) / nch, i1 = n * ch / nch;
+            if (cudaStreamWaitEvent(c->down, ev[nch + ch], 0) != cudaSuccess) { rc = fail(c, BLG_ERR_CUDA, "wait"); break; }
+            cudaError_t e = cudaMemcpyAsync((uint8_t *)out_host + i0 * es, (uint8_t *)d_out + i0 * es,
+                                            (i1 - i0) * es, cudaMemcpyDeviceToHost, c->down);
+            if (e != cudaSuccess) rc = cuda_fail(c, e, "D2H results");
+        }
+    }
+    // frees on the context stream must follow the last copy back
+    if (cudaEventRecord(ev[2 * nch + 1], c->down) == cudaSuccess) cudaStreamWaitEvent(c->stream, ev[2 * nch + 1], 0);
+    return fin(rc);
 }
 
 static void pairs_release(blg_ctx *c, blg_pairs *p) {
@@ -405,18 +543,27 @@ static void pairs_release(blg_ctx *c, blg_pairs *p) {
 }
 
 // ------------------------------------------------------------ search --
-static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq,
-                         const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s) {
-    s->nq = nq;
-    s->nc = nc;
-    int rc = upload_strings(c, bq, oq, nq, s->q);
-    if (!rc) rc = upload_strings(c, bc, oc, nc, s->c);
-    if (rc) return rc;
-    // Query classes by word count (bitlev/gpu.py:116-118 uses 1,2,4,8 and the CPU
-    // above 512; here every length has a GPU class).
+static void free_classes(blg_ctx *c, blg_search *s) {
+    for (auto &k : s->cls) {
+        dev_free(c, k.qidx);
+        dev_free(c, k.qlen);
+        dev_free(c, k.peq);
+        dev_free(c, k.lo);
+        dev_free(c, k.hi);
+        dev_free(c, k.tile_start);
+        dev_free(c, k.work);
+    }
+    s->cls.clear();
+}
+
+// Query classes of queries [q0, q1) by word count (bitlev/gpu.py:116-118
+// uses 1,2,4,8 and the CPU above 512; here every length has a GPU class),
+// each sorted by length; replaces the previous classes.
+static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64_t q1, blg_search *s) {
+    free_classes(c, s);
     std::vector<std::vector<int32_t>> idx(kSeqMaxWords + 1), len(kSeqMaxWords + 1);
     int lanes_nw = 0;
-    for (int64_t i = 0; i < nq; i++) {
+    for (int64_t i = q0; i < q1; i++) {
         const int64_t m = oq[i + 1] - oq[i];
         int64_t W = (m + 63) >> 6;
         if (W < 1) W = 1;
@@ -441,17 +588,28 @@ static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64
         k.lanes = slot == kSeqMaxWords;
         k.nw = k.lanes ? lanes_nw : slot + 1;
         k.nq = (int)idx[slot].size();
-        CK(dev_alloc(c, (void **)&k.qidx, sizeof(int32_t) * k.nq), "cudaMallocAsync(qidx)");
-        CK(dev_alloc(c, (void **)&k.qlen, sizeof(int32_t) * k.nq), "cudaMallocAsync(qlen)");
-        CK(dev_alloc(c, (void **)&k.peq, sizeof(uint64_t) * 256 * (size_t)k.nw * k.nq), "cudaMallocAsync(peq)");
-        CK(cudaMemcpyAsync(k.qidx, idx[slot].data(), sizeof(int32_t) * k.nq, cudaMemcpyHostToDevice, c->stream), "H2D qidx");
-        CK(cudaMemcpyAsync(k.qlen, len[slot].data(), sizeof(int32_t) * k.nq, cudaMemcpyHostToDevice, c->stream), "H2D qlen");
-        CK(dev_alloc(c, (void **)&k.lo, sizeof(int32_t) * k.nq), "cudaMallocAsync(lo)");
-        CK(dev_alloc(c, (void **)&k.hi, sizeof(int32_t) * k.nq), "cudaMallocAsync(hi)");
-        CK(dev_alloc(c, (void **)&k.tile_start, sizeof(int64_t) * (k.nq + 1)), "cudaMallocAsync(tiles)");
-        CK(dev_alloc(c, (void **)&k.work, sizeof(int32_t)), "cudaMallocAsync(work)");
         s->cls.push_back(k);
+        blg_search::Cls &kk = s->cls.back();
+        CK(dev_alloc(c, (void **)&kk.qidx, sizeof(int32_t) * kk.nq), "cudaMallocAsync(qidx)");
+        CK(dev_alloc(c, (void **)&kk.qlen, sizeof(int32_t) * kk.nq), "cudaMallocAsync(qlen)");
+        CK(dev_alloc(c, (void **)&kk.peq, sizeof(uint64_t) * 256 * (size_t)kk.nw * kk.nq), "cudaMallocAsync(peq)");
+        CK(cudaMemcpyAsync(kk.qidx, idx[slot].data(), sizeof(int32_t) * kk.nq, cudaMemcpyHostToDevice, c->stream), "H2D qidx");
+        CK(cudaMemcpyAsync(kk.qlen, len[slot].data(), sizeof(int32_t) * kk.nq, cudaMemcpyHostToDevice, c->stream), "H2D qlen");
+        CK(dev_alloc(c, (void **)&kk.lo, sizeof(int32_t) * kk.nq), "cudaMallocAsync(lo)");
+        CK(dev_alloc(c, (void **)&kk.hi, sizeof(int32_t) * kk.nq), "cudaMallocAsync(hi)");
+        CK(dev_alloc(c, (void **)&kk.tile_start, sizeof(int64_t) * (kk.nq + 1)), "cudaMallocAsync(tiles)");
+        CK(dev_alloc(c, (void **)&kk.work, sizeof(int32_t)), "cudaMallocAsync(work)");
     }
+    // the host vectors above are pageable: the copies completed before return
+    return BLG_OK;
+}
+
+// Choices: the packed strings, a length-sorted copy (thresholded runs) and
+// the tile-transposed form (exact runs).
+static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s) {
+    s->nc = nc;
+    int rc = upload_strings(c, bc, oc, nc, s->c);
+    if (rc) return rc;
     // Choices sorted by length (counting sort on the host, byte gather on the
     // device), when the length range is moderate.
     if (nc > 0) {
@@ -525,6 +683,61 @@ static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64
     return BLG_OK;
 }
 
+static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, int64_t q0 = 0,
+                      int64_t q1 = -1);
+
+// One-call cdist with host results: queries in chunks of rows; the rows of
+// chunk i go back (stream `down`) while chunk i+1 computes.
+static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq, const uint8_t *bc,
+                           const int64_t *oc, int64_t nc, int k, int dtype, void *out_host, void *d_out,
+                           blg_search *s) {
+    s->nq = nq;
+    int rc = upload_strings(c, bq, oq, nq, s->q);
+    if (!rc) rc = search_upload_choices(c, bc, oc, nc, s);
+    if (rc) return rc;
+    const size_t row = dtype_size(dtype) * (size_t)nc;
+    const int nch = (int)std::min<int64_t>(8, nq);
+    std::vector<cudaEvent_t> ev(nch + 1, nullptr);
+    for (auto &e : ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = BLG_ERR_CUDA;
+    auto fin = [&](int r) {
+        cudaStreamSynchronize(c->down);
+        cudaStreamSynchronize(c->stream);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+        return r;
+    };
+    if (rc) return fin(fail(c, rc, "cudaEventCreate"));
+    for (int ch = 0; ch <= nch && !rc; ch++) {
+        if (ch < nch) {
+            const int64_t q0 = nq * ch / nch, q1 = nq * (ch + 1) / nch;
+            rc = search_build_classes(c, oq, q0, q1, s);
+            if (!rc) rc = search_run(c, s, k, dtype, d_out, q0, q1);
+            if (!rc && cudaEventRecord(ev[ch], c->stream) != cudaSuccess) rc = fail(c, BLG_ERR_CUDA, "event");
+            if (rc) break;
+        }
+        if (ch >= 1) {
+            const int64_t q0 = nq * (ch - 1) / nch, q1 = nq * ch / nch;
+            if (cudaStreamWaitEvent(c->down, ev[ch - 1], 0) != cudaSuccess) { rc = fail(c, BLG_ERR_CUDA, "wait"); break; }
+            cudaError_t e = cudaMemcpyAsync((uint8_t *)out_host + q0 * row, (uint8_t *)d_out + q0 * row,
+                                            (size_t)(q1 - q0) * row, cudaMemcpyDeviceToHost, c->down);
+            if (e != cudaSuccess) rc = cuda_fail(c, e, "D2H results");
+        }
+    }
+    // frees on the context stream must follow the last copy back
+    if (cudaEventRecord(ev[nch], c->down) == cudaSuccess) cudaStreamWaitEvent(c->stream, ev[nch], 0);
+    return fin(rc);
+}
+
+static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq,
+                         const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s) {
+    s->nq = nq;
+    int rc = upload_strings(c, bq, oq, nq, s->q);
+    if (!rc) rc = search_upload_choices(c, bc, oc, nc, s);
+    if (!rc) rc = search_build_classes(c, oq, 0, nq, s);
+    return rc;
+}
+
 static int pick_qpb(blg_ctx *c, int nq_cls, int64_t nc) {
     const int64_t tiles = (nc + 1023) / 1024;
     const int64_t target = (int64_t)c->sms * 8;
@@ -536,9 +749,12 @@ static int pick_qpb(blg_ctx *c, int nq_cls, int64_t nc) {
     return (int)qpb;
 }
 
-static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out) {
+// Launch the current classes' kernels; the max_dist fill covers rows [q0, q1)
+// (all rows by default: the classes hold every query).
+static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, int64_t q0, int64_t q1) {
     if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
     if (s->nq == 0 || s->nc == 0) return BLG_OK;
+    if (q1 < 0) q1 = s->nq;
     if (!d_out) return fail(c, BLG_ERR_ARG, "null output");
     const bool hask = k >= 0;
     const bool surv = hask && s->lsorted && c->sched != BLG_SCHED_PLAIN;
@@ -546,7 +762,8 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out) 
         const uint32_t fillv = (uint32_t)(dtype == BLG_UINT8 ? std::min(k + 1, 255)
                                           : dtype == BLG_UINT16 ? std::min(k + 1, 65535) : k + 1);
         CK(launch(c, "fill", [&] {
-               return launch_fill(c->stream, c->sms, d_out, s->nq * s->nc, dtype, fillv);
+               return launch_fill(c->stream, c->sms, (uint8_t *)d_out + q0 * s->nc * (int64_t)dtype_size(dtype),
+                                  (q1 - q0) * s->nc, dtype, fillv);
            }), "fill");
     }
     for (auto &k_ : s->cls)
@@ -605,16 +822,7 @@ static void search_release(blg_ctx *c, blg_search *s) {
     s->tt_base = nullptr;
     s->tt_len = nullptr;
     s->tt = false;
-    for (auto &k : s->cls) {
-        dev_free(c, k.qidx);
-        dev_free(c, k.qlen);
-        dev_free(c, k.peq);
-        dev_free(c, k.lo);
-        dev_free(c, k.hi);
-        dev_free(c, k.tile_start);
-        dev_free(c, k.work);
-    }
-    s->cls.clear();
+    free_classes(c, s);
 }
 
 // ------------------------------------------------------------ batches --
@@ -786,6 +994,8 @@ int blg_init(int device, blg_ctx **out) {
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->up, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->down, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaEventCreate(&c->t0);
@@ -810,6 +1020,8 @@ void blg_destroy(blg_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->up) cudaStreamSynchronize(c->up);
+    if (c->down) cudaStreamSynchronize(c->down);
     for (auto &r : c->prof_recs) {
         cudaEventDestroy(r.e0);
         cudaEventDestroy(r.e1);
@@ -820,6 +1032,8 @@ void blg_destroy(blg_ctx *c) {
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->up) cudaStreamDestroy(c->up);
+    if (c->down) cudaStreamDestroy(c->down);
     delete c;
 }
 
@@ -872,7 +1086,7 @@ int blg_sched_train(blg_ctx *c, blg_pairs *p, int32_t max_dist, int32_t epochs, 
     void *out = nullptr, *cols = nullptr, *x = nullptr, *y = nullptr, *nrows = nullptr;
     CK(dev_alloc(c, &out, sizeof(int32_t) * (size_t)p->n), "alloc");
     CK(dev_alloc(c, &cols, sizeof(int32_t) * (size_t)p->n), "alloc");
-    rc = pairs_run_scheduled(c, p, max_dist, BLG_INT32, out, (int32_t *)cols, true);
+    rc = pairs_run_scheduled(c, p, p->a.d, p->b.d, max_dist, BLG_INT32, out, (int32_t *)cols, true);
     if (rc) return rc;
     // 2. rows (subsampled to at most max_rows)
     int64_t records = 0;
@@ -956,9 +1170,21 @@ int blg_pairwise(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uint8_t
     void *d_out = nullptr;
     CK(dev_alloc(c, &d_out, obytes), "cudaMallocAsync(out)");
     blg_pairs p;
-    int rc = pairs_upload(c, ba, oa, bb, ob, n, &p);
-    if (!rc) rc = pairs_run(c, &p, max_dist, dtype, d_out);
-    if (!rc && !out_device && n > 0) {
+    int rc = check_offsets_host(c, oa, n);
+    if (!rc) rc = check_offsets_host(c, ob, n);
+    // host results of a large set: chunks overlap copies and kernels
+    const bool pipe = !rc && !out_device && n >= (1 << 18);
+    if (pipe) {
+        rc = alloc_strings(c, ba, oa, n, p.a);
+        if (!rc) rc = alloc_strings(c, bb, ob, n, p.b);
+        if (!rc) rc = pairwise_pipelined(c, ba, oa, bb, ob, n, max_dist, dtype, out_host, d_out, &p);
+    } else {
+        if (!rc) rc = pairs_classify(c, oa, ob, n, &p);
+        if (!rc) rc = upload_strings(c, ba, oa, n, p.a);
+        if (!rc) rc = upload_strings(c, bb, ob, n, p.b);
+        if (!rc) rc = pairs_run(c, &p, max_dist, dtype, d_out);
+    }
+    if (!rc && !pipe && !out_device && n > 0) {
         cudaError_t e = cudaMemcpyAsync(out_host, d_out, obytes, cudaMemcpyDeviceToHost, c->stream);
         if (e != cudaSuccess) rc = cuda_fail(c, e, "D2H results");
     }
@@ -987,11 +1213,18 @@ int blg_cdist(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq, cons
     blg_search s;
     int rc = BLG_OK;
     if (nq > 0 && nc > 0) {
-        rc = search_upload(c, bq, oq, nq, bc, oc, nc, &s);
-        if (!rc) rc = search_run(c, &s, max_dist, dtype, d_out);
-        if (!rc && !out_device) {
-            cudaError_t e = cudaMemcpyAsync(out_host, d_out, obytes, cudaMemcpyDeviceToHost, c->stream);
-            if (e != cudaSuccess) rc = cuda_fail(c, e, "D2H results");
+        // a result matrix of 64 MiB or more going to the host: query chunks,
+        // each chunk's rows copied back while the next chunk computes
+        const bool pipe = !out_device && nq >= 2 && obytes >= (64u << 20);
+        if (!pipe) {
+            rc = search_upload(c, bq, oq, nq, bc, oc, nc, &s);
+            if (!rc) rc = search_run(c, &s, max_dist, dtype, d_out);
+            if (!rc && !out_device) {
+                cudaError_t e = cudaMemcpyAsync(out_host, d_out, obytes, cudaMemcpyDeviceToHost, c->stream);
+                if (e != cudaSuccess) rc = cuda_fail(c, e, "D2H results");
+            }
+        } else {
+            rc = cdist_pipelined(c, bq, oq, nq, bc, oc, nc, max_dist, dtype, out_host, d_out, &s);
         }
         search_release(c, &s);
     }
@@ -1058,6 +1291,20 @@ int blg_malloc(blg_ctx *c, size_t bytes, void **d_ptr) {
 int blg_free(blg_ctx *c, void *d_ptr) {
     ENTER(c);
     dev_free(c, d_ptr);
+    return BLG_OK;
+}
+
+int blg_host_alloc(blg_ctx *c, size_t bytes, void **h_ptr) {
+    ENTER(c);
+    if (!h_ptr) return fail(c, BLG_ERR_ARG, "null out");
+    *h_ptr = nullptr;
+    CK(cudaMallocHost(h_ptr, bytes ? bytes : 16), "cudaMallocHost");
+    return BLG_OK;
+}
+
+int blg_host_free(blg_ctx *c, void *h_ptr) {
+    ENTER(c);
+    if (h_ptr) CK(cudaFreeHost(h_ptr), "cudaFreeHost");
     return BLG_OK;
 }
 

@@ -16,7 +16,9 @@ struct blg_ctx {
     };
     int device = 0;
     int sms = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;     // kernels (and every resident-state call)
+    cudaStream_t up = nullptr;         // host -> device copies of the one-call pipelines
+    cudaStream_t down = nullptr;       // device -> host copies of the one-call pipelines
     uint32_t *d_status = nullptr;      // status bits raised by kernels (blg::ST_*)
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     std::mutex mu;                     // serialises calls on one context

@@ -186,6 +186,12 @@ int blg_free(blg_ctx *ctx, void *d_ptr);
 int blg_memcpy_h2d(blg_ctx *ctx, void *d_dst, const void *h_src, size_t bytes);
 int blg_memcpy_d2h(blg_ctx *ctx, void *h_dst, const void *d_src, size_t bytes);
 int blg_memset(blg_ctx *ctx, void *d_dst, int value, size_t bytes);
+/* Page-locked host memory (cudaMallocHost), for inputs and results that move
+ * between host and device at full link speed: the one-call entry points
+ * overlap their copies with the kernels when the host buffers are pinned.
+ * The counterpart of cupyx.empty_pinned for callers of the CuPy path. */
+int blg_host_alloc(blg_ctx *ctx, size_t bytes, void **h_ptr);
+int blg_host_free(blg_ctx *ctx, void *h_ptr);
 /* Wait for the context's stream and report any status a kernel raised. */
 int blg_synchronize(blg_ctx *ctx);
 
