@@ -47,17 +47,18 @@ cudaError_t launch_pairs_staged(cudaStream_t st, int sms, bool hask, const DevSt
 cudaError_t launch_fill(cudaStream_t st, int sms, void *out, int64_t n, int dtype, uint32_t v);
 cudaError_t launch_pairs_tile(cudaStream_t st, int sms, bool hask, const DevStrings &A, const DevStrings &B,
                               int tile_pairs, int k, int dtype, void *out, const LongQueue &q, uint32_t *status);
-cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, const DevStrings &A,
+cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, bool band, const DevStrings &A,
                               const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
                               uint32_t *status);
-cudaError_t launch_order(cudaStream_t st, int sms, bool need_hist, const PairsPlan &plan);
+cudaError_t launch_order(cudaStream_t st, int sms, const PairsPlan &plan);
 cudaError_t launch_solve(cudaStream_t st, int sms, bool hask, const PairsPlan &plan, int k, int dtype,
                          void *out, int32_t *exit_log, bool any_long);
 cudaError_t launch_solve_band(cudaStream_t st, int sms, const PairsPlan &plan, int k, int dtype, void *out,
                               int32_t *exit_log);
 }  // namespace blg
 int sched_model_ensure(blg_ctx *c, blg_sched_model **out);
-cudaError_t launch_mlp_keys(cudaStream_t st, int sms, const blg_sched_model *m, const blg::PairsPlan &plan);
+cudaError_t launch_mlp_keys(cudaStream_t st, int sms, const blg_sched_model *m, const blg::PairsPlan &plan,
+                            bool band);
 cudaError_t launch_collect_rows(cudaStream_t st, int sms, const blg::PairsPlan &plan, const int32_t *cols,
                                 int64_t stride, int64_t max_rows, half *x, float *y, int64_t *n_rows);
 int sched_train_rows(blg_ctx *c, blg_sched_model *m, half *x, float *y, const int64_t *d_rows, int64_t rows,
@@ -331,7 +332,7 @@ static int pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const 
     return rc;
 }
 
-constexpr size_t kPlanCounters = 2 * kPairClasses + 2 * kPairClasses * kCostBuckets;
+constexpr size_t kPlanCounters = 2 * kPairClasses;   // count, head
 
 static int plan_alloc(blg_ctx *c, blg_pairs *p, bool feat) {
     int64_t slots = 0;
@@ -362,8 +363,6 @@ static PairsPlan plan_view(blg_pairs *p) {
     }
     pl.count = p->plan_ctr;
     pl.head = p->plan_ctr + kPairClasses;
-    pl.hist = p->plan_ctr + 2 * kPairClasses;
-    pl.cursor = pl.hist + kPairClasses * kCostBuckets;
     return pl;
 }
 
@@ -380,15 +379,18 @@ static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, const DevStrings &A, co
     CK(cudaMemsetAsync(p->plan_ctr, 0, sizeof(int32_t) * kPlanCounters, c->stream), "reset plan");
     if (exit_log) CK(cudaMemsetAsync(exit_log, 0, sizeof(int32_t) * (size_t)A.n, c->stream), "reset log");
     const int grid = (int)std::min<int64_t>((A.n + 255) / 256, (int64_t)c->sms * 8);
+    const bool band = hask && k <= 31 && !c->no_band;
     CK(launch(c, "pairs_prep", [&] {
-           return launch_pairs_prep(c->stream, grid, hask, learned, A, B, k, dtype, d_out, plan, c->d_status);
+           return launch_pairs_prep(c->stream, grid, hask, learned, band, A, B, k, dtype, d_out, plan,
+                                    c->d_status);
        }), "pairs_prep");
     if (learned && !want_features)
-        CK(launch(c, "sched_keys", [&] { return launch_mlp_keys(c->stream, c->sms, c->model, plan); }), "sched_keys");
-    CK(launch(c, "pairs_order", [&] { return launch_order(c->stream, c->sms, learned, plan); }), "pairs_order");
+        CK(launch(c, "sched_keys", [&] { return launch_mlp_keys(c->stream, c->sms, c->model, plan, band); }),
+           "sched_keys");
+    CK(launch(c, "pairs_order", [&] { return launch_order(c->stream, c->sms, plan); }), "pairs_order");
     bool any_long = false;
     for (int j = 1; j < kPairClasses; j++) any_long |= p->pcap[j] > 0;
-    if (hask && k <= 31 && !c->no_band)
+    if (band)
         CK(launch(c, "pairs_band", [&] {
                return launch_solve_band(c->stream, c->sms, plan, k, dtype, d_out, exit_log);
            }), "pairs_band");

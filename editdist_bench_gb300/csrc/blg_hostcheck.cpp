@@ -145,6 +145,29 @@ extern "C" int blg_host_band(const uint8_t *a, int la, const uint8_t *b, int lb,
     return band_core(la, lb, k, text, eqw, u, nullptr);
 }
 
+// The banded loop as the pairs path runs it (trimmed, shorter string as
+// the pattern), also reporting the text columns it processed before its exit
+// fired (0 for pairs settled by the length gap or an empty pattern).
+extern "C" int blg_host_band_cols(const uint8_t *a, int la, const uint8_t *b, int lb, int k, int *cols) {
+    normalise(a, la, b, lb, 1);
+    *cols = 0;
+    if (k < 0 || k > 31) return -1;
+    if (lb - la > k) return k + 1;
+    if (la == 0) return lb;
+    Pattern P(a, la);
+    const Units u{1u, 2u};
+    auto text = [&](int j) -> uint32_t { return b[j]; };
+    auto eqw = [&](uint32_t c, int p0) -> uint32_t {
+        uint32_t v = 0;
+        for (int q = 0; q < 32; q++) {
+            const int p = p0 + q;
+            if (p >= 0 && p < la && ((P.eq((uint8_t)c, p / 64) >> (p % 64)) & 1u)) v |= 1u << q;
+        }
+        return v;
+    };
+    return band_core(la, lb, k, text, eqw, u, cols);
+}
+
 // Same, with the pattern as the LONGER string (the search kernels' case:
 // the query is the pattern whatever the choice's length), no trimming.
 extern "C" int blg_host_band_query(const uint8_t *q, int m, const uint8_t *t, int n, int k) {

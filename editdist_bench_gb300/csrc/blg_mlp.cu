@@ -162,24 +162,113 @@ __global__ void __launch_bounds__(256) k_mlp_sgd(float *master, float *mom, floa
     }
 }
 
-// Inference: record -> predicted fraction -> cost key (predicted columns x words).
-__global__ void __launch_bounds__(256) k_mlp_keys(const half *w16, PairsPlan plan) {
-    __shared__ float w[kParams];
-    load_weights(w16, w);
+// Inference weights in shared memory, laid out for 16-byte loads:
+//   W1p[32][8]  row j = W1[j][0..6], b1[j]   (input 7 is a constant 1)
+//   W2[32][32], b2[32], W3[32], b3
+constexpr int kInfW1 = 0, kInfW2 = kInfW1 + kH * 8, kInfB2 = kInfW2 + kH * kH, kInfW3 = kInfB2 + kH,
+              kInfB3 = kInfW3 + kH, kInfFloats = kInfB3 + 4;
+
+__device__ __forceinline__ void load_inference_weights(const half *w16, float *w) {
+    for (int x = threadIdx.x; x < kInfFloats; x += blockDim.x) {
+        float v = 0.f;
+        if (x < kInfW2) {
+            const int j = x >> 3, i = x & 7;
+            v = __half2float(w16[i < kFeatures ? kOffW1 + j * kFeatures + i : kOffB1 + j]);
+        } else if (x < kInfB2) v = __half2float(w16[kOffW2 + (x - kInfW2)]);
+        else if (x < kInfW3) v = __half2float(w16[kOffB2 + (x - kInfB2)]);
+        else if (x < kInfB3) v = __half2float(w16[kOffW3 + (x - kInfW3)]);
+        else if (x == kInfB3) v = __half2float(w16[kOffB3]);
+        w[x] = v;
+    }
+}
+
+// 16-byte shared load the compiler may not hoist out of the row loop (the
+// 1345 weights would not fit in registers).
+__device__ __forceinline__ float4 lds4(const float *p) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"((uint32_t)__cvta_generic_to_shared(p)));
+    return v;
+}
+
+// Forward pass of two rows at once (each weight load feeds both), every
+// activation in registers. FP16 weights held as FP32, FP32 sums.
+__device__ __forceinline__ void mlp_forward2(const float *w, const float (&x0)[8], const float (&x1)[8], float &y0,
+                                             float &y1) {
+    float h0[kH], h1[kH];
+#pragma unroll
+    for (int j = 0; j < kH; j++) {
+        const float4 a = lds4(w + kInfW1 + j * 8), b = lds4(w + kInfW1 + j * 8 + 4);
+        float s0 = a.x * x0[0], s1 = a.x * x1[0];
+        s0 = fmaf(a.y, x0[1], s0); s1 = fmaf(a.y, x1[1], s1);
+        s0 = fmaf(a.z, x0[2], s0); s1 = fmaf(a.z, x1[2], s1);
+        s0 = fmaf(a.w, x0[3], s0); s1 = fmaf(a.w, x1[3], s1);
+        s0 = fmaf(b.x, x0[4], s0); s1 = fmaf(b.x, x1[4], s1);
+        s0 = fmaf(b.y, x0[5], s0); s1 = fmaf(b.y, x1[5], s1);
+        s0 = fmaf(b.z, x0[6], s0); s1 = fmaf(b.z, x1[6], s1);
+        h0[j] = fmaxf(s0 + b.w, 0.f);
+        h1[j] = fmaxf(s1 + b.w, 0.f);
+    }
+    const float4 bb3 = lds4(w + kInfB3);
+    y0 = bb3.x;
+    y1 = bb3.x;
+#pragma unroll
+    for (int j = 0; j < kH; j++) {
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int i = 0; i < kH; i += 4) {
+            const float4 a = lds4(w + kInfW2 + j * kH + i);
+            s0 = fmaf(a.x, h0[i], s0); s1 = fmaf(a.x, h1[i], s1);
+            s0 = fmaf(a.y, h0[i + 1], s0); s1 = fmaf(a.y, h1[i + 1], s1);
+            s0 = fmaf(a.z, h0[i + 2], s0); s1 = fmaf(a.z, h1[i + 2], s1);
+            s0 = fmaf(a.w, h0[i + 3], s0); s1 = fmaf(a.w, h1[i + 3], s1);
+        }
+        const float4 bw = lds4(w + ((j & ~3) + kInfB2)), ww = lds4(w + ((j & ~3) + kInfW3));
+        const float b2j = (j & 3) == 0 ? bw.x : (j & 3) == 1 ? bw.y : (j & 3) == 2 ? bw.z : bw.w;
+        const float w3j = (j & 3) == 0 ? ww.x : (j & 3) == 1 ? ww.y : (j & 3) == 2 ? ww.z : ww.w;
+        y0 = fmaf(w3j, fmaxf(s0 + b2j, 0.f), y0);
+        y1 = fmaf(w3j, fmaxf(s1 + b2j, 0.f), y1);
+    }
+}
+
+__device__ __forceinline__ void read_features(const PairsPlan &plan, int cls, int i, int cnt, float (&x)[8]) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = 0.f;
+    if (i < cnt) {
+        const half *f = plan.feat[cls] + (size_t)i * kFeatures;
+#pragma unroll
+        for (int q = 0; q < kFeatures; q++) x[q] = __half2float(f[q]);
+    }
+    x[7] = 1.f;
+}
+
+__device__ __forceinline__ void write_key(const PairsPlan &plan, int cls, int i, float y, int band) {
+    y = y < 0.f ? 0.f : (y > 1.f ? 1.f : y);
+    const LongItem it = plan.raw[cls][i];
+    const float work = band ? y * (float)it.n + 16.f : (y * (float)it.n + 1.f) * (float)((it.m + 63) >> 6);
+    int b = (int)(__log2f(work) * 8.f) + 1;
+    plan.key[cls][i] = (uint8_t)(b < 0 ? 0 : (b > kCostBuckets - 1 ? kCostBuckets - 1 : b));
+}
+
+// Inference: record -> predicted fraction of its text -> cost key. The
+// banded solver's work is the exit column plus a window fill of about 16
+// steps whatever the pattern length; the word solvers' work is columns x
+// pattern words. Two records per thread.
+__global__ void __launch_bounds__(256) k_mlp_keys(const half *w16, PairsPlan plan, int band) {
+    __shared__ __align__(16) float w[kInfFloats];
+    load_inference_weights(w16, w);
     __syncthreads();
-    float h1[kH], h2[kH], x[kFeatures];
     for (int cls = 0; cls < kPairClasses; cls++) {
         const int cnt = min(plan.count[cls], (int)plan.cap[cls]);
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
-            const half *f = plan.feat[cls] + (size_t)i * kFeatures;
-#pragma unroll
-            for (int q = 0; q < kFeatures; q++) x[q] = __half2float(f[q]);
-            float y = mlp_forward(w, x, h1, h2);
-            y = y < 0.f ? 0.f : (y > 1.f ? 1.f : y);
-            const LongItem it = plan.raw[cls][i];
-            const float work = (y * (float)it.n + 1.f) * (float)((it.m + 63) >> 6);
-            int b = (int)(__log2f(work) * 8.f) + 1;
-            plan.key[cls][i] = (uint8_t)(b < 0 ? 0 : (b > kCostBuckets - 1 ? kCostBuckets - 1 : b));
+        const int stride = 2 * gridDim.x * blockDim.x;
+        for (int i = 2 * (blockIdx.x * blockDim.x) + threadIdx.x; i < cnt; i += stride) {
+            float x0[8], x1[8], y0, y1;
+            read_features(plan, cls, i, cnt, x0);
+            read_features(plan, cls, i + blockDim.x, cnt, x1);
+            mlp_forward2(w, x0, x1, y0, y1);
+            write_key(plan, cls, i, y0, band);
+            if (i + (int)blockDim.x < cnt) write_key(plan, cls, i + blockDim.x, y1, band);
         }
     }
 }
@@ -267,8 +356,8 @@ static int set_weights(blg_ctx *c, blg_sched_model *m, const std::vector<float> 
 }
 
 // Host-side pieces the runtime (blg_api.cu) calls.
-cudaError_t launch_mlp_keys(cudaStream_t st, int sms, const blg_sched_model *m, const PairsPlan &plan) {
-    k_mlp_keys<<<sms * 4, 256, 0, st>>>(m->w16, plan);
+cudaError_t launch_mlp_keys(cudaStream_t st, int sms, const blg_sched_model *m, const PairsPlan &plan, bool band) {
+    k_mlp_keys<<<sms * 4, 256, 0, st>>>(m->w16, plan, band ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -420,7 +509,7 @@ int blg_sched_predict(blg_ctx *c, const uint16_t *x_half, int64_t rows, float *o
     return BLG_OK;
 }
 
-// Versioned binary checkpoint: "BLGMLP01", int32 count, FP32 master weights.
+// Versioned binary checkpoint: "BLGMLP02", int32 count, FP32 master weights.
 int blg_sched_save(blg_ctx *c, const char *path) {
     std::vector<float> w(kParams);
     int rc = blg_sched_get_weights(c, w.data(), kParams);
@@ -428,7 +517,7 @@ int blg_sched_save(blg_ctx *c, const char *path) {
     FILE *f = fopen(path, "wb");
     if (!f) return fail(c, BLG_ERR_ARG, std::string("cannot write ") + path);
     const int32_t n = kParams;
-    const bool ok = fwrite("BLGMLP01", 1, 8, f) == 8 && fwrite(&n, 4, 1, f) == 1 &&
+    const bool ok = fwrite("BLGMLP02", 1, 8, f) == 8 && fwrite(&n, 4, 1, f) == 1 &&
                     fwrite(w.data(), sizeof(float), kParams, f) == (size_t)kParams;
     fclose(f);
     return ok ? BLG_OK : fail(c, BLG_ERR_ARG, "short write");
@@ -441,10 +530,10 @@ int blg_sched_load(blg_ctx *c, const char *path) {
     char magic[8];
     int32_t n = 0;
     std::vector<float> w(kParams);
-    const bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "BLGMLP01", 8) == 0 && fread(&n, 4, 1, f) == 1 &&
+    const bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "BLGMLP02", 8) == 0 && fread(&n, 4, 1, f) == 1 &&
                     n == kParams && fread(w.data(), sizeof(float), kParams, f) == (size_t)kParams;
     fclose(f);
-    if (!ok) return fail(c, BLG_ERR_ARG, "not a scheduler checkpoint (BLGMLP01, 1345 weights)");
+    if (!ok) return fail(c, BLG_ERR_ARG, "not a scheduler checkpoint (BLGMLP02, 1345 weights)");
     return blg_sched_set_weights(c, w.data(), kParams);
 }
 

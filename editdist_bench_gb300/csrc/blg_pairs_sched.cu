@@ -9,8 +9,11 @@
 //      into per-class regions (class 0: pattern <= 64, one thread; classes
 //      1..5: 2..32 lanes), each with a cost key and, for the learned
 //      schedule, a feature row;
-//   2. k_order_hist / k_order_scan / k_order_scatter counting-sort every
-//      class by cost key, largest cost first;
+//   2. k_order_segments counting-sorts every 1024-record segment of a class
+//      by cost key, largest cost first: warps get pairs of similar cost
+//      while their strings stay in one neighbourhood of memory (a sort over
+//      the whole class scatters them, and the solvers' per-lane string
+//      reads lose more to cache misses than the order saves);
 //   3. k_solve_word / k_solve_lanes consume the sorted records from device
 //      work counters, so a warp takes pairs of similar cost.
 // Which pairs are computed and their values never change: only the order.
@@ -27,47 +30,37 @@ __device__ __forceinline__ int cost_bucket(float work) {
     return b > kCostBuckets - 1 ? kCostBuckets - 1 : b;
 }
 
-// Features of one trimmed pair (pattern p of m, text t of n; la, lb
-// untrimmed): lengths, trimmed lengths, length gap, k, and the q-gram lower
-// bound sum|h_p - h_t| / (2q) over 4-grams hashed into 32 bins (each edit
-// changes at most 4 4-grams of each string, so the bound holds for any
-// binning). `hist` is this thread's 32-byte scratch in shared memory.
-__device__ __forceinline__ float qgram_bound(const uint8_t *p, int m, const uint8_t *t, int n, int8_t *hist) {
+// Features of one trimmed pair (pattern p of m, text t of n; la0, lb0
+// untrimmed): lengths, trimmed lengths, length gap, k, and a 4-gram sketch
+// distance: each string's first 64 trimmed bytes set one bit of a 64-bit
+// mask per 4-gram (hashed into 64 bins); the feature is the number of bins
+// present in one mask and not the other. Edits change at most 4 grams each,
+// so near-identical pairs score low and unrelated ones high; it costs a few
+// register operations per byte and no shared memory.
+constexpr int kSketchWindow = 64;
+
+__device__ __forceinline__ uint64_t gram_sketch(const uint8_t *p, int m) {
+    if (m > kSketchWindow) m = kSketchWindow;
+    uint64_t sk = 0;
+    uint32_t g = 0;
+    TextScan ts;
+    ts.init(p);
+    for (int i = 0; i < m; i += 4) {
+        const uint32_t w4 = ts.next4();
 #pragma unroll
-    for (int i = 0; i < 32; i++) hist[i] = 0;
-    int overflow = 0;
-    uint32_t h = 0;
-    for (int i = 0; i < m; i++) {
-        h = (h << 8) | p[i];
-        if (i >= 3) {
-            const int bin = (int)((h * 0x9E3779B1u) >> 27);
-            const int v = hist[bin] + 1;
-            if (v > 127) overflow = 1; else hist[bin] = (int8_t)v;
+        for (int b = 0; b < 4; b++) {
+            if (i + b < m) {
+                g = __funnelshift_l(w4 << (24 - 8 * b), g, 8);     // g = (g << 8) | byte b
+                if (i + b >= 3) sk |= 1ull << ((g * 0x9E3779B1u) >> 26);
+            }
         }
     }
-    h = 0;
-    for (int i = 0; i < n; i++) {
-        h = (h << 8) | t[i];
-        if (i >= 3) {
-            const int bin = (int)((h * 0x9E3779B1u) >> 27);
-            const int v = hist[bin] - 1;
-            if (v < -127) overflow = 1; else hist[bin] = (int8_t)v;
-        }
-    }
-    int l1 = 0;
-#pragma unroll
-    for (int i = 0; i < 32; i++) l1 += hist[i] < 0 ? -hist[i] : hist[i];
-    if (overflow) return 0.f;              // saturated counters: report no bound
-    return l1 * 0.125f;
+    return sk;
 }
 
 template <bool HASK, bool FEAT>
 __global__ void __launch_bounds__(256) k_pairs_prep(DevStrings A, DevStrings B, int k, int dtype, void *out,
-                                                    PairsPlan plan, uint32_t *status) {
-    __shared__ int s_hist[kPairClasses * kCostBuckets];
-    __shared__ int8_t s_qg[FEAT ? 256 * 32 : 1];
-    for (int x = threadIdx.x; x < kPairClasses * kCostBuckets; x += blockDim.x) s_hist[x] = 0;
-    __syncthreads();
+                                                    PairsPlan plan, int band, uint32_t *status) {
     const int lane = threadIdx.x & 31;
     const int64_t n = A.n;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -103,9 +96,10 @@ __global__ void __launch_bounds__(256) k_pairs_prep(DevStrings A, DevStrings B, 
         LongItem it;
         it.pat = a; it.txt = b; it.m = la; it.n = lb; it.idx = i;
         plan.raw[cls][pos] = it;
-        int key = cost_bucket((float)lb * (float)((la + 63) >> 6));
+        // the banded loop costs columns plus a window fill, the word solvers columns x words
+        int key = cost_bucket(band ? (float)lb + 16.f : (float)lb * (float)((la + 63) >> 6));
         if (FEAT) {
-            const float qb = qgram_bound(a, la, b, lb, s_qg + threadIdx.x * 32);
+            const float qb = (float)__popcll(gram_sketch(a, la) ^ gram_sketch(b, lb));
             half *f = plan.feat[cls] + (size_t)pos * kFeatures;
             f[0] = __float2half((float)la * (1.f / 256.f));
             f[1] = __float2half((float)lb * (1.f / 256.f));
@@ -117,68 +111,48 @@ __global__ void __launch_bounds__(256) k_pairs_prep(DevStrings A, DevStrings B, 
             key = 0;                       // the network's prediction sets the key later
         }
         plan.key[cls][pos] = (uint8_t)key;
-        if (!FEAT) atomicAdd(&s_hist[cls * kCostBuckets + key], 1);
-    }
-    __syncthreads();
-    if (!FEAT)
-        for (int x = threadIdx.x; x < kPairClasses * kCostBuckets; x += blockDim.x)
-            if (s_hist[x]) atomicAdd(&plan.hist[x], s_hist[x]);
-}
-
-// Histogram of keys already written (learned schedule: keys come from the network).
-__global__ void __launch_bounds__(256) k_order_hist(PairsPlan plan) {
-    __shared__ int s_hist[kCostBuckets];
-    for (int cls = 0; cls < kPairClasses; cls++) {
-        for (int x = threadIdx.x; x < kCostBuckets; x += blockDim.x) s_hist[x] = 0;
-        __syncthreads();
-        const int cnt = min(plan.count[cls], (int)plan.cap[cls]);
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
-            atomicAdd(&s_hist[plan.key[cls][i]], 1);
-        __syncthreads();
-        for (int x = threadIdx.x; x < kCostBuckets; x += blockDim.x)
-            if (s_hist[x]) atomicAdd(&plan.hist[cls * kCostBuckets + x], s_hist[x]);
-        __syncthreads();
     }
 }
 
-// Bucket starts, largest key first: start[cls][b] = sum of counts of keys > b.
-__global__ void __launch_bounds__(kCostBuckets) k_order_scan(PairsPlan plan) {
-    __shared__ int s[kCostBuckets];
-    for (int cls = 0; cls < kPairClasses; cls++) {
-        const int b = threadIdx.x;
-        s[kCostBuckets - 1 - b] = plan.hist[cls * kCostBuckets + b];     // reversed
-        __syncthreads();
-        for (int off = 1; off < kCostBuckets; off <<= 1) {
-            const int v = b >= off ? s[b - off] : 0;
-            __syncthreads();
-            s[b] += v;
-            __syncthreads();
-        }
-        // inclusive scan over reversed buckets; exclusive start of bucket b:
-        const int r = kCostBuckets - 1 - b;
-        plan.cursor[cls * kCostBuckets + b] = s[r] - plan.hist[cls * kCostBuckets + b];
-        __syncthreads();
-    }
-}
+// Segmented counting sort: every segment of kSegRecords consecutive records
+// of a class is sorted by key, largest first, into the same index range of
+// plan.sorted. A persistent grid walks (class, segment) pairs; one CTA owns
+// a segment (shared-memory histogram, scan, scatter; order inside a key is
+// free).
+constexpr int kSegRecords = 1024;
 
-// Scatter records to their sorted slots (order inside a bucket is free).
-// Lanes with equal keys share one atomic (warp-aggregated).
-__global__ void __launch_bounds__(256) k_order_scatter(PairsPlan plan) {
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(kSegRecords) k_order_segments(PairsPlan plan) {
+    __shared__ int s_cnt[kCostBuckets];
+    __shared__ int s_start[kCostBuckets];
+    const int t = threadIdx.x;
     for (int cls = 0; cls < kPairClasses; cls++) {
         const int cnt = min(plan.count[cls], (int)plan.cap[cls]);
-        const int stride = gridDim.x * blockDim.x;
-        for (int base = blockIdx.x * blockDim.x; base < cnt; base += stride) {
-            const int i = base + threadIdx.x;
-            const bool valid = i < cnt;
-            const int key = valid ? plan.key[cls][i] : -1 - lane;          // distinct for idle lanes
-            const unsigned peers = __match_any_sync(kFull, key);
-            const int leader = __ffs(peers) - 1;
-            const int rank = __popc(peers & ((1u << lane) - 1));
-            int start = 0;
-            if (valid && lane == leader) start = atomicAdd(&plan.cursor[cls * kCostBuckets + key], __popc(peers));
-            start = __shfl_sync(kFull, start, leader);
-            if (valid) plan.sorted[cls][start + rank] = plan.raw[cls][i];
+        const int nseg = (cnt + kSegRecords - 1) / kSegRecords;
+        for (int seg = blockIdx.x; seg < nseg; seg += gridDim.x) {
+            const int base = seg * kSegRecords, i = base + t;
+            if (t < kCostBuckets) s_cnt[t] = 0;
+            __syncthreads();
+            const int key = i < cnt ? plan.key[cls][i] : -1;
+            const int rank = key >= 0 ? atomicAdd(&s_cnt[key], 1) : 0;
+            __syncthreads();
+            // exclusive scan over keys in descending order (one warp of 8 keys per lane)
+            if (t < 32) {
+                int v[8], sum = 0;
+#pragma unroll
+                for (int q = 0; q < 8; q++) { v[q] = s_cnt[kCostBuckets - 1 - (t * 8 + q)]; sum += v[q]; }
+                int incl = sum;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int x = __shfl_up_sync(kFull, incl, o);
+                    if (t >= o) incl += x;
+                }
+                int run = incl - sum;
+#pragma unroll
+                for (int q = 0; q < 8; q++) { s_start[kCostBuckets - 1 - (t * 8 + q)] = run; run += v[q]; }
+            }
+            __syncthreads();
+            if (key >= 0) plan.sorted[cls][base + s_start[key] + rank] = plan.raw[cls][i];
+            __syncthreads();
         }
     }
 }
@@ -336,23 +310,22 @@ __global__ void __launch_bounds__(256) k_solve_band(PairsPlan plan, int k, int d
 }
 
 // ------------------------------------------------------------- launchers --
-cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, const DevStrings &A,
+cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, bool band, const DevStrings &A,
                               const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
                               uint32_t *status) {
+    const int bd = band ? 1 : 0;
     if (hask) {
-        if (feat) k_pairs_prep<true, true><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, status);
-        else k_pairs_prep<true, false><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, status);
+        if (feat) k_pairs_prep<true, true><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, status);
+        else k_pairs_prep<true, false><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, status);
     } else {
-        if (feat) k_pairs_prep<false, true><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, status);
-        else k_pairs_prep<false, false><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, status);
+        if (feat) k_pairs_prep<false, true><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, status);
+        else k_pairs_prep<false, false><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, status);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_order(cudaStream_t st, int sms, bool need_hist, const PairsPlan &plan) {
-    if (need_hist) k_order_hist<<<sms * 2, 256, 0, st>>>(plan);
-    k_order_scan<<<1, kCostBuckets, 0, st>>>(plan);
-    k_order_scatter<<<sms * 4, 256, 0, st>>>(plan);
+cudaError_t launch_order(cudaStream_t st, int sms, const PairsPlan &plan) {
+    k_order_segments<<<sms * 2, kSegRecords, 0, st>>>(plan);
     return cudaGetLastError();
 }
 

@@ -12,7 +12,8 @@ constexpr int kCostBuckets = 256;    // counting-sort keys (log-spaced cost or p
 constexpr int kFeatures = 7;         // scheduler network inputs per record
 
 // Pairwise plan: records of non-trivial pairs per class, before (raw) and
-// after (sorted) ordering, their keys, optional feature rows, counters.
+// after (sorted, per 1024-record segment) ordering, their keys, optional
+// feature rows, counters.
 struct PairsPlan {
     LongItem *raw[kPairClasses];
     LongItem *sorted[kPairClasses];
@@ -21,8 +22,6 @@ struct PairsPlan {
     int64_t cap[kPairClasses];
     int32_t *count;                  // [kPairClasses]
     int32_t *head;                   // [kPairClasses]
-    int32_t *hist;                   // [kPairClasses * kCostBuckets]
-    int32_t *cursor;                 // [kPairClasses * kCostBuckets]
 };
 
 }  // namespace blg

@@ -160,7 +160,7 @@ int blg_set_schedule(blg_ctx *ctx, int mode);
  * (FP16 weights, FP32 sums) that predicts the fraction of a pair's text its
  * column loop processes before the max_dist exit. No counterpart in the
  * reference. blg_sched_train runs a logged pass over the batch (features:
- * trimmed and untrimmed lengths, length gap, max_dist, 4-gram lower bound;
+ * trimmed and untrimmed lengths, length gap, max_dist, 4-gram sketch distance;
  * label: logged exit column / text length), keeps at most max_rows rows and
  * trains the context's network for `epochs` epochs on the GPU (momentum
  * SGD, minibatches of 4096, one epoch captured as a CUDA graph); *loss_out
@@ -175,7 +175,7 @@ int blg_sched_get_weights(blg_ctx *ctx, float *w, int n);
 int blg_sched_gradient(blg_ctx *ctx, const uint16_t *x_half, const float *y, int rows, float *grad_out,
                        float *loss_out);
 int blg_sched_predict(blg_ctx *ctx, const uint16_t *x_half, int64_t rows, float *out);
-/* Versioned checkpoint ("BLGMLP01", count, FP32 weights). */
+/* Versioned checkpoint ("BLGMLP02", count, FP32 weights). */
 int blg_sched_save(blg_ctx *ctx, const char *path);
 int blg_sched_load(blg_ctx *ctx, const char *path);
 

@@ -108,3 +108,49 @@ def test_training_learns_and_learned_schedule_is_exact(gpu, tmp_path):
     finally:
         gpu.set_schedule("auto")
     np.testing.assert_array_equal(got, oracle.saturate(oracle.pairs(test.a, test.b, 8), "uint8"))
+
+
+def _solve_ms(ctx, batch, out, k, runs=3):
+    """Event time of the solve kernel (banded for k <= 31) over `runs` runs."""
+    buf = ctypes.create_string_buffer(8192)
+    batch.run(out, max_dist=k)
+    ctx.check(ctx.lib.blg_synchronize(ctx.h))
+    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 1))
+    for _ in range(runs):
+        batch.run(out, max_dist=k)
+    ctx.check(ctx.lib.blg_profile_report(ctx.h, buf, 8192))
+    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 0))
+    rows = dict((l.split()[0], float(l.split()[2])) for l in buf.value.decode().splitlines())
+    return rows.get("pairs_band", rows.get("pairs_solve")) / runs
+
+
+def test_trained_network_order_against_no_network(gpu):
+    """The same pipeline with and without the network: with zero weights
+    every record gets the same key (no ordering); with trained weights each
+    1024-record segment is ordered by predicted exit column. Results are
+    identical. On the banded pairs solver the order barely matters (its time
+    follows the total work of the lanes, not the slowest lane of a warp), so
+    the learned order must simply not be slower; the measured times print."""
+    ctx = _lib.context()
+    train = W.config3(n=1 << 18, seed=2003)
+    tb = gpu.PairsBatch(train.a, train.b)
+    loss = ctypes.c_float()
+    ctx.check(ctx.lib.blg_sched_train(ctx.h, tb.h, 8, 10, ctypes.c_float(0.02), 1 << 18, ctypes.byref(loss)))
+    trained = np.empty(P, dtype=np.float32)
+    ctx.check(ctx.lib.blg_sched_get_weights(ctx.h, trained.ctypes.data, P))
+    test = W.config3(n=1 << 20, seed=1003)
+    batch = gpu.PairsBatch(test.a, test.b)
+    out = batch.alloc("uint8")
+    gpu.set_schedule("learned")
+    try:
+        t_learned = _solve_ms(ctx, batch, out, 8)
+        res_learned = out.get()
+        _set(ctx, np.zeros(P, dtype=np.float32))
+        t_flat = _solve_ms(ctx, batch, out, 8)
+        res_flat = out.get()
+        _set(ctx, trained)
+    finally:
+        gpu.set_schedule("auto")
+    np.testing.assert_array_equal(res_learned, res_flat)
+    print(f"banded solve: learned order {t_learned:.3f} ms, without the network {t_flat:.3f} ms")
+    assert t_learned <= 1.05 * t_flat
