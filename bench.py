@@ -437,6 +437,16 @@ def make_bench(cfg: int, args=None):
     raise SystemExit(f"unknown config {cfg}")
 
 
+def hbm_peak() -> tuple:
+    """Measured copy bandwidth of this GPU pool (MEASURED_PEAKS.json, written
+    beside this file by the environment), else the fallback figure."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s"
+
+
 def read_traffic(kernel: str, workload: str):
     """dram bytes per launch from the committed ncu summary, if one exists."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.txt")
@@ -579,24 +589,30 @@ def run_ours(args, ranks: Ranks):
             cpu = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": sample,
                    "single_thread": {"value": v1, "sample": sample1},
                    "gate": bench.gate(n_s, res)}
-            if bench.runs[0][0] is not None and bench.kind != "batch":
+            if bench.kind == "pairwise" or (bench.runs[0][0] is not None and bench.kind != "batch"):
                 exit_sum = exit_columns(bench, n_s)
         result["cpu_baseline"] = cpu
         if top:
             per_launch_ms = kstats[top]["total_ms"] / kstats[top]["launches"]
             ops = bench.alg_ops(0, exit_sum)
             launches_per_step = kstats[top]["launches"] / 3.0
-            rl = {"kernel": top, "bound": "int", "unit": "Gop/s", "ms_per_launch": per_launch_ms,
-                  "peak": peak.get("gops"), "peak_source": "measured: libblg_probe LOP3/IADD3 stream on this GPU",
-                  "peak_detail": peak,
-                  "traffic": read_traffic(top, bench.w.name)}
-            if ops is not None and peak.get("gops"):
-                rl["achieved"] = ops / launches_per_step / (per_launch_ms / 1e3) / 1e9
-                rl["frac"] = rl["achieved"] / peak["gops"]
+            hpeak, hsrc = hbm_peak()
             hbm_bytes = bench.alg_bytes(0) / launches_per_step
-            rl["hbm"] = {"achieved": hbm_bytes / (per_launch_ms / 1e3) / 1e9, "peak": 6800.0, "unit": "GB/s",
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
-            rl["hbm"]["frac"] = rl["hbm"]["achieved"] / rl["hbm"]["peak"]
+            hbm = {"achieved": hbm_bytes / (per_launch_ms / 1e3) / 1e9, "peak": hpeak, "unit": "GB/s",
+                   "peak_source": hsrc, "alg_bytes_per_launch": hbm_bytes}
+            hbm["frac"] = hbm["achieved"] / hpeak
+            ipart = {"peak": peak.get("gops"), "unit": "Gop/s",
+                     "peak_source": "measured: libblg_probe LOP3/IADD3 stream on this GPU", "peak_detail": peak}
+            if ops is not None and peak.get("gops"):
+                ipart["alg_ops_per_launch"] = ops / launches_per_step
+                ipart["achieved"] = ipart["alg_ops_per_launch"] / (per_launch_ms / 1e3) / 1e9
+                ipart["frac"] = ipart["achieved"] / peak["gops"]
+            # short exact pairs (config 1) are bound by moving their bytes; the rest by the integer pipe
+            primary = hbm if (bench.kind == "pairwise" and bench.runs[0][0] is None) else ipart
+            rl = {"kernel": top, "bound": "hbm" if primary is hbm else "int",
+                  "achieved": primary.get("achieved"), "peak": primary.get("peak"), "unit": primary["unit"],
+                  "frac": primary.get("frac"), "traffic": read_traffic(top, bench.w.name),
+                  "ms_per_launch": per_launch_ms, "int": ipart, "hbm": hbm}
             result["roofline"] = rl
         print(json.dumps(result), flush=True)
 
