@@ -43,6 +43,8 @@ SIGNATURES = [
     ("blg_cdist_batch", ctypes.c_int, [_P, _P, _I32]),
     ("blg_cdist_noalloc", ctypes.c_int, [_P, _P, _SZ, _P, _I64, _P, _SZ, _P, _I64, _I32, _I32, _P]),
     ("blg_sched_train", ctypes.c_int, [_P, _P, _I32, _I32, ctypes.c_float, _I64, ctypes.POINTER(ctypes.c_float)]),
+    ("blg_sched_train_search", ctypes.c_int, [_P, _P, _I32, _I32, ctypes.c_float, _I64,
+                                              ctypes.POINTER(ctypes.c_float)]),
     ("blg_sched_set_weights", ctypes.c_int, [_P, _P, ctypes.c_int]),
     ("blg_sched_get_weights", ctypes.c_int, [_P, _P, ctypes.c_int]),
     ("blg_sched_gradient", ctypes.c_int, [_P, _P, _P, ctypes.c_int, _P, ctypes.POINTER(ctypes.c_float)]),

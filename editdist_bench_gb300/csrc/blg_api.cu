@@ -59,6 +59,8 @@ cudaError_t launch_solve_band(cudaStream_t st, int sms, const PairsPlan &plan, i
 int sched_model_ensure(blg_ctx *c, blg_sched_model **out);
 cudaError_t launch_mlp_keys(cudaStream_t st, int sms, const blg_sched_model *m, const blg::PairsPlan &plan,
                             bool band);
+cudaError_t launch_surv_keytab(cudaStream_t st, int sms, const blg_sched_model *m, const blg::SearchClass &cls, int k,
+                               uint8_t *keytab);
 cudaError_t launch_collect_rows(cudaStream_t st, int sms, const blg::PairsPlan &plan, const int32_t *cols,
                                 int64_t stride, int64_t max_rows, half *x, float *y, int64_t *n_rows);
 int sched_train_rows(blg_ctx *c, blg_sched_model *m, half *x, float *y, const int64_t *d_rows, int64_t rows,
@@ -67,8 +69,13 @@ bool sched_model_trained(const blg_sched_model *m);
 namespace blg {
 cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &src, const int32_t *perm,
                                   const int64_t *dst_off, uint8_t *dst, int64_t n, uint32_t *status);
+cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S, uint64_t *sketch, uint32_t *status);
+cudaError_t launch_search_lpt(cudaStream_t st, int sms, int nw, const DevStrings &CS, const int32_t *perm,
+                              const uint64_t *csk, const uint64_t *qsk, const SearchClass &cls, const int32_t *lo,
+                              const int32_t *hi, const int64_t *tile_start, int32_t *work, const uint8_t *keytab,
+                              int k, int dtype, void *out, int64_t nc, const SurvRows *rows, uint32_t *status);
 cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
-                             int64_t min_len, int64_t n_len, int k, int32_t *lo, int32_t *hi,
+                             int64_t min_len, int64_t n_len, int k, int tile, int32_t *lo, int32_t *hi,
                              int64_t *tile_start, int32_t *work);
 cudaError_t launch_search_surv(cudaStream_t st, int sms, int nw, const DevStrings &CS, const int32_t *perm,
                                const SearchClass &cls, const int32_t *lo, const int32_t *hi,
@@ -130,6 +137,8 @@ struct blg_search {
     int64_t min_len = 0, n_len = 0;
     // choices in tile-transposed form (exact and unsorted runs), when the
     // padding to each tile's longest choice stays small
+    // 4-gram sketches: of the length-sorted choices and of the queries
+    uint64_t *csk = nullptr, *qsk = nullptr;
     bool tt = false;
     uint32_t *tt_words = nullptr;
     int64_t *tt_base = nullptr;
@@ -650,6 +659,9 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
                    return launch_gather_strings(c->stream, c->sms, s->c.d, s->perm, cs.d.off,
                                                 (uint8_t *)cs.d.buf, nc, c->d_status);
                }), "gather_strings");
+            CK(dev_alloc(c, (void **)&s->csk, sizeof(uint64_t) * (size_t)nc), "cudaMallocAsync(sketches)");
+            CK(launch(c, "sketch", [&] { return launch_sketch_strings(c->stream, c->sms, cs.d, s->csk, c->d_status); }),
+               "sketch");
             s->min_len = mn;
             s->n_len = n_len;
             s->lsorted = true;
@@ -688,13 +700,23 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
 static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, int64_t q0 = 0,
                       int64_t q1 = -1);
 
+// Queries into HBM, with their 4-gram sketches.
+static int search_upload_queries(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq, blg_search *s) {
+    s->nq = nq;
+    int rc = upload_strings(c, bq, oq, nq, s->q);
+    if (rc) return rc;
+    CK(dev_alloc(c, (void **)&s->qsk, sizeof(uint64_t) * (size_t)std::max<int64_t>(nq, 1)), "cudaMallocAsync(sketches)");
+    CK(launch(c, "sketch", [&] { return launch_sketch_strings(c->stream, c->sms, s->q.d, s->qsk, c->d_status); }),
+       "sketch");
+    return BLG_OK;
+}
+
 // One-call cdist with host results: queries in chunks of rows; the rows of
 // chunk i go back (stream `down`) while chunk i+1 computes.
 static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq, const uint8_t *bc,
                            const int64_t *oc, int64_t nc, int k, int dtype, void *out_host, void *d_out,
                            blg_search *s) {
-    s->nq = nq;
-    int rc = upload_strings(c, bq, oq, nq, s->q);
+    int rc = search_upload_queries(c, bq, oq, nq, s);
     if (!rc) rc = search_upload_choices(c, bc, oc, nc, s);
     if (rc) return rc;
     const size_t row = dtype_size(dtype) * (size_t)nc;
@@ -733,8 +755,7 @@ static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int
 
 static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq,
                          const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s) {
-    s->nq = nq;
-    int rc = upload_strings(c, bq, oq, nq, s->q);
+    int rc = search_upload_queries(c, bq, oq, nq, s);
     if (!rc) rc = search_upload_choices(c, bc, oc, nc, s);
     if (!rc) rc = search_build_classes(c, oq, 0, nq, s);
     return rc;
@@ -775,14 +796,31 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
     for (auto &k_ : s->cls) {
         SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
         if (surv && !k_.lanes) {
+            // max_dist <= 31: jobs of 4096 survivors ordered by predicted cost
+            const bool lpt = k <= 31;
             CK(launch(c, "surv_plan", [&] {
-                   return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, k, k_.lo,
-                                           k_.hi, k_.tile_start, k_.work);
+                   return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, k, lpt ? 4096 : 1024,
+                                           k_.lo, k_.hi, k_.tile_start, k_.work);
                }), "surv_plan");
-            CK(launch(c, "search_surv", [&] {
-                   return launch_search_surv(c->stream, c->sms, k_.nw, s->cs.d, s->perm, sc, k_.lo, k_.hi,
-                                             k_.tile_start, k_.work, k, dtype, d_out, s->nc, c->d_status);
-               }), "search_surv");
+            if (lpt) {
+                uint8_t *keytab = nullptr;
+                if (c->sched == BLG_SCHED_LEARNED && c->model && sched_model_trained(c->model)) {
+                    CK(dev_alloc(c, (void **)&keytab, (size_t)k_.nq * (2 * k + 1) * 65), "cudaMallocAsync(keytab)");
+                    CK(launch(c, "sched_keytab", [&] { return launch_surv_keytab(c->stream, c->sms, c->model, sc, k, keytab); }),
+                       "sched_keytab");
+                }
+                CK(launch(c, "search_lpt", [&] {
+                       return launch_search_lpt(c->stream, c->sms, k_.nw, s->cs.d, s->perm, s->csk, s->qsk, sc, k_.lo,
+                                                k_.hi, k_.tile_start, k_.work, keytab, k, dtype, d_out, s->nc, nullptr,
+                                                c->d_status);
+                   }), "search_lpt");
+                dev_free(c, keytab);
+            } else {
+                CK(launch(c, "search_surv", [&] {
+                       return launch_search_surv(c->stream, c->sms, k_.nw, s->cs.d, s->perm, sc, k_.lo, k_.hi,
+                                                 k_.tile_start, k_.work, k, dtype, d_out, s->nc, c->d_status);
+                   }), "search_surv");
+            }
             continue;
         }
         if (k_.lanes) {
@@ -820,6 +858,9 @@ static void search_release(blg_ctx *c, blg_search *s) {
     dev_free(c, s->tt_words);
     dev_free(c, s->tt_base);
     dev_free(c, s->tt_len);
+    dev_free(c, s->csk);
+    dev_free(c, s->qsk);
+    s->csk = s->qsk = nullptr;
     s->tt_words = nullptr;
     s->tt_base = nullptr;
     s->tt_len = nullptr;
@@ -1116,6 +1157,72 @@ int blg_sched_train(blg_ctx *c, blg_pairs *p, int32_t max_dist, int32_t epochs, 
                   : fail(c, BLG_ERR_ARG, "no non-trivial pairs to learn from");
     dev_free(c, out);
     dev_free(c, cols);
+    dev_free(c, x);
+    dev_free(c, y);
+    dev_free(c, nrows);
+    const int rc2 = sync_and_status(c);
+    return rc ? rc : rc2;
+}
+
+int blg_sched_train_search(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t epochs, float lr, int64_t max_rows,
+                           float *loss_out) {
+    ENTER(c);
+    if (!s || s->nq == 0 || s->nc == 0) return fail(c, BLG_ERR_ARG, "empty training search");
+    if (!s->lsorted) return fail(c, BLG_ERR_ARG, "choice lengths too spread for the survivor plan");
+    if (max_dist < 0 || max_dist > 31) return fail(c, BLG_ERR_ARG, "max_dist must be in 0..31");
+    if (epochs < 0 || max_rows <= 0 || !(lr > 0.f)) return fail(c, BLG_ERR_ARG, "bad training arguments");
+    blg_sched_model *m = nullptr;
+    int rc = sched_model_ensure(c, &m);
+    if (rc) return rc;
+    // survivors of every sequential class (host estimate from the plans, for the row spacing)
+    for (auto &k_ : s->cls)
+        CK(launch(c, "build_peq", [&] {
+               return launch_build_peq(c->stream, s->q.d, k_.qidx, k_.nq, k_.nw, k_.peq, c->d_status);
+           }), "build_peq");
+    int64_t survivors = 0;
+    for (auto &k_ : s->cls) {
+        if (k_.lanes) continue;
+        SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
+        CK(launch(c, "surv_plan", [&] {
+               return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, max_dist, 1, k_.lo, k_.hi,
+                                       k_.tile_start, k_.work);
+           }), "surv_plan");
+        int64_t t = 0;
+        CK(cudaMemcpyAsync(&t, k_.tile_start + k_.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream), "D2H");
+        CK(cudaStreamSynchronize(c->stream), "sync");
+        survivors += t;
+    }
+    if (survivors == 0) return fail(c, BLG_ERR_ARG, "no survivors to learn from");
+    void *out = nullptr, *x = nullptr, *y = nullptr, *nrows = nullptr;
+    CK(dev_alloc(c, &out, (size_t)s->nq * (size_t)s->nc), "alloc");
+    CK(dev_alloc(c, &x, sizeof(half) * kFeatures * (size_t)max_rows + 16), "alloc");
+    CK(dev_alloc(c, &y, sizeof(float) * (size_t)max_rows + 16), "alloc");
+    CK(dev_alloc(c, &nrows, sizeof(int64_t)), "alloc");
+    CK(cudaMemsetAsync(nrows, 0, sizeof(int64_t), c->stream), "memset");
+    SurvRows R{(half *)x, (float *)y, max_rows, (int64_t *)nrows,
+               (int)std::min<int64_t>(INT32_MAX, std::max<int64_t>(1, (survivors + max_rows - 1) / max_rows))};
+    for (auto &k_ : s->cls) {
+        if (k_.lanes) continue;
+        SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
+        CK(launch(c, "surv_plan", [&] {
+               return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, max_dist, 4096, k_.lo, k_.hi,
+                                       k_.tile_start, k_.work);
+           }), "surv_plan");
+        CK(launch(c, "search_lpt_logged", [&] {
+               return launch_search_lpt(c->stream, c->sms, k_.nw, s->cs.d, s->perm, s->csk, s->qsk, sc, k_.lo, k_.hi,
+                                        k_.tile_start, k_.work, nullptr, max_dist, BLG_UINT8, out, s->nc, &R,
+                                        c->d_status);
+           }), "search_lpt_logged");
+    }
+    int64_t rows = 0;
+    CK(cudaMemcpyAsync(&rows, nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream), "D2H rows");
+    CK(cudaStreamSynchronize(c->stream), "sync");
+    rows = std::min(rows, max_rows);
+    CK(cudaMemcpyAsync(nrows, &rows, sizeof(int64_t), cudaMemcpyHostToDevice, c->stream), "H2D rows");
+    rc = rows > 0 ? sched_train_rows(c, m, (half *)x, (float *)y, (const int64_t *)nrows, rows, epochs, lr, 4096,
+                                     loss_out)
+                  : fail(c, BLG_ERR_ARG, "no survivors to learn from");
+    dev_free(c, out);
     dev_free(c, x);
     dev_free(c, y);
     dev_free(c, nrows);

@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(256) k_gather_strings(DevStrings src, const in
 // length), tile counts, and their exclusive prefix tile_start[0..nq]. One
 // block; the scan walks the queries 1024 at a time.
 __global__ void __launch_bounds__(1024) k_surv_plan(SearchClass cls, const int64_t *lstart, int64_t min_len,
-                                                    int64_t n_len, int k, int32_t *lo, int32_t *hi,
+                                                    int64_t n_len, int k, int tile, int32_t *lo, int32_t *hi,
                                                     int64_t *tile_start, int32_t *work) {
     __shared__ int64_t s_sum[1024];
     __shared__ int64_t s_carry;
@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(1024) k_surv_plan(SearchClass cls, const int64
             const int64_t l = lstart[a], h = b > a ? lstart[b] : l;
             lo[qi] = (int32_t)l;
             hi[qi] = (int32_t)h;
-            tiles = (h - l + 1023) / 1024;
+            tiles = (h - l + tile - 1) / tile;
         }
         s_sum[threadIdx.x] = tiles;
         __syncthreads();
@@ -652,10 +652,10 @@ cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &sr
 }
 
 cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
-                             int64_t min_len, int64_t n_len, int k, int32_t *lo, int32_t *hi,
+                             int64_t min_len, int64_t n_len, int k, int tile, int32_t *lo, int32_t *hi,
                              int64_t *tile_start, int32_t *work) {
     if (cls.nq <= 0) return cudaSuccess;
-    k_surv_plan<<<1, 1024, 0, st>>>(cls, lstart, min_len, n_len, k, lo, hi, tile_start, work);
+    k_surv_plan<<<1, 1024, 0, st>>>(cls, lstart, min_len, n_len, k, tile, lo, hi, tile_start, work);
     return cudaGetLastError();
 }
 

@@ -507,4 +507,30 @@ __device__ __forceinline__ void build_peq_block(const uint8_t *p, int m, int nwc
     for (int x = threadIdx.x; x < words; x += blockDim.x) dst[x] = tab[x];
 }
 
+// 4-gram sketch of a string: its first kSketchWindow bytes set one bit of a
+// 64-bit mask per 4-gram (hashed into 64 bins). popc(sketch(x) ^ sketch(y))
+// counts the bins present in one string and not the other: each edit changes
+// at most 4 grams of each string, so near-identical strings score low and
+// unrelated ones high. A few register operations per byte, no shared memory.
+constexpr int kSketchWindow = 64;
+
+__device__ __forceinline__ uint64_t gram_sketch(const uint8_t *p, int m) {
+    if (m > kSketchWindow) m = kSketchWindow;
+    uint64_t sk = 0;
+    uint32_t g = 0;
+    TextScan ts;
+    ts.init(p);
+    for (int i = 0; i < m; i += 4) {
+        const uint32_t w4 = ts.next4();
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            if (i + b < m) {
+                g = __funnelshift_l(w4 << (24 - 8 * b), g, 8);     // g = (g << 8) | byte b
+                if (i + b >= 3) sk |= 1ull << ((g * 0x9E3779B1u) >> 26);
+            }
+        }
+    }
+    return sk;
+}
+
 }  // namespace blg

@@ -31,32 +31,8 @@ __device__ __forceinline__ int cost_bucket(float work) {
 }
 
 // Features of one trimmed pair (pattern p of m, text t of n; la0, lb0
-// untrimmed): lengths, trimmed lengths, length gap, k, and a 4-gram sketch
-// distance: each string's first 64 trimmed bytes set one bit of a 64-bit
-// mask per 4-gram (hashed into 64 bins); the feature is the number of bins
-// present in one mask and not the other. Edits change at most 4 grams each,
-// so near-identical pairs score low and unrelated ones high; it costs a few
-// register operations per byte and no shared memory.
-constexpr int kSketchWindow = 64;
-
-__device__ __forceinline__ uint64_t gram_sketch(const uint8_t *p, int m) {
-    if (m > kSketchWindow) m = kSketchWindow;
-    uint64_t sk = 0;
-    uint32_t g = 0;
-    TextScan ts;
-    ts.init(p);
-    for (int i = 0; i < m; i += 4) {
-        const uint32_t w4 = ts.next4();
-#pragma unroll
-        for (int b = 0; b < 4; b++) {
-            if (i + b < m) {
-                g = __funnelshift_l(w4 << (24 - 8 * b), g, 8);     // g = (g << 8) | byte b
-                if (i + b >= 3) sk |= 1ull << ((g * 0x9E3779B1u) >> 26);
-            }
-        }
-    }
-    return sk;
-}
+// untrimmed): lengths, trimmed lengths, length gap, k, and the 4-gram sketch
+// distance of their first 64 trimmed bytes (gram_sketch, blg_kernels.cuh).
 
 template <bool HASK, bool FEAT>
 __global__ void __launch_bounds__(256) k_pairs_prep(DevStrings A, DevStrings B, int k, int dtype, void *out,

@@ -24,4 +24,19 @@ struct PairsPlan {
     int32_t *head;                   // [kPairClasses]
 };
 
+// Logged rows of the learned scheduler from the thresholded search (features,
+// label = exit column / text length) for every `stride`-th survivor, up to
+// `cap` rows; `count` counts the rows written.
+struct SurvRows {
+    half *x;
+    float *y;
+    int64_t cap;
+    int64_t *count;
+    int stride;
+};
+
+// Survivor key table of a query class: (2k+1) length gaps x 65 sketch
+// distances per query.
+constexpr int kSketchDistances = 65;
+
 }  // namespace blg

@@ -167,6 +167,15 @@ int blg_set_schedule(blg_ctx *ctx, int mode);
  * = last epoch's mean squared error. */
 int blg_sched_train(blg_ctx *ctx, blg_pairs *p, int32_t max_dist, int32_t epochs, float lr,
                     int64_t max_rows, float *loss_out);
+/* The same network for a thresholded search (max_dist <= 31): a logged run of
+ * the survivor kernel over the resident search `s` collects rows (features:
+ * query and choice lengths, length gap, max_dist, 4-gram sketch distance;
+ * label: the banded loop's exit column / choice length) from every survivor
+ * spaced to keep at most max_rows, then trains as above. Under
+ * BLG_SCHED_LEARNED the survivor kernel then orders each job of survivors by
+ * the network's predicted work (longest first). */
+int blg_sched_train_search(blg_ctx *ctx, blg_search *s, int32_t max_dist, int32_t epochs, float lr,
+                           int64_t max_rows, float *loss_out);
 /* 1345 FP32 master weights: W1[32][7], b1[32], W2[32][32], b2[32], W3[32], b3. */
 int blg_sched_set_weights(blg_ctx *ctx, const float *w, int n);
 int blg_sched_get_weights(blg_ctx *ctx, float *w, int n);

@@ -154,3 +154,55 @@ def test_trained_network_order_against_no_network(gpu):
     np.testing.assert_array_equal(res_learned, res_flat)
     print(f"banded solve: learned order {t_learned:.3f} ms, without the network {t_flat:.3f} ms")
     assert t_learned <= 1.05 * t_flat
+
+
+def _lpt_ms(ctx, s, out, k, runs=3):
+    buf = ctypes.create_string_buffer(8192)
+    s.run(out, max_dist=k)
+    ctx.check(ctx.lib.blg_synchronize(ctx.h))
+    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 1))
+    for _ in range(runs):
+        s.run(out, max_dist=k)
+    ctx.check(ctx.lib.blg_profile_report(ctx.h, buf, 8192))
+    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 0))
+    rows = dict((l.split()[0], float(l.split()[2])) for l in buf.value.decode().splitlines())
+    return rows["search_lpt"] / runs
+
+
+def test_learned_search_order_gain_and_exactness(gpu):
+    """Thresholded search (lengths 100..256, 5% planted near-copies, k = 4):
+    the network trained on the survivor kernel's own logged rows orders each
+    job longest-predicted-first. Results equal the oracle under every order;
+    the survivor kernel with the learned order beats the same kernel without
+    the network (zero weights: one key for all, no ordering)."""
+    ctx = _lib.context()
+    tr = W.config4(nq=32, nc=1 << 17, seed=2004)
+    ts = gpu.SearchBatch(tr.q, tr.c)
+    loss = ctypes.c_float()
+    ctx.check(ctx.lib.blg_sched_train_search(ctx.h, ts.h, 4, 10, ctypes.c_float(0.02), 1 << 18, ctypes.byref(loss)))
+    assert np.isfinite(loss.value)
+    trained = np.empty(P, dtype=np.float32)
+    ctx.check(ctx.lib.blg_sched_get_weights(ctx.h, trained.ctypes.data, P))
+    w = W.config4(nq=128, nc=1 << 17, seed=1004)
+    s = gpu.SearchBatch(w.q, w.c)
+    out = s.alloc("uint8")
+    rows = [0, 1, 63, 127]
+    want = oracle.saturate(oracle.cross(W.take(w.q, rows), w.c, 4, threads=8), "uint8")
+    gpu.set_schedule("learned")
+    try:
+        t_learned = _lpt_ms(ctx, s, out, 4)
+        got_learned = out.get()
+        _set(ctx, np.zeros(P, dtype=np.float32))
+        t_flat = _lpt_ms(ctx, s, out, 4)
+        got_flat = out.get()
+        _set(ctx, trained)
+        gpu.set_schedule("auto")
+        t_auto = _lpt_ms(ctx, s, out, 4)
+        got_auto = out.get()
+    finally:
+        gpu.set_schedule("auto")
+    np.testing.assert_array_equal(got_learned[rows], want)
+    np.testing.assert_array_equal(got_learned, got_flat)
+    np.testing.assert_array_equal(got_learned, got_auto)
+    print(f"survivor kernel: learned {t_learned:.3f} ms, sketch order {t_auto:.3f} ms, no network {t_flat:.3f} ms")
+    assert t_learned * 1.2 < t_flat
