@@ -878,6 +878,7 @@ struct blg_batch {
     int njobs = 0;
     int64_t *d_qprefix = nullptr, *d_job_tiles = nullptr, *d_tile_base = nullptr;
     int32_t *d_work = nullptr;
+    int nbanded = 0;
     BatchFill *d_fills = nullptr;
     int nfill = 0;
     int64_t max_fill = 0, total_queries = 0, pairs = 0;
@@ -949,6 +950,9 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
             j.k = k;
             j.dtype = p.dtype;
             j.nw = cl.nw;
+            j.tile = (k >= 0 && k <= 31) ? 4096 : 1024;
+            j.csk = s->csk;
+            j.qsk = s->qsk;
             j.out = p.d_out;
             jobs.push_back(j);
             qprefix.push_back(qprefix.back() + cl.nq);
@@ -960,6 +964,12 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
             b->max_fill = std::max(b->max_fill, p.nq * p.nc * (int64_t)dtype_size(p.dtype));
         }
     }
+    // banded jobs first (they run in their own persistent kernel); the Peq
+    // prefix follows the job order
+    std::stable_partition(jobs.begin(), jobs.end(), [](const BatchJob &j) { return j.k >= 0 && j.k <= 31; });
+    b->nbanded = (int)std::count_if(jobs.begin(), jobs.end(), [](const BatchJob &j) { return j.k >= 0 && j.k <= 31; });
+    qprefix.assign(1, 0);
+    for (const BatchJob &j : jobs) qprefix.push_back(qprefix.back() + j.cls.nq);
     b->njobs = (int)jobs.size();
     b->nfill = (int)fills.size();
     b->total_queries = qprefix.back();
@@ -970,7 +980,7 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
         CK(cudaMemcpyAsync(b->d_qprefix, qprefix.data(), sizeof(int64_t) * qprefix.size(), cudaMemcpyHostToDevice, c->stream), "H2D qprefix");
         CK(dev_alloc(c, (void **)&b->d_job_tiles, sizeof(int64_t) * jobs.size()), "alloc job tiles");
         CK(dev_alloc(c, (void **)&b->d_tile_base, sizeof(int64_t) * (jobs.size() + 1)), "alloc tile base");
-        CK(dev_alloc(c, (void **)&b->d_work, sizeof(int32_t)), "alloc work");
+        CK(dev_alloc(c, (void **)&b->d_work, 2 * sizeof(int32_t)), "alloc work");
     }
     if (b->nfill > 0) {
         CK(dev_alloc(c, (void **)&b->d_fills, sizeof(BatchFill) * fills.size()), "alloc fills");
@@ -989,7 +999,7 @@ static int batch_run(blg_ctx *c, blg_batch *b) {
         c->prof = false;                      // no per-launch events inside a capture
         const int64_t before = c->launches;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "begin capture");
-        BatchPlan plan{b->d_jobs, b->njobs, b->d_qprefix, b->d_job_tiles, b->d_tile_base, b->d_work};
+        BatchPlan plan{b->d_jobs, b->njobs, b->nbanded, b->d_qprefix, b->d_job_tiles, b->d_tile_base, b->d_work};
         cudaError_t e = launch_batch(c->stream, c->sms, plan, b->d_fills, b->nfill, b->max_fill, b->total_queries,
                                      c->d_status);
         int rc = e == cudaSuccess ? BLG_OK : cuda_fail(c, e, "batch launch");
@@ -1003,7 +1013,9 @@ static int batch_run(blg_ctx *c, blg_batch *b) {
         e = cudaGraphInstantiate(&b->exec, g, 0);
         if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_fail(c, e, "graph instantiate"); }
         b->graph = g;
-        b->graph_kernels = (b->nfill > 0 ? 1 : 0) + (b->njobs > 0 ? 4 : 0) + (c->launches - before);
+        b->graph_kernels = (b->nfill > 0 ? 1 : 0) +
+                           (b->njobs > 0 ? 3 + (b->nbanded > 0 ? 1 : 0) + (b->nbanded < b->njobs ? 1 : 0) : 0) +
+                           (c->launches - before);
         c->launches = before;
     }
     CK(launch(c, "batch_graph", [&] { return cudaGraphLaunch(b->exec, c->stream); }), "graph launch");

@@ -51,16 +51,6 @@ __global__ void __launch_bounds__(256) k_batch_fill(const BatchFill *fills) {
                (int64_t)gridDim.x * blockDim.x);
 }
 
-// largest j in [0, n) with pre[j] <= x (pre non-decreasing, pre[0] <= x)
-__device__ __forceinline__ int upper_index(const int64_t *pre, int n, int64_t x) {
-    int a = 0, b = n;
-    while (b - a > 1) {
-        const int mid = (a + b) >> 1;
-        if (pre[mid] <= x) a = mid; else b = mid;
-    }
-    return a;
-}
-
 __global__ void __launch_bounds__(256) k_batch_peq(BatchPlan plan, uint32_t *status) {
     extern __shared__ uint64_t tab[];
     const int j = upper_index(plan.q_prefix, plan.njobs, blockIdx.x);
@@ -95,7 +85,7 @@ __global__ void __launch_bounds__(1024) k_batch_plan(BatchPlan plan) {
             const int64_t l = job.lstart[a], h = b > a ? job.lstart[b] : l;
             job.lo[qi] = (int32_t)l;
             job.hi[qi] = (int32_t)h;
-            tiles = (h - l + 1023) / 1024;
+            tiles = (h - l + job.tile - 1) / job.tile;
         }
         s_sum[threadIdx.x] = tiles;
         __syncthreads();
@@ -119,7 +109,7 @@ __global__ void __launch_bounds__(1024) k_batch_plan(BatchPlan plan) {
 __global__ void __launch_bounds__(1024) k_batch_scan(BatchPlan plan) {
     __shared__ int64_t s_sum[1024];
     __shared__ int64_t s_carry;
-    if (threadIdx.x == 0) { s_carry = 0; *plan.work = 0; }
+    if (threadIdx.x == 0) { s_carry = 0; plan.work[0] = 0; plan.work[1] = 0; }
     __syncthreads();
     for (int base = 0; base < plan.njobs; base += 1024) {
         const int j = base + threadIdx.x;
@@ -149,33 +139,56 @@ __device__ __forceinline__ void batch_tile(const BatchJob &job, const uint64_t *
     const int64_t row = job.cls.qidx[qi];
     const int64_t s_end = job.hi[qi];
     const int k = job.k >= 0 ? job.k : 0x3fffffff;    // exact problems: no exit can fire
-    const bool banded = job.k >= 0 && job.k <= 31;
-    const uint32_t *rows32 = reinterpret_cast<const uint32_t *>(s_peq);
-    constexpr int kStride = 2 * NW + 6;
 #pragma unroll 1
     for (int t = 0; t < 4; t++) {
         const int64_t sidx = s0 + t;
         if (sidx >= s_end) break;
         int n;
         const uint8_t *tp = string_at(job.CS, sidx, n, status);
-        int d;
-        if (!banded) d = dist_seq_any<NW, true>(s_peq, m, tp, n, k, u, ra);
-        else if (m == 0) d = cap_k(n, k);
-        else if ((n > m ? n - m : m - n) > k) d = k + 1;
-        else d = band_distance(m, tp, n, k,
-                               [&](uint32_t c, int p0) { return band_row_bits(rows32 + c * kStride, p0); }, u);
+        const int d = dist_seq_any<NW, true>(s_peq, m, tp, n, k, u, ra);
         if (d <= k) store1(job.out, job.dtype, row * job.nc + job.perm[sidx], d);
     }
 }
 
-__global__ void __launch_bounds__(256) k_batch_search(BatchPlan plan, uint32_t *status, uint32_t unit) {
-    extern __shared__ uint64_t s_peq[];
-    __shared__ int s_tile;
+// Banded jobs (0 <= k <= 31): persistent CTAs pull (job, query, 4096-survivor)
+// units of the banded part of the tile space and run them longest-first.
+__global__ void __launch_bounds__(256) k_batch_lpt(BatchPlan plan, uint32_t *status, uint32_t unit) {
+    extern __shared__ uint32_t s_rows[];
+    __shared__ LptShared S;
     const Units u{unit, unit + unit};
-    const int64_t total = plan.tile_base[plan.njobs];
+    const int64_t total = plan.tile_base[plan.nbanded];
     int cur_j = -1, cur_q = -1;
     while (true) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(plan.work, 1);
+        if (threadIdx.x == 0) S.job = atomicAdd(&plan.work[0], 1);
+        __syncthreads();
+        const int64_t tile = S.job;
+        if (tile >= total) break;
+        const int j = upper_index(plan.tile_base, plan.nbanded, tile);
+        const BatchJob &job = plan.jobs[j];
+        const int64_t lt = tile - plan.tile_base[j];
+        const int qi = upper_index(job.tile_start, job.cls.nq, lt);
+        if (j != cur_j || qi != cur_q) {
+            stage_band_rows(job.cls.peq + (size_t)qi * 256 * job.nw, job.nw, s_rows);
+            cur_j = j;
+            cur_q = qi;
+        }
+        const int64_t row = job.cls.qidx[qi];
+        const int64_t s0 = job.lo[qi] + (lt - job.tile_start[qi]) * kSurvJob;
+        const int cnt = (int)min((int64_t)kSurvJob, (int64_t)job.hi[qi] - s0);
+        lpt_job(S, job.CS, job.perm, job.csk, job.qsk[row], s_rows, 2 * job.nw + 6, job.cls.qlen[qi], row, s0, cnt,
+                job.k, nullptr, job.dtype, job.out, job.nc, status, u, [](int64_t, int, int) {});
+    }
+}
+
+// The other jobs (exact, or max_dist > 31): 1024-choice tiles, 4 per thread.
+__global__ void __launch_bounds__(256) k_batch_search(BatchPlan plan, uint32_t *status, uint32_t unit) {
+    extern __shared__ uint64_t s_peq[];
+    __shared__ int64_t s_tile;
+    const Units u{unit, unit + unit};
+    const int64_t first = plan.tile_base[plan.nbanded], total = plan.tile_base[plan.njobs];
+    int cur_j = -1, cur_q = -1;
+    while (true) {
+        if (threadIdx.x == 0) s_tile = first + atomicAdd(&plan.work[1], 1);
         __syncthreads();
         const int64_t tile = s_tile;
         if (tile >= total) break;
@@ -186,8 +199,7 @@ __global__ void __launch_bounds__(256) k_batch_search(BatchPlan plan, uint32_t *
         const int nw = job.nw;
         if (j != cur_j || qi != cur_q) {
             const uint64_t *src = job.cls.peq + (size_t)qi * 256 * nw;
-            if (job.k >= 0 && job.k <= 31) stage_band_rows(src, nw, reinterpret_cast<uint32_t *>(s_peq));
-            else for (int x = threadIdx.x; x < 256 * nw; x += blockDim.x) s_peq[x] = __ldg(src + x);
+            for (int x = threadIdx.x; x < 256 * nw; x += blockDim.x) s_peq[x] = __ldg(src + x);
             cur_j = j;
             cur_q = qi;
         }
@@ -208,6 +220,8 @@ cudaError_t batch_set_attributes() {
                                          256 * kBatchMaxWords * 8);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_batch_search, cudaFuncAttributeMaxDynamicSharedMemorySize, kBatchSearchSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch_lpt, cudaFuncAttributeMaxDynamicSharedMemorySize, kBatchSearchSmem);
     return e;
 }
 
@@ -224,7 +238,8 @@ cudaError_t launch_batch(cudaStream_t st, int sms, const BatchPlan &plan, const 
         k_batch_peq<<<(unsigned)total_queries, 256, 256 * kBatchMaxWords * 8, st>>>(plan, status);
         k_batch_plan<<<plan.njobs, 1024, 0, st>>>(plan);
         k_batch_scan<<<1, 1024, 0, st>>>(plan);
-        k_batch_search<<<sms * 4, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
+        if (plan.nbanded > 0) k_batch_lpt<<<sms * 4, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
+        if (plan.nbanded < plan.njobs) k_batch_search<<<sms * 3, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
     }
     return cudaGetLastError();
 }

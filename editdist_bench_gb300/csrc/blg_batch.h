@@ -21,6 +21,9 @@ struct BatchJob {
     int64_t *tile_start;       // tile prefix per query (nq + 1)
     int64_t nc;
     int k, dtype, nw;
+    int tile;                  // survivors per work unit: 4096 (banded, longest-first jobs) or 1024
+    const uint64_t *csk;       // 4-gram sketches of the sorted choices
+    const uint64_t *qsk;       // 4-gram sketches of the queries (by query row)
     void *out;
 };
 
@@ -32,12 +35,13 @@ struct BatchFill {
 };
 
 struct BatchPlan {
-    const BatchJob *jobs;      // device array
+    const BatchJob *jobs;      // device array; banded jobs (0 <= k <= 31) first
     int njobs;
+    int nbanded;               // jobs [0, nbanded) run as longest-first jobs (k_batch_lpt)
     const int64_t *q_prefix;   // [njobs + 1] queries before each job (Peq build CTAs)
     int64_t *job_tiles;        // [njobs]
     int64_t *tile_base;        // [njobs + 1]
-    int32_t *work;             // persistent-kernel tile counter
+    int32_t *work;             // persistent-kernel counters: [0] banded jobs, [1] the others
 };
 
 cudaError_t batch_set_attributes();

@@ -533,4 +533,103 @@ __device__ __forceinline__ uint64_t gram_sketch(const uint8_t *p, int m) {
     return sk;
 }
 
+// ---------------------------------- thresholded search: longest-first jobs --
+// A job is up to kSurvJob survivors (choices within max_dist k <= 31 in length)
+// of one query, whose banded Peq rows are in shared memory. Every survivor
+// gets a predicted-cost key (the query/choice sketch distance, or a row of the
+// learned scheduler's key table indexed by (length gap, sketch distance)),
+// the job is counting-sorted by key in shared memory, most expensive first,
+// and warps pull 32-survivor chunks in that order from a shared counter.
+// Results <= k are stored (the output holds k+1 already).
+constexpr int kSurvJob = 4096;
+
+struct LptShared {
+    uint16_t list[kSurvJob];
+    int cnt[256], start[256];
+    int64_t job;
+    int next;
+};
+
+// largest j in [0, n) with pre[j] <= x (pre non-decreasing, pre[0] <= x)
+__device__ __forceinline__ int upper_index(const int64_t *pre, int n, int64_t x) {
+    int a = 0, b = n;
+    while (b - a > 1) {
+        const int mid = (a + b) >> 1;
+        if (pre[mid] <= x) a = mid; else b = mid;
+    }
+    return a;
+}
+
+// Called by all 256 threads of the CTA; `log(sidx, n, cols)` sees every solved survivor.
+template <typename LogFn>
+__device__ __forceinline__ void lpt_job(LptShared &S, const DevStrings &CS, const int32_t *perm, const uint64_t *csk,
+                                        uint64_t qs, const uint32_t *rows, int stride, int m, int64_t row, int64_t s0,
+                                        int cnt, int k, const uint8_t *keyrow, int dtype, void *out, int64_t nc,
+                                        uint32_t *status, Units u, LogFn log) {
+    constexpr int kPer = kSurvJob / 256;
+    const int tid = threadIdx.x, lane = tid & 31;
+    S.cnt[tid] = 0;
+    if (tid == 0) S.next = 0;
+    __syncthreads();
+    int key[kPer], rank[kPer];
+#pragma unroll
+    for (int r = 0; r < kPer; r++) {
+        const int l = tid + 256 * r;
+        key[r] = -1;
+        if (l < cnt) {
+            const int64_t sidx = s0 + l;
+            const int sd = __popcll(qs ^ csk[sidx]);
+            if (keyrow) {
+                int g = (int)(CS.off[sidx + 1] - CS.off[sidx]) - m + k;
+                g = g < 0 ? 0 : (g > 2 * k ? 2 * k : g);
+                key[r] = keyrow[g * (kSketchWindow + 1) + sd];
+            } else {
+                key[r] = kSketchWindow - sd;                 // near-copies (low distance) run longest
+            }
+            rank[r] = atomicAdd(&S.cnt[key[r]], 1);
+        }
+    }
+    __syncthreads();
+    if (tid < 32) {                                           // bucket starts, largest key first
+        int v[8], sum = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) { v[q] = S.cnt[255 - (tid * 8 + q)]; sum += v[q]; }
+        int incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int x = __shfl_up_sync(kFull, incl, o);
+            if (tid >= o) incl += x;
+        }
+        int run = incl - sum;
+#pragma unroll
+        for (int q = 0; q < 8; q++) { S.start[255 - (tid * 8 + q)] = run; run += v[q]; }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kPer; r++)
+        if (key[r] >= 0) S.list[S.start[key[r]] + rank[r]] = (uint16_t)(tid + 256 * r);
+    __syncthreads();
+    while (true) {
+        int c = 0;
+        if (lane == 0) c = atomicAdd(&S.next, 1);
+        c = __shfl_sync(kFull, c, 0);
+        if (c * 32 >= cnt) break;
+        const int e = c * 32 + lane;
+        if (e < cnt) {
+            const int64_t sidx = s0 + S.list[e];
+            int n;
+            const uint8_t *tp = string_at(CS, sidx, n, status);
+            int d, cols = 0;
+            if (m == 0) d = cap_k(n, k);
+            else if ((n > m ? n - m : m - n) > k) d = k + 1;
+            else d = band_distance(m, tp, n, k,
+                                   [&](uint32_t ch, int p0) { return band_row_bits(rows + ch * stride, p0); }, u,
+                                   &cols);
+            if (d <= k) store1(out, dtype, row * nc + perm[sidx], d);
+            log(sidx, n, cols);
+        }
+    }
+    __syncthreads();
+}
+
 }  // namespace blg
