@@ -37,6 +37,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -495,6 +496,11 @@ def train_scheduler(ctx, args) -> dict:
 # ------------------------------------------------------------------ arms --
 def run_ours(args, ranks: Ranks):
     ctx = _lib.context()
+    tune = None
+    if not args.no_autotune:                     # launch shapes for this GPU, outside the timed region
+        t0 = time.perf_counter()
+        tune = gpu.autotune(os.path.join(tempfile.gettempdir(), f"blg_tune_{ranks.local}.txt"))
+        tune["seconds"] = time.perf_counter() - t0
     gpu.set_schedule(args.schedule)
     bench = make_bench(args.config, args)
     p = ctypes.c_void_p()
@@ -584,7 +590,7 @@ def run_ours(args, ranks: Ranks):
         "e2e": {"value": bench.pairs * ranks.world / e2e_s, "unit": "pairs/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "one-call C-ABI (blg_pairwise / blg_cdist / blg_cdist_batch), pinned host buffers, wall clock"},
-        "gpu_launches": int(launches), "wall_s_timed_region": wall, "scheduler": sched_info,
+        "gpu_launches": int(launches), "wall_s_timed_region": wall, "scheduler": sched_info, "tuning": tune,
         "clocks": clk, "runs": extra_runs, "kernels": kstats,
     }
     if args.config in H100_REF:
@@ -691,6 +697,7 @@ def main():
     ap.add_argument("--scale", type=float, default=None, help="shrink the batch's choice counts (config 5)")
     ap.add_argument("--schedule", default="auto", choices=["auto", "plain", "learned", "lensort"],
                     help="work order of max_dist runs (results are identical)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--epochs", type=int, default=10, help="scheduler training epochs (learned)")
     ap.add_argument("--lr", type=float, default=0.02, help="scheduler learning rate (learned)")
     args = ap.parse_args()

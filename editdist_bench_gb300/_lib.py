@@ -63,6 +63,8 @@ SIGNATURES = [
     ("blg_timer_stop", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float)]),
     ("blg_launch_count", ctypes.c_int64, [_P]),
     ("blg_set_schedule", ctypes.c_int, [_P, ctypes.c_int]),
+    ("blg_autotune", ctypes.c_int, [_P, ctypes.c_char_p]),
+    ("blg_get_tuning", ctypes.c_int, [_P, _P, ctypes.c_int]),
     ("blg_profile_enable", ctypes.c_int, [_P, ctypes.c_int]),
     ("blg_profile_report", ctypes.c_int, [_P, ctypes.c_char_p, _SZ]),
 ]

@@ -53,7 +53,7 @@ cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, b
 cudaError_t launch_order(cudaStream_t st, int sms, const PairsPlan &plan);
 cudaError_t launch_solve(cudaStream_t st, int sms, bool hask, const PairsPlan &plan, int k, int dtype,
                          void *out, int32_t *exit_log, bool any_long);
-cudaError_t launch_solve_band(cudaStream_t st, int sms, const PairsPlan &plan, int k, int dtype, void *out,
+cudaError_t launch_solve_band(cudaStream_t st, int sms, int ctas_per_sm, const PairsPlan &plan, int k, int dtype, void *out,
                               int32_t *exit_log);
 }  // namespace blg
 int sched_model_ensure(blg_ctx *c, blg_sched_model **out);
@@ -70,10 +70,11 @@ namespace blg {
 cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &src, const int32_t *perm,
                                   const int64_t *dst_off, uint8_t *dst, int64_t n, uint32_t *status);
 cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S, uint64_t *sketch, uint32_t *status);
-cudaError_t launch_search_lpt(cudaStream_t st, int sms, int nw, const DevStrings &CS, const int32_t *perm,
-                              const uint64_t *csk, const uint64_t *qsk, const SearchClass &cls, const int32_t *lo,
-                              const int32_t *hi, const int64_t *tile_start, int32_t *work, const uint8_t *keytab,
-                              int k, int dtype, void *out, int64_t nc, const SurvRows *rows, uint32_t *status);
+cudaError_t launch_search_lpt(cudaStream_t st, int sms, int ctas_per_sm, int jobsz, int nw, const DevStrings &CS,
+                              const int32_t *perm, const uint64_t *csk, const uint64_t *qsk, const SearchClass &cls,
+                              const int32_t *lo, const int32_t *hi, const int64_t *tile_start, int32_t *work,
+                              const uint8_t *keytab, int k, int dtype, void *out, int64_t nc, const SurvRows *rows,
+                              uint32_t *status);
 cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
                              int64_t min_len, int64_t n_len, int k, int tile, int32_t *lo, int32_t *hi,
                              int64_t *tile_start, int32_t *work);
@@ -125,6 +126,7 @@ struct blg_search {
         uint64_t *peq;
         int32_t *lo, *hi, *work;   // survivor plan (thresholded runs)
         int64_t *tile_start;
+        std::vector<int32_t> h_qlen;   // host copy of qlen
     };
     std::vector<Cls> cls;
     // choices sorted by length (thresholded runs): cs = sorted copy,
@@ -135,10 +137,11 @@ struct blg_search {
     int32_t *perm = nullptr;
     int64_t *lstart = nullptr;
     int64_t min_len = 0, n_len = 0;
-    // choices in tile-transposed form (exact and unsorted runs), when the
-    // padding to each tile's longest choice stays small
+    std::vector<int64_t> h_lstart;   // host copy of lstart
     // 4-gram sketches: of the length-sorted choices and of the queries
     uint64_t *csk = nullptr, *qsk = nullptr;
+    // choices in tile-transposed form (exact and unsorted runs), when the
+    // padding to each tile's longest choice stays small
     bool tt = false;
     uint32_t *tt_words = nullptr;
     int64_t *tt_base = nullptr;
@@ -401,7 +404,7 @@ static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, const DevStrings &A, co
     for (int j = 1; j < kPairClasses; j++) any_long |= p->pcap[j] > 0;
     if (band)
         CK(launch(c, "pairs_band", [&] {
-               return launch_solve_band(c->stream, c->sms, plan, k, dtype, d_out, exit_log);
+               return launch_solve_band(c->stream, c->sms, c->tune.band_ctas, plan, k, dtype, d_out, exit_log);
            }), "pairs_band");
     else
         CK(launch(c, "pairs_solve", [&] {
@@ -601,6 +604,7 @@ static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64
         k.nq = (int)idx[slot].size();
         s->cls.push_back(k);
         blg_search::Cls &kk = s->cls.back();
+        kk.h_qlen = len[slot];
         CK(dev_alloc(c, (void **)&kk.qidx, sizeof(int32_t) * kk.nq), "cudaMallocAsync(qidx)");
         CK(dev_alloc(c, (void **)&kk.qlen, sizeof(int32_t) * kk.nq), "cudaMallocAsync(qlen)");
         CK(dev_alloc(c, (void **)&kk.peq, sizeof(uint64_t) * 256 * (size_t)kk.nw * kk.nq), "cudaMallocAsync(peq)");
@@ -650,6 +654,7 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
             CK(cudaMemcpyAsync(s->perm, perm.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice, c->stream), "H2D perm");
             CK(dev_alloc(c, (void **)&s->lstart, sizeof(int64_t) * (n_len + 1)), "cudaMallocAsync(lstart)");
             CK(cudaMemcpyAsync(s->lstart, lstart.data(), sizeof(int64_t) * (n_len + 1), cudaMemcpyHostToDevice, c->stream), "H2D lstart");
+            s->h_lstart = lstart;
             cs.d.buf = (uint8_t *)cs.mem_buf + 16;
             cs.d.off = (const int64_t *)cs.mem_off;
             cs.d.n = nc;
@@ -761,12 +766,15 @@ static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64
     return rc;
 }
 
-static int pick_qpb(blg_ctx *c, int nq_cls, int64_t nc) {
+// Queries per CTA of the exact search: the autotuned value for this word
+// count, else enough CTAs for 8 per SM, capped at 16.
+static int pick_qpb(blg_ctx *c, int nw, int nq_cls, int64_t nc) {
     const int64_t tiles = (nc + 1023) / 1024;
     const int64_t target = (int64_t)c->sms * 8;
     int64_t qpb = (int64_t)nq_cls * tiles / target;
     if (qpb < 1) qpb = 1;
     if (qpb > 16) qpb = 16;
+    if (nw >= 1 && nw <= 8 && c->tune.qpb[nw] > 0) qpb = std::min<int64_t>(c->tune.qpb[nw], std::max(1, nq_cls));
     const int64_t min_qpb = ((int64_t)nq_cls + 65534) / 65535;   // grid.y limit
     if (qpb < min_qpb) qpb = min_qpb;
     return (int)qpb;
@@ -774,6 +782,25 @@ static int pick_qpb(blg_ctx *c, int nq_cls, int64_t nc) {
 
 // Launch the current classes' kernels; the max_dist fill covers rows [q0, q1)
 // (all rows by default: the classes hold every query).
+// Survivors per job of the thresholded search for one class: the tuned size,
+// halved (down to 1024) while the class would have fewer than 4 jobs per CTA
+// of the persistent grid, so small searches still spread over the GPU. The
+// survivor count comes from the host copies of the length histogram.
+static int survivor_job_size(blg_ctx *c, const blg_search *s, const blg_search::Cls &k_, int k) {
+    int64_t total = 0;
+    const int64_t nl = s->n_len;
+    for (int32_t m : k_.h_qlen) {
+        int64_t a = m - k - s->min_len, b = m + k - s->min_len + 1;
+        a = std::max<int64_t>(0, std::min(a, nl));
+        b = std::max<int64_t>(0, std::min(b, nl));
+        if (b > a) total += s->h_lstart[b] - s->h_lstart[a];
+    }
+    const int64_t ctas = (int64_t)c->sms * c->tune.lpt_ctas;
+    int job = c->tune.lpt_job;
+    while (job > 1024 && total < 4 * ctas * (int64_t)job) job >>= 1;
+    return job;
+}
+
 static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, int64_t q0, int64_t q1) {
     if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
     if (s->nq == 0 || s->nc == 0) return BLG_OK;
@@ -798,8 +825,9 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
         if (surv && !k_.lanes) {
             // max_dist <= 31: jobs of 4096 survivors ordered by predicted cost
             const bool lpt = k <= 31;
+            const int job = lpt ? survivor_job_size(c, s, k_, k) : 1024;
             CK(launch(c, "surv_plan", [&] {
-                   return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, k, lpt ? 4096 : 1024,
+                   return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, k, job,
                                            k_.lo, k_.hi, k_.tile_start, k_.work);
                }), "surv_plan");
             if (lpt) {
@@ -810,7 +838,8 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
                        "sched_keytab");
                 }
                 CK(launch(c, "search_lpt", [&] {
-                       return launch_search_lpt(c->stream, c->sms, k_.nw, s->cs.d, s->perm, s->csk, s->qsk, sc, k_.lo,
+                       return launch_search_lpt(c->stream, c->sms, c->tune.lpt_ctas, job, k_.nw, s->cs.d,
+                                                s->perm, s->csk, s->qsk, sc, k_.lo,
                                                 k_.hi, k_.tile_start, k_.work, keytab, k, dtype, d_out, s->nc, nullptr,
                                                 c->d_status);
                    }), "search_lpt");
@@ -829,7 +858,7 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
                                               c->d_status);
                }), "search_lanes");
         } else {
-            const int qpb = pick_qpb(c, k_.nq, s->nc);
+            const int qpb = pick_qpb(c, k_.nw, k_.nq, s->nc);
             if (s->tt) {
                 const TransposedChoices T{s->tt_words, s->tt_base, s->tt_len, s->nc};
                 CK(launch(c, "search_tt", [&] {
@@ -950,7 +979,7 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
             j.k = k;
             j.dtype = p.dtype;
             j.nw = cl.nw;
-            j.tile = (k >= 0 && k <= 31) ? 4096 : 1024;
+            j.tile = (k >= 0 && k <= 31) ? 4096 : 1024;   // longest-first jobs of the banded kernel
             j.csk = s->csk;
             j.qsk = s->qsk;
             j.out = p.d_out;
@@ -1021,6 +1050,224 @@ static int batch_run(blg_ctx *c, blg_batch *b) {
     CK(launch(c, "batch_graph", [&] { return cudaGraphLaunch(b->exec, c->stream); }), "graph launch");
     c->launches += b->graph_kernels - 1;
     return BLG_OK;
+}
+
+// ============================================================ autotuner ==
+// Launch shapes are timed on synthetic inputs of each bucket (random DNA,
+// fixed seed) and the fastest kept per device:
+//   exact search:        queries per CTA, for queries of 1, 2 and 4 words
+//                        (1024 queries x 65536 choices of the same length);
+//   thresholded search:  CTAs per SM x largest survivors per job (128 queries
+//                        x 262144 choices, lengths 100..256, 5% planted
+//                        near-copies, max_dist 4);
+//   banded pairs solver: CTAs per SM (2^19 pairs, lengths 8..256, edit rates
+//                        0..30%, max_dist 8).
+// Results never depend on a shape; only time does.
+namespace {
+
+struct Rng {
+    uint64_t s;
+    uint32_t next() {
+        s ^= s << 13;
+        s ^= s >> 7;
+        s ^= s << 17;
+        return (uint32_t)(s >> 16);
+    }
+    double uni() { return (next() & 0xffffff) / 16777216.0; }
+};
+
+struct Packed {
+    std::vector<uint8_t> buf;
+    std::vector<int64_t> off{0};
+    void add(const std::vector<uint8_t> &x) {
+        buf.insert(buf.end(), x.begin(), x.end());
+        off.push_back((int64_t)buf.size());
+    }
+    int64_t n() const { return (int64_t)off.size() - 1; }
+    const uint8_t *data() const { return buf.empty() ? nullptr : buf.data(); }
+};
+
+std::vector<uint8_t> dna(Rng &r, int len) {
+    static const uint8_t A[4] = {'A', 'C', 'G', 'T'};
+    std::vector<uint8_t> x(len);
+    for (auto &ch : x) ch = A[r.next() & 3];
+    return x;
+}
+
+std::vector<uint8_t> mutate(Rng &r, const std::vector<uint8_t> &a, double rate) {
+    static const uint8_t A[4] = {'A', 'C', 'G', 'T'};
+    std::vector<uint8_t> b;
+    for (uint8_t ch : a) {
+        if (r.uni() < rate) {
+            const uint32_t op = r.next() % 3;
+            if (op == 0) b.push_back(A[r.next() & 3]);                 // substitute
+            else if (op == 1) { b.push_back(A[r.next() & 3]); b.push_back(ch); }   // insert before
+            continue;                                                   // delete (op 2) or done
+        }
+        b.push_back(ch);
+    }
+    return b;
+}
+
+}  // namespace
+
+// Event time (ms) of the fastest of `reps` runs of `fn` on the context stream.
+template <typename F>
+static int time_best(blg_ctx *c, int reps, F &&fn, float *best) {
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    int rc = fn();                                      // warm-up
+    *best = 1e30f;
+    for (int r = 0; r < reps && !rc; r++) {
+        cudaEventRecord(e0, c->stream);
+        rc = fn();
+        cudaEventRecord(e1, c->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(c, BLG_ERR_CUDA, "timing");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        *best = std::min(*best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!rc) rc = sync_and_status(c);
+    return rc;
+}
+
+static int tune_exact_search(blg_ctx *c, int nw) {
+    Rng r{0x9E3779B97F4A7C15ull ^ (uint64_t)nw};
+    Packed q, ch;
+    const int len = 64 * nw;
+    for (int i = 0; i < 1024; i++) q.add(dna(r, len));
+    for (int i = 0; i < 65536; i++) ch.add(dna(r, len));
+    blg_search s;
+    int rc = search_upload(c, q.data(), q.off.data(), q.n(), ch.data(), ch.off.data(), ch.n(), &s);
+    void *out = nullptr;
+    if (!rc && dev_alloc(c, &out, sizeof(int32_t) * (size_t)q.n() * ch.n()) != cudaSuccess)
+        rc = fail(c, BLG_ERR_ALLOC, "tuning output");
+    float best_ms = 1e30f;
+    int best = 0;
+    for (int qpb : {4, 8, 16, 32, 64}) {
+        if (rc) break;
+        c->tune.qpb[nw] = qpb;
+        float ms = 0.f;
+        rc = time_best(c, 3, [&] { return search_run(c, &s, -1, BLG_INT32, out); }, &ms);
+        if (!rc && ms < best_ms) { best_ms = ms; best = qpb; }
+    }
+    c->tune.qpb[nw] = rc ? 0 : best;
+    dev_free(c, out);
+    search_release(c, &s);
+    return rc;
+}
+
+static int tune_threshold_search(blg_ctx *c) {
+    Rng r{0x2545F4914F6CDD1Dull};
+    Packed q, ch;
+    std::vector<std::vector<uint8_t>> qs;
+    for (int i = 0; i < 128; i++) {
+        qs.push_back(dna(r, 100 + (int)(r.next() % 157)));
+        q.add(qs.back());
+    }
+    for (int i = 0; i < 262144; i++) {
+        if (r.uni() < 0.05) ch.add(mutate(r, qs[r.next() % qs.size()], 0.05 * r.uni()));
+        else ch.add(dna(r, 100 + (int)(r.next() % 157)));
+    }
+    blg_search s;
+    int rc = search_upload(c, q.data(), q.off.data(), q.n(), ch.data(), ch.off.data(), ch.n(), &s);
+    void *out = nullptr;
+    if (!rc && dev_alloc(c, &out, (size_t)q.n() * ch.n()) != cudaSuccess) rc = fail(c, BLG_ERR_ALLOC, "tuning output");
+    float best_ms = 1e30f;
+    int best_ctas = c->tune.lpt_ctas, best_job = c->tune.lpt_job;
+    for (int ctas : {2, 3, 4}) {
+        for (int job : {2048, 4096}) {
+            if (rc) break;
+            c->tune.lpt_ctas = ctas;
+            c->tune.lpt_job = job;
+            float ms = 0.f;
+            rc = time_best(c, 3, [&] { return search_run(c, &s, 4, BLG_UINT8, out); }, &ms);
+            if (!rc && ms < best_ms) { best_ms = ms; best_ctas = ctas; best_job = job; }
+        }
+    }
+    c->tune.lpt_ctas = best_ctas;
+    c->tune.lpt_job = best_job;
+    dev_free(c, out);
+    search_release(c, &s);
+    return rc;
+}
+
+static int tune_band_pairs(blg_ctx *c) {
+    Rng r{0xD1B54A32D192ED03ull};
+    Packed a, b;
+    for (int i = 0; i < (1 << 19); i++) {
+        std::vector<uint8_t> x = dna(r, 8 + (int)(r.next() % 249));
+        b.add(mutate(r, x, 0.3 * r.uni()));
+        a.add(x);
+    }
+    blg_pairs p;
+    int rc = pairs_upload(c, a.data(), a.off.data(), b.data(), b.off.data(), a.n(), &p);
+    void *out = nullptr;
+    if (!rc && dev_alloc(c, &out, (size_t)a.n()) != cudaSuccess) rc = fail(c, BLG_ERR_ALLOC, "tuning output");
+    const int sched = c->sched;
+    c->sched = BLG_SCHED_AUTO;
+    float best_ms = 1e30f;
+    int best = c->tune.band_ctas;
+    for (int ctas : {3, 4, 5}) {
+        if (rc) break;
+        c->tune.band_ctas = ctas;
+        float ms = 0.f;
+        rc = time_best(c, 3, [&] { return pairs_run(c, &p, 8, BLG_UINT8, out); }, &ms);
+        if (!rc && ms < best_ms) { best_ms = ms; best = ctas; }
+    }
+    c->sched = sched;
+    c->tune.band_ctas = best;
+    dev_free(c, out);
+    pairs_release(c, &p);
+    return rc;
+}
+
+static std::string tuning_header(blg_ctx *c) {
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, c->device);
+    std::string name = prop.name;
+    for (auto &ch : name)
+        if (ch == ' ') ch = '_';
+    return "BLGTUNE1 " + name + " sm" + std::to_string(prop.major * 10 + prop.minor) + " " + std::to_string(c->sms) +
+           " " + std::to_string(blg_version());
+}
+
+static bool tuning_load(blg_ctx *c, const char *path) {
+    FILE *f = fopen(path, "r");
+    if (!f) return false;
+    char line[256];
+    bool ok = fgets(line, sizeof(line), f) && std::string(line) == tuning_header(c) + "\n";
+    blg_tuning t;
+    int fields = 0;
+    while (ok && fgets(line, sizeof(line), f)) {
+        char key[64];
+        int v = 0;
+        if (sscanf(line, "%63s %d", key, &v) != 2) continue;
+        const std::string k = key;
+        if (k.rfind("qpb", 0) == 0) {
+            const int w = atoi(k.c_str() + 3);
+            if (w >= 1 && w <= 8 && v >= 0 && v <= 4096) { t.qpb[w] = v; fields++; }
+        } else if (k == "lpt_ctas" && v >= 1 && v <= 8) { t.lpt_ctas = v; fields++; }
+        else if (k == "lpt_job" && v >= 256 && v <= 4096) { t.lpt_job = v; fields++; }
+        else if (k == "band_ctas" && v >= 1 && v <= 5) { t.band_ctas = v; fields++; }
+    }
+    fclose(f);
+    if (!ok || fields < 11) return false;
+    t.tuned = 2;                                        // loaded from the cache
+    c->tune = t;
+    return true;
+}
+
+static void tuning_save(blg_ctx *c, const char *path) {
+    FILE *f = fopen(path, "w");
+    if (!f) return;
+    fprintf(f, "%s\n", tuning_header(c).c_str());
+    for (int w = 1; w <= 8; w++) fprintf(f, "qpb%d %d\n", w, c->tune.qpb[w]);
+    fprintf(f, "lpt_ctas %d\nlpt_job %d\nband_ctas %d\n", c->tune.lpt_ctas, c->tune.lpt_job, c->tune.band_ctas);
+    fclose(f);
 }
 
 // ============================================================== C-ABI ==
@@ -1216,12 +1463,14 @@ int blg_sched_train_search(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t 
     for (auto &k_ : s->cls) {
         if (k_.lanes) continue;
         SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
+        const int job = survivor_job_size(c, s, k_, max_dist);
         CK(launch(c, "surv_plan", [&] {
-               return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, max_dist, 4096, k_.lo, k_.hi,
+               return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, max_dist, job, k_.lo, k_.hi,
                                        k_.tile_start, k_.work);
            }), "surv_plan");
         CK(launch(c, "search_lpt_logged", [&] {
-               return launch_search_lpt(c->stream, c->sms, k_.nw, s->cs.d, s->perm, s->csk, s->qsk, sc, k_.lo, k_.hi,
+               return launch_search_lpt(c->stream, c->sms, c->tune.lpt_ctas, job, k_.nw, s->cs.d, s->perm,
+                                        s->csk, s->qsk, sc, k_.lo, k_.hi,
                                         k_.tile_start, k_.work, nullptr, max_dist, BLG_UINT8, out, s->nc, &R,
                                         c->d_status);
            }), "search_lpt_logged");
@@ -1474,6 +1723,42 @@ int blg_timer_stop(blg_ctx *c, float *ms) {
 }
 
 int64_t blg_launch_count(const blg_ctx *c) { return c ? c->launches : 0; }
+
+int blg_autotune(blg_ctx *c, const char *cache_path) {
+    ENTER(c);
+    if (cache_path && *cache_path && tuning_load(c, cache_path)) return BLG_OK;
+    const int sched = c->sched;
+    c->sched = BLG_SCHED_AUTO;
+    int rc = BLG_OK;
+    for (int nw : {1, 2, 4})
+        if (!rc) rc = tune_exact_search(c, nw);
+    if (!rc) {
+        // word counts not timed take the nearest timed one
+        c->tune.qpb[3] = c->tune.qpb[4];
+        for (int w = 5; w <= 8; w++) c->tune.qpb[w] = c->tune.qpb[4];
+        rc = tune_threshold_search(c);
+    }
+    if (!rc) rc = tune_band_pairs(c);
+    c->sched = sched;
+    if (rc) {
+        c->tune = blg_tuning();                         // keep the defaults on any failure
+        return rc;
+    }
+    c->tune.tuned = 1;
+    if (cache_path && *cache_path) tuning_save(c, cache_path);
+    return BLG_OK;
+}
+
+int blg_get_tuning(blg_ctx *c, int32_t *values, int n) {
+    ENTER(c);
+    if (!values || n < 12) return fail(c, BLG_ERR_ARG, "need 12 values");
+    for (int w = 1; w <= 8; w++) values[w - 1] = c->tune.qpb[w];
+    values[8] = c->tune.lpt_ctas;
+    values[9] = c->tune.lpt_job;
+    values[10] = c->tune.band_ctas;
+    values[11] = c->tune.tuned;
+    return BLG_OK;
+}
 
 int blg_set_schedule(blg_ctx *c, int mode) {
     ENTER(c);

@@ -173,8 +173,8 @@ __global__ void __launch_bounds__(256) k_batch_lpt(BatchPlan plan, uint32_t *sta
             cur_q = qi;
         }
         const int64_t row = job.cls.qidx[qi];
-        const int64_t s0 = job.lo[qi] + (lt - job.tile_start[qi]) * kSurvJob;
-        const int cnt = (int)min((int64_t)kSurvJob, (int64_t)job.hi[qi] - s0);
+        const int64_t s0 = job.lo[qi] + (lt - job.tile_start[qi]) * job.tile;
+        const int cnt = (int)min((int64_t)job.tile, (int64_t)job.hi[qi] - s0);
         lpt_job(S, job.CS, job.perm, job.csk, job.qsk[row], s_rows, 2 * job.nw + 6, job.cls.qlen[qi], row, s0, cnt,
                 job.k, nullptr, job.dtype, job.out, job.nc, status, u, [](int64_t, int, int) {});
     }

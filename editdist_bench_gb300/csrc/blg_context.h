@@ -9,6 +9,16 @@
 
 struct blg_sched_model;   // the work-order scheduler network (blg_mlp.cu)
 
+// Launch shapes chosen by the autotuner (blg_autotune); the defaults are the
+// hand-picked shapes used before any tuning.
+struct blg_tuning {
+    int qpb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};   // exact search: queries per CTA by query words (0: heuristic)
+    int lpt_ctas = 4;                            // thresholded search: CTAs per SM
+    int lpt_job = 4096;                          // thresholded search: survivors per job
+    int band_ctas = 5;                           // banded pairs solver: CTAs per SM
+    int tuned = 0;
+};
+
 struct blg_ctx {
     struct ProfRec {
         const char *name;
@@ -27,6 +37,7 @@ struct blg_ctx {
     int sched = 0;                     // BLG_SCHED_* (work order of thresholded runs)
     blg_sched_model *model = nullptr;  // trained/loaded scheduler network, if any
     bool no_band = false;              // force the full-word loops even for max_dist <= 31
+    blg_tuning tune;                   // launch shapes (autotuned or defaults)
     bool prof = false;
     std::vector<ProfRec> prof_recs;
     std::map<std::string, std::pair<int64_t, double>> prof_acc;

@@ -305,11 +305,12 @@ cudaError_t launch_order(cudaStream_t st, int sms, const PairsPlan &plan) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_solve_band(cudaStream_t st, int sms, const PairsPlan &plan, int k, int dtype, void *out,
-                              int32_t *exit_log) {
-    // 40 KB of ring tables per CTA: five CTAs per SM
-    if (exit_log) k_solve_band<true><<<sms * 5, 256, 0, st>>>(plan, k, dtype, out, exit_log, 1u);
-    else k_solve_band<false><<<sms * 5, 256, 0, st>>>(plan, k, dtype, out, nullptr, 1u);
+cudaError_t launch_solve_band(cudaStream_t st, int sms, int ctas_per_sm, const PairsPlan &plan, int k, int dtype,
+                              void *out, int32_t *exit_log) {
+    // 40 KB of ring tables per CTA: at most five CTAs per SM
+    const int grid = sms * (ctas_per_sm < 1 ? 1 : (ctas_per_sm > 5 ? 5 : ctas_per_sm));
+    if (exit_log) k_solve_band<true><<<grid, 256, 0, st>>>(plan, k, dtype, out, exit_log, 1u);
+    else k_solve_band<false><<<grid, 256, 0, st>>>(plan, k, dtype, out, nullptr, 1u);
     return cudaGetLastError();
 }
 

@@ -20,6 +20,7 @@ resident ``PairsBatch``/``SearchBatch`` mirror the reference benchmark's
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -233,6 +234,25 @@ def cdist_batch(problems, return_device: bool = True):
 
 _SCHEDULES = {"auto": _lib.SCHED_AUTO, "plain": _lib.SCHED_PLAIN, "learned": _lib.SCHED_LEARNED,
               "lensort": _lib.SCHED_LENSORT}
+
+
+def autotune(cache_path=None) -> dict:
+    """Time candidate launch shapes on this GPU and keep the fastest for the
+    process's context (see blg_autotune); with ``cache_path`` a cache for the
+    same device and library version is reused, a fresh result written."""
+    ctx = _lib.context()
+    ctx.check(ctx.lib.blg_autotune(ctx.h, None if cache_path is None else os.fsencode(cache_path)), "autotune")
+    return tuning()
+
+
+def tuning() -> dict:
+    """The context's current launch shapes."""
+    ctx = _lib.context()
+    v = (ctypes.c_int32 * 12)()
+    ctx.check(ctx.lib.blg_get_tuning(ctx.h, v, 12), "get_tuning")
+    return {"search_queries_per_cta": {w + 1: int(v[w]) for w in range(8)}, "survivor_ctas_per_sm": int(v[8]),
+            "survivors_per_job": int(v[9]), "band_ctas_per_sm": int(v[10]),
+            "source": {0: "defaults", 1: "timed", 2: "cache"}[int(v[11])]}
 
 
 def set_schedule(name: str):
