@@ -674,7 +674,8 @@ def run_reference(args, ranks: Ranks):
         "impl": "reference", "metric": "pairs/s", "value": value, "unit": "pairs/s", "n_gpus": ranks.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": f"config {cfg}", "sample": sample},
+        "config": {"workload": (f"{w.name} cdist {w.nq}x{w.nc}" if isinstance(w, W.SearchWork)
+                                else f"{w.name} pairwise {w.n}"), "sample": sample},
         "gcups": cells / s / 1e9,
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
                          "sample": sample},
