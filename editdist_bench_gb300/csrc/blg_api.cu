@@ -45,8 +45,9 @@ cudaError_t launch_pairs_long(cudaStream_t st, int grid, bool hask, const LongQu
 cudaError_t launch_pairs_staged(cudaStream_t st, int sms, bool hask, const DevStrings &A, const DevStrings &B,
                                 int k, int dtype, void *out, const LongQueue &q, uint32_t *status);
 cudaError_t launch_fill(cudaStream_t st, int sms, void *out, int64_t n, int dtype, uint32_t v);
-cudaError_t launch_pairs_tile(cudaStream_t st, int sms, bool hask, const DevStrings &A, const DevStrings &B,
-                              int tile_pairs, int k, int dtype, void *out, const LongQueue &q, uint32_t *status);
+cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, const DevStrings &A,
+                              const DevStrings &B, int tile_pairs, int k, int dtype, void *out, const LongQueue &q,
+                              uint32_t *status);
 cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, bool band, const DevStrings &A,
                               const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
                               uint32_t *status);
@@ -442,7 +443,8 @@ static int pairs_run_direct(blg_ctx *c, blg_pairs *p, const DevStrings &A, const
         const double avg = (double)p->len_max_side / (double)p->n;
         const int tile = avg <= 33.0 ? 512 : std::max(32, (int)(17000.0 / avg) & ~31);
         CK(launch(c, "pairs_tile", [&] {
-               return launch_pairs_tile(c->stream, c->sms, hask, A, B, tile, k, dtype, d_out, q, c->d_status);
+               return launch_pairs_tile(c->stream, c->sms, c->tune.tile_buffers, hask, A, B, tile, k, dtype, d_out, q,
+                                        c->d_status);
            }), "pairs_tile");
     } else {
         CK(launch(c, "pairs_staged", [&] {
@@ -1061,7 +1063,9 @@ static int batch_run(blg_ctx *c, blg_batch *b) {
 //                        x 262144 choices, lengths 100..256, 5% planted
 //                        near-copies, max_dist 4);
 //   banded pairs solver: CTAs per SM (2^19 pairs, lengths 8..256, edit rates
-//                        0..30%, max_dist 8).
+//                        0..30%, max_dist 8);
+//   short-pair tiles:    one or two stage buffers (2^20 pairs of 32 bytes, 5%
+//                        edits, exact).
 // Results never depend on a shape; only time does.
 namespace {
 
@@ -1225,6 +1229,33 @@ static int tune_band_pairs(blg_ctx *c) {
     return rc;
 }
 
+static int tune_tile_pairs(blg_ctx *c) {
+    Rng r{0x5DEECE66Dull};
+    Packed a, b;
+    for (int i = 0; i < (1 << 20); i++) {
+        std::vector<uint8_t> x = dna(r, 32);
+        b.add(mutate(r, x, 0.05));
+        a.add(x);
+    }
+    blg_pairs p;
+    int rc = pairs_upload(c, a.data(), a.off.data(), b.data(), b.off.data(), a.n(), &p);
+    void *out = nullptr;
+    if (!rc && dev_alloc(c, &out, sizeof(int32_t) * (size_t)a.n()) != cudaSuccess) rc = fail(c, BLG_ERR_ALLOC, "tuning output");
+    float best_ms = 1e30f;
+    int best = c->tune.tile_buffers;
+    for (int bufs : {1, 2}) {
+        if (rc) break;
+        c->tune.tile_buffers = bufs;
+        float ms = 0.f;
+        rc = time_best(c, 5, [&] { return pairs_run(c, &p, -1, BLG_INT32, out); }, &ms);
+        if (!rc && ms < best_ms) { best_ms = ms; best = bufs; }
+    }
+    c->tune.tile_buffers = best;
+    dev_free(c, out);
+    pairs_release(c, &p);
+    return rc;
+}
+
 static std::string tuning_header(blg_ctx *c) {
     cudaDeviceProp prop{};
     cudaGetDeviceProperties(&prop, c->device);
@@ -1253,9 +1284,10 @@ static bool tuning_load(blg_ctx *c, const char *path) {
         } else if (k == "lpt_ctas" && v >= 1 && v <= 8) { t.lpt_ctas = v; fields++; }
         else if (k == "lpt_job" && v >= 256 && v <= 4096) { t.lpt_job = v; fields++; }
         else if (k == "band_ctas" && v >= 1 && v <= 5) { t.band_ctas = v; fields++; }
+        else if (k == "tile_buffers" && v >= 1 && v <= 2) { t.tile_buffers = v; fields++; }
     }
     fclose(f);
-    if (!ok || fields < 11) return false;
+    if (!ok || fields < 12) return false;
     t.tuned = 2;                                        // loaded from the cache
     c->tune = t;
     return true;
@@ -1266,7 +1298,8 @@ static void tuning_save(blg_ctx *c, const char *path) {
     if (!f) return;
     fprintf(f, "%s\n", tuning_header(c).c_str());
     for (int w = 1; w <= 8; w++) fprintf(f, "qpb%d %d\n", w, c->tune.qpb[w]);
-    fprintf(f, "lpt_ctas %d\nlpt_job %d\nband_ctas %d\n", c->tune.lpt_ctas, c->tune.lpt_job, c->tune.band_ctas);
+    fprintf(f, "lpt_ctas %d\nlpt_job %d\nband_ctas %d\ntile_buffers %d\n", c->tune.lpt_ctas, c->tune.lpt_job,
+            c->tune.band_ctas, c->tune.tile_buffers);
     fclose(f);
 }
 
@@ -1739,6 +1772,7 @@ int blg_autotune(blg_ctx *c, const char *cache_path) {
         rc = tune_threshold_search(c);
     }
     if (!rc) rc = tune_band_pairs(c);
+    if (!rc) rc = tune_tile_pairs(c);
     c->sched = sched;
     if (rc) {
         c->tune = blg_tuning();                         // keep the defaults on any failure
@@ -1751,12 +1785,13 @@ int blg_autotune(blg_ctx *c, const char *cache_path) {
 
 int blg_get_tuning(blg_ctx *c, int32_t *values, int n) {
     ENTER(c);
-    if (!values || n < 12) return fail(c, BLG_ERR_ARG, "need 12 values");
+    if (!values || n < 13) return fail(c, BLG_ERR_ARG, "need 13 values");
     for (int w = 1; w <= 8; w++) values[w - 1] = c->tune.qpb[w];
     values[8] = c->tune.lpt_ctas;
     values[9] = c->tune.lpt_job;
     values[10] = c->tune.band_ctas;
     values[11] = c->tune.tuned;
+    values[12] = c->tune.tile_buffers;
     return BLG_OK;
 }
 

@@ -37,8 +37,12 @@ constexpr int kTileSide = kTileCap + 48;         // 16 bytes of slack before, 32
 constexpr int kTileKeys = 64;                    // counting-sort keys: min(columns, 63)
 constexpr int32_t kNoStore = INT32_MIN;          // result slot filled by the long-pair consumer
 
+// NBUF = 2: the next tile's copy flies while this one computes (2 CTAs per
+// SM); NBUF = 1: one stage, the copy is issued when the tile is done and the
+// other CTAs of the SM (3 per SM) compute meanwhile.
+template <int NBUF>
 struct __align__(16) TileShared {
-    uint8_t stage[2][2][kTileSide];               // [buffer][a|b]
+    uint8_t stage[NBUF][2][kTileSide];            // [buffer][a|b]
     uint32_t tab[32 * kTileThreads];              // nibble tables, row r of thread t at [r*256 + t]
     uint2 ent[kTileMaxPairs];                     // sorted work list
     int32_t res[kTileMaxPairs];
@@ -46,7 +50,7 @@ struct __align__(16) TileShared {
     int32_t start[kTileKeys];
     int64_t span_lo[2][2], span_hi[2][2];         // staged span [lo, hi) per buffer/side, lo < 0: none
     uint64_t bar[2];
-    int32_t total;
+    int32_t total, next;
 };
 
 // One 32-bit Myers/Hyyro column step on the top word (carry-in +1), with
@@ -94,6 +98,115 @@ __device__ __forceinline__ uint32_t nib32_eq(const uint32_t *tc, uint32_t c) {
     return tc[(c >> 4) * kTileThreads] & tc[(16 + (c & 15)) * kTileThreads];
 }
 
+// ---- strings in the stage, addressed by byte offset from its 16-byte-aligned
+// base: the alignment comes from the offset, so the pointers never pass
+// through an integer and stay shared-memory addresses (32-bit loads).
+__device__ __forceinline__ uint32_t st_load4(const uint8_t *base, uint32_t off) {
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(base + (off & ~3u));
+    return __funnelshift_r(w[0], w[1], (off & 3u) * 8u);
+}
+
+struct StageScan {
+    const uint32_t *w;
+    uint32_t lo, hi, sh;
+    __device__ __forceinline__ void init(const uint8_t *base, uint32_t off) {
+        w = reinterpret_cast<const uint32_t *>(base + (off & ~3u));
+        sh = (off & 3u) * 8u;
+        lo = w[0];
+        hi = w[1];
+        w += 2;
+    }
+    __device__ __forceinline__ uint32_t next4() {
+        const uint32_t r = __funnelshift_r(lo, hi, sh);
+        lo = hi;
+        hi = *w++;
+        return r;
+    }
+};
+
+// Exact prefix/suffix trimming of staged strings a (offset oa, length la) and
+// b (ob, lb), 4-byte windows (csrc/myers.c:80-87).
+__device__ __forceinline__ void stage_trim(const uint8_t *base, uint32_t &oa, int &la, uint32_t &ob, int &lb) {
+    const int lim = la < lb ? la : lb;
+    int p = 0;
+    while (p < lim) {
+        const uint32_t x = st_load4(base, oa + p) ^ st_load4(base, ob + p);
+        int q = x ? (__ffs(x) - 1) >> 3 : 4;
+        if (q > lim - p) q = lim - p;
+        p += q;
+        if (q < 4) break;
+    }
+    const int lim2 = lim - p;
+    int s = 0;
+    while (s < lim2) {
+        const uint32_t x = st_load4(base, oa + la - s - 4) ^ st_load4(base, ob + lb - s - 4);
+        int q = x ? __clz(x) >> 3 : 4;
+        if (q > lim2 - s) q = lim2 - s;
+        s += q;
+        if (q < 4) break;
+    }
+    oa += p;
+    ob += p;
+    la -= p + s;
+    lb -= p + s;
+}
+
+// Nibble tables of a staged pattern (set or clear its rows).
+__device__ __forceinline__ void stage_nib(uint32_t *tc, const uint8_t *base, uint32_t op, int m, bool set) {
+    StageScan ps;
+    ps.init(base, op);
+    for (int i = 0; i < m; i += 4) {
+        const uint32_t w4 = ps.next4();
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            if (i + b < m) {
+                const uint32_t c = (w4 >> (8 * b)) & 0xffu;
+                uint32_t *h = tc + (c >> 4) * kTileThreads, *l = tc + (16 + (c & 15)) * kTileThreads;
+                if (set) {
+                    const uint32_t bit = 1u << (i + b);
+                    *h |= bit;
+                    *l |= bit;
+                } else {
+                    *h = 0;
+                    *l = 0;
+                }
+            }
+        }
+    }
+}
+
+// solve32 for a staged pair (pattern at op, text at ot).
+template <bool HASK>
+__device__ __forceinline__ int stage_solve32(uint32_t *tc, const uint8_t *base, uint32_t op, int m, uint32_t ot,
+                                             int n, int k, Units u) {
+    stage_nib(tc, base, op, m, true);
+    const uint32_t M = m >= 32 ? 0xffffffffu : ((1u << m) - 1u);
+    uint32_t pv = 0xffffffffu, mv = 0;
+    StageScan ts;
+    ts.init(base, ot);
+    bool dead = false;
+    int j = 0;
+    for (; j + 4 <= n; j += 4) {
+        const uint32_t w4 = ts.next4();
+        step32(pv, mv, nib32_eq(tc, w4 & 0xffu), u);
+        step32(pv, mv, nib32_eq(tc, (w4 >> 8) & 0xffu), u);
+        step32(pv, mv, nib32_eq(tc, (w4 >> 16) & 0xffu), u);
+        step32(pv, mv, nib32_eq(tc, w4 >> 24), u);
+        if (HASK && hopeless(j + 4 + popc32(pv & M) - popc32(mv & M), j + 3, n, k)) {
+            dead = true;
+            break;
+        }
+    }
+    if (!dead && j < n) {
+        uint32_t w4 = ts.next4();
+        for (; j < n; j++, w4 >>= 8) step32(pv, mv, nib32_eq(tc, w4 & 0xffu), u);
+    }
+    stage_nib(tc, base, op, m, false);
+    if (dead) return k + 1;
+    const int d = n + popc32(pv & M) - popc32(mv & M);
+    return HASK ? cap_k(d, k) : d;
+}
+
 // d(p, t) for 1 <= m <= 32, m <= n; min(d, k+1) when HASK.
 template <bool HASK, typename L>
 __device__ __forceinline__ int solve32(uint32_t *tc, const uint8_t *p, int m, const uint8_t *t, int n, int k,
@@ -131,7 +244,8 @@ __device__ __forceinline__ int solve32(uint32_t *tc, const uint8_t *p, int m, co
 // Thread 0: the rounded spans of a tile's strings, one bulk copy per side
 // into `buf`, completing on bar[buf]. (a0, a1) and (b0, b1) are the string
 // offsets bounding the tile, off[t0] and off[t0 + cnt], of each side.
-__device__ __forceinline__ void tile_issue(TileShared &S, int buf, const DevStrings &A, const DevStrings &B,
+template <typename TS>
+__device__ __forceinline__ void tile_issue(TS &S, int buf, const DevStrings &A, const DevStrings &B,
                                            int64_t a0, int64_t a1, int64_t b0, int64_t b1) {
     auto span = [&](const DevStrings &D, int64_t o0, int64_t o1, int side) -> uint32_t {
         const int64_t lo = o0 - D.base, hi = o1 - D.base;
@@ -177,12 +291,12 @@ __device__ __forceinline__ void load_offs(PairOffs &o, const DevStrings &A, cons
     }
 }
 
-template <bool HASK>
-__global__ void __launch_bounds__(kTileThreads, 2)
+template <bool HASK, int NBUF>
+__global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : 3)
     k_pairs_tile(DevStrings A, DevStrings B, int P, int k, int dtype, void *out, LongQueue q, uint32_t *status,
                  uint32_t unit) {
     extern __shared__ __align__(128) uint8_t s_raw[];
-    TileShared &S = *reinterpret_cast<TileShared *>(s_raw);
+    TileShared<NBUF> &S = *reinterpret_cast<TileShared<NBUF> *>(s_raw);
     const Units u{unit, unit + unit};
     const int tid = threadIdx.x;
     const int64_t n = A.n;
@@ -223,21 +337,22 @@ __global__ void __launch_bounds__(kTileThreads, 2)
 
     int it = 0;
     for (int64_t t = first; t < ntiles; t += G, it++) {
-        const int buf = it & 1;
+        const int buf = NBUF == 2 ? (it & 1) : 0;
+        const uint32_t parity = NBUF == 2 ? ((uint32_t)(it >> 1) & 1u) : ((uint32_t)it & 1u);
         const int64_t t0 = t * P;
         const int cnt = (int)(n - t0 < P ? n - t0 : P);
-        if (tid == 0 && t + G < ntiles) {                 // prefetch the next tile's strings
+        if (NBUF == 2 && tid == 0 && t + G < ntiles) {    // prefetch the next tile's strings
             tile_issue(S, buf ^ 1, A, B, nb.a0, nb.a1, nb.b0, nb.b1);
             if (t + 2 * G < ntiles) tile_bounds(t + 2 * G, nb);
         }
-        const bool ok = mbar_wait(&S.bar[buf], (uint32_t)(it >> 1) & 1u);
+        const bool ok = mbar_wait(&S.bar[buf], parity);
         if (__syncthreads_or(!ok)) {
             // a copy did not complete in time: report, wait (bounded) for the
             // copies still in flight, and stop
             if (tid == 0) {
                 atomicOr(status, ST_QUEUE_TIMEOUT);
-                mbar_wait(&S.bar[buf], (uint32_t)(it >> 1) & 1u);
-                if (t + G < ntiles) mbar_wait(&S.bar[buf ^ 1], (uint32_t)((it + 1) >> 1) & 1u);
+                mbar_wait(&S.bar[buf], parity);
+                if (NBUF == 2 && t + G < ntiles) mbar_wait(&S.bar[buf ^ 1], (uint32_t)((it + 1) >> 1) & 1u);
             }
             return;
         }
@@ -256,15 +371,29 @@ __global__ void __launch_bounds__(kTileThreads, 2)
             const int64_t ra = ga - A.buf, rb = gb - B.buf;
             const bool sa = alo >= 0 && ra >= alo && ra + la <= ahi;
             const bool sb = blo >= 0 && rb >= blo && rb + lb <= bhi;
-            const uint8_t *a = sa ? stage + 16 + (ra - alo) : ga;
-            const uint8_t *b = sb ? stage + kTileSide + 16 + (rb - blo) : gb;
-            const uint8_t *a_start = a;
-            trim_windows<GenericLoad>(a, la, b, lb);
-            const int64_t pre = a - a_start;
+            const uint8_t *a, *b;
+            int64_t pre;
+            uint32_t oa = 0, ob = 0;
+            if (sa && sb) {                                 // both staged: 32-bit shared offsets
+                oa = 16 + (uint32_t)(ra - alo);
+                ob = kTileSide + 16 + (uint32_t)(rb - blo);
+                const uint32_t oa0 = oa;
+                stage_trim(stage, oa, la, ob, lb);
+                pre = oa - oa0;
+                a = stage + oa;
+                b = stage + ob;
+            } else {
+                a = sa ? stage + 16 + (ra - alo) : ga;
+                b = sb ? stage + kTileSide + 16 + (rb - blo) : gb;
+                const uint8_t *a_start = a;
+                trim_windows<GenericLoad>(a, la, b, lb);
+                pre = a - a_start;
+            }
             const uint8_t *gpa = ga + pre, *gpb = gb + pre;
             if (la > lb) {                                  // the shorter string is the pattern
                 const uint8_t *x = a; a = b; b = x;
                 x = gpa; gpa = gpb; gpb = x;
+                const uint32_t z = oa; oa = ob; ob = z;
                 const int y = la; la = lb; lb = y;
             }
             int d = kNoStore;
@@ -288,8 +417,7 @@ __global__ void __launch_bounds__(kTileThreads, 2)
             } else if (sa && sb) {
                 key = lb < kTileKeys - 1 ? lb : kTileKeys - 1;
                 rank = atomicAdd(&S.hist[key], 1);
-                const uint32_t pa = (uint32_t)(a - stage), pb = (uint32_t)(b - stage);
-                ent = make_uint2(pa | (pb << 16), (uint32_t)lb | ((uint32_t)la << 16) | ((uint32_t)j << 22));
+                ent = make_uint2(oa | (ob << 16), (uint32_t)lb | ((uint32_t)la << 16) | ((uint32_t)j << 22));
             } else {
                 d = solve32<HASK, GenericLoad>(tc, a, la, b, lb, k, u);   // not staged: read in place
             }
@@ -315,18 +443,29 @@ __global__ void __launch_bounds__(kTileThreads, 2)
             const int excl = incl - h0 - h1;
             S.start[kTileKeys - 1 - 2 * tid] = excl;
             S.start[kTileKeys - 2 - 2 * tid] = excl + h0;
-            if (tid == 31) S.total = incl;
+            if (tid == 31) {
+                S.total = incl;
+                S.next = 0;
+            }
         }
         __syncthreads();
         if (key0 >= 0) S.ent[S.start[key0] + rank0] = ent0;
         if (key1 >= 0) S.ent[S.start[key1] + rank1] = ent1;
         __syncthreads();
-        // ---- phase 3: solve in sorted order; warps take pairs of equal length
+        // ---- phase 3: solve in sorted order, longest first: warps pull 32-pair
+        //      chunks of the list from a shared counter
         const int total = S.total;
-        for (int e = tid; e < total; e += kTileThreads) {
-            const uint2 E = S.ent[e];
-            const int m = (int)((E.y >> 16) & 63u), nn = (int)(E.y & 0xffffu), j = (int)(E.y >> 22);
-            S.res[j] = solve32<HASK, GenericLoad>(tc, stage + (E.x & 0xffffu), m, stage + (E.x >> 16), nn, k, u);
+        while (true) {
+            int c = 0;
+            if ((tid & 31) == 0) c = atomicAdd(&S.next, 1);
+            c = __shfl_sync(kFull, c, 0);
+            if (c * 32 >= total) break;
+            const int e = c * 32 + (tid & 31);
+            if (e < total) {
+                const uint2 E = S.ent[e];
+                const int m = (int)((E.y >> 16) & 63u), nn = (int)(E.y & 0xffffu), j = (int)(E.y >> 22);
+                S.res[j] = stage_solve32<HASK>(tc, stage, E.x & 0xffffu, m, E.x >> 16, nn, k, u);
+            }
         }
         __syncthreads();
         // ---- phase 4: coalesced stores of the tile's results
@@ -345,30 +484,38 @@ __global__ void __launch_bounds__(kTileThreads, 2)
         }
         if (tid < kTileKeys) S.hist[tid] = 0;
         __syncthreads();                                    // the stage buffer and lists are reused
+        if (NBUF == 1 && tid == 0 && t + G < ntiles) {    // the single stage is free: next tile's copy
+            tile_issue(S, 0, A, B, nb.a0, nb.a1, nb.b0, nb.b1);
+            if (t + 2 * G < ntiles) tile_bounds(t + 2 * G, nb);
+        }
     }
 }
 
 // ------------------------------------------------------------- launcher --
-size_t pairs_tile_smem() { return sizeof(TileShared); }
+template <bool HASK, int NBUF>
+static cudaError_t launch_tile(cudaStream_t st, int sms, const DevStrings &A, const DevStrings &B, int P, int k,
+                               int dtype, void *out, const LongQueue &q, uint32_t *status) {
+    const int64_t ntiles = (A.n + P - 1) / P;
+    const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sms * (NBUF == 2 ? 2 : 3));
+    const size_t smem = sizeof(TileShared<NBUF>);
+    cudaFuncSetAttribute(k_pairs_tile<HASK, NBUF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_pairs_tile<HASK, NBUF><<<grid, kTileThreads, smem, st>>>(A, B, P, k, dtype, out, q, status, 1u);
+    return cudaGetLastError();
+}
 
-cudaError_t launch_pairs_tile(cudaStream_t st, int sms, bool hask, const DevStrings &A, const DevStrings &B,
-                              int tile_pairs, int k, int dtype, void *out, const LongQueue &q, uint32_t *status) {
+cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, const DevStrings &A,
+                              const DevStrings &B, int tile_pairs, int k, int dtype, void *out, const LongQueue &q,
+                              uint32_t *status) {
     if (A.n <= 0) return cudaSuccess;
     int P = tile_pairs;
     if (P > kTileMaxPairs) P = kTileMaxPairs;
     if (P < 32) P = 32;
     P &= ~3;                                                // 4-aligned tiles keep the vector stores aligned
-    const int64_t ntiles = (A.n + P - 1) / P;
-    const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sms * 2);
-    const size_t smem = sizeof(TileShared);
-    if (hask) {
-        cudaFuncSetAttribute(k_pairs_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_pairs_tile<true><<<grid, kTileThreads, smem, st>>>(A, B, P, k, dtype, out, q, status, 1u);
-    } else {
-        cudaFuncSetAttribute(k_pairs_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_pairs_tile<false><<<grid, kTileThreads, smem, st>>>(A, B, P, k, dtype, out, q, status, 1u);
-    }
-    return cudaGetLastError();
+    if (buffers == 1)
+        return hask ? launch_tile<true, 1>(st, sms, A, B, P, k, dtype, out, q, status)
+                    : launch_tile<false, 1>(st, sms, A, B, P, k, dtype, out, q, status);
+    return hask ? launch_tile<true, 2>(st, sms, A, B, P, k, dtype, out, q, status)
+                : launch_tile<false, 2>(st, sms, A, B, P, k, dtype, out, q, status);
 }
 
 }  // namespace blg

@@ -97,3 +97,23 @@ def test_tile_resident_repeat(gpu):
         out = batch.run(batch.alloc(dt), max_dist=k)
         want = exact if k is None else np.minimum(exact, k + 1)
         np.testing.assert_array_equal(out.get(), oracle.saturate(want, dt))
+
+
+def test_tile_both_stage_variants(gpu, tmp_path):
+    """The single- and double-buffered tile kernels (an autotuned choice) give
+    identical, exact results; each is forced through an edited tuning cache."""
+    path = tmp_path / "tune.txt"
+    gpu.autotune(str(path))
+    lines = path.read_text().splitlines()
+    rng = np.random.default_rng(21)
+    a, b = _short_pairs(rng, 30001)
+    exact = oracle.pairs(a, b)
+    for bufs in (1, 2):
+        forced = tmp_path / f"tune{bufs}.txt"
+        forced.write_text("\n".join(l if not l.startswith("tile_buffers") else f"tile_buffers {bufs}"
+                                    for l in lines) + "\n")
+        assert gpu.autotune(str(forced))["tile_stage_buffers"] == bufs
+        np.testing.assert_array_equal(gpu.pairwise_packed(a, b), exact)
+        np.testing.assert_array_equal(gpu.pairwise_packed(a, b, 2, "uint8"),
+                                      oracle.saturate(np.minimum(exact, 3), "uint8"))
+    gpu.autotune(str(path))
