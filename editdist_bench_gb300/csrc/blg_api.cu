@@ -203,11 +203,11 @@ static int alloc_strings(blg_ctx *c, const uint8_t *buf, const int64_t *off, int
     const int64_t base = n > 0 ? off[0] : 0;
     const int64_t bytes = n > 0 ? off[n] - off[0] : 0;
     if (bytes > 0 && !buf) return fail(c, BLG_ERR_ARG, "null buffer");
-    CK(dev_alloc(c, &o.mem_buf, (size_t)bytes + 32), "cudaMallocAsync(strings)");
-    uint8_t *dbuf = (uint8_t *)o.mem_buf + 16;
-    // only the 16-byte slack on either side needs defined contents
-    CK(cudaMemsetAsync(o.mem_buf, 0, 16, c->stream), "cudaMemsetAsync(slack)");
-    CK(cudaMemsetAsync(dbuf + bytes, 0, 16, c->stream), "cudaMemsetAsync(slack)");
+    CK(dev_alloc(c, &o.mem_buf, (size_t)bytes + kSlackBefore + kSlackAfter), "cudaMallocAsync(strings)");
+    uint8_t *dbuf = (uint8_t *)o.mem_buf + kSlackBefore;
+    // only the slack on either side needs defined contents
+    CK(cudaMemsetAsync(o.mem_buf, 0, kSlackBefore, c->stream), "cudaMemsetAsync(slack)");
+    CK(cudaMemsetAsync(dbuf + bytes, 0, kSlackAfter, c->stream), "cudaMemsetAsync(slack)");
     CK(dev_alloc(c, &o.mem_off, sizeof(int64_t) * (size_t)(n + 1)), "cudaMallocAsync(offsets)");
     o.d.buf = dbuf;
     o.d.off = (const int64_t *)o.mem_off;
@@ -648,8 +648,9 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
             for (int64_t i = 0; i < nc; i++) soff[i + 1] = soff[i] + (oc[perm[i] + 1] - oc[perm[i]]);
             const int64_t bytes = soff[nc];
             OwnedStrings &cs = s->cs;
-            CK(dev_alloc(c, &cs.mem_buf, (size_t)bytes + 32), "cudaMallocAsync(sorted choices)");
-            CK(cudaMemsetAsync(cs.mem_buf, 0, (size_t)bytes + 32, c->stream), "memset sorted choices");
+            CK(dev_alloc(c, &cs.mem_buf, (size_t)bytes + kSlackBefore + kSlackAfter), "cudaMallocAsync(sorted choices)");
+            CK(cudaMemsetAsync(cs.mem_buf, 0, (size_t)bytes + kSlackBefore + kSlackAfter, c->stream),
+               "memset sorted choices");
             CK(dev_alloc(c, &cs.mem_off, sizeof(int64_t) * (size_t)(nc + 1)), "cudaMallocAsync(sorted offsets)");
             CK(cudaMemcpyAsync(cs.mem_off, soff.data(), sizeof(int64_t) * (nc + 1), cudaMemcpyHostToDevice, c->stream), "H2D soff");
             CK(dev_alloc(c, (void **)&s->perm, sizeof(int32_t) * nc), "cudaMallocAsync(perm)");
@@ -657,7 +658,7 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
             CK(dev_alloc(c, (void **)&s->lstart, sizeof(int64_t) * (n_len + 1)), "cudaMallocAsync(lstart)");
             CK(cudaMemcpyAsync(s->lstart, lstart.data(), sizeof(int64_t) * (n_len + 1), cudaMemcpyHostToDevice, c->stream), "H2D lstart");
             s->h_lstart = lstart;
-            cs.d.buf = (uint8_t *)cs.mem_buf + 16;
+            cs.d.buf = (uint8_t *)cs.mem_buf + kSlackBefore;
             cs.d.off = (const int64_t *)cs.mem_off;
             cs.d.n = nc;
             cs.d.base = 0;

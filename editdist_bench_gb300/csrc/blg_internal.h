@@ -8,8 +8,10 @@ namespace blg {
 
 // A packed string set resident in HBM: bytes of string i are
 // buf[off[i] - base, off[i+1] - base). The byte buffer carries 16 bytes of
-// slack before and after the data so the kernels' aligned 4/16-byte window
-// loads never leave the allocation; `buf` points 16 bytes into it.
+// slack before and 48 after the data, so the kernels' aligned window loads
+// and read-ahead cursors never leave the allocation; `buf` points 16 bytes
+// into it.
+constexpr int kSlackBefore = 16, kSlackAfter = 48;
 struct DevStrings {
     const uint8_t *buf = nullptr;
     const int64_t *off = nullptr;
