@@ -37,9 +37,6 @@ cudaError_t launch_transpose_choices(cudaStream_t st, int sms, const DevStrings 
                                      uint32_t *words, int32_t *len, uint32_t *status);
 cudaError_t launch_search_lanes(cudaStream_t st, bool hask, const DevStrings &C, const SearchClass &cls,
                                 int nwc, int k, int dtype, void *out, uint32_t *status);
-cudaError_t launch_pairs_main(cudaStream_t st, int grid, bool hask, const DevStrings &A,
-                              const DevStrings &B, int k, int dtype, void *out, const LongQueue &q,
-                              uint32_t *status);
 cudaError_t launch_pairs_long(cudaStream_t st, int grid, bool hask, const LongQueue &q, int k,
                               int dtype, void *out);
 cudaError_t launch_pairs_staged(cudaStream_t st, int sms, bool hask, const DevStrings &A, const DevStrings &B,
@@ -392,7 +389,7 @@ static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, const DevStrings &A, co
     CK(cudaMemsetAsync(p->plan_ctr, 0, sizeof(int32_t) * kPlanCounters, c->stream), "reset plan");
     if (exit_log) CK(cudaMemsetAsync(exit_log, 0, sizeof(int32_t) * (size_t)A.n, c->stream), "reset log");
     const int grid = (int)std::min<int64_t>((A.n + 255) / 256, (int64_t)c->sms * 8);
-    const bool band = hask && k <= 31 && !c->no_band;
+    const bool band = hask && k <= 31;
     CK(launch(c, "pairs_prep", [&] {
            return launch_pairs_prep(c->stream, grid, hask, learned, band, A, B, k, dtype, d_out, plan,
                                     c->d_status);

@@ -37,7 +37,6 @@ struct blg_ctx {
     int64_t launches = 0;
     int sched = 0;                     // BLG_SCHED_* (work order of thresholded runs)
     blg_sched_model *model = nullptr;  // trained/loaded scheduler network, if any
-    bool no_band = false;              // force the full-word loops even for max_dist <= 31
     blg_tuning tune;                   // launch shapes (autotuned or defaults)
     bool prof = false;
     std::vector<ProfRec> prof_recs;

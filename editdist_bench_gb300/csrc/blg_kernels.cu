@@ -13,11 +13,14 @@
 //  * k_search_lanes     cdist for queries longer than 512: a query's words
 //                       are spread over L lanes, the add-carry travels lane to
 //                       lane with __shfl_up_sync on an anti-diagonal wavefront.
-//  * k_pairs_main       pairwise: one thread per pair, exact prefix/suffix
+//  * k_pairs_staged     pairwise in natural order: one thread per pair, warp
+//                       spans staged in shared memory, exact prefix/suffix
 //                       trimming on 4-byte windows, single-word solve with
-//                       per-lane nibble Peq tables in shared memory; pairs
-//                       whose trimmed pattern exceeds 64 go to a device queue.
+//                       per-lane nibble Peq tables; pairs whose trimmed
+//                       pattern exceeds 64 go to a device queue.
 //  * k_pairs_long       persistent consumer of that queue, lane-spread.
+//  * k_search_surv      thresholded cdist with max_dist > 31 (full-word loop);
+//                       max_dist <= 31 runs in blg_search_lpt.cu.
 //
 // All arithmetic is integer bit logic on the ALU/FMA pipes; no tensor cores.
 #include <algorithm>
@@ -166,50 +169,8 @@ __global__ void __launch_bounds__(256) k_search_lanes(DevStrings C, SearchClass 
     }
 }
 
-// One thread per pair (grid-stride). Dynamic shared memory: 8 KB per warp.
-template <bool HASK>
-__global__ void __launch_bounds__(256) k_pairs_main(DevStrings A, DevStrings B, int k, int dtype,
-                                                    void *out, LongQueue q, uint32_t *status) {
-    extern __shared__ uint64_t s_tab[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint64_t *tc = s_tab + warp * 1024 + lane;
-#pragma unroll
-    for (int r = 0; r < 32; r++) tc[r * 32] = 0;
-    const int64_t n = A.n;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        int la, lb;
-        const uint8_t *a = string_at(A, i, la, status);
-        const uint8_t *b = string_at(B, i, lb, status);
-        trim_windows(a, la, b, lb);
-        if (la > lb) {                                  // the shorter string is the pattern
-            const uint8_t *t = a; a = b; b = t;
-            const int x = la; la = lb; lb = x;
-        }
-        int d;
-        if (HASK && lb - la > k) d = k + 1;             // length gap alone exceeds k
-        else if (la == 0) d = lb;
-        else if (la <= 64) d = solve_word<HASK>(tc, a, la, b, lb, k);
-        else {
-            const int cls = long_class(la);
-            if (cls < 0) { atomicOr(status, ST_TOO_LONG); d = -1; }
-            else {
-                const int pos = atomicAdd(&q.counts[cls], 1);
-                if (pos < q.cap[cls]) {
-                    LongItem it;
-                    it.pat = a; it.txt = b; it.m = la; it.n = lb; it.idx = i;
-                    q.items[cls][pos] = it;
-                    continue;
-                }
-                atomicOr(status, ST_QUEUE_OVERFLOW);
-                d = -1;
-            }
-        }
-        store1(out, dtype, i, d);
-    }
-}
-
-// Staged variant of k_pairs_main: each warp takes 32 consecutive pairs,
+// Pairs in natural order (the reference's schedule, one thread per pair):
+// each warp takes 32 consecutive pairs,
 // copies the byte spans of their a and b strings into shared memory with
 // coalesced 16-byte loads (one round trip instead of a chain of dependent
 // global reads per pair), then trims and solves from shared memory. Groups
@@ -602,20 +563,6 @@ cudaError_t launch_pairs_staged(cudaStream_t st, int sms, bool hask, const DevSt
     } else {
         cudaFuncSetAttribute(k_pairs_staged<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_pairs_staged<false><<<grid, 128, smem, st>>>(A, B, k, dtype, out, q, status);
-    }
-    return cudaGetLastError();
-}
-
-cudaError_t launch_pairs_main(cudaStream_t st, int grid, bool hask, const DevStrings &A,
-                              const DevStrings &B, int k, int dtype, void *out, const LongQueue &q,
-                              uint32_t *status) {
-    const size_t smem = 8 * 1024 * sizeof(uint64_t);
-    if (hask) {
-        cudaFuncSetAttribute(k_pairs_main<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_pairs_main<true><<<grid, 256, smem, st>>>(A, B, k, dtype, out, q, status);
-    } else {
-        cudaFuncSetAttribute(k_pairs_main<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_pairs_main<false><<<grid, 256, smem, st>>>(A, B, k, dtype, out, q, status);
     }
     return cudaGetLastError();
 }
