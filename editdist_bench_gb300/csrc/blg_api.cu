@@ -1213,7 +1213,7 @@ static int tune_band_pairs(blg_ctx *c) {
     c->sched = BLG_SCHED_AUTO;
     float best_ms = 1e30f;
     int best = c->tune.band_ctas;
-    for (int ctas : {3, 4, 5}) {
+    for (int ctas : {2, 3}) {
         if (rc) break;
         c->tune.band_ctas = ctas;
         float ms = 0.f;
@@ -1255,12 +1255,13 @@ static int tune_tile_pairs(blg_ctx *c) {
 }
 
 static std::string tuning_header(blg_ctx *c) {
+    // the version tag changes whenever a tuned kernel's shape limits change
     cudaDeviceProp prop{};
     cudaGetDeviceProperties(&prop, c->device);
     std::string name = prop.name;
     for (auto &ch : name)
         if (ch == ' ') ch = '_';
-    return "BLGTUNE1 " + name + " sm" + std::to_string(prop.major * 10 + prop.minor) + " " + std::to_string(c->sms) +
+    return "BLGTUNE2 " + name + " sm" + std::to_string(prop.major * 10 + prop.minor) + " " + std::to_string(c->sms) +
            " " + std::to_string(blg_version());
 }
 
@@ -1281,7 +1282,7 @@ static bool tuning_load(blg_ctx *c, const char *path) {
             if (w >= 1 && w <= 8 && v >= 0 && v <= 4096) { t.qpb[w] = v; fields++; }
         } else if (k == "lpt_ctas" && v >= 1 && v <= 8) { t.lpt_ctas = v; fields++; }
         else if (k == "lpt_job" && v >= 256 && v <= 4096) { t.lpt_job = v; fields++; }
-        else if (k == "band_ctas" && v >= 1 && v <= 5) { t.band_ctas = v; fields++; }
+        else if (k == "band_ctas" && v >= 1 && v <= 3) { t.band_ctas = v; fields++; }
         else if (k == "tile_buffers" && v >= 1 && v <= 2) { t.tile_buffers = v; fields++; }
     }
     fclose(f);

@@ -168,6 +168,45 @@ extern "C" int blg_host_band_cols(const uint8_t *a, int la, const uint8_t *b, in
     return band_core(la, lb, k, text, eqw, u, cols);
 }
 
+// The banded loop with the pairs solver's block tables: nibble rows over a
+// 64-position block of the pattern (bit i <-> position 32b - dhi + i), each
+// column's window taken with one funnel shift, rows shifted by 32 positions
+// and the next 32 bytes entered every 32 columns (k_solve_band's scheme).
+extern "C" int blg_host_band_blocks(const uint8_t *a, int la, const uint8_t *b, int lb, int k) {
+    normalise(a, la, b, lb, 1);
+    if (k < 0 || k > 31) return -1;
+    if (lb - la > k) return k + 1;
+    if (la == 0) return lb;
+    const int m = la, n = lb;
+    const BandGeom bg = band_geom(m, n, k);
+    const int dhi = bg.dhi;
+    uint32_t lo[32] = {0}, hi[32] = {0};
+    auto set = [&](uint32_t c, int bitpos) {
+        uint32_t *h = bitpos >= 32 ? hi : lo;
+        h[c >> 4] |= 1u << (bitpos & 31);
+        h[16 + (c & 15)] |= 1u << (bitpos & 31);
+    };
+    const int first_end = m < 64 - dhi ? m : 64 - dhi;
+    for (int p = 0; p < first_end; p++) set(a[p], p + dhi);
+    int next_pos = first_end;
+    const Units u{1u, 2u};
+    auto text = [&](int j) -> uint32_t { return b[j]; };
+    auto eqw = [&](uint32_t c, int p0) -> uint32_t {
+        const int j = p0 + dhi;
+        if ((j & 31) == 0 && j > 0) {
+            for (int r = 0; r < 32; r++) { lo[r] = hi[r]; hi[r] = 0; }
+            int cnt = m - next_pos;
+            if (cnt > 32) cnt = 32;
+            for (int i = 0; i < cnt; i++) set(a[next_pos + i], 32 + i);
+            if (cnt > 0) next_pos += cnt;
+        }
+        const uint32_t xl = lo[c >> 4] & lo[16 + (c & 15)], xh = hi[c >> 4] & hi[16 + (c & 15)];
+        const int s = j & 31;
+        return s == 0 ? xl : (xl >> s) | (xh << (32 - s));
+    };
+    return band_core(m, n, k, text, eqw, u, nullptr);
+}
+
 // Same, with the pattern as the LONGER string (the search kernels' case:
 // the query is the pattern whatever the choice's length), no trimming.
 extern "C" int blg_host_band_query(const uint8_t *q, int m, const uint8_t *t, int n, int k) {

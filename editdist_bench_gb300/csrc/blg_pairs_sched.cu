@@ -194,22 +194,23 @@ __global__ void __launch_bounds__(256) k_solve_lanes(PairsPlan plan, int k, int 
 }
 
 // max_dist <= 31: every record (any pattern length) solved by the banded
-// loop, one thread per record. The window's match bits come from a 32-slot
-// ring per thread: rows 0..15 / 16..31 of a [row][thread] u32 table hold,
-// for each high / low nibble value, the ring slots whose pattern byte has
-// it; slot (p & 31) holds pattern position p. Each column the position
-// leaving the window top and the one entering at its bottom share a slot:
-// the leaving byte (kept in a per-thread byte ring) is cleared, the entering
-// one set, and the slot order is rotated into window order. Both tables are
-// laid out [row or slot][thread], so every access is bank-conflict free.
+// loop, one thread per record. The window's match bits come from per-thread
+// nibble rows over a 64-position block of the pattern: rows 0..15 / 16..31
+// of a [row][thread] table hold, for each high / low nibble value, the
+// positions whose byte has it (bit i <-> position 32b - dhi + i in block b).
+// Columns 32b .. 32b+31 read their 32-bit windows out of the same block with
+// one funnel shift, so within a block the table is read-only and the match
+// loads stay off the column chain; every 32 columns the rows shift down by
+// 32 positions and the next 32 pattern bytes are entered. The [row][thread]
+// layout keeps every access bank-conflict free.
+constexpr int kBandThreads = 256;
+
 template <bool LOG>
-__global__ void __launch_bounds__(256) k_solve_band(PairsPlan plan, int k, int dtype, void *out,
-                                                    int32_t *exit_log, uint32_t unit) {
-    __shared__ uint32_t s_tab[32 * 256];
-    __shared__ uint8_t s_ring[256 * 32];
+__global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int k, int dtype, void *out,
+                                                             int32_t *exit_log, uint32_t unit) {
+    extern __shared__ uint2 s_rows2[];                      // [32 rows][kBandThreads] 64-bit rows
     const Units u{unit, unit + unit};
-    uint32_t *tc = s_tab + threadIdx.x;                     // row r at tc[r * 256]
-    uint8_t *ring = s_ring + threadIdx.x;                  // slot q at ring[q * 256] (conflict-free)
+    uint2 *tc = s_rows2 + threadIdx.x;                      // row r at tc[r * kBandThreads]
     const int lane = threadIdx.x & 31;
     for (int cls = kPairClasses - 1; cls >= 0; cls--) {
         const int count = min(plan.count[cls], (int)plan.cap[cls]);
@@ -227,55 +228,58 @@ __global__ void __launch_bounds__(256) k_solve_band(PairsPlan plan, int k, int d
             if (n - m > k || m - n > k) d = k + 1;
             else {
                 const BandGeom bg = band_geom(m, n, k);
+                const int dhi = bg.dhi;
 #pragma unroll
-                for (int r = 0; r < 32; r++) tc[r * 256] = 0;
-                // window of column 1 holds positions -dhi .. 30 - dhi; real ones first
+                for (int r = 0; r < 32; r++) tc[r * kBandThreads] = make_uint2(0, 0);
+                // block 0: positions 0 .. min(m, 64 - dhi) - 1 at bits pos + dhi
+                const int first_end = min(m, 64 - dhi);
                 {
-                    const int fill = min(31 - bg.dhi, m);
                     TextScan fs;
                     fs.init(pat);
-                    uint32_t f4 = 0;
-                    for (int p = 0; p < fill; p++) {
-                        if ((p & 3) == 0) f4 = fs.next4();
-                        const uint32_t c = f4 & 0xffu, bit = 1u << p;
-                        f4 >>= 8;
-                        tc[(c >> 4) * 256] |= bit;
-                        tc[(16 + (c & 15)) * 256] |= bit;
-                        ring[p * 256] = (uint8_t)c;
+                    for (int p = 0; p < first_end; p += 4) {
+                        const uint32_t w4 = fs.next4();
+#pragma unroll
+                        for (int b = 0; b < 4; b++) {
+                            if (p + b < first_end) {
+                                const uint32_t c = (w4 >> (8 * b)) & 0xffu;
+                                const int bitpos = p + b + dhi;
+                                uint32_t *h = reinterpret_cast<uint32_t *>(tc + (c >> 4) * kBandThreads) + (bitpos >> 5);
+                                uint32_t *l = reinterpret_cast<uint32_t *>(tc + (16 + (c & 15)) * kBandThreads) + (bitpos >> 5);
+                                const uint32_t bit = 1u << (bitpos & 31);
+                                *h |= bit;
+                                *l |= bit;
+                            }
+                        }
                     }
                 }
-                // entering positions p0 + 31 = 31 - dhi + j advance one per column:
-                // a 4-byte cursor keeps the pattern loads off the column chain
-                const int pin0 = 31 - bg.dhi;
+                // later blocks enter the positions from 64 - dhi on, 32 at a time
                 TextScan ps;
-                if (pin0 < m) ps.init(pat + pin0);
-                uint32_t pw = 0;
+                if (first_end < m) ps.init(pat + first_end);
+                int next_pos = first_end;
                 auto eqw = [&](uint32_t c, int p0) -> uint32_t {
-                    const int pin = p0 + 31, pout = p0 - 1;   // same ring slot
-                    const uint32_t slot = (uint32_t)pin & 31u, bit = 1u << slot;
-                    // match bits from the table before this column's update; window
-                    // bit 31 (the entering position) from a register compare instead
-                    const uint32_t x = tc[(c >> 4) * 256] & tc[(16 + (c & 15)) * 256];
-                    uint32_t eq = __funnelshift_r(x, x, (uint32_t)(p0 & 31)) & 0x7fffffffu;
-                    if (pin < m) {
-                        if (((pin - pin0) & 3) == 0) pw = ps.next4();
-                        const uint32_t cn = pw & 0xffu;
-                        pw >>= 8;
-                        if (cn == c) eq |= 0x80000000u;
-                        if (pout >= 0) {
-                            const uint32_t co = ring[slot * 256];
-                            tc[(co >> 4) * 256] &= ~bit;
-                            tc[(16 + (co & 15)) * 256] &= ~bit;
+                    const int j = p0 + dhi;
+                    if ((j & 31) == 0 && j > 0) {               // warp-uniform: lanes share j
+#pragma unroll
+                        for (int r = 0; r < 32; r++) {
+                            const uint32_t hi = tc[r * kBandThreads].y;
+                            tc[r * kBandThreads] = make_uint2(hi, 0);
                         }
-                        tc[(cn >> 4) * 256] |= bit;
-                        tc[(16 + (cn & 15)) * 256] |= bit;
-                        ring[slot * 256] = (uint8_t)cn;
-                    } else if (pout >= 0 && pout < m) {
-                        const uint32_t co = ring[slot * 256];
-                        tc[(co >> 4) * 256] &= ~bit;
-                        tc[(16 + (co & 15)) * 256] &= ~bit;
+                        const int cnt = min(32, m - next_pos);
+                        for (int i = 0; i < cnt; i += 4) {
+                            const uint32_t w4 = ps.next4();
+#pragma unroll
+                            for (int b = 0; b < 4; b++) {
+                                if (i + b < cnt) {
+                                    const uint32_t ch = (w4 >> (8 * b)) & 0xffu, bit = 1u << (i + b);
+                                    tc[(ch >> 4) * kBandThreads].y |= bit;
+                                    tc[(16 + (ch & 15)) * kBandThreads].y |= bit;
+                                }
+                            }
+                        }
+                        next_pos += cnt > 0 ? cnt : 0;
                     }
-                    return eq;
+                    const uint2 h = tc[(c >> 4) * kBandThreads], l = tc[(16 + (c & 15)) * kBandThreads];
+                    return __funnelshift_r(h.x & l.x, h.y & l.y, (uint32_t)(j & 31));
                 };
                 d = band_distance(m, it.txt, n, k, eqw, u, LOG ? &cols : nullptr);
             }
@@ -307,10 +311,16 @@ cudaError_t launch_order(cudaStream_t st, int sms, const PairsPlan &plan) {
 
 cudaError_t launch_solve_band(cudaStream_t st, int sms, int ctas_per_sm, const PairsPlan &plan, int k, int dtype,
                               void *out, int32_t *exit_log) {
-    // 40 KB of ring tables per CTA: at most five CTAs per SM
-    const int grid = sms * (ctas_per_sm < 1 ? 1 : (ctas_per_sm > 5 ? 5 : ctas_per_sm));
-    if (exit_log) k_solve_band<true><<<grid, 256, 0, st>>>(plan, k, dtype, out, exit_log, 1u);
-    else k_solve_band<false><<<grid, 256, 0, st>>>(plan, k, dtype, out, nullptr, 1u);
+    // 64 KB of nibble rows per CTA: at most three CTAs per SM
+    const int grid = sms * (ctas_per_sm < 1 ? 1 : (ctas_per_sm > 3 ? 3 : ctas_per_sm));
+    const size_t smem = sizeof(uint2) * 32 * kBandThreads;
+    if (exit_log) {
+        cudaFuncSetAttribute(k_solve_band<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_solve_band<true><<<grid, kBandThreads, smem, st>>>(plan, k, dtype, out, exit_log, 1u);
+    } else {
+        cudaFuncSetAttribute(k_solve_band<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_solve_band<false><<<grid, kBandThreads, smem, st>>>(plan, k, dtype, out, nullptr, 1u);
+    }
     return cudaGetLastError();
 }
 

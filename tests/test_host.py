@@ -69,6 +69,7 @@ def hostcheck():
     L.blg_host_band.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
                                 ctypes.c_int]
     L.blg_host_band_query.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
+    L.blg_host_band_blocks.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
     return L
 
 
@@ -199,3 +200,4 @@ def test_band_matches_oracle(hostcheck, k):
         assert hostcheck.blg_host_band(a, len(a), b, len(b), 1, k) == want
         assert hostcheck.blg_host_band(a, len(a), b, len(b), 0, k) == want
         assert hostcheck.blg_host_band_query(a, len(a), b, len(b), k) == want
+        assert hostcheck.blg_host_band_blocks(a, len(a), b, len(b), k) == want
