@@ -151,8 +151,16 @@ __device__ __forceinline__ void stage_trim(const uint8_t *base, uint32_t &oa, in
     lb -= p + s;
 }
 
-// Nibble tables of a staged pattern (set or clear its rows).
+// Nibble tables of a staged pattern: set its rows (one shared-memory atomic
+// OR per row update instead of a load-or-store chain), or clear them: all 32
+// rows with plain stores once the pattern has more than 4 bytes, else just
+// the rows it touched.
 __device__ __forceinline__ void stage_nib(uint32_t *tc, const uint8_t *base, uint32_t op, int m, bool set) {
+    if (!set && m > 4) {
+#pragma unroll
+        for (int r = 0; r < 32; r++) tc[r * kTileThreads] = 0;
+        return;
+    }
     StageScan ps;
     ps.init(base, op);
     for (int i = 0; i < m; i += 4) {
@@ -164,8 +172,8 @@ __device__ __forceinline__ void stage_nib(uint32_t *tc, const uint8_t *base, uin
                 uint32_t *h = tc + (c >> 4) * kTileThreads, *l = tc + (16 + (c & 15)) * kTileThreads;
                 if (set) {
                     const uint32_t bit = 1u << (i + b);
-                    *h |= bit;
-                    *l |= bit;
+                    atomicOr(h, bit);
+                    atomicOr(l, bit);
                 } else {
                     *h = 0;
                     *l = 0;

@@ -125,12 +125,11 @@ def _solve_ms(ctx, batch, out, k, runs=3):
 
 
 def test_trained_network_order_against_no_network(gpu):
-    """The same pipeline with and without the network: with zero weights
-    every record gets the same key (no ordering); with trained weights each
-    1024-record segment is ordered by predicted exit column. Results are
-    identical. On the banded pairs solver the order barely matters (its time
-    follows the total work of the lanes, not the slowest lane of a warp), so
-    the learned order must simply not be slower; the measured times print."""
+    """What the network gains over the same pipeline without it: with zero
+    weights every record gets the same key (no ordering); with trained
+    weights each 1024-record segment is ordered by predicted exit column, so
+    warps take pairs that finish together. Results are identical; the banded
+    solver, the same kernel in both runs, is faster on the learned order."""
     ctx = _lib.context()
     train = W.config3(n=1 << 18, seed=2003)
     tb = gpu.PairsBatch(train.a, train.b)
@@ -153,7 +152,7 @@ def test_trained_network_order_against_no_network(gpu):
         gpu.set_schedule("auto")
     np.testing.assert_array_equal(res_learned, res_flat)
     print(f"banded solve: learned order {t_learned:.3f} ms, without the network {t_flat:.3f} ms")
-    assert t_learned <= 1.05 * t_flat
+    assert t_learned * 1.1 < t_flat
 
 
 def _lpt_ms(ctx, s, out, k, runs=3):
