@@ -246,8 +246,8 @@ __global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int
                                 uint32_t *h = reinterpret_cast<uint32_t *>(tc + (c >> 4) * kBandThreads) + (bitpos >> 5);
                                 uint32_t *l = reinterpret_cast<uint32_t *>(tc + (16 + (c & 15)) * kBandThreads) + (bitpos >> 5);
                                 const uint32_t bit = 1u << (bitpos & 31);
-                                *h |= bit;
-                                *l |= bit;
+                                atomicOr(h, bit);
+                                atomicOr(l, bit);
                             }
                         }
                     }
@@ -271,8 +271,8 @@ __global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int
                             for (int b = 0; b < 4; b++) {
                                 if (i + b < cnt) {
                                     const uint32_t ch = (w4 >> (8 * b)) & 0xffu, bit = 1u << (i + b);
-                                    tc[(ch >> 4) * kBandThreads].y |= bit;
-                                    tc[(16 + (ch & 15)) * kBandThreads].y |= bit;
+                                    atomicOr(&tc[(ch >> 4) * kBandThreads].y, bit);
+                                    atomicOr(&tc[(16 + (ch & 15)) * kBandThreads].y, bit);
                                 }
                             }
                         }
