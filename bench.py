@@ -413,6 +413,18 @@ def exit_columns(bench, sample_rows_or_n):
         words = ((np.diff(sub[1]) + 31) // 32).astype(np.float64)
         s = float((cols.astype(np.float64) * words[:, None]).sum())
         return s * bench.w.nq / rows
+    if bench.kind == "batch":
+        # up to 4 query rows of every problem, scaled by its query count
+        total = 0.0
+        for p in bench.probs:
+            rows = min(p.nq, 4)
+            if rows == 0 or p.nc == 0:
+                continue
+            sub = W.take(p.q, np.arange(rows))
+            _, cols = oracle.cross_trace(sub, p.c, p.max_dist)
+            words = ((np.diff(sub[1]) + 31) // 32).astype(np.float64)
+            total += float((cols.astype(np.float64) * words[:, None]).sum()) * p.nq / rows
+        return total
     n = sample_rows_or_n
     sa, sb = W.take(bench.w.a, np.arange(n)), W.take(bench.w.b, np.arange(n))
     _, m, _, cols = oracle.pairs_trace(sa, sb, bench.w.max_dist)
@@ -609,7 +621,7 @@ def run_ours(args, ranks: Ranks):
             cpu = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": sample,
                    "single_thread": {"value": v1, "sample": sample1},
                    "gate": bench.gate(n_s, res)}
-            if bench.kind == "pairwise" or (bench.runs[0][0] is not None and bench.kind != "batch"):
+            if bench.kind in ("pairwise", "batch") or bench.runs[0][0] is not None:
                 exit_sum = exit_columns(bench, n_s)
         result["cpu_baseline"] = cpu
         if top:

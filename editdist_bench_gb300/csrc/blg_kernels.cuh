@@ -384,16 +384,24 @@ __device__ __forceinline__ void nib_build(uint64_t *tc, const uint8_t *p, int m)
         for (int b = 0; b < 4; b++) {
             if (i + b < m) {
                 const uint32_t c = (w4 >> (8 * b)) & 0xffu;
-                const uint64_t bit = 1ull << (i + b);
-                tc[(c >> 4) * 32] |= bit;
-                tc[(16 + (c & 15)) * 32] |= bit;
+                const unsigned long long bit = 1ull << (i + b);
+                // one shared-memory atomic per row update instead of a load-or-store chain
+                atomicOr(reinterpret_cast<unsigned long long *>(tc + (c >> 4) * 32), bit);
+                atomicOr(reinterpret_cast<unsigned long long *>(tc + (16 + (c & 15)) * 32), bit);
             }
         }
     }
 }
 
+// Clear a pattern's rows: all 32 with plain stores once it has more than 4
+// bytes (fewer instructions than revisiting its bytes), else the rows it set.
 template <typename L = LdgLoad>
 __device__ __forceinline__ void nib_clear(uint64_t *tc, const uint8_t *p, int m) {
+    if (m > 4) {
+#pragma unroll
+        for (int r = 0; r < 32; r++) tc[r * 32] = 0;
+        return;
+    }
     TextScanT<L> ps;
     ps.init(p);
     for (int i = 0; i < m; i += 4) {
