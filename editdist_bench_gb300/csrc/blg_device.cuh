@@ -79,11 +79,12 @@ BLG_HD bool hopeless(int score, int j, int n, int k) { return k >= 0 && score - 
 // ---- pipe-balanced step on 32-bit halves --------------------------------
 // A 64-bit Myers step is ~25 32-bit instructions; written plainly they all
 // land on the ALU pipe, which then limits throughput while the FMA pipe
-// (IMAD) idles. The forms below move the 64-bit add, the low-half shifts
-// and the score bits onto IMAD, keeping only the genuinely bitwise work on
-// the ALU. Multipliers come from run-time values (`Units`, loaded from a
-// kernel parameter) so the compiler cannot turn the multiply-adds back into
-// shifts. On the host the same functions are plain integer arithmetic.
+// (IMAD) idles. The forms below move the low-half shifts, the character
+// offsets and the score bits onto IMAD; the 64-bit add stays a carry-chained
+// ALU pair, which measured faster than IMAD.WIDE. Multipliers come from
+// run-time values (`Units`, loaded from a kernel parameter) so the compiler
+// cannot turn the multiply-adds back into shifts. On the host the same
+// functions are plain integer arithmetic.
 struct Units {
     uint32_t one, two;
 };
@@ -109,22 +110,23 @@ BLG_HD uint32_t imad_hi(uint32_t a, uint32_t b, uint32_t c) {
 #endif
 }
 
-BLG_HD uint64_t imad_wide(uint32_t a, uint32_t b, uint64_t c) {
-#if defined(__CUDA_ARCH__)
-    uint64_t r;
-    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(r) : "r"(a), "r"(b), "l"(c));
-    return r;
-#else
-    return (uint64_t)a * b + c;
-#endif
-}
-
 // (hi:lo) << 1, high half
 BLG_HD uint32_t shl1_hi(uint32_t lo, uint32_t hi) {
 #if defined(__CUDA_ARCH__)
     return __funnelshift_l(lo, hi, 1);
 #else
     return (hi << 1) | (lo >> 31);
+#endif
+}
+
+// (ah:al) + (bh:bl) with the carry passed between the halves.
+BLG_HD void add64(uint32_t al, uint32_t ah, uint32_t bl, uint32_t bh, uint32_t &sl, uint32_t &sh) {
+#if defined(__CUDA_ARCH__)
+    asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, %4, %5;" : "=r"(sl), "=r"(sh) : "r"(al), "r"(bl), "r"(ah), "r"(bh));
+#else
+    const uint64_t r = (((uint64_t)ah << 32) | al) + (((uint64_t)bh << 32) | bl);
+    sl = (uint32_t)r;
+    sh = (uint32_t)(r >> 32);
 #endif
 }
 
@@ -140,9 +142,10 @@ BLG_HD void step_h(Word2 &s, uint32_t el, uint32_t eh, uint32_t cin_p, uint32_t 
                    uint32_t &Phl, uint32_t &Phh, uint32_t &Mhl, uint32_t &Mhh) {
     const uint32_t vl = el | s.ml, vh = eh | s.mh;            // Xv = Eq | Mv
     const uint32_t el2 = el | cin_m;                           // a -1 carry acts as a match
-    // sum = (Eq & Pv) + Pv as one 64-bit IMAD.WIDE plus one IMAD for the high half
-    const uint64_t w = imad_wide(el2 & s.pl, u.one, ((uint64_t)s.ph << 32) | s.pl);
-    const uint32_t sl = (uint32_t)w, sh = imad_lo(eh & s.ph, u.one, (uint32_t)(w >> 32));
+    // sum = (Eq & Pv) + Pv as a carry-chained pair of 32-bit adds (ALU). An
+    // IMAD.WIDE form measured 13% slower in the exact search on GB300.
+    uint32_t sl, sh;
+    add64(el2 & s.pl, eh & s.ph, s.pl, s.ph, sl, sh);
     const uint32_t xl = (sl ^ s.pl) | el2, xh = (sh ^ s.ph) | eh;   // Xh
     Phl = s.ml | ~(xl | s.pl);
     Phh = s.mh | ~(xh | s.ph);
@@ -206,12 +209,12 @@ BLG_HD int popc32(uint32_t x) {
 // *cols_out = text columns processed.
 template <typename TextFn, typename EqW>
 BLG_HD int band_core(int m, int n, int k, TextFn text, EqW eqw, Units u, int *cols_out) {
+    (void)u;                                                 // plain shifts here (see the column step)
     const BandGeom bg = band_geom(m, n, k);
     const int nv = bg.dhi + 1;                               // virtual rows -dhi .. 0 at column 0
     uint32_t mv = nv >= 32 ? 0xffffffffu : ((1u << nv) - 1u);
     uint32_t pv = ~mv;
     int A = bg.dhi;                                          // D'[top window row][current column]
-    const uint32_t half_top = u.one << 31;
     for (int j = 0; j < n; j++) {
         if ((j & 3) == 0 && j > 0 && A - popc32(mv & bg.band) > k) {   // every band cell > k
             if (cols_out) *cols_out = j;
@@ -219,15 +222,17 @@ BLG_HD int band_core(int m, int n, int k, TextFn text, EqW eqw, Units u, int *co
         }
         const uint32_t c = text(j);
         // column j's deltas re-indexed one row down; the new bottom row enters with +1
-        pv = imad_hi(pv, half_top, half_top);
-        mv = imad_hi(mv, half_top, 0);
+        // (plain shifts and add: the IMAD forms of the 32-bit step measured
+        // 2-4% slower here, where the column chain is latency-bound)
+        pv = (pv >> 1) | 0x80000000u;
+        mv >>= 1;
         const uint32_t eq = eqw(c, j - bg.dhi);
         const uint32_t xv = eq | mv;
-        const uint32_t sum = imad_lo(eq & pv, u.one, pv);
+        const uint32_t sum = (eq & pv) + pv;
         const uint32_t xh = (sum ^ pv) | eq;
         const uint32_t ph = mv | ~(xh | pv);
         const uint32_t mh = pv & xh;
-        const uint32_t phs = imad_lo(ph, u.two, u.one), mhs = imad_lo(mh, u.two, 0);
+        const uint32_t phs = (ph << 1) | 1u, mhs = mh << 1;
         pv = mhs | ~(xv | phs);
         mv = phs & xv;
         A += 1 + (int)(pv & 1u) - (int)(mv & 1u);

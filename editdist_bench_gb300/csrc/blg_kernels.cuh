@@ -144,6 +144,8 @@ struct RowAddr {
     }
     template <int B>
     __device__ __forceinline__ uint32_t off(uint32_t w4) const {
+        // the top byte needs no mask: hi32(w4 * 2^8) is that byte alone
+        if (kPow2 && B == 3) return imad_lo(imad_hi(w4, ext[3], 0), stride, 0);
         if (kPow2) return (B == 0 ? imad_lo(w4, mul[0], 0) : imad_hi(w4, mul[B], 0)) & mask;
         const uint32_t c = B == 0 ? (w4 & 0xffu) : B == 3 ? imad_hi(w4, ext[3], 0)
                                                           : (imad_hi(w4, ext[B], 0) & 0xffu);
