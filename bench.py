@@ -22,7 +22,9 @@ matrix. The metric is pairs/s (distances per second; GCUPS beside it).
            bounded sample, all host threads.
 * --impl reference: the reference's CPU path (here: the oracle port, since
            the reference's sources are not on the GPU host) on the same
-           workload, all host threads.
+           workload, all host threads; beside it ("reference_cuda") the
+           reference's own CUDA kernels, compiled for sm_103a from its
+           sources, timed kernel-only on this GPU where that cubin exists.
 
 Under torchrun (N > 1) every rank runs its own replica of the workload on
 its own GPU (weak scaling, no data-path collective); rank 0 reports the
@@ -105,6 +107,10 @@ class Clocks:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.time()                        # the sampler is running before the timed region opens
+            while not self.rows and time.time() - t0 < 3.0 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.n_before = len(self.rows)
         except (OSError, FileNotFoundError):
             self.proc = None
 
@@ -116,6 +122,12 @@ class Clocks:
 
     def stop(self) -> dict:
         if self.proc:
+            # a timed region shorter than the sampling period still gets the
+            # first sample taken after it (the clocks of the just-ended load)
+            t0 = time.time()
+            while len(self.rows) <= getattr(self, "n_before", 0) and time.time() - t0 < 0.5:
+                time.sleep(0.01)
+            self.rows = self.rows[max(0, getattr(self, "n_before", 1) - 1):]
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -649,16 +661,64 @@ def run_ours(args, ranks: Ranks):
         print(json.dumps(result), flush=True)
 
 
+def reference_cuda_leg(w, steps: int, warmup: int) -> dict:
+    """The reference's own CUDA kernels (csrc/gpu_kernels.cu compiled for
+    sm_103a from its sources, launched with bitlev/gpu.py's geometry by
+    oracle/ref_cuda.py) on the same workload, kernel-only, inputs resident."""
+    from oracle import ref_cuda as RC
+    if not RC.available():
+        return {"unavailable": "the reference's CUDA kernels were not compiled (its sources are read where they lie, "
+                               "so the cubin is built only where the reference checkout exists)"}
+    r = RC.RefCuda(int(os.environ.get("BLG_DEVICE", "0")))
+    try:
+        probs = w if isinstance(w, list) else [w]
+        runs, pairs = [], 0
+        for p in probs:
+            k = -1 if p.max_dist is None else int(p.max_dist)
+            out8 = p.dtype == "uint8"
+            item = 1 if out8 else 4                # uint16 is an int32 launch plus a conversion in bitlev
+            if isinstance(p, W.SearchWork):
+                st = r.cross_setup(p.q, p.c)
+                out = r._keep(r.d.alloc(p.nq * p.nc * item))
+                runs.append((r.cross_run, st, out, k, out8))
+                pairs += p.nq * p.nc
+            else:
+                st = r.pairs_setup(p.a, p.b)
+                out = r._keep(r.d.alloc(p.n * item))
+                runs.append((r.pairs_run, st, out, k, out8))
+                pairs += p.n
+
+        def call():
+            for fn, st, out, k, out8 in runs:
+                fn(st, out, k, out8)
+        t = r.time_calls(call, steps, warmup)
+        ms = float(np.mean(t))
+        return {"value": pairs / (ms / 1e3), "unit": "pairs/s", "ms_per_step": ms, "steps": steps,
+                "kind": "reference kernels (csrc/gpu_kernels.cu) compiled for sm_103a, bitlev/gpu.py launch "
+                        "geometry, CUDA events, inputs resident, L2 flushed between steps"}
+    finally:
+        r.close()
+
+
 def run_reference(args, ranks: Ranks):
     """The reference's CPU path on the host cores (oracle port: the reference's
-    sources are not present on the GPU host), same workload and metric."""
+    sources are not present on the GPU host), same workload and metric; beside
+    it, the reference's own CUDA kernels on this GPU where they were compiled."""
     if ranks.rank != 0:
         return
     import oracle
     cfg = args.config
-    w = {1: W.config1, 2: W.config2, 3: W.config3, 4: W.config4}[cfg]()
+    w = {1: W.config1, 2: W.config2, 3: W.config3, 4: W.config4, 5: W.config5}[cfg]()
     threads = effective_cpus()
-    if isinstance(w, W.SearchWork):
+    if isinstance(w, list):                        # the many-problem batch: up to 4 rows of each problem
+        probs = w
+        per = sum(min(p.nq, 4) * p.nc for p in probs)
+        cells = sum(W.cross_cells(W.take(p.q, np.arange(min(p.nq, 4))), p.c) for p in probs)
+        fn = lambda: [oracle.cross(W.take(p.q, np.arange(min(p.nq, 4))), p.c, p.max_dist,  # noqa: E731
+                                   threads=threads) for p in probs]
+        sample = f"up to 4 query rows of each of the {len(probs)} problems ({per} pairs) per step"
+        workload = f"cdist batch of {len(probs)} problems"
+    elif isinstance(w, W.SearchWork):
         k = w.max_dist
         rows = max(1, min(w.nq, 16 * threads))
         sub = W.take(w.q, np.arange(rows))
@@ -666,6 +726,7 @@ def run_reference(args, ranks: Ranks):
         per = rows * w.nc
         cells = W.cross_cells(sub, w.c)
         sample = f"{rows} query rows x {w.nc} choices per step"
+        workload = f"{w.name} cdist {w.nq}x{w.nc}"
     else:
         n = min(w.n, 1 << 18)
         sa, sb = W.take(w.a, np.arange(n)), W.take(w.b, np.arange(n))
@@ -673,6 +734,7 @@ def run_reference(args, ranks: Ranks):
         per = n
         cells = W.cells(sa, sb)
         sample = f"first {n} pairs per step"
+        workload = f"{w.name} pairwise {w.n}"
     for _ in range(args.warmup):
         fn()
     t = []
@@ -682,16 +744,20 @@ def run_reference(args, ranks: Ranks):
         t.append(time.perf_counter() - t0)
     s = sum(t) / len(t)
     value = per / s
+    try:
+        ref_cuda = reference_cuda_leg(w, args.steps, max(args.warmup, 3))
+    except Exception as e:                         # reported, never fatal to the CPU arm
+        ref_cuda = {"unavailable": f"{type(e).__name__}: {e}"}
     print(json.dumps({
         "impl": "reference", "metric": "pairs/s", "value": value, "unit": "pairs/s", "n_gpus": ranks.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": (f"{w.name} cdist {w.nq}x{w.nc}" if isinstance(w, W.SearchWork)
-                                else f"{w.name} pairwise {w.n}"), "sample": sample},
+        "config": {"workload": workload, "sample": sample},
         "gcups": cells / s / 1e9,
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_cuda": ref_cuda,
     }), flush=True)
 
 

@@ -4,6 +4,13 @@
   (myers_oracle.c) into ``oracle/_build/liborc.so`` with gcc. It runs here
   and on the GPU host (the .so is rebuilt there; nothing compiled on one
   machine is used on the other).
+* ``build_ref_cuda()`` compiles the reference's OWN CUDA kernels
+  (csrc/gpu_kernels.cu with csrc/gpu_myers.cuh), where they lie, into
+  ``oracle/_ref/ref_gpu_kernels.cubin`` for sm_103a with nvcc, so that
+  ``oracle/ref_cuda.py`` can time them on the same GB300 with the launch
+  geometry of bitlev/gpu.py (CuPy, the reference's own launcher, is not
+  installable offline). The cubin is device code, the same on x86 and Arm
+  hosts, so one built here serves the GPU host too.
 * ``build_ref()`` compiles the reference's OWN CPU sources, where they lie in
   the read-only reference checkout, into ``oracle/_ref/`` (git-ignored):
   ``libmyers.so`` (csrc/myers.c), the CPython extension ``_edpy`` that
@@ -68,6 +75,28 @@ def ref_paths() -> dict:
             "gpucheck": os.path.join(REF_OUT, "libgpucheck.so")}
 
 
+def ref_cuda_cubin() -> str:
+    return os.path.join(REF_OUT, "ref_gpu_kernels.cubin")
+
+
+def build_ref_cuda(force: bool = False) -> str:
+    """Compile the reference's CUDA kernels in place into a sm_103a cubin."""
+    if not ref_available():
+        raise FileNotFoundError(f"reference checkout not found at {REF_SRC}")
+    csrc = os.path.join(REF_SRC, "csrc")
+    src = os.path.join(csrc, "gpu_kernels.cu")
+    out = ref_cuda_cubin()
+    if force or _stale(out, src, os.path.join(csrc, "gpu_myers.cuh")):
+        os.makedirs(REF_OUT, exist_ok=True)
+        nvcc = os.environ.get("NVCC") or "/usr/local/cuda/bin/nvcc"
+        tmp = out + f".{os.getpid()}.tmp"
+        # the reference's NVRTC options are -std=c++17 -I<csrc> (bitlev/gpu.py:44-51)
+        _run([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+              f"-I{csrc}", "-o", tmp, src])
+        os.replace(tmp, out)
+    return out
+
+
 def build_ref(force: bool = False) -> dict:
     """Compile the reference's CPU sources in place into oracle/_ref/."""
     if not ref_available():
@@ -96,3 +125,4 @@ if __name__ == "__main__":
         print(build_oracle(force=True))
     if what in ("ref", "all"):
         print(build_ref(force=True))
+        print(build_ref_cuda(force=True))
