@@ -686,7 +686,10 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
         }
         const int64_t bytes = oc[nc] - oc[0];
         if (base[tiles] * 4 <= 2 * bytes + (64ll << 20)) {
-            CK(dev_alloc(c, (void **)&s->tt_words, sizeof(uint32_t) * (size_t)base[tiles] + 16), "cudaMallocAsync(tt)");
+            // + kTtSlackRows rows: the search loop prefetches up to 4 words past a choice's end
+            CK(dev_alloc(c, (void **)&s->tt_words,
+                         sizeof(uint32_t) * ((size_t)base[tiles] + (size_t)kTtSlackRows * kTileCands)),
+               "cudaMallocAsync(tt)");
             CK(dev_alloc(c, (void **)&s->tt_base, sizeof(int64_t) * (size_t)(tiles + 1)), "cudaMallocAsync(tt base)");
             CK(dev_alloc(c, (void **)&s->tt_len, sizeof(int32_t) * (size_t)nc), "cudaMallocAsync(tt len)");
             CK(cudaMemcpyAsync(s->tt_base, base.data(), sizeof(int64_t) * (tiles + 1), cudaMemcpyHostToDevice,

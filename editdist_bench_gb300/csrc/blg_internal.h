@@ -55,6 +55,10 @@ struct LongQueue {
 // base[T] = kTileCands * ceil(longest choice of T / 4); len[c] = length.
 constexpr int kTileCands = 1024;
 
+// Rows of words allocated past the last tile of transposed choices, so the
+// search loop may prefetch up to this many words beyond any choice's end.
+constexpr int kTtSlackRows = 4;
+
 struct TransposedChoices {
     const uint32_t *words = nullptr;
     const int64_t *base = nullptr;    // [tiles + 1]

@@ -112,6 +112,43 @@ __global__ void __launch_bounds__(256) k_search_tt(TransposedChoices T, SearchCl
     }
 }
 
+// Exact search of short queries, QI queries per thread: the CTA stages the
+// Peq tables of QI consecutive queries of its chunk and every thread runs its
+// 4 choices against all QI at once (dist_tt_q). Partial groups at the end of
+// a chunk run with zero tables and store nothing for the missing queries.
+template <int NW, int QI>
+__global__ void __launch_bounds__(256) k_search_ttq(TransposedChoices T, SearchClass cls, int qpb, int dtype,
+                                                    void *out, uint32_t unit) {
+    extern __shared__ uint64_t s_peq[];
+    const Units u{unit, unit + unit};
+    RowAddr<NW> ra;
+    ra.init(u);
+    const int64_t nc = T.n;
+    const int64_t tile = blockIdx.x;
+    const int64_t c0 = tile * kTileCands + threadIdx.x;
+    const uint32_t *tw = T.words + T.base[tile] + threadIdx.x;
+    const int q_begin = blockIdx.y * qpb;
+    const int q_end = min(q_begin + qpb, cls.nq);
+    constexpr int kWords = 256 * NW;
+    for (int qg = q_begin; qg < q_end; qg += QI) {
+        const int nqg = min(QI, q_end - qg);
+        __syncthreads();
+        const uint64_t *src = cls.peq + (size_t)qg * kWords;
+        for (int x = threadIdx.x; x < QI * kWords; x += blockDim.x) s_peq[x] = x < nqg * kWords ? __ldg(src + x) : 0;
+        __syncthreads();
+#pragma unroll 1
+        for (int t = 0; t < 4; t++) {
+            const int64_t c = c0 + 256 * t;
+            if (c >= nc) break;
+            int d[QI];
+            dist_tt_q<NW, QI>(s_peq, cls.qlen + qg, nqg, tw + 256 * t, __ldg(T.len + c), u, ra, d);
+#pragma unroll
+            for (int i = 0; i < QI; i++)
+                if (i < nqg) store1(out, dtype, cls.qidx[qg + i] * nc + c, d[i]);
+        }
+    }
+}
+
 // Transpose choices into tiles (see TransposedChoices); one thread per
 // (choice, word), bytes past a choice's end are zero.
 __global__ void __launch_bounds__(256) k_transpose_choices(DevStrings C, const int64_t *base, uint32_t *words,
@@ -492,9 +529,22 @@ cudaError_t launch_search_seq(cudaStream_t st, int nw, bool hask, const DevStrin
     }
 }
 
+template <int NW, int QI>
+static cudaError_t launch_ttq(dim3 grid, cudaStream_t st, const TransposedChoices &T, const SearchClass &cls,
+                              int qpb, int dtype, void *out) {
+    const size_t smem = (size_t)QI * 256 * NW * sizeof(uint64_t);
+    cudaFuncSetAttribute(k_search_ttq<NW, QI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_search_ttq<NW, QI><<<grid, 256, smem, st>>>(T, cls, qpb, dtype, out, 1u);
+    return cudaGetLastError();
+}
+
 template <int NW>
 static cudaError_t launch_tt(bool hask, dim3 grid, size_t smem, cudaStream_t st, const TransposedChoices &T,
                              const SearchClass &cls, int qpb, int k, int dtype, void *out) {
+    // exact short queries: several queries per thread (one text pass serves them all)
+    // (measured on 1024 x 65536 L64: 1 query per thread 4.48 ms, 2: 4.19 ms, 4: 4.09 ms, 8: 5.0 ms)
+    if (!hask && NW == 1) return launch_ttq<1, 4>(grid, st, T, cls, qpb, dtype, out);
+    if (!hask && NW == 2) return launch_ttq<2, 2>(grid, st, T, cls, qpb, dtype, out);
     if (hask) {
         cudaFuncSetAttribute(k_search_tt<NW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_search_tt<NW, true><<<grid, 256, smem, st>>>(T, cls, qpb, k, dtype, out, 1u);

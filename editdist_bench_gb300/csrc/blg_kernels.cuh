@@ -249,7 +249,11 @@ __device__ __forceinline__ int vsum(const Word2 (&st)[NW], uint32_t ml, uint32_t
 }
 
 // d(query, choice) with the choice in tile-transposed form: word w of the
-// text at txt[w * kTileCands] (one coalesced line per warp).
+// text at txt[w * kTileCands] (one coalesced line per warp). The loop runs 16
+// columns (4 words) per iteration with the next 4 words already in flight, so
+// the loop's own bookkeeping is spread over 16 columns; the prefetch may read
+// up to 4 words past the text (the transposed buffer has kTtSlackRows spare
+// rows after its last tile).
 template <int NW, bool HASK>
 __device__ __forceinline__ int dist_tt(const uint64_t *peq, int m, const uint32_t *txt, int n, int k, Units u,
                                        const RowAddr<NW> &ra) {
@@ -262,22 +266,113 @@ __device__ __forceinline__ int dist_tt(const uint64_t *peq, int m, const uint32_
     const uint32_t ml = lb >= 32 ? ~0u : ((1u << lb) - 1u);
     const uint32_t mh = lb >= 64 ? ~0u : (lb <= 32 ? 0u : ((1u << (lb - 32)) - 1u));
     const char *base = reinterpret_cast<const char *>(peq);
-    int j = 0;
-    uint32_t nxt = n > 0 ? __ldg(txt) : 0u;            // one word ahead
-    for (; j + 4 <= n; j += 4) {
-        const uint32_t w4 = nxt;
-        if (j + 4 < n) nxt = __ldg(txt + ((j >> 2) + 1) * kTileCands);
+    auto col4 = [&](uint32_t w4) {
         column_v<NW>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<0>(w4)), u);
         column_v<NW>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<1>(w4)), u);
         column_v<NW>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<2>(w4)), u);
         column_v<NW>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<3>(w4)), u);
+    };
+    const uint32_t *p = txt;
+    uint32_t w0 = __ldg(p), w1 = __ldg(p + kTileCands), w2 = __ldg(p + 2 * kTileCands),
+             w3 = __ldg(p + 3 * kTileCands);
+    int j = 0;
+    for (; j + 16 <= n; j += 16) {
+        const uint32_t a0 = w0, a1 = w1, a2 = w2, a3 = w3;
+        p += 4 * kTileCands;
+        w0 = __ldg(p);
+        w1 = __ldg(p + kTileCands);
+        w2 = __ldg(p + 2 * kTileCands);
+        w3 = __ldg(p + 3 * kTileCands);
         // the exit test is monotone in j, so testing every 4th column is exact
+        col4(a0);
         if (HASK && hopeless(j + 4 + vsum<NW>(st, ml, mh), j + 3, n, k)) return k + 1;
+        col4(a1);
+        if (HASK && hopeless(j + 8 + vsum<NW>(st, ml, mh), j + 7, n, k)) return k + 1;
+        col4(a2);
+        if (HASK && hopeless(j + 12 + vsum<NW>(st, ml, mh), j + 11, n, k)) return k + 1;
+        col4(a3);
+        if (HASK && hopeless(j + 16 + vsum<NW>(st, ml, mh), j + 15, n, k)) return k + 1;
     }
-    for (uint32_t w4 = nxt; j < n; j++, w4 >>= 8)
-        column_v<NW>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<0>(w4)), u);
+    // up to 15 columns left, in w0..w3
+    const uint32_t rest[4] = {w0, w1, w2, w3};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        if (j + 4 <= n) {
+            col4(rest[q]);
+            if (HASK && hopeless(j + 4 + vsum<NW>(st, ml, mh), j + 3, n, k)) return k + 1;
+            j += 4;
+        } else {
+            for (uint32_t w4 = rest[q]; j < n; j++, w4 >>= 8)
+                column_v<NW>(st, reinterpret_cast<const uint64_t *>(base + ra.template off<0>(w4)), u);
+            break;
+        }
+    }
     const int d = n + vsum<NW>(st, ml, mh);
     return HASK ? cap_k(d, k) : d;
+}
+
+// Exact distances of QI queries (Peq tables consecutive in shared memory,
+// 256 * NW words apart) against one tile-transposed choice: each text word
+// is loaded and each character's row offset computed once for the QI
+// queries, whose column chains are independent (instruction-level
+// parallelism). Queries past `nq` (a partial group) and queries of length 0
+// have all-zero tables and masks, so their result is n, as the exact rule
+// wants for an empty query.
+template <int NW, int QI>
+__device__ __forceinline__ void dist_tt_q(const uint64_t *peq, const int32_t *qlen, int nq, const uint32_t *txt,
+                                          int n, Units u, const RowAddr<NW> &ra, int (&d)[QI]) {
+    Word2 st[QI][NW];
+#pragma unroll
+    for (int i = 0; i < QI; i++)
+#pragma unroll
+        for (int w = 0; w < NW; w++) { st[i][w].pl = st[i][w].ph = ~0u; st[i][w].ml = st[i][w].mh = 0; }
+    const char *base = reinterpret_cast<const char *>(peq);
+    auto col = [&](uint32_t off) {
+#pragma unroll
+        for (int i = 0; i < QI; i++)
+            column_v<NW>(st[i], reinterpret_cast<const uint64_t *>(base + i * (256 * NW * 8) + off), u);
+    };
+    auto col4 = [&](uint32_t w4) {
+        col(ra.template off<0>(w4));
+        col(ra.template off<1>(w4));
+        col(ra.template off<2>(w4));
+        col(ra.template off<3>(w4));
+    };
+    const uint32_t *p = txt;
+    uint32_t w0 = __ldg(p), w1 = __ldg(p + kTileCands), w2 = __ldg(p + 2 * kTileCands),
+             w3 = __ldg(p + 3 * kTileCands);
+    int j = 0;
+    for (; j + 16 <= n; j += 16) {
+        const uint32_t a0 = w0, a1 = w1, a2 = w2, a3 = w3;
+        p += 4 * kTileCands;
+        w0 = __ldg(p);
+        w1 = __ldg(p + kTileCands);
+        w2 = __ldg(p + 2 * kTileCands);
+        w3 = __ldg(p + 3 * kTileCands);
+        col4(a0);
+        col4(a1);
+        col4(a2);
+        col4(a3);
+    }
+    const uint32_t rest[4] = {w0, w1, w2, w3};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        if (j + 4 <= n) {
+            col4(rest[q]);
+            j += 4;
+        } else {
+            for (uint32_t w4 = rest[q]; j < n; j++, w4 >>= 8) col(ra.template off<0>(w4));
+            break;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < QI; i++) {
+        const int m = i < nq ? __ldg(qlen + i) : 0;    // lengths read here, not held through the loop
+        const int lb = m - 64 * (NW - 1);
+        const uint32_t ml = m <= 0 ? 0u : (lb >= 32 ? ~0u : ((1u << lb) - 1u));
+        const uint32_t mh = m <= 0 ? 0u : (lb >= 64 ? ~0u : (lb <= 32 ? 0u : ((1u << (lb - 32)) - 1u)));
+        d[i] = n + vsum<NW>(st[i], ml, mh);
+    }
 }
 
 template <int NW, bool HASK>
