@@ -10,6 +10,8 @@
 
 #include <algorithm>
 #include <array>
+#include <condition_variable>
+#include <functional>
 #include <thread>
 #include <cstdio>
 #include <cstring>
@@ -274,6 +276,82 @@ static bool dtype_ok(int dt) { return dt == BLG_INT32 || dt == BLG_UINT16 || dt 
 // length reaches it. The tile kernel queues every pattern longer than 32
 // (32 < m <= 64 goes to class 0 too); the other pairs kernels queue
 // patterns longer than 64.
+// Persistent host threads for the passes over offsets. Spawning threads per
+// call cost about 0.3 ms on the GPU host (Grace), as much as the pass itself,
+// and the one-call pipeline waits for the pass before its first kernel.
+// run(nt, fn) runs fn(0) on the caller and fn(1..nt-1) on workers, and
+// returns when all are done; calls from several contexts take turns.
+class HostPool {
+public:
+    static HostPool &get() {
+        static HostPool pool;
+        return pool;
+    }
+    int size() const { return (int)workers_.size() + 1; }
+    void run(int nt, const std::function<void(int)> &fn) {
+        nt = std::max(1, std::min(nt, size()));
+        if (nt == 1) {
+            fn(0);
+            return;
+        }
+        std::lock_guard<std::mutex> turn(turn_);
+        {
+            std::lock_guard<std::mutex> g(m_);
+            job_ = &fn;
+            njob_ = nt;
+            remaining_ = nt - 1;
+            gen_++;
+        }
+        cv_.notify_all();
+        fn(0);
+        std::unique_lock<std::mutex> g(m_);
+        done_.wait(g, [&] { return remaining_ == 0; });
+        job_ = nullptr;
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            stop_ = true;
+            gen_++;
+        }
+        cv_.notify_all();
+        for (auto &t : workers_) t.join();
+    }
+
+private:
+    HostPool() {
+        const int n = (int)std::min<unsigned>(8, std::max(1u, std::thread::hardware_concurrency()));
+        for (int i = 1; i < n; i++) workers_.emplace_back([this, i] { loop(i); });
+    }
+    void loop(int idx) {
+        uint64_t seen = 0;
+        while (true) {
+            const std::function<void(int)> *job;
+            int nj;
+            {
+                std::unique_lock<std::mutex> g(m_);
+                cv_.wait(g, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+                job = job_;
+                nj = njob_;
+            }
+            if (idx < nj) {
+                (*job)(idx);
+                std::lock_guard<std::mutex> g(m_);
+                if (--remaining_ == 0) done_.notify_one();
+            }
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex m_, turn_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)> *job_ = nullptr;
+    int njob_ = 0, remaining_ = 0;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
+
 static int pairs_classify(blg_ctx *c, const int64_t *oa, const int64_t *ob, int64_t n, blg_pairs *p) {
     int rc = check_offsets_host(c, oa, n);
     if (!rc) rc = check_offsets_host(c, ob, n);
@@ -283,7 +361,7 @@ static int pairs_classify(blg_ctx *c, const int64_t *oa, const int64_t *ob, int6
     p->len_max_side = n > 0 ? std::max(oa[n] - oa[0], ob[n] - ob[0]) : 0;
     // the pass reads 16 bytes of offsets per pair: large sets are split
     // over host threads
-    const int nt = n >= (1 << 20) ? (int)std::min<unsigned>(8, std::max(1u, std::thread::hardware_concurrency())) : 1;
+    const int nt = n >= (1 << 17) ? HostPool::get().size() : 1;
     std::vector<std::array<int64_t, kLongClasses + 2>> part(nt);
     auto work = [&](int t) {
         std::array<int64_t, kLongClasses + 2> h{};
@@ -305,14 +383,8 @@ static int pairs_classify(blg_ctx *c, const int64_t *oa, const int64_t *ob, int6
         h[kLongClasses + 1] = shorts;
         part[t] = h;
     };
-    if (nt == 1) {
-        work(0);
-    } else {
-        std::vector<std::thread> th;
-        for (int t = 1; t < nt; t++) th.emplace_back(work, t);
-        work(0);
-        for (auto &x : th) x.join();
-    }
+    if (nt == 1) work(0);
+    else HostPool::get().run(nt, work);
     p->short_pairs = 0;
     for (int t = 0; t < nt; t++) {
         for (int j = 0; j <= kLongClasses; j++) hist[j] += part[t][j];
@@ -620,13 +692,20 @@ static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64
 
 // Choices: the packed strings, a length-sorted copy (thresholded runs) and
 // the tile-transposed form (exact runs).
-static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s) {
+// What a search needs beside the choices themselves: the length-sorted copy
+// with sketches (survivor kernels of max_dist runs) and the tile-transposed
+// copy (exact and plain-order runs). A resident search set builds both; a
+// one-call search knows its max_dist and schedule and builds one.
+enum { NEED_SORTED = 1, NEED_TT = 2, NEED_ALL = 3 };
+
+static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s,
+                                 unsigned need = NEED_ALL) {
     s->nc = nc;
     int rc = upload_strings(c, bc, oc, nc, s->c);
     if (rc) return rc;
     // Choices sorted by length (counting sort on the host, byte gather on the
     // device), when the length range is moderate.
-    if (nc > 0) {
+    if (nc > 0 && (need & NEED_SORTED)) {
         int64_t mn = INT64_MAX, mx = 0;
         for (int64_t i = 0; i < nc; i++) {
             const int64_t l = oc[i + 1] - oc[i];
@@ -675,7 +754,7 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
     // Tile-transposed choices: padded size = sum over tiles of kTileCands x
     // the tile's longest choice; kept when at most twice the packed bytes
     // (plus 64 MiB), so a few long choices cannot blow up the copy.
-    if (nc > 0) {
+    if (nc > 0 && (need & NEED_TT)) {
         const int64_t tiles = (nc + kTileCands - 1) / kTileCands;
         std::vector<int64_t> base(tiles + 1, 0);
         for (int64_t t = 0; t < tiles; t++) {
@@ -724,8 +803,9 @@ static int search_upload_queries(blg_ctx *c, const uint8_t *bq, const int64_t *o
 static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq, const uint8_t *bc,
                            const int64_t *oc, int64_t nc, int k, int dtype, void *out_host, void *d_out,
                            blg_search *s) {
+    const bool surv = k >= 0 && c->sched != BLG_SCHED_PLAIN;      // the survivor kernels run (search_run)
     int rc = search_upload_queries(c, bq, oq, nq, s);
-    if (!rc) rc = search_upload_choices(c, bc, oc, nc, s);
+    if (!rc) rc = search_upload_choices(c, bc, oc, nc, s, surv ? NEED_SORTED : NEED_TT);
     if (rc) return rc;
     const size_t row = dtype_size(dtype) * (size_t)nc;
     const int nch = (int)std::min<int64_t>(8, nq);
