@@ -414,6 +414,52 @@ class BatchBench:
         return bool(np.array_equal(o.get(), oracle.saturate(oracle.cross(p.q, p.c, p.max_dist), p.dtype)))
 
 
+def matches_leg(bench, ctx, pin, flush, args):
+    """The same thresholded search in its matches-only form (records of the
+    pairs with d <= max_dist, sorted): kernel-only through a resident
+    search (blg_search_matches, records left in HBM, the count read back)
+    and one-call from pinned host buffers (blg_cdist_matches)."""
+    k = bench.runs[0][0]
+    if k is None or bench.kind != "cdist":
+        return None
+    start, stop = device_timer(ctx)
+    n = bench.batch.matches_into(bench.batch.match_buffer(1), k)
+    buf = bench.batch.match_buffer(max(n, 1))
+    for _ in range(3):
+        bench.batch.matches_into(buf, k)
+    t = []
+    for _ in range(max(3, min(args.steps, 10))):
+        flush_l2(ctx, flush)
+        start()
+        bench.batch.matches_into(buf, k)
+        t.append(stop())
+    ms = statistics.median(t)
+    (bq, oq), (bc, oc) = bench._pq, bench._pc
+    rec = pin.empty((max(n, 1),), gpu.MATCH_DTYPE)
+    cnt = ctypes.c_int64()
+
+    def call():
+        ctx.check(ctx.lib.blg_cdist_matches(ctx.h, bq.ctypes.data, oq.ctypes.data, bench.w.nq, bc.ctypes.data,
+                                            oc.ctypes.data, bench.w.nc, k, rec.ctypes.data, rec.shape[0],
+                                            ctypes.byref(cnt)))
+    for _ in range(3):
+        call()
+    e = []
+    for _ in range(max(3, min(args.steps, 10))):
+        t0 = time.perf_counter()
+        call()
+        e.append(time.perf_counter() - t0)
+    e_s = statistics.median(e)
+    assert cnt.value == n
+    h2d, _ = bench.io_bytes(0)
+    return {"matches": int(n), "record_bytes": gpu.MATCH_DTYPE.itemsize,
+            "value": bench.pairs / (ms / 1e3), "unit": "pairs/s", "ms_per_step": ms,
+            "e2e": {"value": bench.pairs / e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": int(n) * gpu.MATCH_DTYPE.itemsize + 8,
+                    "path": "blg_cdist_matches, pinned host buffers, wall clock"},
+            "path": "blg_search_matches on the resident search: dense scratch, count, compaction; CUDA events"}
+
+
 def exit_columns(bench, sample_rows_or_n):
     """Oracle trace (columns processed under the reference's exit rule) on the
     CPU sample, scaled to the full workload — algorithmic ops for max_dist runs."""
@@ -601,6 +647,7 @@ def run_ours(args, ranks: Ranks):
         e2e_t.append(time.perf_counter() - t0)
     e2e_s = ranks.max(statistics.median(e2e_t))
     h2d, d2h = bench.io_bytes(0)
+    matches = matches_leg(bench, ctx, pin, flush, args)
     pin.free()
 
     result = {
@@ -617,6 +664,8 @@ def run_ours(args, ranks: Ranks):
         "gpu_launches": int(launches), "wall_s_timed_region": wall, "scheduler": sched_info, "tuning": tune,
         "clocks": clk, "runs": extra_runs, "kernels": kstats,
     }
+    if matches:
+        result["matches"] = matches
     if args.config in H100_REF:
         ref, src = H100_REF[args.config]
         result["vs_baseline"] = value / ref

@@ -53,6 +53,8 @@ SIGNATURES = [
     ("blg_sched_load", ctypes.c_int, [_P, ctypes.c_char_p]),
     ("blg_malloc", ctypes.c_int, [_P, _SZ, ctypes.POINTER(_P)]),
     ("blg_free", ctypes.c_int, [_P, _P]),
+    ("blg_cdist_matches", ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _I64, _I32, _P, _I64, ctypes.POINTER(_I64)]),
+    ("blg_search_matches", ctypes.c_int, [_P, _P, _I32, _P, _I64, ctypes.POINTER(_I64)]),
     ("blg_host_alloc", ctypes.c_int, [_P, _SZ, ctypes.POINTER(_P)]),
     ("blg_host_free", ctypes.c_int, [_P, _P]),
     ("blg_memcpy_h2d", ctypes.c_int, [_P, _P, _P, _SZ]),

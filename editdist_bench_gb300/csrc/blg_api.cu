@@ -44,6 +44,10 @@ cudaError_t launch_pairs_long(cudaStream_t st, int grid, bool hask, const LongQu
 cudaError_t launch_pairs_staged(cudaStream_t st, int sms, bool hask, const DevStrings &A, const DevStrings &B,
                                 int k, int dtype, void *out, const LongQueue &q, uint32_t *status);
 cudaError_t launch_fill(cudaStream_t st, int sms, void *out, int64_t n, int dtype, uint32_t v);
+cudaError_t launch_match_compact(cudaStream_t st, int sms, int dtype, const void *dense, int64_t n, int k,
+                                 int64_t *counts, int64_t *total, int64_t nc, int64_t row0, blg_match *out,
+                                 int64_t capacity, bool emit);
+int64_t match_blocks(int64_t n);
 cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, const DevStrings &A,
                               const DevStrings &B, int tile_pairs, int k, int dtype, void *out, const LongQueue &q,
                               uint32_t *status);
@@ -958,6 +962,55 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
     return BLG_OK;
 }
 
+// ---- matches-only search
+// Dense scratch element type of a threshold k: the narrowest holding k + 1.
+static int match_dtype(int k) { return k <= 254 ? BLG_UINT8 : k <= 65534 ? BLG_UINT16 : BLG_INT32; }
+
+// Rows [q0, q1) of search s (classes built for them) into the dense scratch
+// (row q0 at its start), then the compaction: the chunk's match total comes
+// back to the host (*total); up to `cap` records go to d_out (device) when
+// d_out is given — or, when it is not, to a device buffer allocated for the
+// chunk and copied to host_out. Synchronises once per call.
+static int search_matches_rows(blg_ctx *c, blg_search *s, int k, int64_t q0, int64_t q1, void *scratch,
+                               blg_match *d_out, blg_match *host_out, int64_t cap, int64_t *total) {
+    const int sdt = match_dtype(k);
+    const size_t es = dtype_size(sdt);
+    const int64_t n = (q1 - q0) * s->nc;
+    *total = 0;
+    if (n <= 0) return BLG_OK;
+    // the search writes absolute rows: offset the base so row q0 lands at the scratch's start
+    uint8_t *base = (uint8_t *)scratch - (size_t)q0 * (size_t)s->nc * es;
+    int rc = search_run(c, s, k, sdt, base, q0, q1);
+    if (rc) return rc;
+    int64_t *counts = nullptr;
+    CK(dev_alloc(c, (void **)&counts, sizeof(int64_t) * (size_t)(match_blocks(n) + 1)), "cudaMallocAsync(match counts)");
+    int64_t *d_total = counts + match_blocks(n);
+    CK(launch(c, "match_count", [&] {
+           return launch_match_compact(c->stream, c->sms, sdt, scratch, n, k, counts, d_total, s->nc, q0, nullptr, 0,
+                                       false);
+       }), "match_count");
+    int64_t tot = 0;
+    CK(cudaMemcpyAsync(&tot, d_total, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream), "D2H match total");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    *total = tot;
+    const int64_t m = std::min(tot, cap);
+    if (m > 0) {
+        blg_match *dst = d_out;
+        if (!dst) CK(dev_alloc(c, (void **)&dst, sizeof(blg_match) * (size_t)m), "cudaMallocAsync(matches)");
+        CK(launch(c, "match_emit", [&] {
+               return launch_match_compact(c->stream, c->sms, sdt, scratch, n, k, counts, d_total, s->nc, q0, dst, m,
+                                           true);
+           }), "match_emit");
+        if (!d_out) {
+            CK(cudaMemcpyAsync(host_out, dst, sizeof(blg_match) * (size_t)m, cudaMemcpyDeviceToHost, c->stream),
+               "D2H matches");
+            dev_free(c, dst);
+        }
+    }
+    dev_free(c, counts);
+    return BLG_OK;
+}
+
 static void search_release(blg_ctx *c, blg_search *s) {
     free_strings(c, s->q);
     free_strings(c, s->c);
@@ -1721,6 +1774,66 @@ int blg_cdist(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq, cons
         return rc2;
     }
     if (out_device) *out_device = d_out;
+    return BLG_OK;
+}
+
+int blg_search_matches(blg_ctx *c, blg_search *s, int32_t max_dist, blg_match *d_out, int64_t capacity,
+                       int64_t *count) {
+    ENTER(c);
+    if (!s || !count) return fail(c, BLG_ERR_ARG, "null search or count");
+    if (max_dist < 0) return fail(c, BLG_ERR_ARG, "matches need max_dist >= 0");
+    if (capacity < 0 || (capacity > 0 && !d_out)) return fail(c, BLG_ERR_ARG, "bad match buffer");
+    *count = 0;
+    if (s->nq == 0 || s->nc == 0) return BLG_OK;
+    void *scratch = nullptr;
+    CK(dev_alloc(c, &scratch, dtype_size(match_dtype(max_dist)) * (size_t)s->nq * (size_t)s->nc),
+       "cudaMallocAsync(match scratch)");
+    int64_t total = 0;
+    int rc = search_matches_rows(c, s, max_dist, 0, s->nq, scratch, d_out, nullptr, capacity, &total);
+    dev_free(c, scratch);
+    const int rc2 = sync_and_status(c);
+    if (rc) return rc;
+    if (rc2) return rc2;
+    *count = total;
+    return BLG_OK;
+}
+
+int blg_cdist_matches(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq, const uint8_t *bc,
+                      const int64_t *oc, int64_t nc, int32_t max_dist, blg_match *out, int64_t capacity,
+                      int64_t *count) {
+    ENTER(c);
+    if (!count) return fail(c, BLG_ERR_ARG, "null count");
+    if (max_dist < 0) return fail(c, BLG_ERR_ARG, "matches need max_dist >= 0");
+    if (nq < 0 || nc < 0) return fail(c, BLG_ERR_ARG, "negative count");
+    if (capacity < 0 || (capacity > 0 && !out)) return fail(c, BLG_ERR_ARG, "bad match buffer");
+    *count = 0;
+    if (nq == 0 || nc == 0) return BLG_OK;
+    blg_search s;
+    const bool surv = c->sched != BLG_SCHED_PLAIN;
+    int rc = search_upload_queries(c, bq, oq, nq, &s);
+    if (!rc) rc = search_upload_choices(c, bc, oc, nc, &s, surv ? NEED_SORTED : NEED_TT);
+    // query rows in chunks whose dense scratch stays within 1 GiB
+    const size_t row = dtype_size(match_dtype(max_dist)) * (size_t)nc;
+    const int64_t rows = std::max<int64_t>(1, std::min<int64_t>(nq, (int64_t)((size_t(1) << 30) / row)));
+    void *scratch = nullptr;
+    if (!rc && dev_alloc(c, &scratch, row * (size_t)rows) != cudaSuccess)
+        rc = fail(c, BLG_ERR_ALLOC, "cudaMallocAsync(match scratch)");
+    int64_t total = 0;
+    for (int64_t q0 = 0; q0 < nq && !rc; q0 += rows) {
+        const int64_t q1 = std::min(nq, q0 + rows);
+        rc = search_build_classes(c, oq, q0, q1, &s);
+        int64_t t = 0;
+        const int64_t written = std::min(total, capacity);
+        if (!rc) rc = search_matches_rows(c, &s, max_dist, q0, q1, scratch, nullptr, out + written,
+                                          capacity - written, &t);
+        total += t;
+    }
+    dev_free(c, scratch);
+    search_release(c, &s);
+    const int rc2 = sync_and_status(c);
+    if (rc) return rc;
+    if (rc2) return rc2;
+    *count = total;
     return BLG_OK;
 }
 

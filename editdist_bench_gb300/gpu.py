@@ -98,6 +98,46 @@ def cdist_packed(pq, pc, max_dist=None, dtype=np.int32, return_device: bool = Fa
     return out
 
 
+# one record of blg_cdist_matches / blg_search_matches (include/bitlev_gb300.h: blg_match)
+MATCH_DTYPE = np.dtype([("query", "<i8"), ("choice", "<i8"), ("dist", "<i4"), ("reserved", "<i4")])
+
+
+def _match_k(max_dist) -> int:
+    k = check_k(max_dist)
+    if k < 0:
+        raise ValueError("matches need a max_dist (>= 0); the exact result is the dense cdist")
+    return k
+
+
+def cdist_matches_packed(pq, pc, max_dist, capacity: int | None = None):
+    """Every (query, choice) with d(q, c) <= max_dist, sorted by (query,
+    choice): arrays (query, choice, dist). Packed inputs. The records are
+    found on the GPU; only they cross to the host, not the nq x nc matrix."""
+    (bq, oq), (bc, oc) = _packed(pq), _packed(pc)
+    nq, nc = len(oq) - 1, len(oc) - 1
+    k = _match_k(max_dist)
+    ctx = _lib.context()
+    cap = capacity if capacity is not None else min(max(nq, nc, 1) * 4, nq * nc, 1 << 20)
+    while True:
+        rec = np.empty(max(cap, 0), dtype=MATCH_DTYPE)
+        cnt = ctypes.c_int64()
+        ctx.check(ctx.lib.blg_cdist_matches(ctx.h, bq.ctypes.data, oq.ctypes.data, nq, bc.ctypes.data,
+                                            oc.ctypes.data, nc, k, rec.ctypes.data if cap else None, cap,
+                                            ctypes.byref(cnt)), "cdist_matches")
+        if cnt.value <= cap or capacity is not None:
+            rec = rec[:min(cnt.value, cap)]
+            return rec["query"].copy(), rec["choice"].copy(), rec["dist"].copy()
+        cap = cnt.value
+
+
+def cdist_matches(queries, choices, max_dist, capacity: int | None = None):
+    """(query, choice, dist) of every pair within max_dist — the matches-only
+    form of cdist(queries, choices, max_dist)."""
+    q, c = as_list(queries), as_list(choices)
+    _match_k(max_dist)
+    return cdist_matches_packed(pack(q), pack(c), max_dist, capacity)
+
+
 def pairwise(a, b, max_dist=None, dtype=np.int32, return_device: bool = False):
     """out[i] = d(a[i], b[i]) on the GPU (bitlev/gpu.py:71-103)."""
     a, b = as_list(a), as_list(b)
@@ -178,6 +218,32 @@ class SearchBatch:
         self.ctx.check(self.ctx.lib.blg_search_run(self.ctx.h, self.h, k, DTYPE_CODE[out.dtype],
                                                    out.ptr), "search_run")
         return out
+
+    def match_buffer(self, capacity: int) -> DeviceArray:
+        """Device room for `capacity` match records."""
+        p = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.blg_malloc(self.ctx.h, max(1, capacity * MATCH_DTYPE.itemsize),
+                                               ctypes.byref(p)), "malloc")
+        return DeviceArray(p.value, (capacity,), MATCH_DTYPE, self.ctx)
+
+    def matches_into(self, buf: DeviceArray, max_dist) -> int:
+        """Match records (d <= max_dist, sorted by (query, choice)) into the
+        device buffer; returns the total number of matches (records past the
+        buffer's length are not written)."""
+        cnt = ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.blg_search_matches(self.ctx.h, self.h, _match_k(max_dist), buf.ptr,
+                                                       buf.shape[0], ctypes.byref(cnt)), "search_matches")
+        return cnt.value
+
+    def matches(self, max_dist):
+        """(query, choice, dist) arrays of every pair within max_dist."""
+        buf = self.match_buffer(1 << 16)
+        n = self.matches_into(buf, max_dist)
+        if n > buf.shape[0]:
+            buf = self.match_buffer(n)
+            n = self.matches_into(buf, max_dist)
+        rec = buf.get()[:n]
+        return rec["query"].copy(), rec["choice"].copy(), rec["dist"].copy()
 
     def __del__(self):
         if getattr(self, "h", None) and self.h.value:

@@ -98,6 +98,28 @@ int blg_search_upload(blg_ctx *ctx, const uint8_t *buf_q, const int64_t *off_q, 
 int blg_search_run(blg_ctx *ctx, blg_search *s, int32_t max_dist, int32_t dtype, void *d_out);
 void blg_search_free(blg_ctx *ctx, blg_search *s);
 
+/* Matches-only thresholded search: every (query, choice) with distance
+ * <= max_dist, as records sorted by (query, choice), instead of the dense
+ * nq*nc matrix. No counterpart in the reference, which names it as what
+ * fuzzy search usually wants (README.md:319-321). max_dist >= 0 (a dense
+ * result is the exact case). At most `capacity` records are written; *count
+ * receives the total number of matches either way, so a caller whose buffer
+ * was too small can call again with *count records of room.
+ * blg_cdist_matches: host inputs, records in host memory (`out`).
+ * blg_search_matches: a resident search, records in device memory (`d_out`);
+ * synchronises (the count comes back to the host). */
+typedef struct {
+    int64_t query;
+    int64_t choice;
+    int32_t dist;
+    int32_t reserved;      /* 0 */
+} blg_match;
+int blg_cdist_matches(blg_ctx *ctx, const uint8_t *buf_q, const int64_t *off_q, int64_t nq,
+                      const uint8_t *buf_c, const int64_t *off_c, int64_t nc, int32_t max_dist,
+                      blg_match *out, int64_t capacity, int64_t *count);
+int blg_search_matches(blg_ctx *ctx, blg_search *s, int32_t max_dist, blg_match *d_out, int64_t capacity,
+                       int64_t *count);
+
 /* Many independent cdist problems (host inputs, device outputs — the
  * return_device form), run by one persistent kernel that pulls
  * (problem, query, 1024-choice) tiles from a device work counter; the batch's

@@ -1,0 +1,91 @@
+"""Matches-only thresholded search (blg_cdist_matches / blg_search_matches):
+the records are exactly the oracle's pairs with d <= max_dist, sorted by
+(query, choice), with their distances; capacity truncation reports the full
+count; every scratch width (uint8 / uint16 / int32 by max_dist) and every
+schedule gives the same records."""
+import numpy as np
+import pytest
+
+import oracle
+from editdist_bench_gb300 import gpu, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _want(q, c, k):
+    d = oracle.cross(q, c, k)
+    qi, ci = np.nonzero(d <= k)                 # row-major: sorted by (query, choice)
+    return qi, ci, d[qi, ci]
+
+
+def _check(got, want):
+    for g, w, name in zip(got, want, ("query", "choice", "dist")):
+        np.testing.assert_array_equal(np.asarray(g, dtype=np.int64), np.asarray(w, dtype=np.int64), err_msg=name)
+
+
+@pytest.mark.parametrize("k", [0, 1, 3, 8, 31, 40])
+def test_matches_equal_oracle(k):
+    rng = np.random.default_rng(100 + k)
+    q = W.random_strings(rng, rng.integers(0, 200, 37))
+    c = W.concat(W.mutate(rng, W.take(q, rng.integers(0, 37, 300)), rng.uniform(0, 0.2, 300)),
+                 W.random_strings(rng, rng.integers(0, 220, 900)))
+    want = _want(q, c, k)
+    assert len(want[0]) > 0
+    _check(gpu.cdist_matches_packed(q, c, k), want)
+    s = gpu.SearchBatch(q, c)
+    _check(s.matches(k), want)
+
+
+def test_matches_config4_shape():
+    w = W.config4(nq=48, nc=1 << 15, seed=9)
+    want = _want(w.q, w.c, 4)
+    _check(gpu.cdist_matches_packed(w.q, w.c, 4), want)
+
+
+@pytest.mark.parametrize("k", [300, 70000])
+def test_matches_wide_thresholds(k):
+    """k > 254 uses a uint16 scratch, k > 65534 an int32 one."""
+    rng = np.random.default_rng(7)
+    q = W.random_strings(rng, rng.integers(0, 400, 9))
+    c = W.random_strings(rng, rng.integers(0, 700, 200))
+    _check(gpu.cdist_matches_packed(q, c, k), _want(q, c, k))
+
+
+def test_matches_capacity_reports_total():
+    rng = np.random.default_rng(8)
+    q = W.random_strings(rng, rng.integers(1, 40, 20))
+    c = W.concat(q, W.mutate(rng, q, 0.1))
+    want = _want(q, c, 5)
+    n = len(want[0])
+    assert n > 10
+    part = gpu.cdist_matches_packed(q, c, 5, capacity=7)
+    _check(part, tuple(x[:7] for x in want))
+    s = gpu.SearchBatch(q, c)
+    buf = s.match_buffer(5)
+    assert s.matches_into(buf, 5) == n
+    rec = buf.get()
+    np.testing.assert_array_equal(rec["query"], want[0][:5])
+    np.testing.assert_array_equal(rec["choice"], want[1][:5])
+
+
+@pytest.mark.parametrize("sched", ["auto", "plain", "learned"])
+def test_matches_every_schedule(sched):
+    w = W.config4(nq=16, nc=1 << 13, seed=10)
+    want = _want(w.q, w.c, 4)
+    gpu.set_schedule(sched)
+    try:
+        _check(gpu.cdist_matches_packed(w.q, w.c, 4), want)
+    finally:
+        gpu.set_schedule("auto")
+
+
+def test_matches_edges():
+    rng = np.random.default_rng(11)
+    q = W.random_strings(rng, np.array([0, 0, 3]))
+    c = W.random_strings(rng, np.array([0, 1, 2, 5]))
+    _check(gpu.cdist_matches_packed(q, c, 2), _want(q, c, 2))
+    empty = W.random_strings(rng, np.array([], dtype=np.int64))
+    got = gpu.cdist_matches_packed(empty, c, 2)
+    assert all(len(x) == 0 for x in got)
+    with pytest.raises(ValueError):
+        gpu.cdist_matches_packed(q, c, None)
