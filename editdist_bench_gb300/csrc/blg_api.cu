@@ -71,6 +71,8 @@ int sched_train_rows(blg_ctx *c, blg_sched_model *m, half *x, float *y, const in
                      int epochs, float lr, int batch, float *loss_out);
 bool sched_model_trained(const blg_sched_model *m);
 namespace blg {
+cudaError_t launch_sorted_offsets(cudaStream_t st, int sms, const int64_t *lstart, int64_t n_len, int64_t min_len,
+                                  const int64_t *bstart, int64_t n, int64_t *soff);
 cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &src, const int32_t *perm,
                                   const int64_t *dst_off, uint8_t *dst, int64_t n, uint32_t *status);
 cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S, uint64_t *sketch, uint32_t *status);
@@ -696,6 +698,24 @@ static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64
 
 // Choices: the packed strings, a length-sorted copy (thresholded runs) and
 // the tile-transposed form (exact runs).
+// Pinned host room for `bytes` of host-built data on its way to the device:
+// the context's staging buffer, grown when needed, after the last copy out
+// of it has finished.
+static void *host_stage(blg_ctx *c, size_t bytes) {
+    if (c->stage_done) cudaEventSynchronize(c->stage_done);
+    if (bytes > c->stage_bytes) {
+        const size_t want = std::max(bytes, c->stage_bytes * 2);
+        if (c->stage) cudaFreeHost(c->stage);
+        c->stage = nullptr;
+        c->stage_bytes = 0;
+        if (cudaHostAlloc(&c->stage, want, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+        c->stage_bytes = want;
+    }
+    if (!c->stage_done && cudaEventCreateWithFlags(&c->stage_done, cudaEventDisableTiming) != cudaSuccess)
+        return nullptr;
+    return c->stage;
+}
+
 // What a search needs beside the choices themselves: the length-sorted copy
 // with sketches (survivor kernels of max_dist runs) and the tile-transposed
 // copy (exact and plain-order runs). A resident search set builds both; a
@@ -707,36 +727,75 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
     s->nc = nc;
     int rc = upload_strings(c, bc, oc, nc, s->c);
     if (rc) return rc;
-    // Choices sorted by length (counting sort on the host, byte gather on the
-    // device), when the length range is moderate.
-    if (nc > 0 && (need & NEED_SORTED)) {
-        int64_t mn = INT64_MAX, mx = 0;
-        for (int64_t i = 0; i < nc; i++) {
-            const int64_t l = oc[i + 1] - oc[i];
-            mn = std::min(mn, l);
-            mx = std::max(mx, l);
-        }
-        if (mx - mn < (1 << 22) && nc < INT32_MAX) {
+    // Choices sorted by length (a stable counting sort on the host's thread
+    // pool, the byte gather on the device), when the length range is
+    // moderate. Every string of a length bucket has the bucket's length, so
+    // the sorted offsets follow from the bucket starts: the device computes
+    // them, and only the permutation (pinned) and the bucket tables travel.
+    if (nc > 0 && (need & NEED_SORTED) && nc < INT32_MAX) {
+        HostPool &pool = HostPool::get();
+        const int nt = nc >= (1 << 16) ? pool.size() : 1;
+        auto lo_of = [&](int t, int parts) { return nc * t / parts; };
+        std::vector<int64_t> tmn(nt, INT64_MAX), tmx(nt, 0);
+        pool.run(nt, [&](int t) {
+            int64_t a = INT64_MAX, b = 0;
+            for (int64_t i = lo_of(t, nt), e = lo_of(t + 1, nt); i < e; i++) {
+                const int64_t l = oc[i + 1] - oc[i];
+                a = std::min(a, l);
+                b = std::max(b, l);
+            }
+            tmn[t] = a;
+            tmx[t] = b;
+        });
+        const int64_t mn = *std::min_element(tmn.begin(), tmn.end()), mx = *std::max_element(tmx.begin(), tmx.end());
+        if (mx - mn < (1 << 22)) {
             const int64_t n_len = mx - mn + 1;
-            std::vector<int64_t> lstart(n_len + 1, 0);
-            for (int64_t i = 0; i < nc; i++) lstart[oc[i + 1] - oc[i] - mn + 1]++;
-            for (int64_t r = 0; r < n_len; r++) lstart[r + 1] += lstart[r];
-            std::vector<int64_t> fillp(lstart.begin(), lstart.end() - 1);
-            std::vector<int32_t> perm(nc);
-            for (int64_t i = 0; i < nc; i++) perm[fillp[oc[i + 1] - oc[i] - mn]++] = (int32_t)i;
-            std::vector<int64_t> soff(nc + 1, 0);
-            for (int64_t i = 0; i < nc; i++) soff[i + 1] = soff[i] + (oc[perm[i] + 1] - oc[perm[i]]);
-            const int64_t bytes = soff[nc];
+            // per-thread histograms [thread][bucket] while they stay small
+            const int nh = n_len * nt <= (1 << 22) ? nt : 1;
+            std::vector<int64_t> hist((size_t)(n_len * nh), 0);
+            pool.run(nh, [&](int t) {
+                int64_t *h = hist.data() + (size_t)t * n_len;
+                for (int64_t i = lo_of(t, nh), e = lo_of(t + 1, nh); i < e; i++) h[oc[i + 1] - oc[i] - mn]++;
+            });
+            // bucket starts; each thread's cursor per bucket after the lower threads (stable)
+            std::vector<int64_t> lstart(n_len + 1, 0), bstart(n_len, 0);
+            int64_t run = 0, bytes = 0;
+            for (int64_t b = 0; b < n_len; b++) {
+                lstart[b] = run;
+                bstart[b] = bytes;
+                for (int t = 0; t < nh; t++) {
+                    const int64_t cnt = hist[(size_t)t * n_len + b];
+                    hist[(size_t)t * n_len + b] = run;
+                    run += cnt;
+                }
+                bytes += (run - lstart[b]) * (b + mn);
+            }
+            lstart[n_len] = run;
+            int32_t *perm = (int32_t *)host_stage(c, sizeof(int32_t) * (size_t)nc);
+            if (!perm) return fail(c, BLG_ERR_ALLOC, "cudaHostAlloc(staging)");
+            pool.run(nh, [&](int t) {
+                int64_t *cur = hist.data() + (size_t)t * n_len;
+                for (int64_t i = lo_of(t, nh), e = lo_of(t + 1, nh); i < e; i++)
+                    perm[cur[oc[i + 1] - oc[i] - mn]++] = (int32_t)i;
+            });
             OwnedStrings &cs = s->cs;
-            CK(dev_alloc(c, &cs.mem_buf, (size_t)bytes + kSlackBefore + kSlackAfter), "cudaMallocAsync(sorted choices)");
-            CK(cudaMemsetAsync(cs.mem_buf, 0, (size_t)bytes + kSlackBefore + kSlackAfter, c->stream),
-               "memset sorted choices");
-            CK(dev_alloc(c, &cs.mem_off, sizeof(int64_t) * (size_t)(nc + 1)), "cudaMallocAsync(sorted offsets)");
-            CK(cudaMemcpyAsync(cs.mem_off, soff.data(), sizeof(int64_t) * (nc + 1), cudaMemcpyHostToDevice, c->stream), "H2D soff");
             CK(dev_alloc(c, (void **)&s->perm, sizeof(int32_t) * nc), "cudaMallocAsync(perm)");
-            CK(cudaMemcpyAsync(s->perm, perm.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice, c->stream), "H2D perm");
+            CK(cudaMemcpyAsync(s->perm, perm, sizeof(int32_t) * nc, cudaMemcpyHostToDevice, c->stream), "H2D perm");
+            CK(cudaEventRecord(c->stage_done, c->stream), "event");
             CK(dev_alloc(c, (void **)&s->lstart, sizeof(int64_t) * (n_len + 1)), "cudaMallocAsync(lstart)");
             CK(cudaMemcpyAsync(s->lstart, lstart.data(), sizeof(int64_t) * (n_len + 1), cudaMemcpyHostToDevice, c->stream), "H2D lstart");
+            int64_t *d_bstart = nullptr;
+            CK(dev_alloc(c, (void **)&d_bstart, sizeof(int64_t) * n_len), "cudaMallocAsync(bstart)");
+            CK(cudaMemcpyAsync(d_bstart, bstart.data(), sizeof(int64_t) * n_len, cudaMemcpyHostToDevice, c->stream), "H2D bstart");
+            CK(dev_alloc(c, &cs.mem_off, sizeof(int64_t) * (size_t)(nc + 1)), "cudaMallocAsync(sorted offsets)");
+            CK(launch(c, "sorted_offsets", [&] {
+                   return launch_sorted_offsets(c->stream, c->sms, s->lstart, n_len, mn, d_bstart, nc,
+                                                (int64_t *)cs.mem_off);
+               }), "sorted_offsets");
+            dev_free(c, d_bstart);
+            CK(dev_alloc(c, &cs.mem_buf, (size_t)bytes + kSlackBefore + kSlackAfter), "cudaMallocAsync(sorted choices)");
+            CK(cudaMemsetAsync(cs.mem_buf, 0, kSlackBefore, c->stream), "memset slack");
+            CK(cudaMemsetAsync((uint8_t *)cs.mem_buf + kSlackBefore + bytes, 0, kSlackAfter, c->stream), "memset slack");
             s->h_lstart = lstart;
             cs.d.buf = (uint8_t *)cs.mem_buf + kSlackBefore;
             cs.d.off = (const int64_t *)cs.mem_off;
@@ -761,12 +820,17 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
     if (nc > 0 && (need & NEED_TT)) {
         const int64_t tiles = (nc + kTileCands - 1) / kTileCands;
         std::vector<int64_t> base(tiles + 1, 0);
-        for (int64_t t = 0; t < tiles; t++) {
-            int64_t mx = 0;
-            const int64_t e = std::min(nc, (t + 1) * kTileCands);
-            for (int64_t i = t * kTileCands; i < e; i++) mx = std::max(mx, oc[i + 1] - oc[i]);
-            base[t + 1] = base[t] + kTileCands * ((mx + 3) / 4);
-        }
+        HostPool &pool = HostPool::get();
+        const int nt = nc >= (1 << 16) ? pool.size() : 1;
+        pool.run(nt, [&](int w) {                               // each tile's longest choice
+            for (int64_t t = tiles * w / nt, te = tiles * (w + 1) / nt; t < te; t++) {
+                int64_t mx = 0;
+                const int64_t e = std::min(nc, (t + 1) * kTileCands);
+                for (int64_t i = t * kTileCands; i < e; i++) mx = std::max(mx, oc[i + 1] - oc[i]);
+                base[t + 1] = kTileCands * ((mx + 3) / 4);
+            }
+        });
+        for (int64_t t = 0; t < tiles; t++) base[t + 1] += base[t];
         const int64_t bytes = oc[nc] - oc[0];
         if (base[tiles] * 4 <= 2 * bytes + (64ll << 20)) {
             // + kTtSlackRows rows: the search loop prefetches up to 4 words past a choice's end
@@ -1298,15 +1362,20 @@ static int tune_exact_search(blg_ctx *c, int nw) {
     return rc;
 }
 
+// The survivor kernel's CTAs per SM and job size, on a search big enough
+// that the run-time job size (survivor_job_size) keeps the candidate job
+// sizes: 512 queries x 2^19 choices (about 15 M survivors at max_dist 4).
+// A smaller search had its jobs halved at run time whatever the candidate,
+// so the choice was noise, and config-4-sized runs paid for it (up to 14%).
 static int tune_threshold_search(blg_ctx *c) {
     Rng r{0x2545F4914F6CDD1Dull};
     Packed q, ch;
     std::vector<std::vector<uint8_t>> qs;
-    for (int i = 0; i < 128; i++) {
+    for (int i = 0; i < 512; i++) {
         qs.push_back(dna(r, 100 + (int)(r.next() % 157)));
         q.add(qs.back());
     }
-    for (int i = 0; i < 262144; i++) {
+    for (int i = 0; i < (1 << 19); i++) {
         if (r.uni() < 0.05) ch.add(mutate(r, qs[r.next() % qs.size()], 0.05 * r.uni()));
         else ch.add(dna(r, 100 + (int)(r.next() % 157)));
     }
@@ -1322,7 +1391,7 @@ static int tune_threshold_search(blg_ctx *c) {
             c->tune.lpt_ctas = ctas;
             c->tune.lpt_job = job;
             float ms = 0.f;
-            rc = time_best(c, 3, [&] { return search_run(c, &s, 4, BLG_UINT8, out); }, &ms);
+            rc = time_best(c, 5, [&] { return search_run(c, &s, 4, BLG_UINT8, out); }, &ms);
             if (!rc && ms < best_ms) { best_ms = ms; best_ctas = ctas; best_job = job; }
         }
     }
@@ -1397,7 +1466,7 @@ static std::string tuning_header(blg_ctx *c) {
     std::string name = prop.name;
     for (auto &ch : name)
         if (ch == ' ') ch = '_';
-    return "BLGTUNE2 " + name + " sm" + std::to_string(prop.major * 10 + prop.minor) + " " + std::to_string(c->sms) +
+    return "BLGTUNE3 " + name + " sm" + std::to_string(prop.major * 10 + prop.minor) + " " + std::to_string(c->sms) +
            " " + std::to_string(blg_version());
 }
 
@@ -1501,6 +1570,8 @@ void blg_destroy(blg_ctx *c) {
     if (c->d_status) cudaFree(c->d_status);
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
+    if (c->stage_done) cudaEventDestroy(c->stage_done);
+    if (c->stage) cudaFreeHost(c->stage);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->up) cudaStreamDestroy(c->up);
     if (c->down) cudaStreamDestroy(c->down);

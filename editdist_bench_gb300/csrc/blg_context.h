@@ -39,6 +39,11 @@ struct blg_ctx {
     blg_sched_model *model = nullptr;  // trained/loaded scheduler network, if any
     blg_tuning tune;                   // launch shapes (autotuned or defaults)
     bool prof = false;
+    // pinned host staging for arrays the host builds and copies (grown on
+    // demand; stage_done marks the end of the last copy out of it)
+    void *stage = nullptr;
+    size_t stage_bytes = 0;
+    cudaEvent_t stage_done = nullptr;
     std::vector<ProfRec> prof_recs;
     std::map<std::string, std::pair<int64_t, double>> prof_acc;
 };

@@ -639,6 +639,25 @@ cudaError_t launch_fill(cudaStream_t st, int sms, void *out, int64_t n, int dtyp
     return cudaGetLastError();
 }
 
+// Offsets of the length-sorted copy: every string of length bucket b
+// (positions lstart[b] .. lstart[b+1]-1) is min_len + b bytes long, so
+// soff[j] = bstart[b] + (j - lstart[b]) * (min_len + b); soff[n] = the total.
+__global__ void __launch_bounds__(256) k_sorted_offsets(const int64_t *lstart, int64_t n_len, int64_t min_len,
+                                                        const int64_t *bstart, int64_t n, int64_t *soff) {
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j <= n; j += (int64_t)gridDim.x * blockDim.x) {
+        const int b = j < n ? upper_index(lstart, (int)n_len, j) : (int)n_len - 1;
+        soff[j] = bstart[b] + (j - lstart[b]) * (min_len + b);
+    }
+}
+
+cudaError_t launch_sorted_offsets(cudaStream_t st, int sms, const int64_t *lstart, int64_t n_len, int64_t min_len,
+                                  const int64_t *bstart, int64_t n, int64_t *soff) {
+    if (n < 0 || n_len <= 0) return cudaSuccess;
+    const int64_t blocks = std::min<int64_t>((n + 256) / 256, (int64_t)sms * 8);
+    k_sorted_offsets<<<(unsigned)blocks, 256, 0, st>>>(lstart, n_len, min_len, bstart, n, soff);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &src, const int32_t *perm,
                                   const int64_t *dst_off, uint8_t *dst, int64_t n, uint32_t *status) {
     if (n <= 0) return cudaSuccess;
