@@ -101,11 +101,6 @@ __device__ __forceinline__ uint32_t nib32_eq(const uint32_t *tc, uint32_t c) {
 // ---- strings in the stage, addressed by byte offset from its 16-byte-aligned
 // base: the alignment comes from the offset, so the pointers never pass
 // through an integer and stay shared-memory addresses (32-bit loads).
-__device__ __forceinline__ uint32_t st_load4(const uint8_t *base, uint32_t off) {
-    const uint32_t *w = reinterpret_cast<const uint32_t *>(base + (off & ~3u));
-    return __funnelshift_r(w[0], w[1], (off & 3u) * 8u);
-}
-
 struct StageScan {
     const uint32_t *w;
     uint32_t lo, hi, sh;
@@ -125,25 +120,47 @@ struct StageScan {
 };
 
 // Exact prefix/suffix trimming of staged strings a (offset oa, length la) and
-// b (ob, lb), 4-byte windows (csrc/myers.c:80-87).
+// b (ob, lb), 4-byte windows (csrc/myers.c:80-87). Each side is read by a
+// running pair of aligned words, so a window costs one shared-memory load per
+// string plus a funnel shift; the prefix walks forward, the suffix backward
+// (a window's alignment remainder does not change as it moves by 4).
 __device__ __forceinline__ void stage_trim(const uint8_t *base, uint32_t &oa, int &la, uint32_t &ob, int &lb) {
     const int lim = la < lb ? la : lb;
     int p = 0;
-    while (p < lim) {
-        const uint32_t x = st_load4(base, oa + p) ^ st_load4(base, ob + p);
-        int q = x ? (__ffs(x) - 1) >> 3 : 4;
-        if (q > lim - p) q = lim - p;
-        p += q;
-        if (q < 4) break;
+    if (lim > 0) {
+        const uint32_t *wa = reinterpret_cast<const uint32_t *>(base + (oa & ~3u));
+        const uint32_t *wb = reinterpret_cast<const uint32_t *>(base + (ob & ~3u));
+        const uint32_t sa = (oa & 3u) * 8u, sb = (ob & 3u) * 8u;
+        uint32_t a0 = wa[0], b0 = wb[0];
+        while (p < lim) {
+            const uint32_t a1 = *++wa, b1 = *++wb;
+            const uint32_t x = __funnelshift_r(a0, a1, sa) ^ __funnelshift_r(b0, b1, sb);
+            int q = x ? (__ffs(x) - 1) >> 3 : 4;
+            if (q > lim - p) q = lim - p;
+            p += q;
+            if (q < 4) break;
+            a0 = a1;
+            b0 = b1;
+        }
     }
     const int lim2 = lim - p;
     int s = 0;
-    while (s < lim2) {
-        const uint32_t x = st_load4(base, oa + la - s - 4) ^ st_load4(base, ob + lb - s - 4);
-        int q = x ? __clz(x) >> 3 : 4;
-        if (q > lim2 - s) q = lim2 - s;
-        s += q;
-        if (q < 4) break;
+    if (lim2 > 0) {
+        const uint32_t ea = oa + (uint32_t)la - 4u, eb = ob + (uint32_t)lb - 4u;   // first suffix window
+        const uint32_t *wa = reinterpret_cast<const uint32_t *>(base + (ea & ~3u));
+        const uint32_t *wb = reinterpret_cast<const uint32_t *>(base + (eb & ~3u));
+        const uint32_t sa = (ea & 3u) * 8u, sb = (eb & 3u) * 8u;
+        uint32_t a1 = wa[1], b1 = wb[1];
+        while (s < lim2) {
+            const uint32_t a0 = *wa--, b0 = *wb--;
+            const uint32_t x = __funnelshift_r(a0, a1, sa) ^ __funnelshift_r(b0, b1, sb);
+            int q = x ? __clz(x) >> 3 : 4;
+            if (q > lim2 - s) q = lim2 - s;
+            s += q;
+            if (q < 4) break;
+            a1 = a0;
+            b1 = b0;
+        }
     }
     oa += p;
     ob += p;
