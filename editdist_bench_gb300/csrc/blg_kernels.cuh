@@ -438,26 +438,50 @@ __device__ __forceinline__ int lane_wavefront(bool valid, int m, const uint8_t *
 
 // ------------------------------------------------------------ pairs: main --
 // Trim the common prefix and suffix with 4-byte window compares (exact:
-// d(xPy, xQy) = d(P, Q), csrc/myers.c:80-87).
+// d(xPy, xQy) = d(P, Q), csrc/myers.c:80-87). Each side is read by a running
+// pair of aligned words with the next word already requested, so a window
+// costs one load per string and its latency overlaps the previous compare.
+// The reads stay within 11 bytes of the strings' ends (the buffers' slack is
+// 16 bytes before and at least 32 after).
 template <typename L = LdgLoad>
 __device__ __forceinline__ void trim_windows(const uint8_t *&a, int &la, const uint8_t *&b, int &lb) {
     const int lim = la < lb ? la : lb;
     int p = 0;
-    while (p < lim) {
-        const uint32_t x = load4<L>(a + p) ^ load4<L>(b + p);
-        int q = x ? (__ffs(x) - 1) >> 3 : 4;               // equal leading bytes
-        if (q > lim - p) q = lim - p;
-        p += q;
-        if (q < 4) break;
+    if (lim > 0) {
+        const uintptr_t ua = reinterpret_cast<uintptr_t>(a), ub = reinterpret_cast<uintptr_t>(b);
+        const uint32_t *wa = reinterpret_cast<const uint32_t *>(ua & ~uintptr_t(3));
+        const uint32_t *wb = reinterpret_cast<const uint32_t *>(ub & ~uintptr_t(3));
+        const uint32_t sa = (uint32_t)(ua & 3) * 8u, sb = (uint32_t)(ub & 3) * 8u;
+        uint32_t a0 = L::ld(wa), a1 = L::ld(wa + 1), b0 = L::ld(wb), b1 = L::ld(wb + 1);
+        while (p < lim) {
+            const uint32_t a2 = L::ld(wa + 2), b2 = L::ld(wb + 2);     // the next window's new words
+            const uint32_t x = __funnelshift_r(a0, a1, sa) ^ __funnelshift_r(b0, b1, sb);
+            int q = x ? (__ffs(x) - 1) >> 3 : 4;               // equal leading bytes
+            if (q > lim - p) q = lim - p;
+            p += q;
+            if (q < 4) break;
+            a0 = a1; a1 = a2; b0 = b1; b1 = b2;
+            wa++; wb++;
+        }
     }
     const int lim2 = lim - p;
     int s = 0;
-    while (s < lim2) {
-        const uint32_t x = load4<L>(a + la - s - 4) ^ load4<L>(b + lb - s - 4);
-        int q = x ? __clz(x) >> 3 : 4;                     // equal trailing bytes
-        if (q > lim2 - s) q = lim2 - s;
-        s += q;
-        if (q < 4) break;
+    if (lim2 > 0) {
+        const uintptr_t ua = reinterpret_cast<uintptr_t>(a + la - 4), ub = reinterpret_cast<uintptr_t>(b + lb - 4);
+        const uint32_t *wa = reinterpret_cast<const uint32_t *>(ua & ~uintptr_t(3));
+        const uint32_t *wb = reinterpret_cast<const uint32_t *>(ub & ~uintptr_t(3));
+        const uint32_t sa = (uint32_t)(ua & 3) * 8u, sb = (uint32_t)(ub & 3) * 8u;
+        uint32_t a0 = L::ld(wa), a1 = L::ld(wa + 1), b0 = L::ld(wb), b1 = L::ld(wb + 1);
+        while (s < lim2) {
+            const uint32_t am = L::ld(wa - 1), bm = L::ld(wb - 1);     // the next window's new words
+            const uint32_t x = __funnelshift_r(a0, a1, sa) ^ __funnelshift_r(b0, b1, sb);
+            int q = x ? __clz(x) >> 3 : 4;                     // equal trailing bytes
+            if (q > lim2 - s) q = lim2 - s;
+            s += q;
+            if (q < 4) break;
+            a1 = a0; a0 = am; b1 = b0; b0 = bm;
+            wa--; wb--;
+        }
     }
     a += p; b += p;
     la -= p + s; lb -= p + s;
