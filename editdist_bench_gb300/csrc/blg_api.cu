@@ -876,7 +876,19 @@ static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int
     if (!rc) rc = search_upload_choices(c, bc, oc, nc, s, surv ? NEED_SORTED : NEED_TT);
     if (rc) return rc;
     const size_t row = dtype_size(dtype) * (size_t)nc;
-    const int nch = (int)std::min<int64_t>(8, nq);
+    // Query chunks of relative sizes 4,4,4,4,4,4,4,2,1,1: the last chunk's
+    // copy back is the part of the result stream no kernel hides, so the
+    // tail chunks are small (1/32 of the rows instead of 1/8).
+    static const int kWeights[] = {4, 4, 4, 4, 4, 4, 4, 2, 1, 1};
+    std::vector<int64_t> cut{0};
+    if (nq >= 32) {
+        int acc = 0;
+        for (int w : kWeights) cut.push_back(nq * (acc += w) / 32);
+    } else {
+        const int n8 = (int)std::min<int64_t>(8, nq);
+        for (int i = 1; i <= n8; i++) cut.push_back(nq * i / n8);
+    }
+    const int nch = (int)cut.size() - 1;
     std::vector<cudaEvent_t> ev(nch + 1, nullptr);
     for (auto &e : ev)
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = BLG_ERR_CUDA;
@@ -890,14 +902,14 @@ static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int
     if (rc) return fin(fail(c, rc, "cudaEventCreate"));
     for (int ch = 0; ch <= nch && !rc; ch++) {
         if (ch < nch) {
-            const int64_t q0 = nq * ch / nch, q1 = nq * (ch + 1) / nch;
+            const int64_t q0 = cut[ch], q1 = cut[ch + 1];
             rc = search_build_classes(c, oq, q0, q1, s);
             if (!rc) rc = search_run(c, s, k, dtype, d_out, q0, q1);
             if (!rc && cudaEventRecord(ev[ch], c->stream) != cudaSuccess) rc = fail(c, BLG_ERR_CUDA, "event");
             if (rc) break;
         }
         if (ch >= 1) {
-            const int64_t q0 = nq * (ch - 1) / nch, q1 = nq * ch / nch;
+            const int64_t q0 = cut[ch - 1], q1 = cut[ch];
             if (cudaStreamWaitEvent(c->down, ev[ch - 1], 0) != cudaSuccess) { rc = fail(c, BLG_ERR_CUDA, "wait"); break; }
             cudaError_t e = cudaMemcpyAsync((uint8_t *)out_host + q0 * row, (uint8_t *)d_out + q0 * row,
                                             (size_t)(q1 - q0) * row, cudaMemcpyDeviceToHost, c->down);
