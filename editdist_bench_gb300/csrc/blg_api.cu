@@ -1378,7 +1378,7 @@ static int tune_exact_search(blg_ctx *c, int nw) {
 // that the run-time job size (survivor_job_size) keeps the candidate job
 // sizes: 512 queries x 2^19 choices (about 15 M survivors at max_dist 4).
 // A smaller search had its jobs halved at run time whatever the candidate,
-// so the choice was noise, and config-4-sized runs paid for it (up to 14%).
+// so the choice was noise, and a 1024 x 2^20 search paid for it (up to 14%).
 static int tune_threshold_search(blg_ctx *c) {
     Rng r{0x2545F4914F6CDD1Dull};
     Packed q, ch;

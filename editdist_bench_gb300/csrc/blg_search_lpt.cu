@@ -1,5 +1,5 @@
 // Thresholded search, longest-predicted-first: the survivor kernel for
-// max_dist <= 31 (configs 2b, 4).
+// max_dist <= 31.
 //
 // With max_dist = k only (query, choice) pairs whose lengths differ by at
 // most k need the column loop (csrc/myers.c:101-106); they are a contiguous

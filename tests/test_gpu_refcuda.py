@@ -42,7 +42,7 @@ def test_reference_cross_kernels_match_oracle_and_engine(k, out8):
 
 
 def test_reference_kernels_on_config_shapes():
-    """Config 1 (L32 pairs) and config 2 (L64 search) shapes, small counts."""
+    """The benchmark shapes of L32 DNA pairs and the L64 DNA search, small counts."""
     w1 = W.config1(n=20000, seed=71)
     np.testing.assert_array_equal(ref_cuda.pairwise(w1.a, w1.b), oracle.pairs(w1.a, w1.b))
     w2 = W.config2(nq=16, nc=4096, seed=72)

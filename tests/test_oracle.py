@@ -75,7 +75,7 @@ def test_config_subsamples(csuite):
         k = None if tag == "c1" else 8
         dt = "int32" if tag == "c1" else "uint8"
         np.testing.assert_array_equal(oracle.saturate(oracle.pairs(pa, pb, k), dt), csuite[f"{tag}_out"])
-    # config 1 also against the reference's textbook DP on its 300-pair subsample
+    # the L32 pairs workload also against the reference's textbook DP on its 300-pair subsample
     pa = (csuite["c1_a_buf"], csuite["c1_a_off"])
     pb = (csuite["c1_b_buf"], csuite["c1_b_off"])
     np.testing.assert_array_equal(oracle.pairs(pa, pb)[:300], csuite["c1_dp300"])
