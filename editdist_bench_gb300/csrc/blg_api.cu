@@ -722,8 +722,11 @@ static void *host_stage(blg_ctx *c, size_t bytes) {
 // one-call search knows its max_dist and schedule and builds one.
 enum { NEED_SORTED = 1, NEED_TT = 2, NEED_ALL = 3 };
 
+// perm_stage: pinned room for the permutation (nc int32) reserved by the
+// caller for this upload alone (a batch reserves one region per problem, so
+// no upload waits for an earlier one's copy); null: the context's stage.
 static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s,
-                                 unsigned need = NEED_ALL) {
+                                 unsigned need = NEED_ALL, int32_t *perm_stage = nullptr) {
     s->nc = nc;
     int rc = upload_strings(c, bc, oc, nc, s->c);
     if (rc) return rc;
@@ -771,7 +774,7 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
                 bytes += (run - lstart[b]) * (b + mn);
             }
             lstart[n_len] = run;
-            int32_t *perm = (int32_t *)host_stage(c, sizeof(int32_t) * (size_t)nc);
+            int32_t *perm = perm_stage ? perm_stage : (int32_t *)host_stage(c, sizeof(int32_t) * (size_t)nc);
             if (!perm) return fail(c, BLG_ERR_ALLOC, "cudaHostAlloc(staging)");
             pool.run(nh, [&](int t) {
                 int64_t *cur = hist.data() + (size_t)t * n_len;
@@ -922,9 +925,10 @@ static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int
 }
 
 static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq,
-                         const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s) {
+                         const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s,
+                         unsigned need = NEED_ALL, int32_t *perm_stage = nullptr) {
     int rc = search_upload_queries(c, bq, oq, nq, s);
-    if (!rc) rc = search_upload_choices(c, bc, oc, nc, s);
+    if (!rc) rc = search_upload_choices(c, bc, oc, nc, s, need, perm_stage);
     if (!rc) rc = search_build_classes(c, oq, 0, nq, s);
     return rc;
 }
@@ -1152,6 +1156,13 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
     std::vector<BatchJob> jobs;
     std::vector<BatchFill> fills;
     std::vector<int64_t> qprefix(1, 0);
+    // one pinned region per problem for its permutation, reserved up front
+    size_t stage_words = 0;
+    for (int i = 0; i < nprob; i++)
+        if (pr[i].nq > 0 && pr[i].nc > 0) stage_words += (size_t)pr[i].nc;
+    int32_t *stage = stage_words ? (int32_t *)host_stage(c, sizeof(int32_t) * stage_words) : nullptr;
+    if (stage_words && !stage) return fail(c, BLG_ERR_ALLOC, "cudaHostAlloc(staging)");
+    size_t stage_at = 0;
     for (int i = 0; i < nprob; i++) {
         const blg_problem &p = pr[i];
         if (!dtype_ok(p.dtype)) return fail(c, BLG_ERR_ARG, "problem " + std::to_string(i) + ": bad dtype");
@@ -1166,7 +1177,9 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
         b->dt.push_back(p.dtype);
         b->outs.push_back(p.d_out);
         if (p.nq == 0 || p.nc == 0) continue;
-        int rc = search_upload(c, p.buf_q, p.off_q, p.nq, p.buf_c, p.off_c, p.nc, s);
+        // the batch kernels read the length-sorted copy only (no tile-transposed copy)
+        int rc = search_upload(c, p.buf_q, p.off_q, p.nq, p.buf_c, p.off_c, p.nc, s, NEED_SORTED, stage + stage_at);
+        stage_at += (size_t)p.nc;
         if (rc) return rc;
         b->pairs += p.nq * p.nc;
         bool eligible = s->lsorted;
