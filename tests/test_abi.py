@@ -54,3 +54,30 @@ def test_product_package_does_not_import_oracle():
             text = open(path, encoding="utf-8").read()
             assert not re.search(r"^\s*(import|from)\s+oracle\b", text, flags=re.M), path
             assert "liborc" not in text and "myers_oracle" not in text, path
+
+
+def test_match_record_layout_matches_header():
+    """gpu.MATCH_DTYPE mirrors blg_match (include/bitlev_gb300.h): int64
+    query, int64 choice, int32 dist, int32 reserved, 24 bytes."""
+    from editdist_bench_gb300 import gpu
+    text = open(os.path.join(ROOT, "include", "bitlev_gb300.h")).read()
+    body = re.search(r"typedef struct \{([^}]*)\} blg_match;", text).group(1)
+    fields = re.findall(r"(int64_t|int32_t)\s+(\w+);", body)
+    assert fields == [("int64_t", "query"), ("int64_t", "choice"), ("int32_t", "dist"), ("int32_t", "reserved")]
+
+    class M(ctypes.Structure):
+        _fields_ = [("query", ctypes.c_int64), ("choice", ctypes.c_int64), ("dist", ctypes.c_int32),
+                    ("reserved", ctypes.c_int32)]
+    assert gpu.MATCH_DTYPE.itemsize == ctypes.sizeof(M) == 24
+    assert [gpu.MATCH_DTYPE.fields[n][1] for n in ("query", "choice", "dist", "reserved")] == \
+        [M.query.offset, M.choice.offset, M.dist.offset, M.reserved.offset]
+
+
+def test_matches_reject_exact_runs_before_any_device_call():
+    """A matches-only search needs max_dist (the exact result is the dense
+    cdist); the check runs in Python, so it raises without a GPU too."""
+    from editdist_bench_gb300 import gpu
+    with pytest.raises(ValueError):
+        gpu.cdist_matches(["ACGT"], ["ACGA"], None)
+    with pytest.raises(ValueError):
+        gpu.cdist_matches(["ACGT"], ["ACGA"], -1)
