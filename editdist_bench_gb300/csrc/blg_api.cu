@@ -99,8 +99,7 @@ constexpr int kLaneMaxWords = 32;        // queries up to 2048: lane-spread
 
 struct OwnedStrings {
     DevStrings d;
-    void *mem_buf = nullptr;   // allocation (d.buf - 16)
-    void *mem_off = nullptr;
+    void *mem_buf = nullptr;   // the one allocation: d.buf - 16, with the offsets after the bytes
 };
 
 }  // namespace
@@ -132,6 +131,7 @@ struct blg_search {
         uint64_t *peq;
         int32_t *lo, *hi, *work;   // survivor plan (thresholded runs)
         int64_t *tile_start;
+        void *mem;                 // the one device block all of the above live in
         std::vector<int32_t> h_qlen;   // host copy of qlen
     };
     std::vector<Cls> cls;
@@ -140,6 +140,7 @@ struct blg_search {
     // first sorted index of length L (n_len + 1 entries)
     bool lsorted = false;
     OwnedStrings cs;
+    void *sorted_mem = nullptr;   // one device block: perm, lstart, bucket starts, offsets, sketches, bytes
     int32_t *perm = nullptr;
     int64_t *lstart = nullptr;
     int64_t min_len = 0, n_len = 0;
@@ -208,14 +209,15 @@ static int alloc_strings(blg_ctx *c, const uint8_t *buf, const int64_t *off, int
     const int64_t base = n > 0 ? off[0] : 0;
     const int64_t bytes = n > 0 ? off[n] - off[0] : 0;
     if (bytes > 0 && !buf) return fail(c, BLG_ERR_ARG, "null buffer");
-    CK(dev_alloc(c, &o.mem_buf, (size_t)bytes + kSlackBefore + kSlackAfter), "cudaMallocAsync(strings)");
+    // one block: 16 bytes of slack | the bytes | 48 bytes of slack | offsets (256-byte aligned)
+    const size_t o_off = ((size_t)bytes + kSlackBefore + kSlackAfter + 255) & ~size_t(255);
+    CK(dev_alloc(c, &o.mem_buf, o_off + sizeof(int64_t) * (size_t)(n + 1)), "cudaMallocAsync(strings)");
     uint8_t *dbuf = (uint8_t *)o.mem_buf + kSlackBefore;
     // only the slack on either side needs defined contents
     CK(cudaMemsetAsync(o.mem_buf, 0, kSlackBefore, c->stream), "cudaMemsetAsync(slack)");
     CK(cudaMemsetAsync(dbuf + bytes, 0, kSlackAfter, c->stream), "cudaMemsetAsync(slack)");
-    CK(dev_alloc(c, &o.mem_off, sizeof(int64_t) * (size_t)(n + 1)), "cudaMallocAsync(offsets)");
     o.d.buf = dbuf;
-    o.d.off = (const int64_t *)o.mem_off;
+    o.d.off = (const int64_t *)((uint8_t *)o.mem_buf + o_off);
     o.d.n = n;
     o.d.base = base;
     o.d.bytes = bytes;
@@ -231,7 +233,7 @@ static int copy_strings(blg_ctx *c, const uint8_t *buf, const int64_t *off, int6
     if (b1 > b0)
         CK(cudaMemcpyAsync((uint8_t *)o.d.buf + b0, buf + off[i0], (size_t)(b1 - b0), cudaMemcpyHostToDevice, st),
            "H2D strings");
-    CK(cudaMemcpyAsync((int64_t *)o.mem_off + i0, off + i0, sizeof(int64_t) * (size_t)(i1 - i0 + 1),
+    CK(cudaMemcpyAsync(const_cast<int64_t *>(o.d.off) + i0, off + i0, sizeof(int64_t) * (size_t)(i1 - i0 + 1),
                        cudaMemcpyHostToDevice, st), "H2D offsets");
     return BLG_OK;
 }
@@ -246,7 +248,6 @@ static int upload_strings(blg_ctx *c, const uint8_t *buf, const int64_t *off, in
 
 static void free_strings(blg_ctx *c, OwnedStrings &o) {
     dev_free(c, o.mem_buf);
-    dev_free(c, o.mem_off);
     o = OwnedStrings();
 }
 
@@ -635,15 +636,7 @@ static void pairs_release(blg_ctx *c, blg_pairs *p) {
 
 // ------------------------------------------------------------ search --
 static void free_classes(blg_ctx *c, blg_search *s) {
-    for (auto &k : s->cls) {
-        dev_free(c, k.qidx);
-        dev_free(c, k.qlen);
-        dev_free(c, k.peq);
-        dev_free(c, k.lo);
-        dev_free(c, k.hi);
-        dev_free(c, k.tile_start);
-        dev_free(c, k.work);
-    }
+    for (auto &k : s->cls) dev_free(c, k.mem);
     s->cls.clear();
 }
 
@@ -682,15 +675,27 @@ static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64
         s->cls.push_back(k);
         blg_search::Cls &kk = s->cls.back();
         kk.h_qlen = len[slot];
-        CK(dev_alloc(c, (void **)&kk.qidx, sizeof(int32_t) * kk.nq), "cudaMallocAsync(qidx)");
-        CK(dev_alloc(c, (void **)&kk.qlen, sizeof(int32_t) * kk.nq), "cudaMallocAsync(qlen)");
-        CK(dev_alloc(c, (void **)&kk.peq, sizeof(uint64_t) * 256 * (size_t)kk.nw * kk.nq), "cudaMallocAsync(peq)");
-        CK(cudaMemcpyAsync(kk.qidx, idx[slot].data(), sizeof(int32_t) * kk.nq, cudaMemcpyHostToDevice, c->stream), "H2D qidx");
-        CK(cudaMemcpyAsync(kk.qlen, len[slot].data(), sizeof(int32_t) * kk.nq, cudaMemcpyHostToDevice, c->stream), "H2D qlen");
-        CK(dev_alloc(c, (void **)&kk.lo, sizeof(int32_t) * kk.nq), "cudaMallocAsync(lo)");
-        CK(dev_alloc(c, (void **)&kk.hi, sizeof(int32_t) * kk.nq), "cudaMallocAsync(hi)");
-        CK(dev_alloc(c, (void **)&kk.tile_start, sizeof(int64_t) * (kk.nq + 1)), "cudaMallocAsync(tiles)");
-        CK(dev_alloc(c, (void **)&kk.work, sizeof(int32_t)), "cudaMallocAsync(work)");
+        // one device block per class: [qidx | qlen] (filled by one copy), lo,
+        // hi, work, tile_start, peq — 256-byte aligned parts
+        auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+        const size_t nq = (size_t)kk.nq;
+        const size_t o_qidx = 0, o_qlen = nq * 4, o_lo = up(2 * nq * 4), o_hi = o_lo + up(nq * 4),
+                     o_work = o_hi + up(nq * 4), o_ts = o_work + 256, o_peq = o_ts + up((nq + 1) * 8),
+                     total = o_peq + sizeof(uint64_t) * 256 * (size_t)kk.nw * nq;
+        CK(dev_alloc(c, &kk.mem, total), "cudaMallocAsync(class)");
+        uint8_t *m = (uint8_t *)kk.mem;
+        kk.qidx = (int32_t *)(m + o_qidx);
+        kk.qlen = (int32_t *)(m + o_qlen);
+        kk.lo = (int32_t *)(m + o_lo);
+        kk.hi = (int32_t *)(m + o_hi);
+        kk.work = (int32_t *)(m + o_work);
+        kk.tile_start = (int64_t *)(m + o_ts);
+        kk.peq = (uint64_t *)(m + o_peq);
+        std::vector<int32_t> both(2 * nq);
+        std::copy(idx[slot].begin(), idx[slot].end(), both.begin());
+        std::copy(len[slot].begin(), len[slot].end(), both.begin() + nq);
+        CK(cudaMemcpyAsync(kk.qidx, both.data(), sizeof(int32_t) * 2 * nq, cudaMemcpyHostToDevice, c->stream),
+           "H2D class queries");
     }
     // the host vectors above are pageable: the copies completed before return
     return BLG_OK;
@@ -781,27 +786,36 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
                 for (int64_t i = lo_of(t, nh), e = lo_of(t + 1, nh); i < e; i++)
                     perm[cur[oc[i + 1] - oc[i] - mn]++] = (int32_t)i;
             });
-            OwnedStrings &cs = s->cs;
-            CK(dev_alloc(c, (void **)&s->perm, sizeof(int32_t) * nc), "cudaMallocAsync(perm)");
+            // one device block: perm | lstart, bucket starts | sorted offsets | sketches | sorted bytes
+            auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+            const size_t o_perm = 0, o_tab = up(sizeof(int32_t) * (size_t)nc),
+                         o_soff = o_tab + up(sizeof(int64_t) * (size_t)(2 * n_len + 1)),
+                         o_csk = o_soff + up(sizeof(int64_t) * (size_t)(nc + 1)),
+                         o_buf = o_csk + up(sizeof(uint64_t) * (size_t)nc),
+                         total = o_buf + (size_t)bytes + kSlackBefore + kSlackAfter;
+            CK(dev_alloc(c, &s->sorted_mem, total), "cudaMallocAsync(sorted choices)");
+            uint8_t *m = (uint8_t *)s->sorted_mem;
+            s->perm = (int32_t *)(m + o_perm);
+            s->lstart = (int64_t *)(m + o_tab);
+            int64_t *d_bstart = s->lstart + (n_len + 1);
+            int64_t *d_soff = (int64_t *)(m + o_soff);
+            s->csk = (uint64_t *)(m + o_csk);
+            uint8_t *d_buf = m + o_buf;
             CK(cudaMemcpyAsync(s->perm, perm, sizeof(int32_t) * nc, cudaMemcpyHostToDevice, c->stream), "H2D perm");
             CK(cudaEventRecord(c->stage_done, c->stream), "event");
-            CK(dev_alloc(c, (void **)&s->lstart, sizeof(int64_t) * (n_len + 1)), "cudaMallocAsync(lstart)");
-            CK(cudaMemcpyAsync(s->lstart, lstart.data(), sizeof(int64_t) * (n_len + 1), cudaMemcpyHostToDevice, c->stream), "H2D lstart");
-            int64_t *d_bstart = nullptr;
-            CK(dev_alloc(c, (void **)&d_bstart, sizeof(int64_t) * n_len), "cudaMallocAsync(bstart)");
-            CK(cudaMemcpyAsync(d_bstart, bstart.data(), sizeof(int64_t) * n_len, cudaMemcpyHostToDevice, c->stream), "H2D bstart");
-            CK(dev_alloc(c, &cs.mem_off, sizeof(int64_t) * (size_t)(nc + 1)), "cudaMallocAsync(sorted offsets)");
+            std::vector<int64_t> tab(lstart);                 // lstart then the bucket starts: one copy
+            tab.insert(tab.end(), bstart.begin(), bstart.end());
+            CK(cudaMemcpyAsync(s->lstart, tab.data(), sizeof(int64_t) * tab.size(), cudaMemcpyHostToDevice, c->stream),
+               "H2D length tables");
             CK(launch(c, "sorted_offsets", [&] {
-                   return launch_sorted_offsets(c->stream, c->sms, s->lstart, n_len, mn, d_bstart, nc,
-                                                (int64_t *)cs.mem_off);
+                   return launch_sorted_offsets(c->stream, c->sms, s->lstart, n_len, mn, d_bstart, nc, d_soff);
                }), "sorted_offsets");
-            dev_free(c, d_bstart);
-            CK(dev_alloc(c, &cs.mem_buf, (size_t)bytes + kSlackBefore + kSlackAfter), "cudaMallocAsync(sorted choices)");
-            CK(cudaMemsetAsync(cs.mem_buf, 0, kSlackBefore, c->stream), "memset slack");
-            CK(cudaMemsetAsync((uint8_t *)cs.mem_buf + kSlackBefore + bytes, 0, kSlackAfter, c->stream), "memset slack");
+            CK(cudaMemsetAsync(d_buf, 0, kSlackBefore, c->stream), "memset slack");
+            CK(cudaMemsetAsync(d_buf + kSlackBefore + bytes, 0, kSlackAfter, c->stream), "memset slack");
+            OwnedStrings &cs = s->cs;                          // owned by sorted_mem
             s->h_lstart = lstart;
-            cs.d.buf = (uint8_t *)cs.mem_buf + kSlackBefore;
-            cs.d.off = (const int64_t *)cs.mem_off;
+            cs.d.buf = d_buf + kSlackBefore;
+            cs.d.off = d_soff;
             cs.d.n = nc;
             cs.d.base = 0;
             cs.d.bytes = bytes;
@@ -809,7 +823,6 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
                    return launch_gather_strings(c->stream, c->sms, s->c.d, s->perm, cs.d.off,
                                                 (uint8_t *)cs.d.buf, nc, c->d_status);
                }), "gather_strings");
-            CK(dev_alloc(c, (void **)&s->csk, sizeof(uint64_t) * (size_t)nc), "cudaMallocAsync(sketches)");
             CK(launch(c, "sketch", [&] { return launch_sketch_strings(c->stream, c->sms, cs.d, s->csk, c->d_status); }),
                "sketch");
             s->min_len = mn;
@@ -1095,15 +1108,15 @@ static void search_release(blg_ctx *c, blg_search *s) {
     free_strings(c, s->q);
     free_strings(c, s->c);
     free_strings(c, s->cs);
-    dev_free(c, s->perm);
-    dev_free(c, s->lstart);
+    dev_free(c, s->sorted_mem);      // perm, lstart, sketches and the sorted copy live in it
+    s->sorted_mem = nullptr;
     s->perm = nullptr;
     s->lstart = nullptr;
+    s->csk = nullptr;
     s->lsorted = false;
     dev_free(c, s->tt_words);
     dev_free(c, s->tt_base);
     dev_free(c, s->tt_len);
-    dev_free(c, s->csk);
     dev_free(c, s->qsk);
     s->csk = s->qsk = nullptr;
     s->tt_words = nullptr;
