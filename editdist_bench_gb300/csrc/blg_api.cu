@@ -14,6 +14,7 @@
 #include <functional>
 #include <thread>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -135,6 +136,7 @@ struct blg_search {
         std::vector<int32_t> h_qlen;   // host copy of qlen
     };
     std::vector<Cls> cls;
+    std::vector<int64_t> h_oq;    // host copy of the query offsets (resident searches: class rebuilds)
     // choices sorted by length (thresholded runs): cs = sorted copy,
     // perm[i] = original index of sorted choice i, lstart[L - min_len] =
     // first sorted index of length L (n_len + 1 entries)
@@ -941,6 +943,7 @@ static int search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64
                          const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s,
                          unsigned need = NEED_ALL, int32_t *perm_stage = nullptr) {
     int rc = search_upload_queries(c, bq, oq, nq, s);
+    if (!rc && need == NEED_ALL && nq > 0) s->h_oq.assign(oq, oq + nq + 1);   // a resident search keeps them
     if (!rc) rc = search_upload_choices(c, bc, oc, nc, s, need, perm_stage);
     if (!rc) rc = search_build_classes(c, oq, 0, nq, s);
     return rc;
@@ -1058,6 +1061,14 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
 // ---- matches-only search
 // Dense scratch element type of a threshold k: the narrowest holding k + 1.
 static int match_dtype(int k) { return k <= 254 ? BLG_UINT8 : k <= 65534 ? BLG_UINT16 : BLG_INT32; }
+
+// Upper bound of the dense scratch of one query chunk: 1 GiB, or the
+// environment's BLG_MATCH_SCRATCH_BYTES (a memory budget; at least one row).
+static size_t match_scratch_bytes() {
+    const char *e = getenv("BLG_MATCH_SCRATCH_BYTES");
+    const long long v = e ? atoll(e) : 0;
+    return v > 0 ? (size_t)v : (size_t(1) << 30);
+}
 
 // Rows [q0, q1) of search s (classes built for them) into the dense scratch
 // (row q0 at its start), then the compaction: the chunk's match total comes
@@ -1894,11 +1905,27 @@ int blg_search_matches(blg_ctx *c, blg_search *s, int32_t max_dist, blg_match *d
     if (capacity < 0 || (capacity > 0 && !d_out)) return fail(c, BLG_ERR_ARG, "bad match buffer");
     *count = 0;
     if (s->nq == 0 || s->nc == 0) return BLG_OK;
+    // query rows in chunks whose dense scratch stays within the budget
+    // (1 GiB); the all-query classes are rebuilt afterwards for the
+    // search's other runs
+    const size_t row = dtype_size(match_dtype(max_dist)) * (size_t)s->nc;
+    const int64_t rows = std::max<int64_t>(1, std::min<int64_t>(s->nq, (int64_t)(match_scratch_bytes() / row)));
+    const bool chunked = rows < s->nq && (int64_t)s->h_oq.size() == s->nq + 1;
+    const int64_t step = chunked ? rows : s->nq;
     void *scratch = nullptr;
-    CK(dev_alloc(c, &scratch, dtype_size(match_dtype(max_dist)) * (size_t)s->nq * (size_t)s->nc),
-       "cudaMallocAsync(match scratch)");
+    CK(dev_alloc(c, &scratch, row * (size_t)step), "cudaMallocAsync(match scratch)");
     int64_t total = 0;
-    int rc = search_matches_rows(c, s, max_dist, 0, s->nq, scratch, d_out, nullptr, capacity, &total);
+    int rc = BLG_OK;
+    for (int64_t q0 = 0; q0 < s->nq && !rc; q0 += step) {
+        const int64_t q1 = std::min(s->nq, q0 + step);
+        if (chunked) rc = search_build_classes(c, s->h_oq.data(), q0, q1, s);
+        int64_t t = 0;
+        const int64_t written = std::min(total, capacity);
+        if (!rc) rc = search_matches_rows(c, s, max_dist, q0, q1, scratch, d_out ? d_out + written : nullptr,
+                                          nullptr, capacity - written, &t);
+        total += t;
+    }
+    if (chunked && !rc) rc = search_build_classes(c, s->h_oq.data(), 0, s->nq, s);
     dev_free(c, scratch);
     const int rc2 = sync_and_status(c);
     if (rc) return rc;
@@ -1921,9 +1948,9 @@ int blg_cdist_matches(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t 
     const bool surv = c->sched != BLG_SCHED_PLAIN;
     int rc = search_upload_queries(c, bq, oq, nq, &s);
     if (!rc) rc = search_upload_choices(c, bc, oc, nc, &s, surv ? NEED_SORTED : NEED_TT);
-    // query rows in chunks whose dense scratch stays within 1 GiB
+    // query rows in chunks whose dense scratch stays within the budget (1 GiB)
     const size_t row = dtype_size(match_dtype(max_dist)) * (size_t)nc;
-    const int64_t rows = std::max<int64_t>(1, std::min<int64_t>(nq, (int64_t)((size_t(1) << 30) / row)));
+    const int64_t rows = std::max<int64_t>(1, std::min<int64_t>(nq, (int64_t)(match_scratch_bytes() / row)));
     void *scratch = nullptr;
     if (!rc && dev_alloc(c, &scratch, row * (size_t)rows) != cudaSuccess)
         rc = fail(c, BLG_ERR_ALLOC, "cudaMallocAsync(match scratch)");

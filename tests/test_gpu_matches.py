@@ -89,3 +89,20 @@ def test_matches_edges():
     assert all(len(x) == 0 for x in got)
     with pytest.raises(ValueError):
         gpu.cdist_matches_packed(q, c, None)
+
+
+def test_matches_in_query_chunks(monkeypatch):
+    """A small scratch budget (BLG_MATCH_SCRATCH_BYTES) makes both entry
+    points walk several query chunks; the records are the same, and the
+    resident search still runs dense afterwards (its classes are rebuilt)."""
+    rng = np.random.default_rng(13)
+    q = W.random_strings(rng, rng.integers(0, 120, 41))
+    c = W.concat(W.mutate(rng, W.take(q, rng.integers(0, 41, 500)), 0.1), W.random_strings(rng, rng.integers(0, 130, 2500)))
+    nc = len(c[1]) - 1
+    want = _want(q, c, 3)
+    monkeypatch.setenv("BLG_MATCH_SCRATCH_BYTES", str(5 * nc))      # 5 rows of uint8 per chunk
+    _check(gpu.cdist_matches_packed(q, c, 3), want)
+    s = gpu.SearchBatch(q, c)
+    _check(s.matches(3), want)
+    out = s.alloc("uint8")
+    np.testing.assert_array_equal(s.run(out, max_dist=3).get(), oracle.saturate(oracle.cross(q, c, 3), "uint8"))
