@@ -15,6 +15,7 @@
 #include <thread>
 #include <cstdio>
 #include <cstdlib>
+#include <unistd.h>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -296,9 +297,13 @@ public:
         static HostPool pool;
         return pool;
     }
-    int size() const { return (int)workers_.size() + 1; }
+    int size() const { return (int)workers_->size() + 1; }
     void run(int nt, const std::function<void(int)> &fn) {
         nt = std::max(1, std::min(nt, size()));
+        if (getpid() != owner_) {                   // a forked child: the workers stayed with the parent
+            for (int t = 0; t < nt; t++) fn(t);
+            return;
+        }
         if (nt == 1) {
             fn(0);
             return;
@@ -318,19 +323,23 @@ public:
         job_ = nullptr;
     }
     ~HostPool() {
+        // a forked child has no running workers: their thread objects are
+        // left alone (destroying or detaching them there is not defined)
+        if (getpid() != owner_) return;
         {
             std::lock_guard<std::mutex> g(m_);
             stop_ = true;
             gen_++;
         }
         cv_.notify_all();
-        for (auto &t : workers_) t.join();
+        for (auto &t : *workers_) t.join();
+        delete workers_;
     }
 
 private:
-    HostPool() {
+    HostPool() : owner_(getpid()) {
         const int n = (int)std::min<unsigned>(8, std::max(1u, std::thread::hardware_concurrency()));
-        for (int i = 1; i < n; i++) workers_.emplace_back([this, i] { loop(i); });
+        for (int i = 1; i < n; i++) workers_->emplace_back([this, i] { loop(i); });
     }
     void loop(int idx) {
         uint64_t seen = 0;
@@ -352,7 +361,8 @@ private:
             }
         }
     }
-    std::vector<std::thread> workers_;
+    pid_t owner_;
+    std::vector<std::thread> *workers_ = new std::vector<std::thread>();
     std::mutex m_, turn_;
     std::condition_variable cv_, done_;
     const std::function<void(int)> *job_ = nullptr;
