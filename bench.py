@@ -20,6 +20,9 @@ matrix. The metric is pairs/s (distances per second; GCUPS beside it).
            libblg_probe.so; plus its HBM figure.
 * cpu_baseline: the oracle's C restatement of the reference's CPU core on a
            bounded sample, all host threads.
+* matches: for a thresholded search, the same search in its matches-only
+           form (sorted (query, choice, distance) records instead of the
+           dense matrix), kernel-only and end to end.
 * --impl reference: the reference's CPU path (here: the oracle port, since
            the reference's sources are not on the GPU host) on the same
            workload, all host threads; beside it ("reference_cuda") the
