@@ -52,7 +52,7 @@ cudaError_t launch_match_compact(cudaStream_t st, int sms, int dtype, const void
 int64_t match_blocks(int64_t n);
 cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, const DevStrings &A,
                               const DevStrings &B, int tile_pairs, int k, int dtype, void *out, const LongQueue &q,
-                              uint32_t *status);
+                              uint32_t *status, int32_t wait_polls);
 cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, bool band, const DevStrings &A,
                               const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
                               uint32_t *status);
@@ -189,6 +189,10 @@ static cudaError_t launch(blg_ctx *c, const char *name, F &&fn) {
 }
 
 static cudaError_t dev_alloc(blg_ctx *c, void **p, size_t bytes) {
+    if (c->fault_alloc_after >= 0 && c->fault_alloc_after-- == 0) {   // injected failure (tests)
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
     return cudaMallocAsync(p, bytes ? bytes : 16, c->stream);
 }
 
@@ -438,10 +442,12 @@ constexpr size_t kPlanCounters = 2 * kPairClasses;   // count, head
 static int plan_alloc(blg_ctx *c, blg_pairs *p, bool feat) {
     int64_t slots = 0;
     for (int j = 0; j < kPairClasses; j++) slots += p->pcap[j];
-    if (!p->plan_mem) {
+    // each buffer on its own: after a failed allocation a resident plan must
+    // not keep one buffer and run with the other missing
+    if (!p->plan_mem)
         CK(dev_alloc(c, &p->plan_mem, (size_t)slots * (2 * sizeof(LongItem) + 1) + 64), "cudaMallocAsync(plan)");
+    if (!p->plan_ctr)
         CK(dev_alloc(c, (void **)&p->plan_ctr, sizeof(int32_t) * kPlanCounters), "cudaMallocAsync(plan ctr)");
-    }
     if (feat && !p->feat_mem)
         CK(dev_alloc(c, (void **)&p->feat_mem, sizeof(half) * kFeatures * (size_t)slots + 16), "cudaMallocAsync(features)");
     return BLG_OK;
@@ -532,7 +538,7 @@ static int pairs_run_direct(blg_ctx *c, blg_pairs *p, const DevStrings &A, const
         const int tile = avg <= 33.0 ? 512 : std::max(32, (int)(17000.0 / avg) & ~31);
         CK(launch(c, "pairs_tile", [&] {
                return launch_pairs_tile(c->stream, c->sms, c->tune.tile_buffers, hask, A, B, tile, k, dtype, d_out, q,
-                                        c->d_status);
+                                        c->d_status, c->fault_wait_polls);
            }), "pairs_tile");
     } else {
         CK(launch(c, "pairs_staged", [&] {
@@ -684,17 +690,19 @@ static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64
         k.lanes = slot == kSeqMaxWords;
         k.nw = k.lanes ? lanes_nw : slot + 1;
         k.nq = (int)idx[slot].size();
+        // one device block per class: [qidx | qlen] (filled by one copy), lo,
+        // hi, work, tile_start, peq — 256-byte aligned parts. A class joins
+        // the search only once its block exists, so a failed allocation never
+        // leaves a class without memory behind for a later run.
+        auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+        const size_t nq = (size_t)k.nq;
+        const size_t o_qidx = 0, o_qlen = nq * 4, o_lo = up(2 * nq * 4), o_hi = o_lo + up(nq * 4),
+                     o_work = o_hi + up(nq * 4), o_ts = o_work + 256, o_peq = o_ts + up((nq + 1) * 8),
+                     total = o_peq + sizeof(uint64_t) * 256 * (size_t)k.nw * nq;
+        CK(dev_alloc(c, &k.mem, total), "cudaMallocAsync(class)");
         s->cls.push_back(k);
         blg_search::Cls &kk = s->cls.back();
         kk.h_qlen = len[slot];
-        // one device block per class: [qidx | qlen] (filled by one copy), lo,
-        // hi, work, tile_start, peq — 256-byte aligned parts
-        auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
-        const size_t nq = (size_t)kk.nq;
-        const size_t o_qidx = 0, o_qlen = nq * 4, o_lo = up(2 * nq * 4), o_hi = o_lo + up(nq * 4),
-                     o_work = o_hi + up(nq * 4), o_ts = o_work + 256, o_peq = o_ts + up((nq + 1) * 8),
-                     total = o_peq + sizeof(uint64_t) * 256 * (size_t)kk.nw * nq;
-        CK(dev_alloc(c, &kk.mem, total), "cudaMallocAsync(class)");
         uint8_t *m = (uint8_t *)kk.mem;
         kk.qidx = (int32_t *)(m + o_qidx);
         kk.qlen = (int32_t *)(m + o_qlen);
@@ -2140,6 +2148,13 @@ int blg_set_schedule(blg_ctx *c, int mode) {
     ENTER(c);
     if (mode < BLG_SCHED_AUTO || mode > BLG_SCHED_LENSORT) return fail(c, BLG_ERR_ARG, "unknown schedule");
     c->sched = mode;
+    return BLG_OK;
+}
+
+int blg_set_fault_injection(blg_ctx *c, int64_t alloc_fail_after, int32_t wait_polls) {
+    ENTER(c);
+    c->fault_alloc_after = alloc_fail_after < 0 ? -1 : alloc_fail_after;
+    c->fault_wait_polls = wait_polls < 0 ? -1 : wait_polls;
     return BLG_OK;
 }
 

@@ -39,6 +39,12 @@ struct blg_ctx {
     blg_sched_model *model = nullptr;  // trained/loaded scheduler network, if any
     blg_tuning tune;                   // launch shapes (autotuned or defaults)
     bool prof = false;
+    // fault injection for tests of the error paths (blg_set_fault_injection):
+    // the device allocation after `fault_alloc_after` more successes fails
+    // (-1: off); the short-pair tile kernel's first bounded copy wait gives
+    // up after `fault_wait_polls` polls (-1: the normal bound)
+    int64_t fault_alloc_after = -1;
+    int32_t fault_wait_polls = -1;
     // pinned host staging for arrays the host builds and copies (grown on
     // demand; stage_done marks the end of the last copy out of it)
     void *stage = nullptr;

@@ -18,7 +18,13 @@
 // Host code must not pass `g_noalloc_peq` itself to a kernel: on the host
 // that name is a stand-in, not a device address. The device address comes
 // from cudaGetSymbolAddress, looked up once per device (first call on that
-// device, with the device current) and cached.
+// device, with the device current) and cached. With CUDA's lazy module
+// loading that first call is also when this file's kernels and the 2 MiB
+// array are loaded onto the device, so it can still fail for lack of memory:
+// callers make one small call at start-up, before any stream capture. The
+// cached address belongs to the device's primary context; after a device
+// reset (cudaDeviceReset) this entry point must not be used again in the
+// process.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -118,7 +124,7 @@ int scratch_address(blg_ctx *c, uint64_t **out) {
     return BLG_OK;
 }
 
-bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+bool aligned(const void *p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
 
 }  // namespace
 
@@ -136,8 +142,15 @@ extern "C" int blg_cdist_noalloc(blg_ctx *c, const uint8_t *d_buf_q, size_t q_by
     if (nq == 0 || nc == 0) return BLG_OK;
     if (!d_buf_q || !d_off_q || !d_buf_c || !d_off_c || !d_out)
         return fail(c, BLG_ERR_ARG, "null device pointer");
-    if (!aligned16(d_buf_q) || !aligned16(d_buf_c) || !aligned16(d_out))
-        return fail(c, BLG_ERR_ARG, "device buffers must be 16-byte aligned");
+    // the string buffers feed aligned 4-byte window loads from their 16-byte
+    // aligned start; offsets are read as int64; results are stored as whole
+    // elements (vector stores only where 16 bytes line up)
+    if (!aligned(d_buf_q, 16) || !aligned(d_buf_c, 16))
+        return fail(c, BLG_ERR_ARG, "string buffers must be 16-byte aligned");
+    if (!aligned(d_off_q, 8) || !aligned(d_off_c, 8))
+        return fail(c, BLG_ERR_ARG, "offset arrays must be 8-byte aligned");
+    if (!aligned(d_out, dtype == BLG_INT32 ? 4 : dtype == BLG_UINT16 ? 2 : 1))
+        return fail(c, BLG_ERR_ARG, "output must be aligned to its element size");
     if (q_bytes < 16 || c_bytes < 16)
         return fail(c, BLG_ERR_ARG, "string buffers need 16 readable bytes after the last string");
     uint64_t *scratch = nullptr;
@@ -164,7 +177,16 @@ extern "C" int blg_cdist_noalloc(blg_ctx *c, const uint8_t *d_buf_q, size_t q_by
                                                                dtype, d_out, c->d_status, 1u);
         c->launches += 2;
         const cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return cuda_fail(c, e, "blg_cdist_noalloc launch");
+        if (e != cudaSuccess) {
+            // earlier chunks may still be running on the caller's buffers:
+            // let them finish and clear any status they raised before
+            // reporting the launch error
+            const int rc_launch = cuda_fail(c, e, "blg_cdist_noalloc launch");
+            const std::string msg = c->err;
+            sync_and_status(c);
+            c->err = msg;
+            return rc_launch;
+        }
     }
     rc = sync_and_status(c);
     if (rc == BLG_ERR_ARG && c->err.find("longer than") != std::string::npos)

@@ -319,7 +319,7 @@ __device__ __forceinline__ void load_offs(PairOffs &o, const DevStrings &A, cons
 template <bool HASK, int NBUF>
 __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : 3)
     k_pairs_tile(DevStrings A, DevStrings B, int P, int k, int dtype, void *out, LongQueue q, uint32_t *status,
-                 uint32_t unit) {
+                 uint32_t unit, uint32_t wait_polls) {
     extern __shared__ __align__(128) uint8_t s_raw[];
     TileShared<NBUF> &S = *reinterpret_cast<TileShared<NBUF> *>(s_raw);
     const Units u{unit, unit + unit};
@@ -370,10 +370,11 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : 3)
             tile_issue(S, buf ^ 1, A, B, nb.a0, nb.a1, nb.b0, nb.b1);
             if (t + 2 * G < ntiles) tile_bounds(t + 2 * G, nb);
         }
-        const bool ok = mbar_wait(&S.bar[buf], parity);
+        const bool ok = mbar_wait(&S.bar[buf], parity, wait_polls);
         if (__syncthreads_or(!ok)) {
-            // a copy did not complete in time: report, wait (bounded) for the
-            // copies still in flight, and stop
+            // a copy did not complete in time: report, wait (bounded, at the
+            // normal bound whatever `wait_polls` was) for the copies still in
+            // flight, and stop
             if (tid == 0) {
                 atomicOr(status, ST_QUEUE_TIMEOUT);
                 mbar_wait(&S.bar[buf], parity);
@@ -519,28 +520,29 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : 3)
 // ------------------------------------------------------------- launcher --
 template <bool HASK, int NBUF>
 static cudaError_t launch_tile(cudaStream_t st, int sms, const DevStrings &A, const DevStrings &B, int P, int k,
-                               int dtype, void *out, const LongQueue &q, uint32_t *status) {
+                               int dtype, void *out, const LongQueue &q, uint32_t *status, uint32_t polls) {
     const int64_t ntiles = (A.n + P - 1) / P;
     const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sms * (NBUF == 2 ? 2 : 3));
     const size_t smem = sizeof(TileShared<NBUF>);
     cudaFuncSetAttribute(k_pairs_tile<HASK, NBUF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_pairs_tile<HASK, NBUF><<<grid, kTileThreads, smem, st>>>(A, B, P, k, dtype, out, q, status, 1u);
+    k_pairs_tile<HASK, NBUF><<<grid, kTileThreads, smem, st>>>(A, B, P, k, dtype, out, q, status, 1u, polls);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, const DevStrings &A,
                               const DevStrings &B, int tile_pairs, int k, int dtype, void *out, const LongQueue &q,
-                              uint32_t *status) {
+                              uint32_t *status, int32_t wait_polls) {
     if (A.n <= 0) return cudaSuccess;
+    const uint32_t polls = wait_polls < 0 ? kMbarPolls : (uint32_t)wait_polls;
     int P = tile_pairs;
     if (P > kTileMaxPairs) P = kTileMaxPairs;
     if (P < 32) P = 32;
     P &= ~3;                                                // 4-aligned tiles keep the vector stores aligned
     if (buffers == 1)
-        return hask ? launch_tile<true, 1>(st, sms, A, B, P, k, dtype, out, q, status)
-                    : launch_tile<false, 1>(st, sms, A, B, P, k, dtype, out, q, status);
-    return hask ? launch_tile<true, 2>(st, sms, A, B, P, k, dtype, out, q, status)
-                : launch_tile<false, 2>(st, sms, A, B, P, k, dtype, out, q, status);
+        return hask ? launch_tile<true, 1>(st, sms, A, B, P, k, dtype, out, q, status, polls)
+                    : launch_tile<false, 1>(st, sms, A, B, P, k, dtype, out, q, status, polls);
+    return hask ? launch_tile<true, 2>(st, sms, A, B, P, k, dtype, out, q, status, polls)
+                : launch_tile<false, 2>(st, sms, A, B, P, k, dtype, out, q, status, polls);
 }
 
 }  // namespace blg

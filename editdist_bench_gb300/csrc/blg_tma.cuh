@@ -46,8 +46,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // any copy's latency. Returns false when it gave up.
 constexpr uint32_t kMbarPolls = 1u << 24;
 
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kMbarPolls; i++)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t polls = kMbarPolls) {
+    for (uint32_t i = 0; i < polls; i++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }

@@ -152,13 +152,18 @@ int blg_cdist_batch(blg_ctx *ctx, const blg_problem *probs, int32_t nprob);
  * allocation. The only scratch (per-query Peq tables) is a fixed 2 MiB
  * array inside the library, per device, for the life of the process.
  * Limits: every query at most 256 bytes (longer -> BLG_ERR_ARG after the
- * call; that row is not written); buffers 16-byte aligned; offsets relative
- * to each buffer's start; q_bytes/c_bytes are the readable sizes of the byte
- * buffers and must leave 16 bytes after the last string. The first call on a
- * device looks up the scratch address (do it before any stream capture).
- * All calls share the scratch: calls whose work overlaps on the GPU (other
- * contexts or threads on the same device) race; calls on one context are
- * ordered. Returns after the results are complete (synchronises). */
+ * call; that row is not written); string buffers 16-byte aligned, offset
+ * arrays 8-byte aligned, the output aligned to its element size (checked
+ * before anything runs: BLG_ERR_ARG); offsets relative to each buffer's
+ * start; q_bytes/c_bytes are the readable sizes of the byte buffers and must
+ * leave 16 bytes after the last string. The first call on a device looks up
+ * the scratch address and, with CUDA's lazy module loading, loads the
+ * library's kernels and the 2 MiB array onto the device: make one small
+ * call at start-up (before any stream capture), so that later calls allocate
+ * nothing. Not usable after a device reset (cudaDeviceReset) in the same
+ * process. All calls share the scratch: calls whose work overlaps on the GPU
+ * (other contexts or threads on the same device) race; calls on one context
+ * are ordered. Returns after the results are complete (synchronises). */
 int blg_cdist_noalloc(blg_ctx *ctx, const uint8_t *d_buf_q, size_t q_bytes, const int64_t *d_off_q,
                       int64_t nq, const uint8_t *d_buf_c, size_t c_bytes, const int64_t *d_off_c,
                       int64_t nc, int32_t max_dist, int32_t dtype, void *d_out);
@@ -240,6 +245,19 @@ int blg_host_alloc(blg_ctx *ctx, size_t bytes, void **h_ptr);
 int blg_host_free(blg_ctx *ctx, void *h_ptr);
 /* Wait for the context's stream and report any status a kernel raised. */
 int blg_synchronize(blg_ctx *ctx);
+
+/* Fault injection for tests of the error paths; no counterpart in the
+ * reference, whose one failure mode besides bad arguments is an allocation
+ * failure (csrc/myers.c:162-164 returns -1, bench/cmyers.py:82-84 raises
+ * MemoryError). alloc_fail_after >= 0: after that many more device
+ * allocations of this context succeed, the next one fails as if the device
+ * were out of memory (BLG_ERR_ALLOC); the hook is then spent. -1: off.
+ * wait_polls >= 0: the short-pair tile kernel's bounded wait for its staged
+ * strings gives up after that many polls instead of its normal bound, so the
+ * call ends with BLG_ERR_TIMEOUT (the kernel still waits, at the normal
+ * bound, for its copies in flight before it returns). -1: normal bound.
+ * Nothing here faults, traps or hangs the GPU; the context stays usable. */
+int blg_set_fault_injection(blg_ctx *ctx, int64_t alloc_fail_after, int32_t wait_polls);
 
 /* Timing on the context's stream with CUDA events (ms between start/stop). */
 int blg_timer_start(blg_ctx *ctx);

@@ -32,7 +32,9 @@ import sysconfig
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REF_SRC = os.environ.get("BLG_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: BLG_REFERENCE_ROOT, else a sibling directory
+# named "reference" next to this repository
+REF_SRC = os.environ.get("BLG_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 CC = os.environ.get("CC", "gcc")
 CXX = os.environ.get("CXX", "g++")
 

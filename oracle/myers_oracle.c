@@ -23,7 +23,7 @@
  * roofline count and the exit-column labels of the learned scheduler.
  *
  * Parity of this restatement is pinned against the reference's own C core
- * compiled from its sources (oracle/Makefile, target `ref`) and against the
+ * compiled from its sources (oracle/build_oracle.py, `build_ref`) and against the
  * reference's known answers (tests/golden/).
  */
 #include <stdint.h>
