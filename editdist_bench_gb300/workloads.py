@@ -16,6 +16,8 @@ go to the engine without a Python string per item.
 """
 from __future__ import annotations
 
+import os
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -26,18 +28,49 @@ DNA_N_P = np.array([0.2475, 0.2475, 0.2475, 0.2475, 0.01])
 
 
 def _symbols(rng, n, alphabet, probs=None) -> np.ndarray:
+    """n i.i.d. symbols of `alphabet`, uniform or with probabilities `probs`.
+    Probabilities that are multiples of 1/D for a small D (the benchmark's
+    {A,C,G,T: 0.2475, N: 0.01} is 99/400 and 4/400) are drawn as integers
+    in [0, D) through a lookup table, which is exact and far faster than a
+    weighted choice over hundreds of millions of draws."""
     if probs is None:
         return alphabet[rng.integers(0, len(alphabet), n, dtype=np.int64)]
+    probs = np.asarray(probs, dtype=np.float64)
+    for d in (100, 400, 1000, 10000):
+        cnt = np.rint(probs * d)
+        if np.allclose(cnt / d, probs, rtol=0, atol=1e-12) and cnt.sum() == d:
+            table = np.repeat(alphabet, cnt.astype(np.int64))
+            return table[rng.integers(0, d, n, dtype=np.int32)]
     return alphabet[rng.choice(len(alphabet), size=n, p=probs)]
 
 
-def random_strings(rng, lengths, alphabet=DNA, probs=None):
-    """Packed i.i.d. strings with the given lengths."""
+_PAR_BYTES = 1 << 24          # sets larger than this are drawn in parallel pieces
+
+
+def _pool():
+    return ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
+
+
+def random_strings(rng, lengths, alphabet=DNA, probs=None, parallel=True):
+    """Packed i.i.d. strings with the given lengths. Large sets are drawn in
+    pieces of 2^24 bytes on a thread pool, each piece from its own child
+    generator of `rng` (numpy's generators release the GIL while filling)."""
     lengths = np.asarray(lengths, dtype=np.int64)
     off = np.zeros(len(lengths) + 1, dtype=np.int64)
     np.cumsum(lengths, out=off[1:])
-    buf = _symbols(rng, int(off[-1]), alphabet, probs).astype(np.uint8)
-    return _nonempty(buf), off
+    total = int(off[-1])
+    if total <= _PAR_BYTES or not parallel:
+        buf = _symbols(rng, total, alphabet, probs).astype(np.uint8)
+        return _nonempty(buf), off
+    cuts = list(range(0, total, _PAR_BYTES)) + [total]
+    kids = rng.spawn(len(cuts) - 1)
+    buf = np.empty(total, dtype=np.uint8)
+
+    def piece(i):
+        buf[cuts[i]:cuts[i + 1]] = _symbols(kids[i], cuts[i + 1] - cuts[i], alphabet, probs)
+    with _pool() as ex:
+        list(ex.map(piece, range(len(kids))))
+    return buf, off
 
 
 def _nonempty(buf):
@@ -46,37 +79,49 @@ def _nonempty(buf):
 
 def mutate(rng, packed, rates, alphabet=DNA, probs=None, chunk=1 << 16):
     """Apply i.i.d. per-position edits at per-string ``rates`` (scalar or
-    array). Substitution and insertion-before draw a fresh symbol; deletion
-    drops the position. Processed ``chunk`` strings at a time to bound memory."""
+    array): a position is edited with probability rate; the edit is uniform
+    over {substitute, insert-before, delete}; substitution and insertion
+    draw a fresh symbol from the workload's distribution (it may equal the
+    original). Strings are processed ``chunk`` at a time, each chunk with
+    its own child generator of `rng` (on a thread pool when there are
+    several); edit kinds and fresh symbols are drawn for edited positions
+    only."""
     buf, off = packed
     n = len(off) - 1
     rates = np.broadcast_to(np.asarray(rates, dtype=np.float64), (n,))
-    out_parts = []
+    starts = list(range(0, n, chunk))
+    kids = rng.spawn(len(starts))
     new_len = np.zeros(n, dtype=np.int64)
-    for i0 in range(0, n, chunk):
+
+    def one(ci):
+        r, i0 = kids[ci], starts[ci]
         i1 = min(n, i0 + chunk)
         p0, p1 = int(off[i0]), int(off[i1])
         lens = np.diff(off[i0:i1 + 1])
-        sid = np.repeat(np.arange(i1 - i0, dtype=np.int64), lens)
         orig = buf[p0:p1]
-        u = rng.random(p1 - p0)
-        op = rng.integers(0, 3, p1 - p0, dtype=np.int8)
-        edit = u < rates[i0:i1][sid]
-        # emitted symbols per position: 1 (keep / substitute), 2 (insert-before), 0 (delete)
-        cnt = np.ones(p1 - p0, dtype=np.int64)
-        cnt[edit & (op == 1)] = 2
-        cnt[edit & (op == 2)] = 0
-        start = np.zeros(p1 - p0 + 1, dtype=np.int64)
-        np.cumsum(cnt, out=start[1:])
-        out = np.empty(int(start[-1]), dtype=np.uint8)
-        fresh = _symbols(rng, p1 - p0, alphabet, probs).astype(np.uint8)
-        first = np.where(edit & (op != 2), fresh, orig)
-        has = cnt > 0
-        out[start[:-1][has]] = first[has]
-        ins = edit & (op == 1)
-        out[start[:-1][ins] + 1] = orig[ins]
-        out_parts.append(out)
-        new_len[i0:i1] = np.bincount(sid, weights=cnt, minlength=i1 - i0).astype(np.int64)
+        pos = np.flatnonzero(r.random(p1 - p0) < np.repeat(rates[i0:i1], lens))   # edited positions
+        op = r.integers(0, 3, len(pos), dtype=np.int8)                    # 0 sub, 1 insert-before, 2 delete
+        fresh = _symbols(r, len(pos), alphabet, probs).astype(np.uint8)
+        # every position emits its own symbol once (keep, substitute), twice
+        # (insert-before: the fresh symbol, then the original) or not at all
+        cnt = np.ones(p1 - p0, dtype=np.intp)
+        cnt[pos[op == 1]] = 2
+        cnt[pos[op == 2]] = 0
+        out = np.repeat(orig, cnt)
+        delta = (op == 1).astype(np.int64) - (op == 2)
+        dest = pos + np.cumsum(delta) - delta                  # output index of each edited position
+        out[dest[op == 0]] = fresh[op == 0]
+        out[dest[op == 1]] = fresh[op == 1]
+        sid = np.searchsorted(off[i0 + 1:i1 + 1] - p0, pos, side="right")   # string of each edit
+        m = i1 - i0
+        new_len[i0:i1] = lens + np.bincount(sid[op == 1], minlength=m) - np.bincount(sid[op == 2], minlength=m)
+        return out
+
+    if len(starts) > 1:
+        with _pool() as ex:
+            out_parts = list(ex.map(one, range(len(starts))))
+    else:
+        out_parts = [one(i) for i in range(len(starts))]
     noff = np.zeros(n + 1, dtype=np.int64)
     np.cumsum(new_len, out=noff[1:])
     nbuf = np.concatenate(out_parts) if out_parts else np.zeros(0, dtype=np.uint8)
@@ -220,17 +265,25 @@ def config4(nq=1024, nc=1 << 20, seed=1004) -> SearchWork:
 def config5(n_problems=256, seed=1005, scale=1.0):
     """mixed many-problem batch: query counts log-uniform in [1,512], choice
     counts log-uniform in [1024, 262144] (times ``scale``), lengths ~
-    U[16,256] over U{ACGT}, max_dist ~ U{0..8}, dtype ~ U{int32,uint16,uint8}."""
+    U[16,256] over U{ACGT}, max_dist ~ U{0..8}, dtype ~ U{int32,uint16,uint8}.
+    The problems' shapes come from `seed` first; each problem's strings then
+    come from its own child generator, on a thread pool."""
     rng = np.random.default_rng(seed)
-    probs = []
     dts = ("int32", "uint16", "uint8")
-    for i in range(n_problems):
+    shapes = []
+    for _ in range(n_problems):
         nq = int(np.exp(rng.uniform(np.log(1), np.log(512 + 1))))
         nq = max(1, min(512, nq))
         nc = int(np.exp(rng.uniform(np.log(1024), np.log(262144 + 1))))
         nc = max(1, min(262144, int(nc * scale)))
-        q = random_strings(rng, rng.integers(16, 257, nq))
-        c = random_strings(rng, rng.integers(16, 257, nc))
-        probs.append(SearchWork(f"problem{i}", q, c, int(rng.integers(0, 9)),
-                                dts[int(rng.integers(0, 3))], {"nq": nq, "nc": nc}))
-    return probs
+        shapes.append((nq, nc, int(rng.integers(0, 9)), dts[int(rng.integers(0, 3))]))
+    kids = rng.spawn(n_problems)
+
+    def one(i):
+        nq, nc, k, dt = shapes[i]
+        r = kids[i]
+        q = random_strings(r, r.integers(16, 257, nq), parallel=False)
+        c = random_strings(r, r.integers(16, 257, nc), parallel=False)
+        return SearchWork(f"problem{i}", q, c, k, dt, {"nq": nq, "nc": nc})
+    with _pool() as ex:
+        return list(ex.map(one, range(n_problems)))

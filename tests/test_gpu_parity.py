@@ -206,6 +206,10 @@ def test_config2_full_properties(gpu):
     rows = np.random.default_rng(0).choice(w.nq, 6, replace=False)
     sub = W.take(w.q, rows)
     np.testing.assert_array_equal(d32[rows], oracle.cross(sub, w.c, threads=6))
+    # the max_dist=2 run against the oracle directly (its own exit rule)
+    rows8 = np.random.default_rng(1).choice(w.nq, 16, replace=False)
+    np.testing.assert_array_equal(d8[rows8], oracle.saturate(oracle.cross(W.take(w.q, rows8), w.c, 2, threads=8),
+                                                             "uint8"))
     # every planted choice is within 3% mutation of some query: its row minimum is small
     assert (d32.min(axis=0) <= 64).all()
 
