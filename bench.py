@@ -14,20 +14,31 @@ matrix. The metric is pairs/s (distances per second; GCUPS beside it).
            L2 flushed by a 256 MB memset between steps (outside the events).
 * e2e:     the same metric through the C-ABI one-call entry point with host
            buffers: H2D of the packed inputs, kernels, D2H of the matrix.
-* roofline: the dominant kernel's algorithmic integer operations per launch
+* roofline: the dominant kernel's algorithmic integer operations per step
            (15 per 32-bit word-step) over its event-timed
            duration, against the integer-pipe peak measured on this GPU by
-           libblg_probe.so; plus its HBM figure.
+           libblg_probe.so; its HBM figure; and its issue-slot utilisation
+           (warp instructions per pair from its ncu summary in profiles/,
+           over SMs x 4 issue slots x the sampled SM clock).
 * cpu_baseline: the oracle's C restatement of the reference's CPU core on a
            bounded sample, all host threads.
 * matches: for a thresholded search, the same search in its matches-only
            form (sorted (query, choice, distance) records instead of the
            dense matrix), kernel-only and end to end.
+* runs:    the headline's max_dist=2 uint8 run, and each of the other four
+           benchmark configurations (config1 .. config5 but the headline):
+           kernel-only pairs/s, e2e, a CPU sample, the dominant kernel's
+           roofline (HBM, integer pipe, issue slots) and, for the uneven
+           pairs (3) and the thresholded search (4), every work order side
+           by side (plain = the reference's natural order, auto, lensort,
+           learned with its training time). --no-suite skips them.
 * --impl reference: the reference's CPU path (here: the oracle port, since
            the reference's sources are not on the GPU host) on the same
            workload, all host threads; beside it ("reference_cuda") the
            reference's own CUDA kernels, compiled for sm_103a from its
-           sources, timed kernel-only on this GPU where that cubin exists.
+           sources, timed kernel-only on this GPU where that cubin exists,
+           and the same for the other four configurations
+           ("reference_cuda_runs").
 
 Under torchrun (N > 1) every rank runs its own replica of the workload on
 its own GPU (weak scaling, no data-path collective); rank 0 reports the
@@ -521,24 +532,41 @@ def hbm_peak() -> tuple:
         return 6800.0, "fallback 6.8 TB/s"
 
 
-def read_traffic(kernel: str, workload: str):
-    """dram bytes per launch from the committed ncu summary, if one exists."""
+def read_profile(kernel: str, workload: str) -> dict:
+    """Machine-readable ``key=value`` lines of the committed ncu summary of a
+    kernel launch label on a workload (profiles/<label>_<workload>.txt):
+    traffic_bytes_per_launch (DRAM bytes of a full launch), inst_per_unit
+    (warp instructions per pair, all launches of the label in one step),
+    alu_pipe / issue_active (ncu's pipe and issue utilisation)."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.txt")
+    out = {"path": os.path.relpath(path, ROOT)}
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch="):
-                return float(line.split("=", 1)[1])
+            if "=" in line and not line.startswith((" ", "#")):
+                k, v = line.strip().split("=", 1)
+                try:
+                    out[k] = float(v)
+                except ValueError:
+                    out[k] = v
     except OSError:
-        pass
-    return None
+        return {}
+    return out
 
 
-def train_scheduler(ctx, args) -> dict:
+def device_info(device: int) -> dict:
+    lib = ctypes.CDLL(_build.build_probe())
+    sms, khz = ctypes.c_int(), ctypes.c_int()
+    if lib.blg_probe_device_info(device, ctypes.byref(sms), ctypes.byref(khz)):
+        return {}
+    return {"sms": sms.value, "max_mhz": khz.value / 1e3}
+
+
+def train_scheduler(ctx, cfg: int, args) -> dict:
     """Train the work-order network on up to 2^20 logged rows of the same
     workload shape drawn with a different seed (2000 + config), outside the
     timed region: pairs for configs 1 and 3; for config 4 the survivors of 64
     queries against 2^20 choices (the thresholded search's own rows)."""
-    if args.config == 4:
+    if cfg == 4:
         t0 = time.perf_counter()
         w = W.config4(nq=64, nc=1 << 20, seed=2004)
         batch = gpu.SearchBatch(w.q, w.c)
@@ -550,11 +578,11 @@ def train_scheduler(ctx, args) -> dict:
         return {"trained": True, "rows_max": 1 << 20, "seed": 2004, "rows_from": "64 queries x 2^20 choices",
                 "epochs": args.epochs, "lr": args.lr, "final_mse": loss.value, "train_s": t2 - t1,
                 "data_s": t1 - t0}
-    gen = {1: W.config1, 3: W.config3}.get(args.config)
+    gen = {1: W.config1, 3: W.config3}.get(cfg)
     if gen is None:
         return {"trained": False, "why": "the learned order applies to pairwise and thresholded-search workloads"}
     t0 = time.perf_counter()
-    w = gen(n=1 << 20, seed=2000 + args.config)
+    w = gen(n=1 << 20, seed=2000 + cfg)
     batch = gpu.PairsBatch(w.a, w.b)
     t1 = time.perf_counter()
     loss = ctypes.c_float()
@@ -562,8 +590,158 @@ def train_scheduler(ctx, args) -> dict:
     ctx.check(ctx.lib.blg_sched_train(ctx.h, batch.h, k, args.epochs, ctypes.c_float(args.lr), 1 << 20,
                                       ctypes.byref(loss)))
     t2 = time.perf_counter()
-    return {"trained": True, "rows_max": 1 << 20, "seed": 2000 + args.config, "epochs": args.epochs,
+    return {"trained": True, "rows_max": 1 << 20, "seed": 2000 + cfg, "epochs": args.epochs,
             "lr": args.lr, "final_mse": loss.value, "train_s": t2 - t1, "data_s": t1 - t0}
+
+
+def timed_steps(ctx, flush, fn, steps):
+    """CUDA-event times (ms) of `steps` calls of fn, L2 flushed before each."""
+    start, stop = device_timer(ctx)
+    times = []
+    for _ in range(steps):
+        flush_l2(ctx, flush)
+        start()
+        fn()
+        times.append(stop())
+    return times
+
+
+def kernel_stats(ctx, flush, fn, reps=3):
+    """Per-launch-label event timing of `reps` steps: ({label: {launches,
+    total_ms}}, the label with the largest total)."""
+    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 1))
+    for _ in range(reps):
+        flush_l2(ctx, flush)
+        fn()
+    buf = ctypes.create_string_buffer(8192)
+    ctx.check(ctx.lib.blg_profile_report(ctx.h, buf, 8192))
+    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 0))
+    kstats = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.split()
+        kstats[name] = {"launches": int(cnt) / reps, "ms_per_step": float(ms) / reps}
+    top = max(kstats, key=lambda n: kstats[n]["ms_per_step"]) if kstats else None
+    return kstats, top
+
+
+def e2e_leg(bench, pin, steps, warmup, i=0) -> dict:
+    """The same metric through the one-call C-ABI from pinned host buffers:
+    wall clock of whole calls (copies in, kernels, copies out)."""
+    for _ in range(max(warmup, 3)):              # the first calls on fresh pinned pages run slow
+        bench.e2e_call(i)
+    t = []
+    for _ in range(max(3, steps)):
+        t0 = time.perf_counter()
+        bench.e2e_call(i)
+        t.append(time.perf_counter() - t0)
+    s = statistics.median(t)
+    h2d, d2h = bench.io_bytes(i)
+    return {"value": bench.pairs / s, "unit": "pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "ms_per_call": s * 1e3,
+            "path": "one-call C-ABI (blg_pairwise / blg_cdist / blg_cdist_batch), pinned host buffers, wall clock"}
+
+
+def roofline_block(bench, kstats, top, peak, exit_sum, dev, clock_mhz) -> dict:
+    """The dominant launch label's roofline: algorithmic bytes and integer
+    ops per step over its event time (HBM and integer-pipe fractions, the
+    binding one first), plus its issue-slot utilisation from the warp
+    instructions per pair its ncu summary records."""
+    ms = kstats[top]["ms_per_step"]
+    ops = bench.alg_ops(0, exit_sum)
+    hpeak, hsrc = hbm_peak()
+    hbm = {"achieved": bench.alg_bytes(0) / (ms / 1e3) / 1e9, "peak": hpeak, "unit": "GB/s",
+           "peak_source": hsrc, "alg_bytes_per_step": bench.alg_bytes(0)}
+    hbm["frac"] = hbm["achieved"] / hpeak
+    ipart = {"peak": peak.get("gops"), "unit": "Gop/s",
+             "peak_source": "measured: libblg_probe LOP3/IADD3 stream on this GPU", "peak_detail": peak}
+    if ops is not None and peak.get("gops"):
+        ipart["alg_ops_per_step"] = ops
+        ipart["achieved"] = ops / (ms / 1e3) / 1e9
+        ipart["frac"] = ipart["achieved"] / peak["gops"]
+    prof = read_profile(top, bench.w.name)
+    issue = None
+    if prof.get("inst_per_unit") and dev.get("sms"):
+        mhz = clock_mhz or dev["max_mhz"]
+        slots = dev["sms"] * 4 * mhz * 1e6 * ms / 1e3
+        inst = prof["inst_per_unit"] * bench.pairs
+        issue = {"frac": inst / slots, "inst_per_unit": prof["inst_per_unit"], "unit": "warp instructions per pair",
+                 "clock_mhz": mhz, "alu_pipe_ncu": prof.get("alu_pipe"), "issue_active_ncu": prof.get("issue_active"),
+                 "source": prof["path"],
+                 "how": "inst_per_unit x pairs per step / (event ms x SMs x 4 issue slots per clock x SM clock)"}
+    # short exact pairs (config 1) are bound by moving their bytes; the rest by the integer pipe
+    primary = hbm if (bench.kind == "pairwise" and bench.runs[0][0] is None) else ipart
+    traffic = prof.get("traffic_bytes_per_launch")
+    launches = kstats[top]["launches"]
+    return {"kernel": top, "bound": "hbm" if primary is hbm else "int", "achieved": primary.get("achieved"),
+            "peak": primary.get("peak"), "unit": primary["unit"], "frac": primary.get("frac"),
+            "traffic": traffic, "ms_per_launch": ms / launches, "launches_per_step": launches,
+            "int": ipart, "hbm": hbm, "issue": issue}
+
+
+def cpu_leg(bench, budget_s: float) -> tuple:
+    """The oracle on a bounded sample (all host threads, then one thread):
+    the cpu_baseline object, and the exit-column total of the reference's
+    rule scaled to the workload (the algorithmic ops of max_dist runs)."""
+    threads = effective_cpus()
+    v, sample, n_s, res = bench.cpu_sample(threads, budget_s)
+    v1, sample1, _, _ = bench.cpu_sample(1, budget_s / 3)
+    cpu = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": sample,
+           "single_thread": {"value": v1, "sample": sample1}, "gate": bench.gate(n_s, res)}
+    exit_sum = None
+    if bench.kind in ("pairwise", "batch") or bench.runs[0][0] is not None:
+        exit_sum = exit_columns(bench, n_s)
+    return cpu, exit_sum
+
+
+SUITE_SCHEDULES = {3: ["plain", "auto", "lensort", "learned"], 4: ["plain", "auto", "lensort", "learned"]}
+
+
+def suite_config(cfg, ctx, flush, pin, args, peak, dev, clock_mhz) -> dict:
+    """One benchmark configuration besides the headline: kernel-only pairs/s
+    under each work order it has, e2e, CPU sample, roofline."""
+    t0 = time.perf_counter()
+    bench = make_bench(cfg)
+    gen_s = time.perf_counter() - t0
+    steps = max(3, min(args.steps, 10))
+    scheds = SUITE_SCHEDULES.get(cfg, ["auto"])
+    res = {"workload": bench.describe()["workload"], "config": cfg, "data_gen_s": gen_s, "steps": steps,
+           "warmup": args.warmup}
+    sched_out = {}
+    kstats = top = None
+    try:
+        for sch in scheds:
+            gpu.set_schedule(sch)
+            entry = {}
+            if sch == "learned":
+                entry["training"] = train_scheduler(ctx, cfg, args)
+            for _ in range(args.warmup):
+                bench.step(0)
+            gpu.synchronize()
+            ms = statistics.median(timed_steps(ctx, flush, lambda: bench.step(0), steps))
+            entry.update({"value": bench.pairs / (ms / 1e3), "ms_per_step": ms,
+                          "gcups": bench.cells / (ms / 1e3) / 1e9})
+            sched_out[sch] = entry
+            if sch == "auto":
+                kstats, top = kernel_stats(ctx, flush, lambda: bench.step(0))
+    finally:
+        gpu.set_schedule("auto")
+    a = sched_out["auto"]
+    res.update({"value": a["value"], "unit": "pairs/s", "ms_per_step": a["ms_per_step"], "gcups": a["gcups"],
+                "schedule": "auto", "kernels": kstats})
+    if len(scheds) > 1:
+        res["schedules"] = sched_out
+        res["speedup_vs_plain"] = {s: sched_out["plain"]["ms_per_step"] / v["ms_per_step"]
+                                   for s, v in sched_out.items() if s != "plain"}
+    bench.e2e_setup(pin)
+    res["e2e"] = e2e_leg(bench, pin, steps, args.warmup)
+    m = matches_leg(bench, ctx, pin, flush, args)
+    if m:
+        res["matches"] = m
+    cpu, exit_sum = (None, None) if args.no_cpu_baseline else cpu_leg(bench, args.suite_cpu_budget)
+    res["cpu_baseline"] = cpu
+    if top:
+        res["roofline"] = roofline_block(bench, kstats, top, peak, exit_sum, dev, clock_mhz)
+    return res
 
 
 # ------------------------------------------------------------------ arms --
@@ -579,20 +757,10 @@ def run_ours(args, ranks: Ranks):
     p = ctypes.c_void_p()
     ctx.check(ctx.lib.blg_malloc(ctx.h, L2_FLUSH_BYTES, ctypes.byref(p)))
     flush = gpu.DeviceArray(p.value, (L2_FLUSH_BYTES,), np.uint8, ctx)
-    start, stop = device_timer(ctx)
-
-    def timed(i, steps):
-        times = []
-        for _ in range(steps):
-            flush_l2(ctx, flush)
-            start()
-            bench.step(i)
-            times.append(stop())
-        return times
 
     sched_info = None
     if args.schedule == "learned":
-        sched_info = train_scheduler(ctx, args)
+        sched_info = train_scheduler(ctx, args.config, args)
     for i in range(len(bench.runs)):          # warm-up every run variant
         for _ in range(args.warmup):
             bench.step(i)
@@ -606,7 +774,7 @@ def run_ours(args, ranks: Ranks):
     ranks.barrier()
     launches0 = ctx.lib.blg_launch_count(ctx.h)
     wall0 = time.perf_counter()
-    times = timed(0, args.steps)
+    times = timed_steps(ctx, flush, lambda: bench.step(0), args.steps)
     wall = time.perf_counter() - wall0
     launches = ctx.lib.blg_launch_count(ctx.h) - launches0
     gpu.synchronize()
@@ -618,40 +786,20 @@ def run_ours(args, ranks: Ranks):
 
     extra_runs = {}
     for i in range(1, len(bench.runs)):
-        t = timed(i, max(3, args.steps // 2))
-        ms = statistics.median(t)
+        ms = statistics.median(timed_steps(ctx, flush, lambda: bench.step(i), max(3, args.steps // 2)))
         k, dt = bench.runs[i]
         extra_runs[f"max_dist={k},{dt}"] = {"pairs_per_s": bench.pairs / (ms / 1e3), "ms_per_step": ms,
                                             "gcups": bench.cells / (ms / 1e3) / 1e9}
 
     # per-kernel event timing for the roofline (a separate, profiled pass)
-    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 1))
-    for _ in range(3):
-        flush_l2(ctx, flush)
-        bench.step(0)
-    buf = ctypes.create_string_buffer(4096)
-    ctx.check(ctx.lib.blg_profile_report(ctx.h, buf, 4096))
-    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 0))
-    kstats = {}
-    for line in buf.value.decode().splitlines():
-        name, cnt, ms = line.split()
-        kstats[name] = {"launches": int(cnt), "total_ms": float(ms)}
-    top = max(kstats, key=lambda n: kstats[n]["total_ms"]) if kstats else None
+    kstats, top = kernel_stats(ctx, flush, lambda: bench.step(0))
 
     # e2e through the C-ABI with pinned host buffers
     pin = Pinned(ctx)
     bench.e2e_setup(pin)
-    for _ in range(max(args.warmup, 5)):           # the first calls on fresh pinned pages run slow
-        bench.e2e_call(0)
-    e2e_t = []
-    for _ in range(max(3, min(args.steps, 10))):
-        t0 = time.perf_counter()
-        bench.e2e_call(0)
-        e2e_t.append(time.perf_counter() - t0)
-    e2e_s = ranks.max(statistics.median(e2e_t))
-    h2d, d2h = bench.io_bytes(0)
+    e2e = e2e_leg(bench, pin, min(args.steps, 10), args.warmup)
+    e2e["value"] = bench.pairs * ranks.world / (ranks.max(bench.pairs / e2e["value"]))
     matches = matches_leg(bench, ctx, pin, flush, args)
-    pin.free()
 
     result = {
         "metric": "pairs/s", "value": value, "unit": "pairs/s", "n_gpus": ranks.world,
@@ -661,9 +809,7 @@ def run_ours(args, ranks: Ranks):
         "config": dict(bench.describe(), l2="flushed between steps (256 MB memset outside the timed events)",
                        parallelism="replicas" if ranks.world > 1 else "single GPU", schedule=args.schedule),
         "gcups": bench.cells * ranks.world / (ms_per_step / 1e3) / 1e9,
-        "e2e": {"value": bench.pairs * ranks.world / e2e_s, "unit": "pairs/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "path": "one-call C-ABI (blg_pairwise / blg_cdist / blg_cdist_batch), pinned host buffers, wall clock"},
+        "e2e": e2e,
         "gpu_launches": int(launches), "wall_s_timed_region": wall, "scheduler": sched_info, "tuning": tune,
         "clocks": clk, "runs": extra_runs, "kernels": kstats,
     }
@@ -676,41 +822,30 @@ def run_ours(args, ranks: Ranks):
 
     if ranks.rank == 0:
         peak = int_peak(ranks.local)
+        dev = device_info(ranks.local)
         exit_sum = None
         cpu = None
         if not args.no_cpu_baseline:
-            threads = effective_cpus()
-            v, sample, n_s, res = bench.cpu_sample(threads, args.cpu_budget)
-            v1, sample1, _, _ = bench.cpu_sample(1, args.cpu_budget / 3)
-            cpu = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": sample,
-                   "single_thread": {"value": v1, "sample": sample1},
-                   "gate": bench.gate(n_s, res)}
-            if bench.kind in ("pairwise", "batch") or bench.runs[0][0] is not None:
-                exit_sum = exit_columns(bench, n_s)
+            cpu, exit_sum = cpu_leg(bench, args.cpu_budget)
         result["cpu_baseline"] = cpu
         if top:
-            per_launch_ms = kstats[top]["total_ms"] / kstats[top]["launches"]
-            ops = bench.alg_ops(0, exit_sum)
-            launches_per_step = kstats[top]["launches"] / 3.0
-            hpeak, hsrc = hbm_peak()
-            hbm_bytes = bench.alg_bytes(0) / launches_per_step
-            hbm = {"achieved": hbm_bytes / (per_launch_ms / 1e3) / 1e9, "peak": hpeak, "unit": "GB/s",
-                   "peak_source": hsrc, "alg_bytes_per_launch": hbm_bytes}
-            hbm["frac"] = hbm["achieved"] / hpeak
-            ipart = {"peak": peak.get("gops"), "unit": "Gop/s",
-                     "peak_source": "measured: libblg_probe LOP3/IADD3 stream on this GPU", "peak_detail": peak}
-            if ops is not None and peak.get("gops"):
-                ipart["alg_ops_per_launch"] = ops / launches_per_step
-                ipart["achieved"] = ipart["alg_ops_per_launch"] / (per_launch_ms / 1e3) / 1e9
-                ipart["frac"] = ipart["achieved"] / peak["gops"]
-            # short exact pairs (config 1) are bound by moving their bytes; the rest by the integer pipe
-            primary = hbm if (bench.kind == "pairwise" and bench.runs[0][0] is None) else ipart
-            rl = {"kernel": top, "bound": "hbm" if primary is hbm else "int",
-                  "achieved": primary.get("achieved"), "peak": primary.get("peak"), "unit": primary["unit"],
-                  "frac": primary.get("frac"), "traffic": read_traffic(top, bench.w.name),
-                  "ms_per_launch": per_launch_ms, "int": ipart, "hbm": hbm}
-            result["roofline"] = rl
+            result["roofline"] = roofline_block(bench, kstats, top, peak, exit_sum, dev, clk.get("sm_mhz"))
+        # the other benchmark configurations (rank 0 of a single-GPU run):
+        # kernel-only, e2e, work orders, roofline each; results identical to
+        # the oracle's by the parity tests
+        if not args.no_suite and ranks.world == 1:
+            del bench
+            suite_t0 = time.perf_counter()
+            for cfg in (1, 2, 3, 4, 5):
+                if cfg == args.config:
+                    continue
+                result["runs"][f"config{cfg}"] = suite_config(cfg, ctx, flush, pin, args, peak, dev,
+                                                              clk.get("sm_mhz"))
+            result["suite_s"] = time.perf_counter() - suite_t0
+        pin.free()
         print(json.dumps(result), flush=True)
+    else:
+        pin.free()
 
 
 def reference_cuda_leg(w, steps: int, warmup: int) -> dict:
@@ -800,6 +935,20 @@ def run_reference(args, ranks: Ranks):
         ref_cuda = reference_cuda_leg(w, args.steps, max(args.warmup, 3))
     except Exception as e:                         # reported, never fatal to the CPU arm
         ref_cuda = {"unavailable": f"{type(e).__name__}: {e}"}
+    # the reference's CUDA kernels on the other benchmark configurations too
+    # (kernel-only, same GPU), beside the per-configuration lines of our arm
+    ref_runs = {}
+    if not args.no_suite and ranks.world == 1 and "unavailable" not in ref_cuda:
+        del w
+        for c2 in (1, 2, 3, 4, 5):
+            if c2 == cfg:
+                continue
+            try:
+                w2 = {1: W.config1, 2: W.config2, 3: W.config3, 4: W.config4, 5: W.config5}[c2]()
+                ref_runs[f"config{c2}"] = reference_cuda_leg(w2, max(3, min(args.steps, 5)), 2)
+                del w2
+            except Exception as e:
+                ref_runs[f"config{c2}"] = {"unavailable": f"{type(e).__name__}: {e}"}
     print(json.dumps({
         "impl": "reference", "metric": "pairs/s", "value": value, "unit": "pairs/s", "n_gpus": ranks.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
@@ -810,6 +959,7 @@ def run_reference(args, ranks: Ranks):
                          "sample": sample},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "reference_cuda": ref_cuda,
+        "reference_cuda_runs": ref_runs,
     }), flush=True)
 
 
@@ -822,6 +972,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of oracle work per leg")
+    ap.add_argument("--suite-cpu-budget", type=float, default=3.0,
+                    help="seconds of oracle work per leg for the other configurations")
+    ap.add_argument("--no-suite", action="store_true",
+                    help="report the headline configuration only (not the other four under runs)")
     ap.add_argument("--nq", type=int, default=None, help="override the query count (profiling)")
     ap.add_argument("--nc", type=int, default=None, help="override the choice count (profiling)")
     ap.add_argument("--n", type=int, default=None, help="override the pair count (profiling)")

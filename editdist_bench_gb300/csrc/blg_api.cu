@@ -55,7 +55,7 @@ cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, 
                               uint32_t *status, int32_t wait_polls);
 cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, bool band, const DevStrings &A,
                               const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
-                              uint32_t *status);
+                              bool lengap_key, uint32_t *status);
 cudaError_t launch_order(cudaStream_t st, int sms, const PairsPlan &plan);
 cudaError_t launch_solve(cudaStream_t st, int sms, bool hask, const PairsPlan &plan, int k, int dtype,
                          void *out, int32_t *exit_log, bool any_long);
@@ -81,8 +81,8 @@ cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S,
 cudaError_t launch_search_lpt(cudaStream_t st, int sms, int ctas_per_sm, int jobsz, int nw, const DevStrings &CS,
                               const int32_t *perm, const uint64_t *csk, const uint64_t *qsk, const SearchClass &cls,
                               const int32_t *lo, const int32_t *hi, const int64_t *tile_start, int32_t *work,
-                              const uint8_t *keytab, int k, int dtype, void *out, int64_t nc, const SurvRows *rows,
-                              uint32_t *status);
+                              const uint8_t *keytab, int64_t keystride, int k, int dtype, void *out, int64_t nc,
+                              const SurvRows *rows, uint32_t *status);
 cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
                              int64_t min_len, int64_t n_len, int k, int tile, int32_t *lo, int32_t *hi,
                              int64_t *tile_start, int32_t *work);
@@ -489,7 +489,7 @@ static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, const DevStrings &A, co
     const bool band = hask && k <= 31;
     CK(launch(c, "pairs_prep", [&] {
            return launch_pairs_prep(c->stream, grid, hask, learned, band, A, B, k, dtype, d_out, plan,
-                                    c->d_status);
+                                    c->sched == BLG_SCHED_LENSORT, c->d_status);
        }), "pairs_prep");
     if (learned && !want_features)
         CK(launch(c, "sched_keys", [&] { return launch_mlp_keys(c->stream, c->sms, c->model, plan, band); }),
@@ -1032,17 +1032,31 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
                                            k_.lo, k_.hi, k_.tile_start, k_.work);
                }), "surv_plan");
             if (lpt) {
+                // survivor keys: the sketch distance (auto), the network's
+                // per-query table (learned), or one table of the length
+                // difference alone, shared by every query (lensort)
                 uint8_t *keytab = nullptr;
+                int64_t keystride = 0;
+                const int E = (2 * k + 1) * kSketchDistances;
                 if (c->sched == BLG_SCHED_LEARNED && c->model && sched_model_trained(c->model)) {
-                    CK(dev_alloc(c, (void **)&keytab, (size_t)k_.nq * (2 * k + 1) * 65), "cudaMallocAsync(keytab)");
+                    CK(dev_alloc(c, (void **)&keytab, (size_t)k_.nq * E), "cudaMallocAsync(keytab)");
+                    keystride = E;
                     CK(launch(c, "sched_keytab", [&] { return launch_surv_keytab(c->stream, c->sms, c->model, sc, k, keytab); }),
                        "sched_keytab");
+                } else if (c->sched == BLG_SCHED_LENSORT) {
+                    CK(dev_alloc(c, (void **)&keytab, (size_t)E), "cudaMallocAsync(keytab)");
+                    std::vector<uint8_t> tab((size_t)E);
+                    for (int g = 0; g <= 2 * k; g++)              // g = length gap + k: equal lengths first
+                        for (int d = 0; d < kSketchDistances; d++)
+                            tab[(size_t)g * kSketchDistances + d] = (uint8_t)(255 - 8 * std::abs(g - k));
+                    CK(cudaMemcpyAsync(keytab, tab.data(), (size_t)E, cudaMemcpyHostToDevice, c->stream), "H2D keytab");
+                    CK(cudaStreamSynchronize(c->stream), "sync keytab");   // the host table is pageable
                 }
                 CK(launch(c, "search_lpt", [&] {
                        return launch_search_lpt(c->stream, c->sms, c->tune.lpt_ctas, job, k_.nw, s->cs.d,
                                                 s->perm, s->csk, s->qsk, sc, k_.lo,
-                                                k_.hi, k_.tile_start, k_.work, keytab, k, dtype, d_out, s->nc, nullptr,
-                                                c->d_status);
+                                                k_.hi, k_.tile_start, k_.work, keytab, keystride, k, dtype, d_out, s->nc,
+                                                nullptr, c->d_status);
                    }), "search_lpt");
                 dev_free(c, keytab);
             } else {
@@ -1777,7 +1791,7 @@ int blg_sched_train_search(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t 
         CK(launch(c, "search_lpt_logged", [&] {
                return launch_search_lpt(c->stream, c->sms, c->tune.lpt_ctas, job, k_.nw, s->cs.d, s->perm,
                                         s->csk, s->qsk, sc, k_.lo, k_.hi,
-                                        k_.tile_start, k_.work, nullptr, max_dist, BLG_UINT8, out, s->nc, &R,
+                                        k_.tile_start, k_.work, nullptr, 0, max_dist, BLG_UINT8, out, s->nc, &R,
                                         c->d_status);
            }), "search_lpt_logged");
     }

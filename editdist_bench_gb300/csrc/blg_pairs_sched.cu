@@ -36,7 +36,7 @@ __device__ __forceinline__ int cost_bucket(float work) {
 
 template <bool HASK, bool FEAT>
 __global__ void __launch_bounds__(256) k_pairs_prep(DevStrings A, DevStrings B, int k, int dtype, void *out,
-                                                    PairsPlan plan, int band, uint32_t *status) {
+                                                    PairsPlan plan, int band, int lengap_key, uint32_t *status) {
     const int lane = threadIdx.x & 31;
     const int64_t n = A.n;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -72,8 +72,11 @@ __global__ void __launch_bounds__(256) k_pairs_prep(DevStrings A, DevStrings B, 
         LongItem it;
         it.pat = a; it.txt = b; it.m = la; it.n = lb; it.idx = i;
         plan.raw[cls][pos] = it;
-        // the banded loop costs columns plus a window fill, the word solvers columns x words
-        int key = cost_bucket(band ? (float)lb + 16.f : (float)lb * (float)((la + 63) >> 6));
+        // the banded loop costs columns plus a window fill, the word solvers
+        // columns x words; the length-difference order (an ablation) puts
+        // equal lengths first
+        int key = lengap_key ? 255 - min(255, 8 * (lb - la))
+                             : cost_bucket(band ? (float)lb + 16.f : (float)lb * (float)((la + 63) >> 6));
         if (FEAT) {
             const float qb = (float)__popcll(gram_sketch(a, la) ^ gram_sketch(b, lb));
             half *f = plan.feat[cls] + (size_t)pos * kFeatures;
@@ -292,14 +295,14 @@ __global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int
 // ------------------------------------------------------------- launchers --
 cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, bool band, const DevStrings &A,
                               const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
-                              uint32_t *status) {
-    const int bd = band ? 1 : 0;
+                              bool lengap_key, uint32_t *status) {
+    const int bd = band ? 1 : 0, lg = lengap_key ? 1 : 0;
     if (hask) {
-        if (feat) k_pairs_prep<true, true><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, status);
-        else k_pairs_prep<true, false><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, status);
+        if (feat) k_pairs_prep<true, true><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, lg, status);
+        else k_pairs_prep<true, false><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, lg, status);
     } else {
-        if (feat) k_pairs_prep<false, true><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, status);
-        else k_pairs_prep<false, false><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, status);
+        if (feat) k_pairs_prep<false, true><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, lg, status);
+        else k_pairs_prep<false, false><<<grid, 256, 0, st>>>(A, B, k, dtype, out, plan, bd, lg, status);
     }
     return cudaGetLastError();
 }

@@ -97,4 +97,13 @@ int blg_probe_int_peak(int device, int iters, double *logic_ops_per_s, double *m
     return 0;
 }
 
+// SM count and maximum SM clock (kHz) of `device`: the issue-slot
+// denominator of the per-kernel utilisation figure (4 warp instructions per
+// SM per clock).
+int blg_probe_device_info(int device, int *sms, int *clock_khz) {
+    if (cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return -3;
+    if (cudaDeviceGetAttribute(clock_khz, cudaDevAttrClockRate, device) != cudaSuccess) return -3;
+    return 0;
+}
+
 }  // extern "C"

@@ -41,14 +41,14 @@ template <int NW, bool LOG>
 __global__ void __launch_bounds__(256) k_search_lpt(DevStrings CS, const int32_t *perm, const uint64_t *csk,
                                                     const uint64_t *qsk, SearchClass cls, const int32_t *lo,
                                                     const int32_t *hi, const int64_t *tile_start, int32_t *work,
-                                                    const uint8_t *keytab, int k, int dtype, void *out, int64_t nc,
-                                                    int jobsz, SurvRows rows, uint32_t *status, uint32_t unit) {
+                                                    const uint8_t *keytab, int64_t keystride, int k, int dtype,
+                                                    void *out, int64_t nc, int jobsz, SurvRows rows, uint32_t *status,
+                                                    uint32_t unit) {
     extern __shared__ uint32_t s_rows[];              // the query's padded Peq halves (banded layout)
     __shared__ LptShared S;
     const Units u{unit, unit + unit};
     const int tid = threadIdx.x;
     const int64_t total = tile_start[cls.nq];
-    const int E = (2 * k + 1) * kSketchDistances;
     int cur = -1;
     while (true) {
         if (tid == 0) S.job = atomicAdd(work, 1);
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256) k_search_lpt(DevStrings CS, const int32_t
         const uint64_t qs = qsk[row];
         const int64_t s0 = lo[qi] + (job - tile_start[qi]) * jobsz;
         const int cnt = (int)min((int64_t)jobsz, (int64_t)hi[qi] - s0);
-        lpt_job(S, CS, perm, csk, qs, s_rows, 2 * NW + 6, m, row, s0, cnt, k, keytab ? keytab + (size_t)qi * E : nullptr,
+        lpt_job(S, CS, perm, csk, qs, s_rows, 2 * NW + 6, m, row, s0, cnt, k, keytab ? keytab + qi * keystride : nullptr,
                 dtype, out, nc, status, u, [&](int64_t sidx, int n, int cols) {
                     if (!LOG || m == 0 || n == 0 || (sidx % rows.stride) != 0) return;
                     const int64_t at = atomicAdd((unsigned long long *)rows.count, 1ull);
@@ -95,18 +95,18 @@ template <int NW>
 static cudaError_t launch_lpt_nw(cudaStream_t st, int grid, const DevStrings &CS, const int32_t *perm,
                                  const uint64_t *csk, const uint64_t *qsk, const SearchClass &cls, const int32_t *lo,
                                  const int32_t *hi, const int64_t *tile_start, int32_t *work, const uint8_t *keytab,
-                                 int k, int dtype, void *out, int64_t nc, int jobsz, const SurvRows *rows,
-                                 uint32_t *status) {
+                                 int64_t keystride, int k, int dtype, void *out, int64_t nc, int jobsz,
+                                 const SurvRows *rows, uint32_t *status) {
     const size_t smem = (size_t)256 * (2 * NW + 6) * sizeof(uint32_t);
     if (rows) {
         cudaFuncSetAttribute(k_search_lpt<NW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_search_lpt<NW, true><<<grid, 256, smem, st>>>(CS, perm, csk, qsk, cls, lo, hi, tile_start, work, keytab, k,
-                                                        dtype, out, nc, jobsz, *rows, status, 1u);
+        k_search_lpt<NW, true><<<grid, 256, smem, st>>>(CS, perm, csk, qsk, cls, lo, hi, tile_start, work, keytab,
+                                                        keystride, k, dtype, out, nc, jobsz, *rows, status, 1u);
     } else {
         const SurvRows none{nullptr, nullptr, 0, nullptr, 1};
         cudaFuncSetAttribute(k_search_lpt<NW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_search_lpt<NW, false><<<grid, 256, smem, st>>>(CS, perm, csk, qsk, cls, lo, hi, tile_start, work, keytab, k,
-                                                         dtype, out, nc, jobsz, none, status, 1u);
+        k_search_lpt<NW, false><<<grid, 256, smem, st>>>(CS, perm, csk, qsk, cls, lo, hi, tile_start, work, keytab,
+                                                         keystride, k, dtype, out, nc, jobsz, none, status, 1u);
     }
     return cudaGetLastError();
 }
@@ -114,14 +114,14 @@ static cudaError_t launch_lpt_nw(cudaStream_t st, int grid, const DevStrings &CS
 cudaError_t launch_search_lpt(cudaStream_t st, int sms, int ctas_per_sm, int jobsz, int nw, const DevStrings &CS,
                               const int32_t *perm, const uint64_t *csk, const uint64_t *qsk, const SearchClass &cls,
                               const int32_t *lo, const int32_t *hi, const int64_t *tile_start, int32_t *work,
-                              const uint8_t *keytab, int k, int dtype, void *out, int64_t nc, const SurvRows *rows,
-                              uint32_t *status) {
+                              const uint8_t *keytab, int64_t keystride, int k, int dtype, void *out, int64_t nc,
+                              const SurvRows *rows, uint32_t *status) {
     if (cls.nq <= 0) return cudaSuccess;
     if (k < 0 || k > 31 || jobsz < 256 || jobsz > kSurvJob) return cudaErrorInvalidValue;
     const int grid = sms * std::max(1, std::min(ctas_per_sm, 8));
     switch (nw) {
 #define BLG_LPT(W) \
-    case W: return launch_lpt_nw<W>(st, grid, CS, perm, csk, qsk, cls, lo, hi, tile_start, work, keytab, k, dtype, out, nc, jobsz, rows, status);
+    case W: return launch_lpt_nw<W>(st, grid, CS, perm, csk, qsk, cls, lo, hi, tile_start, work, keytab, keystride, k, dtype, out, nc, jobsz, rows, status);
     BLG_LPT(1) BLG_LPT(2) BLG_LPT(3) BLG_LPT(4) BLG_LPT(5) BLG_LPT(6) BLG_LPT(7) BLG_LPT(8)
 #undef BLG_LPT
     default: return cudaErrorInvalidValue;

@@ -176,7 +176,9 @@ int blg_cdist_noalloc(blg_ctx *ctx, const uint8_t *d_buf_q, size_t q_bytes, cons
  *            (the reference's schedule, csrc/gpu_kernels.cu:6-69);
  *  LEARNED — AUTO plus survivors ordered by the scheduler network's
  *            predicted exit column;
- *  LENSORT — AUTO plus survivors ordered by length difference (ablation). */
+ *  LENSORT — AUTO with the work ordered by length difference alone, equal
+ *            lengths first (an ablation: survivors of a search, records of
+ *            the pairs plan). */
 #define BLG_SCHED_AUTO 0
 #define BLG_SCHED_PLAIN 1
 #define BLG_SCHED_LEARNED 2
