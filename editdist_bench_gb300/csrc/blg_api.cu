@@ -35,6 +35,12 @@ cudaError_t launch_build_peq(cudaStream_t st, const DevStrings &Q, const int32_t
 cudaError_t launch_search_seq(cudaStream_t st, int nw, bool hask, const DevStrings &C,
                               const SearchClass &cls, int qpb, int k, int dtype, void *out,
                               uint32_t *status);
+bool search_pfx_supported(int nw);
+cudaError_t launch_search_pfx(cudaStream_t st, int sms, int ctas_per_sm, int nw, const PrefixChoices &P,
+                              const SearchClass &cls, unsigned long long *work, int dtype, void *out);
+cudaError_t launch_prefix_text(cudaStream_t st, int sms, const DevStrings &C, const int32_t *order,
+                               const int64_t *woff, const uint16_t *rowoff, uint32_t *text, int32_t *len,
+                               uint32_t *status);
 cudaError_t launch_search_tt(cudaStream_t st, int nw, bool hask, const TransposedChoices &T,
                              const SearchClass &cls, int qpb, int k, int dtype, void *out);
 cudaError_t launch_transpose_choices(cudaStream_t st, int sms, const DevStrings &C, const int64_t *base,
@@ -153,6 +159,13 @@ struct blg_search {
     // choices in tile-transposed form (exact and unsorted runs), when the
     // padding to each tile's longest choice stays small
     bool tt = false;
+    // choices sorted lexicographically for the exact search with prefix
+    // reuse (PrefixChoices), when the sorted neighbours share enough
+    bool pfx = false;
+    void *pfx_mem = nullptr;          // one device block: order, restarts, base, words, len, orig, work
+    PrefixChoices pd;
+    unsigned long long *pfx_work = nullptr;
+    double pfx_saving = 0.0;          // fraction of text columns the restarts skip
     uint32_t *tt_words = nullptr;
     int64_t *tt_base = nullptr;
     int32_t *tt_len = nullptr;
@@ -745,11 +758,151 @@ static void *host_stage(blg_ctx *c, size_t bytes) {
 // with sketches (survivor kernels of max_dist runs) and the tile-transposed
 // copy (exact and plain-order runs). A resident search set builds both; a
 // one-call search knows its max_dist and schedule and builds one.
-enum { NEED_SORTED = 1, NEED_TT = 2, NEED_ALL = 3 };
+enum { NEED_SORTED = 1, NEED_TT = 2, NEED_PFX = 4, NEED_ALL = 7 };
 
 // perm_stage: pinned room for the permutation (nc int32) reserved by the
 // caller for this upload alone (a batch reserves one region per problem, so
 // no upload waits for an earlier one's copy); null: the context's stage.
+// ---- exact search with prefix reuse (k_search_pfx): the choices sorted
+// lexicographically on the host's thread pool by their first 16 bytes (ties
+// in any order: only the exact common prefixes computed next matter), the
+// common prefix of every sorted neighbour pair, and the two checkpoint
+// columns that skip the most text columns over the warps' chains of
+// kPfxChain consecutive choices. Built when the choices use at most
+// kPfxMaxSymbols distinct bytes and at least kPfxMinSaving of the columns
+// are skipped; the text is laid out on the device (k_prefix_text).
+constexpr int64_t kPfxMinChoices = 4096;
+constexpr double kPfxMinSaving = 0.02;
+
+static int search_build_prefix(blg_ctx *c, const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s) {
+    if (nc < kPfxMinChoices || nc >= INT32_MAX) return BLG_OK;
+    const int64_t cols = oc[nc] - oc[0];
+    if (cols <= 0) return BLG_OK;
+    HostPool &pool = HostPool::get();
+    const int nt = pool.size();
+    std::vector<int64_t> cut((size_t)nt + 1);
+    for (int t = 0; t <= nt; t++) cut[t] = nc * t / nt;
+    // the alphabet: the bytes the choices use
+    std::vector<std::array<uint8_t, 256>> seen((size_t)nt);
+    pool.run(nt, [&](int t) {
+        seen[t].fill(0);
+        for (int64_t x = oc[cut[t]]; x < oc[cut[t + 1]]; x++) seen[t][bc[x]] = 1;
+    });
+    std::vector<uint8_t> sym;
+    std::vector<uint16_t> rowoff(256, 0);
+    for (int v = 0; v < 256; v++) {
+        bool any = false;
+        for (int t = 0; t < nt; t++) any |= seen[t][v] != 0;
+        if (any) {
+            rowoff[v] = (uint16_t)(sym.size() * kPfxRowBytes);
+            sym.push_back((uint8_t)v);
+        }
+    }
+    if (sym.empty() || (int)sym.size() > kPfxMaxSymbols) return BLG_OK;
+    struct Key {
+        uint64_t hi, lo;
+        int32_t idx;
+    };
+    std::vector<Key> keys((size_t)nc);
+    auto be8 = [](const uint8_t *p, int64_t len, int64_t from) {
+        uint64_t v = 0;
+        for (int b = 0; b < 8; b++) v = (v << 8) | (from + b < len ? p[from + b] : 0u);
+        return v;
+    };
+    auto less = [](const Key &a, const Key &b) { return a.hi != b.hi ? a.hi < b.hi : a.lo < b.lo; };
+    pool.run(nt, [&](int t) {
+        for (int64_t i = cut[t]; i < cut[t + 1]; i++) {
+            const uint8_t *p = bc + oc[i];
+            const int64_t len = oc[i + 1] - oc[i];
+            keys[i] = Key{be8(p, len, 0), be8(p, len, 8), (int32_t)i};
+        }
+        std::sort(keys.begin() + cut[t], keys.begin() + cut[t + 1], less);
+    });
+    std::vector<Key> tmp((size_t)nc);
+    for (int w = 1; w < nt; w *= 2) {                        // merge sorted runs pairwise, in parallel
+        const int groups = (nt + 2 * w - 1) / (2 * w);
+        pool.run(groups, [&](int g) {
+            const int64_t lo = cut[std::min(nt, 2 * g * w)], mid = cut[std::min(nt, 2 * g * w + w)],
+                          hi = cut[std::min(nt, 2 * g * w + 2 * w)];
+            std::merge(keys.begin() + lo, keys.begin() + mid, keys.begin() + mid, keys.begin() + hi,
+                       tmp.begin() + lo, less);
+        });
+        keys.swap(tmp);
+    }
+    // common prefixes of sorted neighbours (capped at 255: a restart column is a byte)
+    std::vector<uint8_t> lcp((size_t)nc, 0);
+    std::vector<std::vector<int64_t>> hist((size_t)nt, std::vector<int64_t>(256, 0));
+    pool.run(nt, [&](int t) {
+        for (int64_t p = std::max<int64_t>(1, cut[t]); p < cut[t + 1]; p++) {
+            const int64_t a = keys[p - 1].idx, b = keys[p].idx;
+            const int64_t lim = std::min<int64_t>(255, std::min(oc[a + 1] - oc[a], oc[b + 1] - oc[b]));
+            const uint8_t *x = bc + oc[a], *y = bc + oc[b];
+            int64_t l = 0;
+            while (l < lim && x[l] == y[l]) l++;
+            lcp[p] = (uint8_t)l;
+            if (p % kPfxChain) hist[t][l]++;                  // a chain's first choice never restarts
+        }
+    });
+    std::vector<int64_t> G(257, 0);                           // G[v] = restartable choices with lcp >= v
+    for (int v = 255; v >= 0; v--) {
+        int64_t h = 0;
+        for (int t = 0; t < nt; t++) h += hist[t][v];
+        G[v] = G[v + 1] + h;
+    }
+    int64_t best = 0;
+    int c1 = 0, c2 = 0;
+    for (int a = 1; a < 255; a++)
+        for (int b = a + 1; b <= 255; b++) {
+            const int64_t sv = (int64_t)a * (G[a] - G[b]) + (int64_t)b * G[b];
+            if (sv > best) { best = sv; c1 = a; c2 = b; }
+        }
+    if ((double)best < kPfxMinSaving * (double)cols) return BLG_OK;
+    // sorted order, restart columns, text word offsets (two characters per word)
+    std::vector<int32_t> order((size_t)nc);
+    std::vector<uint8_t> restart((size_t)nc);
+    std::vector<int64_t> woff((size_t)nc + 1, 0);
+    for (int64_t p = 0; p < nc; p++) {
+        order[p] = keys[p].idx;
+        restart[p] = (uint8_t)(p % kPfxChain == 0 ? 0 : lcp[p] >= c2 ? c2 : lcp[p] >= c1 ? c1 : 0);
+        woff[p + 1] = woff[p] + (oc[keys[p].idx + 1] - oc[keys[p].idx] + 1) / 2;
+    }
+    auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t words = (size_t)woff[nc] + kPfxTextSlack;
+    const size_t o_order = 0, o_rs = up(4 * (size_t)nc), o_woff = o_rs + up((size_t)nc),
+                 o_len = o_woff + up(8 * ((size_t)nc + 1)), o_sym = o_len + up(4 * (size_t)nc),
+                 o_rowoff = o_sym + 256, o_text = o_rowoff + 512, o_work = o_text + up(4 * words),
+                 total = o_work + 256;
+    CK(dev_alloc(c, &s->pfx_mem, total), "cudaMallocAsync(prefix layout)");
+    uint8_t *m = (uint8_t *)s->pfx_mem;
+    CK(cudaMemcpyAsync(m + o_order, order.data(), 4 * (size_t)nc, cudaMemcpyHostToDevice, c->stream), "H2D order");
+    CK(cudaMemcpyAsync(m + o_rs, restart.data(), (size_t)nc, cudaMemcpyHostToDevice, c->stream), "H2D restarts");
+    CK(cudaMemcpyAsync(m + o_woff, woff.data(), 8 * ((size_t)nc + 1), cudaMemcpyHostToDevice, c->stream),
+       "H2D word offsets");
+    CK(cudaMemcpyAsync(m + o_sym, sym.data(), sym.size(), cudaMemcpyHostToDevice, c->stream), "H2D alphabet");
+    CK(cudaMemcpyAsync(m + o_rowoff, rowoff.data(), 512, cudaMemcpyHostToDevice, c->stream), "H2D row offsets");
+    CK(cudaMemsetAsync(m + o_text + 4 * (size_t)woff[nc], 0, 4 * kPfxTextSlack, c->stream), "memset slack");
+    PrefixChoices &P = s->pd;
+    P.text = (const uint32_t *)(m + o_text);
+    P.woff = (const int64_t *)(m + o_woff);
+    P.len = (const int32_t *)(m + o_len);
+    P.orig = (const int32_t *)(m + o_order);
+    P.restart = (const uint8_t *)(m + o_rs);
+    P.sym = (const uint8_t *)(m + o_sym);
+    P.nsym = (int)sym.size();
+    P.n = nc;
+    P.ck[0] = c1;
+    P.ck[1] = c2;
+    s->pfx_work = (unsigned long long *)(m + o_work);
+    CK(launch(c, "prefix_text", [&] {
+           return launch_prefix_text(c->stream, c->sms, s->c.d, P.orig, P.woff, (const uint16_t *)(m + o_rowoff),
+                                     (uint32_t *)P.text, (int32_t *)P.len, c->d_status);
+       }), "prefix_text");
+    s->pfx_saving = (double)best / (double)cols;
+    s->pfx = true;
+    // the host vectors above are pageable: the copies completed before return
+    return BLG_OK;
+}
+
 static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *oc, int64_t nc, blg_search *s,
                                  unsigned need = NEED_ALL, int32_t *perm_stage = nullptr) {
     s->nc = nc;
@@ -883,6 +1036,10 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
                }), "transpose_choices");
             s->tt = true;
         }
+        if (need & NEED_PFX) {
+            const int rc2 = search_build_prefix(c, bc, oc, nc, s);
+            if (rc2) return rc2;
+        }
     }
     // the host vectors above are pageable: the copies completed before return
     return BLG_OK;
@@ -942,6 +1099,10 @@ static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int
             rc = search_build_classes(c, oq, q0, q1, s);
             if (!rc) rc = search_run(c, s, k, dtype, d_out, q0, q1);
             if (!rc && cudaEventRecord(ev[ch], c->stream) != cudaSuccess) rc = fail(c, BLG_ERR_CUDA, "event");
+            // exact runs: the host sorts the choices for the prefix-reuse
+            // kernel while the first chunk computes on the tile-transposed
+            // copy; the later chunks use it
+            if (!rc && ch == 0 && k < 0 && nch > 1) rc = search_build_prefix(c, bc, oc, nc, s);
             if (rc) break;
         }
         if (ch >= 1) {
@@ -1074,7 +1235,13 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
                }), "search_lanes");
         } else {
             const int qpb = pick_qpb(c, k_.nw, k_.nq, s->nc);
-            if (s->tt) {
+            if (!hask && s->pfx && search_pfx_supported(k_.nw)) {
+                // exact short queries over the prefix-sorted choices
+                CK(cudaMemsetAsync(s->pfx_work, 0, sizeof(unsigned long long), c->stream), "reset work");
+                CK(launch(c, "search_pfx", [&] {
+                       return launch_search_pfx(c->stream, c->sms, 4, k_.nw, s->pd, sc, s->pfx_work, dtype, d_out);
+                   }), "search_pfx");
+            } else if (s->tt) {
                 const TransposedChoices T{s->tt_words, s->tt_base, s->tt_len, s->nc};
                 CK(launch(c, "search_tt", [&] {
                        return launch_search_tt(c->stream, k_.nw, hask, T, sc, qpb, k, dtype, d_out);
@@ -1160,6 +1327,10 @@ static void search_release(blg_ctx *c, blg_search *s) {
     dev_free(c, s->tt_words);
     dev_free(c, s->tt_base);
     dev_free(c, s->tt_len);
+    dev_free(c, s->pfx_mem);
+    s->pfx_mem = nullptr;
+    s->pfx_work = nullptr;
+    s->pfx = false;
     dev_free(c, s->qsk);
     s->csk = s->qsk = nullptr;
     s->tt_words = nullptr;

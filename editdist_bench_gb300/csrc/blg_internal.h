@@ -66,6 +66,38 @@ struct TransposedChoices {
     int64_t n = 0;
 };
 
+// Choices sorted lexicographically for the exact search with prefix reuse
+// (k_search_pfx). A warp's 32 lanes hold different queries and share one
+// choice at a time, so the text, its length and its restart column are the
+// same on every lane. Each warp walks a chain of kPfxChain consecutive sorted
+// choices; a choice restarts at the largest checkpoint column not above its
+// common prefix with the previous sorted choice (0 at a chain start), from
+// the column state that choice's run saved there.
+// Text: sorted choice p occupies words text[woff[p] ..] with two characters
+// per 32-bit word, each character stored as its shared-memory Peq row offset
+// (alphabet index x kPfxRowBytes, 16 bits), so a column's Peq address needs
+// no byte extraction or scaling. The alphabet is the set of bytes that occur
+// in the choices (at most kPfxMaxSymbols).
+constexpr int kPfxChain = 32;
+constexpr int kPfxWarps = 8;                         // warps per CTA; a work item = kPfxWarps chains
+constexpr int kPfxItem = kPfxChain * kPfxWarps;      // sorted choices per work item
+constexpr int kPfxCheckpoints = 2;
+constexpr int kPfxMaxSymbols = 32;
+constexpr int kPfxRowBytes = 1024;                   // one symbol's Peq entries: 32 lanes x QI x NW x 8 B
+constexpr int kPfxTextSlack = 8;                     // words readable past the last choice (prefetch)
+
+struct PrefixChoices {
+    const uint32_t *text = nullptr;   // row offsets, 2 per word
+    const int64_t *woff = nullptr;    // [n + 1] first word of sorted choice p
+    const int32_t *len = nullptr;     // [n] length of sorted choice p
+    const int32_t *orig = nullptr;    // [n] original index of sorted choice p
+    const uint8_t *restart = nullptr; // [n] first column to compute for sorted choice p
+    const uint8_t *sym = nullptr;     // [nsym] the byte of each alphabet index
+    int nsym = 0;
+    int64_t n = 0;
+    int ck[kPfxCheckpoints] = {0, 0};
+};
+
 // Per-query-class search launch description.
 struct SearchClass {
     int nw;                 // pattern words (sequential kernels) or 0 for lane-spread

@@ -149,6 +149,178 @@ __global__ void __launch_bounds__(256) k_search_ttq(TransposedChoices T, SearchC
     }
 }
 
+// ------------------------------------------- exact search with prefix reuse --
+// Choices sorted lexicographically share prefixes with their neighbours: the
+// column state of a query after the first c text columns depends on those c
+// characters only, so a choice that shares c characters with the previous
+// one can start at column c from the state the previous run passed there.
+// Here a warp's 32 lanes hold QI queries each (QI*32 per warp, the same block
+// of queries for the whole CTA) and share one choice at a time: the text, the
+// choice length and the restart column are warp-uniform, so a skipped column
+// is skipped by the whole warp. Each warp walks a chain of kPfxChain
+// consecutive sorted choices (PrefixChoices), saving its lanes' column states
+// at the launch's checkpoint columns in shared memory; a choice restarts from
+// the checkpoint P.restart names (computed on the host). The block's Peq rows
+// are staged per alphabet symbol as [symbol][query][lane] (conflict-free
+// 64-bit loads) and the text carries each character's row offset, so a
+// column's row address is one half-word extract for QI queries. A persistent
+// grid pulls (query block, chain group) items from a device counter, query
+// block outermost, so a CTA restages its Peq rows only when the block changes.
+// Results leave through the sort's permutation (P.orig).
+template <int NW, int QI>
+__global__ void __launch_bounds__(256) k_search_pfx(PrefixChoices P, SearchClass cls, unsigned long long *work,
+                                                    int64_t items, int dtype, void *out, uint32_t unit) {
+    static_assert(QI * NW * 32 * 8 == kPfxRowBytes, "one symbol's entries fill a row");
+    static_assert(kPfxCheckpoints == 2, "two checkpoint columns");
+    static_assert(kPfxWarps * 32 == 256, "256 threads");
+    extern __shared__ uint64_t s_peq[];                        // [nsym][QI][32][NW], then the checkpoints
+    constexpr int kState = QI * NW * 4;                        // u32 of one lane's column states
+    uint32_t *s_ck = reinterpret_cast<uint32_t *>(s_peq + (size_t)P.nsym * (kPfxRowBytes / 8));
+    __shared__ int64_t s_item;
+    const Units u{unit, unit + unit};
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t nc = P.n;
+    const int64_t segs = (nc + kPfxItem - 1) / kPfxItem;
+    const int ck0 = P.ck[0], ck1 = P.ck[1];                    // (no dynamic index into the parameter block)
+    const uint32_t hi16 = u.one << 16;
+    const char *pl = reinterpret_cast<const char *>(s_peq) + lane * NW * 8;
+    Word2 st[QI][NW];
+    auto col = [&](uint32_t off) {
+#pragma unroll
+        for (int i = 0; i < QI; i++)
+            column_v<NW>(st[i], reinterpret_cast<const uint64_t *>(pl + off + i * (32 * NW * 8)), u);
+    };
+    auto col2 = [&](uint32_t w) {                              // the two characters of a text word
+        col(w & 0xffffu);
+        col(imad_hi(w, hi16, 0));
+    };
+    int cur = -1;
+    while (true) {
+        __syncthreads();                                       // the previous item is done with s_item
+        if (tid == 0) s_item = (int64_t)atomicAdd(work, 1ull);
+        __syncthreads();
+        const int64_t item = s_item;
+        if (item >= items) break;
+        const int qb = (int)(item / segs);
+        const int64_t seg = item - (int64_t)qb * segs;
+        const int q0 = qb * (QI * 32);
+        if (qb != cur) {                                       // uniform: every thread read the same item
+            const int entries = P.nsym * (QI * 32 * NW);
+            for (int x = tid; x < entries; x += 256) {
+                const int w = x % NW, ql = (x / NW) % (QI * 32), a = x / (NW * QI * 32);
+                const int q = q0 + ql;                         // ql = i * 32 + lane
+                s_peq[x] = q < cls.nq ? __ldg(cls.peq + ((size_t)q * 256 + P.sym[a]) * NW + w) : 0;
+            }
+            __syncthreads();
+            cur = qb;
+        }
+        const int64_t p0 = seg * kPfxItem + (int64_t)warp * kPfxChain;
+#pragma unroll 1
+        for (int r = 0; r < kPfxChain; r++) {
+            const int64_t p = p0 + r;
+            if (p >= nc) break;                                // warp-uniform
+            const int n = __ldg(P.len + p);
+            const int b = __ldg(P.restart + p);
+            const uint32_t *tx = P.text + __ldg(P.woff + p);
+            if (b == 0) {
+#pragma unroll
+                for (int i = 0; i < QI; i++)
+#pragma unroll
+                    for (int w = 0; w < NW; w++) { st[i][w].pl = st[i][w].ph = ~0u; st[i][w].ml = st[i][w].mh = 0; }
+            } else {
+                const uint32_t *ck = s_ck + (b == ck1 ? kState * 256 : 0) + tid;
+#pragma unroll
+                for (int i = 0; i < QI; i++)
+#pragma unroll
+                    for (int w = 0; w < NW; w++) {
+                        const int x = (i * NW + w) * 4;
+                        st[i][w].pl = ck[(x + 0) * 256];
+                        st[i][w].ph = ck[(x + 1) * 256];
+                        st[i][w].ml = ck[(x + 2) * 256];
+                        st[i][w].mh = ck[(x + 3) * 256];
+                    }
+            }
+            // columns [b, n): up to the checkpoints it passes (saving there), then to the end
+            int j = b;
+#pragma unroll 1
+            for (int sg = 0; sg <= kPfxCheckpoints; sg++) {
+                int end = n;
+                if (sg < kPfxCheckpoints) {
+                    end = sg == 0 ? ck0 : ck1;
+                    if (!(j < end && end <= n)) continue;
+                }
+                if ((j & 1) && j < end) {                      // the second character of a started word
+                    col(imad_hi(__ldg(tx + (j >> 1)), hi16, 0));
+                    j++;
+                }
+                if (j + 8 <= end) {                            // 8 columns per step, the next 4 words in flight
+                    const uint32_t *q = tx + (j >> 1);
+                    uint32_t a0 = __ldg(q), a1 = __ldg(q + 1), a2 = __ldg(q + 2), a3 = __ldg(q + 3);
+                    for (; j + 8 <= end; j += 8) {
+                        const uint32_t c0 = a0, c1 = a1, c2 = a2, c3 = a3;
+                        q += 4;
+                        a0 = __ldg(q);                         // may read up to 4 words past the choice
+                        a1 = __ldg(q + 1);
+                        a2 = __ldg(q + 2);
+                        a3 = __ldg(q + 3);
+                        col2(c0);
+                        col2(c1);
+                        col2(c2);
+                        col2(c3);
+                    }
+                }
+                for (; j + 2 <= end; j += 2) col2(__ldg(tx + (j >> 1)));
+                if (j < end) {
+                    col(__ldg(tx + (j >> 1)) & 0xffffu);
+                    j++;
+                }
+                if (sg < kPfxCheckpoints) {                    // the state after `end` columns
+                    uint32_t *ck = s_ck + sg * kState * 256 + tid;
+#pragma unroll
+                    for (int i = 0; i < QI; i++)
+#pragma unroll
+                        for (int w = 0; w < NW; w++) {
+                            const int x = (i * NW + w) * 4;
+                            ck[(x + 0) * 256] = st[i][w].pl;
+                            ck[(x + 1) * 256] = st[i][w].ph;
+                            ck[(x + 2) * 256] = st[i][w].ml;
+                            ck[(x + 3) * 256] = st[i][w].mh;
+                        }
+                }
+            }
+            const int64_t c = __ldg(P.orig + p);
+#pragma unroll
+            for (int i = 0; i < QI; i++) {
+                const int q = q0 + i * 32 + lane;
+                if (q >= cls.nq) continue;
+                const int m = __ldg(cls.qlen + q);
+                const int lb = m - 64 * (NW - 1);
+                const uint32_t ml = m <= 0 ? 0u : (lb >= 32 ? ~0u : ((1u << lb) - 1u));
+                const uint32_t mh = m <= 0 ? 0u : (lb >= 64 ? ~0u : (lb <= 32 ? 0u : ((1u << (lb - 32)) - 1u)));
+                store1(out, dtype, (int64_t)__ldg(cls.qidx + q) * nc + c, n + vsum<NW>(st[i], ml, mh));
+            }
+        }
+    }
+}
+
+// The prefix layout's text (PrefixChoices): one thread per sorted choice p
+// reads its original string (order[p]) and writes each character's Peq row
+// offset (rowoff[byte]), two per word, from word woff[p]; and its length.
+__global__ void __launch_bounds__(256) k_prefix_text(DevStrings C, const int32_t *order, const int64_t *woff,
+                                                     const uint16_t *rowoff, uint32_t *text, int32_t *len,
+                                                     uint32_t *status) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < C.n; p += (int64_t)gridDim.x * blockDim.x) {
+        int n;
+        const uint8_t *s = string_at(C, order[p], n, status);
+        len[p] = n;
+        uint32_t *t = text + woff[p];
+        for (int j = 0; j < n; j += 2) {
+            const uint32_t lo = rowoff[s[j]], hi = j + 1 < n ? rowoff[s[j + 1]] : 0u;
+            t[j >> 1] = lo | (hi << 16);
+        }
+    }
+}
+
 // Transpose choices into tiles (see TransposedChoices); one thread per
 // (choice, word), bytes past a choice's end are zero.
 __global__ void __launch_bounds__(256) k_transpose_choices(DevStrings C, const int64_t *base, uint32_t *words,
@@ -572,6 +744,38 @@ cudaError_t launch_search_tt(cudaStream_t st, int nw, bool hask, const Transpose
     case 8: return launch_tt<8>(hask, grid, smem, st, T, cls, qpb, k, dtype, out);
     default: return cudaErrorInvalidValue;
     }
+}
+
+template <int NW, int QI>
+static cudaError_t launch_pfx_nw(cudaStream_t st, int grid, const PrefixChoices &P, const SearchClass &cls,
+                                 unsigned long long *work, int64_t items, int dtype, void *out) {
+    const size_t smem = (size_t)P.nsym * kPfxRowBytes + (size_t)kPfxCheckpoints * QI * NW * 4 * 256 * 4;
+    cudaFuncSetAttribute(k_search_pfx<NW, QI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_search_pfx<NW, QI><<<grid, 256, smem, st>>>(P, cls, work, items, dtype, out, 1u);
+    return cudaGetLastError();
+}
+
+bool search_pfx_supported(int nw) { return nw == 1 || nw == 2; }
+
+// `work` must be zero when the launch starts (the caller clears it on the stream).
+cudaError_t launch_search_pfx(cudaStream_t st, int sms, int ctas_per_sm, int nw, const PrefixChoices &P,
+                              const SearchClass &cls, unsigned long long *work, int dtype, void *out) {
+    if (cls.nq <= 0 || P.n <= 0) return cudaSuccess;
+    if (P.nsym < 1 || P.nsym > kPfxMaxSymbols) return cudaErrorInvalidValue;
+    const int64_t segs = (P.n + kPfxItem - 1) / kPfxItem;
+    const int grid = sms * std::max(1, std::min(ctas_per_sm, 8));
+    if (nw == 1) return launch_pfx_nw<1, 4>(st, grid, P, cls, work, segs * ((cls.nq + 127) / 128), dtype, out);
+    if (nw == 2) return launch_pfx_nw<2, 2>(st, grid, P, cls, work, segs * ((cls.nq + 63) / 64), dtype, out);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_prefix_text(cudaStream_t st, int sms, const DevStrings &C, const int32_t *order,
+                               const int64_t *woff, const uint16_t *rowoff, uint32_t *text, int32_t *len,
+                               uint32_t *status) {
+    if (C.n <= 0) return cudaSuccess;
+    const int grid = (int)std::min<int64_t>((C.n + 255) / 256, (int64_t)sms * 8);
+    k_prefix_text<<<grid, 256, 0, st>>>(C, order, woff, rowoff, text, len, status);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_transpose_choices(cudaStream_t st, int sms, const DevStrings &C, const int64_t *base,
