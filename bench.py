@@ -641,6 +641,37 @@ def e2e_leg(bench, pin, steps, warmup, i=0) -> dict:
             "path": "one-call C-ABI (blg_pairwise / blg_cdist / blg_cdist_batch), pinned host buffers, wall clock"}
 
 
+def list_leg(bench, calls: int = 3) -> dict | None:
+    """The drop-in call on Python lists of bytes, as a bitlev user makes it:
+    gpu.pairwise(a, b) / gpu.cdist(q, c) with packing (the native packer into
+    page-locked staging), the copies, the kernels and the result returned as
+    a new numpy array, all inside the wall-clock time. The lists are built
+    outside it."""
+    from editdist_bench_gb300 import _common
+    if bench.kind == "pairwise":
+        a, b = W.unpack(bench.w.a), W.unpack(bench.w.b)
+        k, dt = bench.runs[0]
+        call = lambda: gpu.pairwise(a, b, max_dist=k, dtype=dt)  # noqa: E731
+    elif bench.kind == "cdist":
+        a, b = W.unpack(bench.w.q), W.unpack(bench.w.c)
+        k, dt = bench.runs[0]
+        call = lambda: gpu.cdist(a, b, max_dist=k, dtype=dt)  # noqa: E731
+    else:
+        return None
+    call()
+    t = []
+    for _ in range(max(2, calls)):
+        t0 = time.perf_counter()
+        r = call()
+        t.append(time.perf_counter() - t0)
+        del r
+    s = statistics.median(t)
+    return {"value": bench.pairs / s, "unit": "pairs/s", "ms_per_call": s * 1e3, "calls": len(t),
+            "packer": "native (csrc/blg_pack.c)" if _common._blgpack is not None else "python",
+            "path": "gpu.pairwise / gpu.cdist on Python lists of bytes: packing into pinned staging, copies, "
+                    "kernels, result into a new numpy array; wall clock"}
+
+
 def roofline_block(bench, kstats, top, peak, exit_sum, dev, clock_mhz) -> dict:
     """The dominant launch label's roofline: algorithmic bytes and integer
     ops per step over its event time (HBM and integer-pipe fractions, the
@@ -734,6 +765,8 @@ def suite_config(cfg, ctx, flush, pin, args, peak, dev, clock_mhz) -> dict:
                                    for s, v in sched_out.items() if s != "plain"}
     bench.e2e_setup(pin)
     res["e2e"] = e2e_leg(bench, pin, steps, args.warmup)
+    if cfg in (1, 4):
+        res["e2e_list"] = list_leg(bench)
     m = matches_leg(bench, ctx, pin, flush, args)
     if m:
         res["matches"] = m
@@ -800,6 +833,7 @@ def run_ours(args, ranks: Ranks):
     e2e = e2e_leg(bench, pin, min(args.steps, 10), args.warmup)
     e2e["value"] = bench.pairs * ranks.world / (ranks.max(bench.pairs / e2e["value"]))
     matches = matches_leg(bench, ctx, pin, flush, args)
+    e2e_list = list_leg(bench) if ranks.world == 1 and not args.no_suite else None
 
     result = {
         "metric": "pairs/s", "value": value, "unit": "pairs/s", "n_gpus": ranks.world,
@@ -815,6 +849,8 @@ def run_ours(args, ranks: Ranks):
     }
     if matches:
         result["matches"] = matches
+    if e2e_list:
+        result["e2e_list"] = e2e_list
     if args.config in H100_REF:
         ref, src = H100_REF[args.config]
         result["vs_baseline"] = value / ref

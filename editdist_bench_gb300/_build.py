@@ -89,6 +89,35 @@ def build_probe(force: bool = False) -> str:
     return PROBE
 
 
+def packer_path() -> str:
+    import sysconfig
+    return os.path.join(HERE, "_blgpack" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
+
+
+def build_packer(force: bool = False) -> str | None:
+    """gcc build of the native str/bytes packer (csrc/blg_pack.c, a CPython
+    extension). Returns None when this Python has no development headers:
+    the package then packs with its numpy/bytes code (same layout, same
+    errors, slower)."""
+    import sysconfig
+    src = os.path.join(CSRC, "blg_pack.c")
+    out = packer_path()
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
+        return out
+    inc = sysconfig.get_paths().get("include")
+    if not inc or not os.path.exists(os.path.join(inc, "Python.h")):
+        return None
+    tmp = out + f".{os.getpid()}.tmp"
+    cc = os.environ.get("CC", "gcc")
+    r = subprocess.run([cc, "-O2", "-shared", "-fPIC", "-Wall", f"-I{inc}", "-o", tmp, src],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(f"native packer not built (numpy packing is used):\n{r.stderr}\n")
+        return None
+    os.replace(tmp, out)
+    return out
+
+
 def build_hostcheck(force: bool = False) -> str:
     """g++ build of the device header's host path (blg_hostcheck.cpp)."""
     src = os.path.join(CSRC, "blg_hostcheck.cpp")

@@ -56,9 +56,29 @@ def _encode_one(s) -> bytes:
     raise TypeError(_TYPE_MSG)
 
 
+try:                                    # the native packer (csrc/blg_pack.c), when built
+    from . import _blgpack
+except ImportError:
+    _blgpack = None
+
+
 def pack(strings):
     """Packed (uint8 buffer, int64 offsets[n+1]) of a sequence of str/bytes:
-    1 character = 1 byte, str must be Latin-1, the buffer is never empty."""
+    1 character = 1 byte, str must be Latin-1, the buffer is never empty.
+    The native packer validates every item, then copies each string's bytes
+    once; without it the bytes are joined by Python."""
+    seq = as_list(strings)
+    if _blgpack is not None:
+        n, total = _blgpack.size(seq)
+        buf = np.empty(max(total, 1), dtype=np.uint8)
+        off = np.empty(n + 1, dtype=np.int64)
+        _blgpack.pack_into(seq, buf.ctypes.data, buf.size, off.ctypes.data)
+        return buf, off
+    return pack_python(seq)
+
+
+def pack_python(strings):
+    """pack() in Python: one join of the str or bytes items."""
     seq = as_list(strings)
     n = len(seq)
     off = np.zeros(n + 1, dtype=np.int64)

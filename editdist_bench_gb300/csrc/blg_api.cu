@@ -83,12 +83,13 @@ cudaError_t launch_sorted_offsets(cudaStream_t st, int sms, const int64_t *lstar
                                   const int64_t *bstart, int64_t n, int64_t *soff);
 cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &src, const int32_t *perm,
                                   const int64_t *dst_off, uint8_t *dst, int64_t n, uint32_t *status);
-cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S, uint64_t *sketch, uint32_t *status);
+cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S, uint64_t *sketch, uint4 *counts,
+                                  uint32_t *status);
 cudaError_t launch_search_lpt(cudaStream_t st, int sms, int ctas_per_sm, int jobsz, int nw, const DevStrings &CS,
-                              const int32_t *perm, const uint64_t *csk, const uint64_t *qsk, const SearchClass &cls,
-                              const int32_t *lo, const int32_t *hi, const int64_t *tile_start, int32_t *work,
-                              const uint8_t *keytab, int64_t keystride, int k, int dtype, void *out, int64_t nc,
-                              const SurvRows *rows, uint32_t *status);
+                              const int32_t *perm, const uint64_t *csk, const uint64_t *qsk, const uint4 *ccnt,
+                              const uint4 *qcnt, const SearchClass &cls, const int32_t *lo, const int32_t *hi,
+                              const int64_t *tile_start, int32_t *work, const uint8_t *keytab, int64_t keystride, int k,
+                              int dtype, void *out, int64_t nc, const SurvRows *rows, uint32_t *status);
 cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
                              int64_t min_len, int64_t n_len, int k, int tile, int32_t *lo, int32_t *hi,
                              int64_t *tile_start, int32_t *work);
@@ -154,8 +155,10 @@ struct blg_search {
     int64_t *lstart = nullptr;
     int64_t min_len = 0, n_len = 0;
     std::vector<int64_t> h_lstart;   // host copy of lstart
-    // 4-gram sketches: of the length-sorted choices and of the queries
+    // 4-gram sketches and binned 4-gram counts: of the length-sorted choices
+    // and of the queries
     uint64_t *csk = nullptr, *qsk = nullptr;
+    uint4 *ccnt = nullptr, *qcnt = nullptr;
     // choices in tile-transposed form (exact and unsorted runs), when the
     // padding to each tile's longest choice stays small
     bool tt = false;
@@ -964,7 +967,8 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
             const size_t o_perm = 0, o_tab = up(sizeof(int32_t) * (size_t)nc),
                          o_soff = o_tab + up(sizeof(int64_t) * (size_t)(2 * n_len + 1)),
                          o_csk = o_soff + up(sizeof(int64_t) * (size_t)(nc + 1)),
-                         o_buf = o_csk + up(sizeof(uint64_t) * (size_t)nc),
+                         o_ccnt = o_csk + up(sizeof(uint64_t) * (size_t)nc),
+                         o_buf = o_ccnt + up(sizeof(uint4) * (size_t)nc),
                          total = o_buf + (size_t)bytes + kSlackBefore + kSlackAfter;
             CK(dev_alloc(c, &s->sorted_mem, total), "cudaMallocAsync(sorted choices)");
             uint8_t *m = (uint8_t *)s->sorted_mem;
@@ -973,6 +977,7 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
             int64_t *d_bstart = s->lstart + (n_len + 1);
             int64_t *d_soff = (int64_t *)(m + o_soff);
             s->csk = (uint64_t *)(m + o_csk);
+            s->ccnt = (uint4 *)(m + o_ccnt);
             uint8_t *d_buf = m + o_buf;
             CK(cudaMemcpyAsync(s->perm, perm, sizeof(int32_t) * nc, cudaMemcpyHostToDevice, c->stream), "H2D perm");
             CK(cudaEventRecord(c->stage_done, c->stream), "event");
@@ -996,7 +1001,7 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
                    return launch_gather_strings(c->stream, c->sms, s->c.d, s->perm, cs.d.off,
                                                 (uint8_t *)cs.d.buf, nc, c->d_status);
                }), "gather_strings");
-            CK(launch(c, "sketch", [&] { return launch_sketch_strings(c->stream, c->sms, cs.d, s->csk, c->d_status); }),
+            CK(launch(c, "sketch", [&] { return launch_sketch_strings(c->stream, c->sms, cs.d, s->csk, s->ccnt, c->d_status); }),
                "sketch");
             s->min_len = mn;
             s->n_len = n_len;
@@ -1053,8 +1058,11 @@ static int search_upload_queries(blg_ctx *c, const uint8_t *bq, const int64_t *o
     s->nq = nq;
     int rc = upload_strings(c, bq, oq, nq, s->q);
     if (rc) return rc;
-    CK(dev_alloc(c, (void **)&s->qsk, sizeof(uint64_t) * (size_t)std::max<int64_t>(nq, 1)), "cudaMallocAsync(sketches)");
-    CK(launch(c, "sketch", [&] { return launch_sketch_strings(c->stream, c->sms, s->q.d, s->qsk, c->d_status); }),
+    // one block: the sketches (8 B each), then the 4-gram counts (16 B each, 16-byte aligned)
+    const size_t nq1 = (size_t)std::max<int64_t>(nq, 1), o_cnt = (8 * nq1 + 15) & ~size_t(15);
+    CK(dev_alloc(c, (void **)&s->qsk, o_cnt + 16 * nq1), "cudaMallocAsync(sketches)");
+    s->qcnt = (uint4 *)((uint8_t *)s->qsk + o_cnt);
+    CK(launch(c, "sketch", [&] { return launch_sketch_strings(c->stream, c->sms, s->q.d, s->qsk, s->qcnt, c->d_status); }),
        "sketch");
     return BLG_OK;
 }
@@ -1198,7 +1206,7 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
                 // difference alone, shared by every query (lensort)
                 uint8_t *keytab = nullptr;
                 int64_t keystride = 0;
-                const int E = (2 * k + 1) * kSketchDistances;
+                const int E = (2 * k + 1) * (8 * k + 1);   // (length gap, 4-gram count distance)
                 if (c->sched == BLG_SCHED_LEARNED && c->model && sched_model_trained(c->model)) {
                     CK(dev_alloc(c, (void **)&keytab, (size_t)k_.nq * E), "cudaMallocAsync(keytab)");
                     keystride = E;
@@ -1208,14 +1216,14 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
                     CK(dev_alloc(c, (void **)&keytab, (size_t)E), "cudaMallocAsync(keytab)");
                     std::vector<uint8_t> tab((size_t)E);
                     for (int g = 0; g <= 2 * k; g++)              // g = length gap + k: equal lengths first
-                        for (int d = 0; d < kSketchDistances; d++)
-                            tab[(size_t)g * kSketchDistances + d] = (uint8_t)(255 - 8 * std::abs(g - k));
+                        for (int d = 0; d <= 8 * k; d++)
+                            tab[(size_t)g * (8 * k + 1) + d] = (uint8_t)(255 - 8 * std::abs(g - k));
                     CK(cudaMemcpyAsync(keytab, tab.data(), (size_t)E, cudaMemcpyHostToDevice, c->stream), "H2D keytab");
                     CK(cudaStreamSynchronize(c->stream), "sync keytab");   // the host table is pageable
                 }
                 CK(launch(c, "search_lpt", [&] {
                        return launch_search_lpt(c->stream, c->sms, c->tune.lpt_ctas, job, k_.nw, s->cs.d,
-                                                s->perm, s->csk, s->qsk, sc, k_.lo,
+                                                s->perm, s->csk, s->qsk, s->ccnt, s->qcnt, sc, k_.lo,
                                                 k_.hi, k_.tile_start, k_.work, keytab, keystride, k, dtype, d_out, s->nc,
                                                 nullptr, c->d_status);
                    }), "search_lpt");
@@ -1333,6 +1341,7 @@ static void search_release(blg_ctx *c, blg_search *s) {
     s->pfx = false;
     dev_free(c, s->qsk);
     s->csk = s->qsk = nullptr;
+    s->ccnt = s->qcnt = nullptr;
     s->tt_words = nullptr;
     s->tt_base = nullptr;
     s->tt_len = nullptr;
@@ -1434,6 +1443,8 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
             j.tile = (k >= 0 && k <= 31) ? 4096 : 1024;   // longest-first jobs of the banded kernel
             j.csk = s->csk;
             j.qsk = s->qsk;
+            j.ccnt = s->ccnt;
+            j.qcnt = s->qcnt;
             j.out = p.d_out;
             jobs.push_back(j);
             qprefix.push_back(qprefix.back() + cl.nq);
@@ -1961,7 +1972,7 @@ int blg_sched_train_search(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t 
            }), "surv_plan");
         CK(launch(c, "search_lpt_logged", [&] {
                return launch_search_lpt(c->stream, c->sms, c->tune.lpt_ctas, job, k_.nw, s->cs.d, s->perm,
-                                        s->csk, s->qsk, sc, k_.lo, k_.hi,
+                                        s->csk, s->qsk, s->ccnt, s->qcnt, sc, k_.lo, k_.hi,
                                         k_.tile_start, k_.work, nullptr, 0, max_dist, BLG_UINT8, out, s->nc, &R,
                                         c->d_status);
            }), "search_lpt_logged");

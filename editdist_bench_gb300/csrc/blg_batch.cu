@@ -175,8 +175,9 @@ __global__ void __launch_bounds__(256) k_batch_lpt(BatchPlan plan, uint32_t *sta
         const int64_t row = job.cls.qidx[qi];
         const int64_t s0 = job.lo[qi] + (lt - job.tile_start[qi]) * job.tile;
         const int cnt = (int)min((int64_t)job.tile, (int64_t)job.hi[qi] - s0);
-        lpt_job(S, job.CS, job.perm, job.csk, job.qsk[row], s_rows, 2 * job.nw + 6, job.cls.qlen[qi], row, s0, cnt,
-                job.k, nullptr, job.dtype, job.out, job.nc, status, u, [](int64_t, int, int) {});
+        lpt_job(S, job.CS, job.perm, job.csk, job.ccnt, job.qsk[row], job.qcnt[row], s_rows, 2 * job.nw + 6,
+                job.cls.qlen[qi], row, s0, cnt, job.k, nullptr, job.dtype, job.out, job.nc, status, u,
+                [](int64_t, int, int, uint32_t) {});
     }
 }
 

@@ -24,6 +24,8 @@ struct BatchJob {
     int tile;                  // survivors per work unit: 4096 (banded, longest-first jobs) or 1024
     const uint64_t *csk;       // 4-gram sketches of the sorted choices
     const uint64_t *qsk;       // 4-gram sketches of the queries (by query row)
+    const uint4 *ccnt;         // binned 4-gram counts of the sorted choices
+    const uint4 *qcnt;         // binned 4-gram counts of the queries (by query row)
     void *out;
 };
 

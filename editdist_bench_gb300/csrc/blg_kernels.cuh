@@ -662,6 +662,44 @@ __device__ __forceinline__ uint64_t gram_sketch(const uint8_t *p, int m) {
     return sk;
 }
 
+// 4-gram counts of a string, binned: its 4-grams hashed into 16 bins (the
+// top 4 bits of gram_sketch's hash), one saturating byte counter per bin. An
+// edit removes at most 4 grams of a string and adds at most 4, so it changes
+// the sum over bins of |count(x) - count(y)| by at most 8: for any x, y,
+// gram_bound(x, y) = that sum / 8 <= d(x, y) (q-gram lemma, q = 4; merging
+// grams into bins and saturating counters only lower the sum). It is the
+// scheduler network's similarity feature, and an exact filter: a pair whose
+// bound exceeds max_dist has distance > max_dist.
+__device__ __forceinline__ uint4 gram_counts(const uint8_t *p, int m) {
+    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+    uint32_t g = 0;
+    TextScan ts;
+    ts.init(p);
+    for (int i = 0; i < m; i += 4) {
+        const uint32_t w4 = ts.next4();
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            if (i + b < m) {
+                g = __funnelshift_l(w4 << (24 - 8 * b), g, 8);     // g = (g << 8) | byte b
+                if (i + b >= 3) {
+                    const uint32_t h = (g * 0x9E3779B1u) >> 28;    // bin 0..15
+                    const uint32_t add = 1u << (8 * (h & 3u)), word = h >> 2;
+                    c0 = word == 0 ? __vaddus4(c0, add) : c0;
+                    c1 = word == 1 ? __vaddus4(c1, add) : c1;
+                    c2 = word == 2 ? __vaddus4(c2, add) : c2;
+                    c3 = word == 3 ? __vaddus4(c3, add) : c3;
+                }
+            }
+        }
+    }
+    return make_uint4(c0, c1, c2, c3);
+}
+
+// Sum over the 16 bins of |count(x) - count(y)| (8 x gram_bound).
+__device__ __forceinline__ uint32_t gram_dist(uint4 a, uint4 b) {
+    return __vsadu4(a.x, b.x) + __vsadu4(a.y, b.y) + __vsadu4(a.z, b.z) + __vsadu4(a.w, b.w);
+}
+
 // ---------------------------------- thresholded search: longest-first jobs --
 // A job is up to kSurvJob survivors (choices within max_dist k <= 31 in length)
 // of one query, whose banded Peq rows are in shared memory. Every survivor
@@ -677,6 +715,7 @@ struct LptShared {
     int cnt[256], start[256];
     int64_t job;
     int next;
+    int listed;            // survivors that passed the 4-gram bound
 };
 
 // largest j in [0, n) with pre[j] <= x (pre non-decreasing, pre[0] <= x)
@@ -689,33 +728,40 @@ __device__ __forceinline__ int upper_index(const int64_t *pre, int n, int64_t x)
     return a;
 }
 
-// Called by all 256 threads of the CTA; `log(sidx, n, cols)` sees every solved survivor.
+// Called by all 256 threads of the CTA; `log(sidx, n, cols, gd)` sees every
+// solved survivor (gd: its 4-gram count distance). Survivors whose 4-gram
+// bound already exceeds k are not listed: their output keeps the k+1 fill.
+// With the learned schedule, `keyrow` is the query's key table indexed by
+// (length gap + k, 4-gram count distance 0..8k).
 template <typename LogFn>
 __device__ __forceinline__ void lpt_job(LptShared &S, const DevStrings &CS, const int32_t *perm, const uint64_t *csk,
-                                        uint64_t qs, const uint32_t *rows, int stride, int m, int64_t row, int64_t s0,
-                                        int cnt, int k, const uint8_t *keyrow, int dtype, void *out, int64_t nc,
-                                        uint32_t *status, Units u, LogFn log) {
+                                        const uint4 *ccnt, uint64_t qs, uint4 qc, const uint32_t *rows, int stride,
+                                        int m, int64_t row, int64_t s0, int cnt, int k, const uint8_t *keyrow,
+                                        int dtype, void *out, int64_t nc, uint32_t *status, Units u, LogFn log) {
     constexpr int kPer = kSurvJob / 256;
     const int tid = threadIdx.x, lane = tid & 31;
     S.cnt[tid] = 0;
     if (tid == 0) S.next = 0;
     __syncthreads();
     int key[kPer], rank[kPer];
+    const uint32_t gmax = 8u * (uint32_t)k;
 #pragma unroll
     for (int r = 0; r < kPer; r++) {
         const int l = tid + 256 * r;
         key[r] = -1;
         if (l < cnt) {
             const int64_t sidx = s0 + l;
-            const int sd = __popcll(qs ^ csk[sidx]);
-            if (keyrow) {
-                int g = (int)(CS.off[sidx + 1] - CS.off[sidx]) - m + k;
-                g = g < 0 ? 0 : (g > 2 * k ? 2 * k : g);
-                key[r] = keyrow[g * (kSketchWindow + 1) + sd];
-            } else {
-                key[r] = kSketchWindow - sd;                 // near-copies (low distance) run longest
+            const uint32_t gd = gram_dist(qc, ccnt[sidx]);
+            if (gd <= gmax) {                                 // else the bound alone proves d > k
+                if (keyrow) {
+                    int g = (int)(CS.off[sidx + 1] - CS.off[sidx]) - m + k;
+                    g = g < 0 ? 0 : (g > 2 * k ? 2 * k : g);
+                    key[r] = keyrow[g * (8 * k + 1) + (gd > gmax ? gmax : gd)];
+                } else {
+                    key[r] = kSketchWindow - __popcll(qs ^ csk[sidx]);   // near-copies (low distance) run longest
+                }
+                rank[r] = atomicAdd(&S.cnt[key[r]], 1);
             }
-            rank[r] = atomicAdd(&S.cnt[key[r]], 1);
         }
     }
     __syncthreads();
@@ -732,19 +778,21 @@ __device__ __forceinline__ void lpt_job(LptShared &S, const DevStrings &CS, cons
         int run = incl - sum;
 #pragma unroll
         for (int q = 0; q < 8; q++) { S.start[255 - (tid * 8 + q)] = run; run += v[q]; }
+        if (tid == 31) S.listed = incl;
     }
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < kPer; r++)
         if (key[r] >= 0) S.list[S.start[key[r]] + rank[r]] = (uint16_t)(tid + 256 * r);
     __syncthreads();
+    const int listed = S.listed;
     while (true) {
         int c = 0;
         if (lane == 0) c = atomicAdd(&S.next, 1);
         c = __shfl_sync(kFull, c, 0);
-        if (c * 32 >= cnt) break;
+        if (c * 32 >= listed) break;
         const int e = c * 32 + lane;
-        if (e < cnt) {
+        if (e < listed) {
             const int64_t sidx = s0 + S.list[e];
             int n;
             const uint8_t *tp = string_at(CS, sidx, n, status);
@@ -755,7 +803,7 @@ __device__ __forceinline__ void lpt_job(LptShared &S, const DevStrings &CS, cons
                                    [&](uint32_t ch, int p0) { return band_row_bits(rows + ch * stride, p0); }, u,
                                    &cols);
             if (d <= k) store1(out, dtype, row * nc + perm[sidx], d);
-            log(sidx, n, cols);
+            log(sidx, n, cols, gram_dist(qc, ccnt[sidx]));
         }
     }
     __syncthreads();

@@ -275,17 +275,19 @@ __global__ void __launch_bounds__(256) k_mlp_keys(const half *w16, PairsPlan pla
 }
 
 // Survivor key table of a thresholded search: for every query of the class
-// and every (length gap g = n - m + k in 0..2k, sketch distance sd in 0..64)
-// the network's predicted work, as a cost bucket. The search's features are
-// (m, n, m, n, n - m, sd, k): the query is the pattern whatever its length,
-// with no trimming. One CTA per query, two table entries per thread.
-__device__ __forceinline__ void search_features(int m, int n, int sd, int k, float (&x)[8]) {
+// and every (length gap g = n - m + k in 0..2k, 4-gram count distance gd in
+// 0..8k: survivors with a larger one are filtered out before) the network's
+// predicted work, as a cost bucket. The search's features are (m, n, m, n,
+// n - m, gd / 8 = the 4-gram count lower bound, k): the query is the pattern
+// whatever its length, with no trimming. One CTA per query, two table
+// entries per thread.
+__device__ __forceinline__ void search_features(int m, int n, int gd, int k, float (&x)[8]) {
     x[0] = (float)m * (1.f / 256.f);
     x[1] = (float)n * (1.f / 256.f);
     x[2] = x[0];
     x[3] = x[1];
     x[4] = (float)(n - m) * (1.f / 16.f);
-    x[5] = (float)sd * (1.f / 16.f);
+    x[5] = (float)gd * (1.f / 128.f);
     x[6] = (float)k * (1.f / 16.f);
     x[7] = 1.f;
 }
@@ -300,15 +302,15 @@ __global__ void __launch_bounds__(256) k_surv_keytab(const half *w16, SearchClas
     __shared__ __align__(16) float w[kInfFloats];
     load_inference_weights(w16, w);
     __syncthreads();
-    const int E = (2 * k + 1) * kSketchDistances;
+    const int D = 8 * k + 1, E = (2 * k + 1) * D;
     for (int qi = blockIdx.x; qi < cls.nq; qi += gridDim.x) {
         const int m = cls.qlen[qi];
         for (int e0 = threadIdx.x; e0 < E; e0 += 2 * blockDim.x) {
             const int e1 = e0 + blockDim.x;
-            const int n0 = m - k + e0 / kSketchDistances, n1 = m - k + e1 / kSketchDistances;
+            const int n0 = m - k + e0 / D, n1 = m - k + e1 / D;
             float x0[8], x1[8], y0, y1;
-            search_features(m, n0 < 0 ? 0 : n0, e0 % kSketchDistances, k, x0);
-            search_features(m, n1 < 0 ? 0 : n1, e1 % kSketchDistances, k, x1);
+            search_features(m, n0 < 0 ? 0 : n0, e0 % D, k, x0);
+            search_features(m, n1 < 0 ? 0 : n1, e1 % D, k, x1);
             mlp_forward2(w, x0, x1, y0, y1);
             keytab[(size_t)qi * E + e0] = n0 <= 0 ? 0 : work_bucket(y0, n0);
             if (e1 < E) keytab[(size_t)qi * E + e1] = n1 <= 0 ? 0 : work_bucket(y1, n1);

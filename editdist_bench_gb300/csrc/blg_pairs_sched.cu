@@ -31,8 +31,13 @@ __device__ __forceinline__ int cost_bucket(float work) {
 }
 
 // Features of one trimmed pair (pattern p of m, text t of n; la0, lb0
-// untrimmed): lengths, trimmed lengths, length gap, k, and the 4-gram sketch
-// distance of their first 64 trimmed bytes (gram_sketch, blg_kernels.cuh).
+// untrimmed): lengths, trimmed lengths, length gap, k, and a 4-gram count
+// lower bound from the first kSketchWindow (64) trimmed bytes of each string:
+// with A, B those prefixes, d(A, B) <= 2 d(a, b) (an optimal alignment of a
+// and b aligns A with some prefix B' of b at cost <= d, and |B'| differs from
+// |B| by at most d), and gram_dist(A, B) / 8 <= d(A, B), so gram_dist / 16 <=
+// d(a, b). The window keeps the count pass short (whole strings cost the
+// learned pipeline more than its order gains).
 
 template <bool HASK, bool FEAT>
 __global__ void __launch_bounds__(256) k_pairs_prep(DevStrings A, DevStrings B, int k, int dtype, void *out,
@@ -78,14 +83,14 @@ __global__ void __launch_bounds__(256) k_pairs_prep(DevStrings A, DevStrings B, 
         int key = lengap_key ? 255 - min(255, 8 * (lb - la))
                              : cost_bucket(band ? (float)lb + 16.f : (float)lb * (float)((la + 63) >> 6));
         if (FEAT) {
-            const float qb = (float)__popcll(gram_sketch(a, la) ^ gram_sketch(b, lb));
+            const float gd = (float)gram_dist(gram_counts(a, min(la, kSketchWindow)), gram_counts(b, min(lb, kSketchWindow)));
             half *f = plan.feat[cls] + (size_t)pos * kFeatures;
             f[0] = __float2half((float)la * (1.f / 256.f));
             f[1] = __float2half((float)lb * (1.f / 256.f));
             f[2] = __float2half((float)la0 * (1.f / 256.f));
             f[3] = __float2half((float)lb0 * (1.f / 256.f));
             f[4] = __float2half((float)(lb - la) * (1.f / 16.f));
-            f[5] = __float2half(qb * (1.f / 16.f));
+            f[5] = __float2half(gd * (1.f / 256.f));   // the windowed lower bound gd / 16, over 16
             f[6] = __float2half(HASK ? (float)k * (1.f / 16.f) : 16.f);
             key = 0;                       // the network's prediction sets the key later
         }

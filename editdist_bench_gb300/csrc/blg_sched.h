@@ -35,8 +35,5 @@ struct SurvRows {
     int stride;
 };
 
-// Survivor key table of a query class: (2k+1) length gaps x 65 sketch
-// distances per query.
-constexpr int kSketchDistances = 65;
 
 }  // namespace blg

@@ -28,18 +28,21 @@
 namespace blg {
 
 
-// sketch[i] = gram_sketch(string i)
-__global__ void __launch_bounds__(256) k_sketch_strings(DevStrings S, uint64_t *sketch, uint32_t *status) {
+// sketch[i] = gram_sketch(string i), counts[i] = gram_counts(string i)
+__global__ void __launch_bounds__(256) k_sketch_strings(DevStrings S, uint64_t *sketch, uint4 *counts,
+                                                        uint32_t *status) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += (int64_t)gridDim.x * blockDim.x) {
         int n;
         const uint8_t *p = string_at(S, i, n, status);
         sketch[i] = gram_sketch(p, n);
+        counts[i] = gram_counts(p, n);
     }
 }
 
 template <int NW, bool LOG>
 __global__ void __launch_bounds__(256) k_search_lpt(DevStrings CS, const int32_t *perm, const uint64_t *csk,
-                                                    const uint64_t *qsk, SearchClass cls, const int32_t *lo,
+                                                    const uint64_t *qsk, const uint4 *ccnt, const uint4 *qcnt,
+                                                    SearchClass cls, const int32_t *lo,
                                                     const int32_t *hi, const int64_t *tile_start, int32_t *work,
                                                     const uint8_t *keytab, int64_t keystride, int k, int dtype,
                                                     void *out, int64_t nc, int jobsz, SurvRows rows, uint32_t *status,
@@ -65,8 +68,9 @@ __global__ void __launch_bounds__(256) k_search_lpt(DevStrings CS, const int32_t
         const uint64_t qs = qsk[row];
         const int64_t s0 = lo[qi] + (job - tile_start[qi]) * jobsz;
         const int cnt = (int)min((int64_t)jobsz, (int64_t)hi[qi] - s0);
-        lpt_job(S, CS, perm, csk, qs, s_rows, 2 * NW + 6, m, row, s0, cnt, k, keytab ? keytab + qi * keystride : nullptr,
-                dtype, out, nc, status, u, [&](int64_t sidx, int n, int cols) {
+        lpt_job(S, CS, perm, csk, ccnt, qs, qcnt[row], s_rows, 2 * NW + 6, m, row, s0, cnt, k,
+                keytab ? keytab + qi * keystride : nullptr, dtype, out, nc, status, u,
+                [&](int64_t sidx, int n, int cols, uint32_t gd) {
                     if (!LOG || m == 0 || n == 0 || (sidx % rows.stride) != 0) return;
                     const int64_t at = atomicAdd((unsigned long long *)rows.count, 1ull);
                     if (at >= rows.cap) return;
@@ -76,7 +80,7 @@ __global__ void __launch_bounds__(256) k_search_lpt(DevStrings CS, const int32_t
                     f[2] = f[0];
                     f[3] = f[1];
                     f[4] = __float2half((float)(n - m) * (1.f / 16.f));
-                    f[5] = __float2half((float)__popcll(qs ^ csk[sidx]) * (1.f / 16.f));
+                    f[5] = __float2half((float)gd * (1.f / 128.f));
                     f[6] = __float2half((float)k * (1.f / 16.f));
                     rows.y[at] = (float)cols / (float)n;
                 });
@@ -84,36 +88,38 @@ __global__ void __launch_bounds__(256) k_search_lpt(DevStrings CS, const int32_t
 }
 
 // ------------------------------------------------------------- launchers --
-cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S, uint64_t *sketch, uint32_t *status) {
+cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S, uint64_t *sketch, uint4 *counts,
+                                  uint32_t *status) {
     if (S.n <= 0) return cudaSuccess;
     const int grid = (int)std::min<int64_t>((S.n + 255) / 256, (int64_t)sms * 8);
-    k_sketch_strings<<<grid, 256, 0, st>>>(S, sketch, status);
+    k_sketch_strings<<<grid, 256, 0, st>>>(S, sketch, counts, status);
     return cudaGetLastError();
 }
 
 template <int NW>
 static cudaError_t launch_lpt_nw(cudaStream_t st, int grid, const DevStrings &CS, const int32_t *perm,
-                                 const uint64_t *csk, const uint64_t *qsk, const SearchClass &cls, const int32_t *lo,
-                                 const int32_t *hi, const int64_t *tile_start, int32_t *work, const uint8_t *keytab,
+                                 const uint64_t *csk, const uint64_t *qsk, const uint4 *ccnt, const uint4 *qcnt,
+                                 const SearchClass &cls, const int32_t *lo, const int32_t *hi, const int64_t *tile_start, int32_t *work, const uint8_t *keytab,
                                  int64_t keystride, int k, int dtype, void *out, int64_t nc, int jobsz,
                                  const SurvRows *rows, uint32_t *status) {
     const size_t smem = (size_t)256 * (2 * NW + 6) * sizeof(uint32_t);
     if (rows) {
         cudaFuncSetAttribute(k_search_lpt<NW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_search_lpt<NW, true><<<grid, 256, smem, st>>>(CS, perm, csk, qsk, cls, lo, hi, tile_start, work, keytab,
+        k_search_lpt<NW, true><<<grid, 256, smem, st>>>(CS, perm, csk, qsk, ccnt, qcnt, cls, lo, hi, tile_start, work, keytab,
                                                         keystride, k, dtype, out, nc, jobsz, *rows, status, 1u);
     } else {
         const SurvRows none{nullptr, nullptr, 0, nullptr, 1};
         cudaFuncSetAttribute(k_search_lpt<NW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_search_lpt<NW, false><<<grid, 256, smem, st>>>(CS, perm, csk, qsk, cls, lo, hi, tile_start, work, keytab,
+        k_search_lpt<NW, false><<<grid, 256, smem, st>>>(CS, perm, csk, qsk, ccnt, qcnt, cls, lo, hi, tile_start, work, keytab,
                                                          keystride, k, dtype, out, nc, jobsz, none, status, 1u);
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_search_lpt(cudaStream_t st, int sms, int ctas_per_sm, int jobsz, int nw, const DevStrings &CS,
-                              const int32_t *perm, const uint64_t *csk, const uint64_t *qsk, const SearchClass &cls,
-                              const int32_t *lo, const int32_t *hi, const int64_t *tile_start, int32_t *work,
+                              const int32_t *perm, const uint64_t *csk, const uint64_t *qsk, const uint4 *ccnt,
+                              const uint4 *qcnt, const SearchClass &cls, const int32_t *lo, const int32_t *hi,
+                              const int64_t *tile_start, int32_t *work,
                               const uint8_t *keytab, int64_t keystride, int k, int dtype, void *out, int64_t nc,
                               const SurvRows *rows, uint32_t *status) {
     if (cls.nq <= 0) return cudaSuccess;
@@ -121,7 +127,7 @@ cudaError_t launch_search_lpt(cudaStream_t st, int sms, int ctas_per_sm, int job
     const int grid = sms * std::max(1, std::min(ctas_per_sm, 8));
     switch (nw) {
 #define BLG_LPT(W) \
-    case W: return launch_lpt_nw<W>(st, grid, CS, perm, csk, qsk, cls, lo, hi, tile_start, work, keytab, keystride, k, dtype, out, nc, jobsz, rows, status);
+    case W: return launch_lpt_nw<W>(st, grid, CS, perm, csk, qsk, ccnt, qcnt, cls, lo, hi, tile_start, work, keytab, keystride, k, dtype, out, nc, jobsz, rows, status);
     BLG_LPT(1) BLG_LPT(2) BLG_LPT(3) BLG_LPT(4) BLG_LPT(5) BLG_LPT(6) BLG_LPT(7) BLG_LPT(8)
 #undef BLG_LPT
     default: return cudaErrorInvalidValue;

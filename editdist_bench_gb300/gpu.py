@@ -21,10 +21,11 @@ from __future__ import annotations
 
 import ctypes
 import os
+import threading
 
 import numpy as np
 
-from . import _lib
+from . import _common, _lib
 from ._common import DTYPE_CODE, as_list, check_dtype, check_k, pack
 from .device_array import DeviceArray
 
@@ -138,6 +139,37 @@ def cdist_matches(queries, choices, max_dist, capacity: int | None = None):
     return cdist_matches_packed(pack(q), pack(c), max_dist, capacity)
 
 
+# Page-locked staging of the list API's packed inputs: the native packer
+# writes each string's bytes straight into it, so the one-call entry points
+# copy them to the device at full link speed. Grown on demand and kept for
+# the process (reused by every call; calls take turns on it).
+_stage_lock = threading.Lock()
+_stage = {}
+
+
+def _pinned(ctx, slot: str, nbytes: int) -> int:
+    ptr, cap = _stage.get(slot, (None, 0))
+    if cap < nbytes:
+        if ptr:
+            ctx.lib.blg_host_free(ctx.h, ptr)
+            _stage.pop(slot)
+        cap = max(nbytes, 2 * cap, 1 << 16)
+        p = ctypes.c_void_p()
+        ctx.check(ctx.lib.blg_host_alloc(ctx.h, ctypes.c_size_t(cap), ctypes.byref(p)), "host_alloc")
+        ptr = p.value
+        _stage[slot] = (ptr, cap)
+    return ptr
+
+
+def _pack_pinned(ctx, seq, slot: str):
+    """(buf address, offsets address, n) of `seq` packed into pinned staging."""
+    n, total = _common._blgpack.size(seq)
+    bp = _pinned(ctx, slot + "/buf", max(total, 1))
+    op = _pinned(ctx, slot + "/off", 8 * (n + 1))
+    _common._blgpack.pack_into(seq, bp, max(total, 1), op)
+    return bp, op, n
+
+
 def pairwise(a, b, max_dist=None, dtype=np.int32, return_device: bool = False):
     """out[i] = d(a[i], b[i]) on the GPU (bitlev/gpu.py:71-103)."""
     a, b = as_list(a), as_list(b)
@@ -146,7 +178,22 @@ def pairwise(a, b, max_dist=None, dtype=np.int32, return_device: bool = False):
     k, dt = check_k(max_dist), check_dtype(dtype)
     if len(a) == 0:
         return _empty((0,), dt, return_device)
-    return pairwise_packed(pack(a), pack(b), k if k >= 0 else None, dt, return_device)
+    if _common._blgpack is None:
+        return pairwise_packed(pack(a), pack(b), k if k >= 0 else None, dt, return_device)
+    ctx = _lib.context()
+    n = len(a)
+    with _stage_lock:
+        ba, oa, _ = _pack_pinned(ctx, a, "a")
+        bb, ob, _ = _pack_pinned(ctx, b, "b")
+        if return_device:
+            dptr = ctypes.c_void_p()
+            ctx.check(ctx.lib.blg_pairwise(ctx.h, ba, oa, bb, ob, n, k, DTYPE_CODE[dt], None, ctypes.byref(dptr)),
+                      "pairwise")
+            return DeviceArray(dptr.value, (n,), dt, ctx)
+        out = np.empty(n, dtype=dt)
+        ctx.check(ctx.lib.blg_pairwise(ctx.h, ba, oa, bb, ob, n, k, DTYPE_CODE[dt], out.ctypes.data, None),
+                  "pairwise")
+        return out
 
 
 def cdist(queries, choices, max_dist=None, dtype=np.int32, return_device: bool = False):
@@ -155,7 +202,22 @@ def cdist(queries, choices, max_dist=None, dtype=np.int32, return_device: bool =
     k, dt = check_k(max_dist), check_dtype(dtype)
     if not q or not c:
         return _empty((len(q), len(c)), dt, return_device)
-    return cdist_packed(pack(q), pack(c), k if k >= 0 else None, dt, return_device)
+    if _common._blgpack is None:
+        return cdist_packed(pack(q), pack(c), k if k >= 0 else None, dt, return_device)
+    ctx = _lib.context()
+    nq, nc = len(q), len(c)
+    with _stage_lock:
+        bq, oq, _ = _pack_pinned(ctx, q, "q")
+        bc, oc, _ = _pack_pinned(ctx, c, "c")
+        if return_device:
+            dptr = ctypes.c_void_p()
+            ctx.check(ctx.lib.blg_cdist(ctx.h, bq, oq, nq, bc, oc, nc, k, DTYPE_CODE[dt], None, ctypes.byref(dptr)),
+                      "cdist")
+            return DeviceArray(dptr.value, (nq, nc), dt, ctx)
+        out = np.empty((nq, nc), dtype=dt)
+        ctx.check(ctx.lib.blg_cdist(ctx.h, bq, oq, nq, bc, oc, nc, k, DTYPE_CODE[dt], out.ctypes.data, None),
+                  "cdist")
+        return out
 
 
 class PairsBatch:

@@ -201,3 +201,74 @@ def test_band_matches_oracle(hostcheck, k):
         assert hostcheck.blg_host_band(a, len(a), b, len(b), 0, k) == want
         assert hostcheck.blg_host_band_query(a, len(a), b, len(b), k) == want
         assert hostcheck.blg_host_band_blocks(a, len(a), b, len(b), k) == want
+
+
+def _gram_counts(s: bytes) -> np.ndarray:
+    """Restatement of the device's binned 4-gram counts (gram_counts in
+    blg_kernels.cuh): each 4-gram g = (b[i-3] << 24 | ... | b[i]) hashed by
+    (g * 0x9E3779B1 mod 2^32) >> 28 into 16 bins, counters saturating at 255."""
+    c = np.zeros(16, dtype=np.int64)
+    for i in range(3, len(s)):
+        g = (s[i - 3] << 24) | (s[i - 2] << 16) | (s[i - 1] << 8) | s[i]
+        c[((g * 0x9E3779B1) & 0xFFFFFFFF) >> 28] += 1
+    return np.minimum(c, 255)
+
+
+def test_gram_count_bound_is_a_lower_bound():
+    """The survivor filter's premise: sum over bins |count(x) - count(y)| / 8
+    never exceeds the edit distance (an edit changes at most 4 grams of each
+    string), on near-copies, unrelated strings, short strings and repeats."""
+    import oracle
+    rng = np.random.default_rng(17)
+    a = W.concat(W.random_strings(rng, rng.integers(0, 120, 400)),
+                 W.random_strings(rng, rng.integers(0, 40, 200), np.frombuffer(b"AC", dtype=np.uint8)))
+    b = W.concat(W.mutate(rng, W.take(a, np.arange(300)), rng.uniform(0, 0.3, 300)),
+                 W.random_strings(rng, rng.integers(0, 120, 300)))
+    d = oracle.pairs(a, b)
+    sa, sb = W.unpack(a), W.unpack(b)
+    tight = 0
+    for x, y, dist in zip(sa, sb, d):
+        gd = int(np.abs(_gram_counts(x) - _gram_counts(y)).sum())
+        assert gd <= 8 * dist, (x, y, dist, gd)
+        tight += gd > 8 * (dist - 1)
+    assert tight > 0            # the bound is reached often enough to filter
+
+
+def test_native_pack_matches_python_pack():
+    """The native packer (csrc/blg_pack.c) gives the same buffer, offsets and
+    errors as the Python packer (the rules of csrc/edpy.c:14-35, 200-224)."""
+    from editdist_bench_gb300 import _build, _common
+    if _build.build_packer() is None:
+        pytest.skip("no Python development headers: the numpy packer is the only one")
+    import importlib
+    importlib.reload(_common)
+    assert _common._blgpack is not None
+    rng = np.random.default_rng(3)
+    cases = [[], [""], ["", b""], ["kitten", b"sitting", "caf\xe9", b"\x00\xff", "\x00"],
+             [bytes(rng.integers(0, 256, int(n), dtype=np.uint8)) for n in rng.integers(0, 300, 500)],
+             ["".join(chr(c) for c in rng.integers(0, 256, int(n))) for n in rng.integers(0, 50, 300)]]
+    for seq in cases:
+        got, want = _common.pack(seq), _common.pack_python(seq)
+        np.testing.assert_array_equal(got[0], want[0])
+        np.testing.assert_array_equal(got[1], want[1])
+        assert len(got[0]) >= 1
+    for bad, exc in ((["ok", "ā"], ValueError), (["ok", 3], TypeError), ([None], TypeError)):
+        with pytest.raises(exc) as e1:
+            _common.pack(bad)
+        with pytest.raises(exc) as e2:
+            _common.pack_python(bad)
+        assert str(e1.value) == str(e2.value)
+
+
+def test_windowed_gram_bound_is_a_lower_bound():
+    """The pairs scheduler's feature: the 4-gram count distance of the first 64
+    bytes of each (trimmed) string, over 16, never exceeds the distance."""
+    import oracle
+    rng = np.random.default_rng(19)
+    a = W.random_strings(rng, rng.integers(0, 260, 600))
+    b = W.concat(W.mutate(rng, W.take(a, np.arange(400)), rng.uniform(0, 0.4, 400)),
+                 W.random_strings(rng, rng.integers(0, 260, 200)))
+    d = oracle.pairs(a, b, trim=False)
+    for x, y, dist in zip(W.unpack(a), W.unpack(b), d):
+        gd = int(np.abs(_gram_counts(x[:64]) - _gram_counts(y[:64])).sum())
+        assert gd <= 16 * dist, (x, y, dist, gd)
