@@ -24,7 +24,8 @@ matrix. The metric is pairs/s (distances per second; GCUPS beside it).
            bounded sample, all host threads.
 * matches: for a thresholded search, the same search in its matches-only
            form (sorted (query, choice, distance) records instead of the
-           dense matrix), kernel-only and end to end.
+           dense matrix), kernel-only and end to end; and (e2e_u4) the dense
+           matrix end to end with 4-bit results, two per byte.
 * runs:    the headline's max_dist=2 uint8 run, and each of the other four
            benchmark configurations (config1 .. config5 but the headline):
            kernel-only pairs/s, e2e, a CPU sample, the dominant kernel's
@@ -641,6 +642,35 @@ def e2e_leg(bench, pin, steps, warmup, i=0) -> dict:
             "path": "one-call C-ABI (blg_pairwise / blg_cdist / blg_cdist_batch), pinned host buffers, wall clock"}
 
 
+def u4_leg(bench, pin, steps: int, warmup: int) -> dict | None:
+    """A thresholded search with max_dist <= 14 in its 4-bit form (BLG_UINT4:
+    two results per byte, exact below 15): the one-call C-ABI from pinned
+    host buffers, the packed matrix copied back (half of uint8's bytes)."""
+    k = bench.runs[0][0]
+    if bench.kind != "cdist" or k is None or k > 14:
+        return None
+    ctx = _lib.context()
+    (bq, oq), (bc, oc) = bench._pq, bench._pc
+    nbytes = (bench.w.nq * bench.w.nc + 1) // 2
+    out = pin.empty((nbytes,), np.uint8)
+
+    def call():
+        ctx.check(ctx.lib.blg_cdist(ctx.h, bq.ctypes.data, oq.ctypes.data, bench.w.nq, bc.ctypes.data,
+                                    oc.ctypes.data, bench.w.nc, k, _lib.UINT4, out.ctypes.data, None))
+    for _ in range(max(warmup, 3)):
+        call()
+    t = []
+    for _ in range(max(3, steps)):
+        t0 = time.perf_counter()
+        call()
+        t.append(time.perf_counter() - t0)
+    s = statistics.median(t)
+    h2d, _ = bench.io_bytes(0)
+    return {"value": bench.pairs / s, "unit": "pairs/s", "ms_per_call": s * 1e3, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": nbytes,
+            "path": "blg_cdist with 4-bit results (two per byte), pinned host buffers, wall clock"}
+
+
 def list_leg(bench, calls: int = 3) -> dict | None:
     """The drop-in call on Python lists of bytes, as a bitlev user makes it:
     gpu.pairwise(a, b) / gpu.cdist(q, c) with packing (the native packer into
@@ -770,6 +800,9 @@ def suite_config(cfg, ctx, flush, pin, args, peak, dev, clock_mhz) -> dict:
     m = matches_leg(bench, ctx, pin, flush, args)
     if m:
         res["matches"] = m
+    u4 = u4_leg(bench, pin, steps, args.warmup)
+    if u4:
+        res["e2e_u4"] = u4
     cpu, exit_sum = (None, None) if args.no_cpu_baseline else cpu_leg(bench, args.suite_cpu_budget)
     res["cpu_baseline"] = cpu
     if top:

@@ -16,6 +16,7 @@ from . import _build
 
 OK, ERR_ALLOC, ERR_ARG, ERR_CUDA, ERR_TIMEOUT, ERR_NODEVICE = 0, -1, -2, -3, -4, -5
 SCHED_AUTO, SCHED_PLAIN, SCHED_LEARNED, SCHED_LENSORT = 0, 1, 2, 3
+UINT4 = 3            # BLG_UINT4: 4-bit results, two per byte
 
 _P = ctypes.c_void_p
 _I32, _I64, _SZ = ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t

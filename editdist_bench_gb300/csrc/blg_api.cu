@@ -56,6 +56,7 @@ cudaError_t launch_match_compact(cudaStream_t st, int sms, int dtype, const void
                                  int64_t *counts, int64_t *total, int64_t nc, int64_t row0, blg_match *out,
                                  int64_t capacity, bool emit);
 int64_t match_blocks(int64_t n);
+cudaError_t launch_pack_nibbles(cudaStream_t st, int sms, const uint8_t *src, int64_t e0, int64_t e1, uint8_t *dst);
 cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, const DevStrings &A,
                               const DevStrings &B, int tile_pairs, int k, int dtype, void *out, const LongQueue &q,
                               uint32_t *status, int32_t wait_polls);
@@ -298,6 +299,19 @@ int sync_and_status(blg_ctx *c) {
 static size_t dtype_size(int dt) { return dt == BLG_UINT8 ? 1 : dt == BLG_UINT16 ? 2 : 4; }
 
 static bool dtype_ok(int dt) { return dt == BLG_INT32 || dt == BLG_UINT16 || dt == BLG_UINT8; }
+
+// 4-bit results (BLG_UINT4): the kernels write uint8, then k_pack_nibbles
+// saturates at 15 and packs two results per byte.
+static bool dtype_ok_out(int dt) { return dtype_ok(dt) || dt == BLG_UINT4; }
+static size_t out_bytes(int dt, int64_t n) {
+    return dt == BLG_UINT4 ? (size_t)(n + 1) / 2 : dtype_size(dt) * (size_t)n;
+}
+static int pack_u4(blg_ctx *c, const void *d8, int64_t e0, int64_t e1, void *d4) {
+    CK(launch(c, "pack_u4", [&] {
+           return launch_pack_nibbles(c->stream, c->sms, (const uint8_t *)d8, e0, e1, (uint8_t *)d4);
+       }), "pack_u4");
+    return BLG_OK;
+}
 
 // ------------------------------------------------------------- pairs --
 // Host pass over the offsets: how many pairs are short (shorter string <= 32
@@ -1069,9 +1083,12 @@ static int search_upload_queries(blg_ctx *c, const uint8_t *bq, const int64_t *o
 
 // One-call cdist with host results: queries in chunks of rows; the rows of
 // chunk i go back (stream `down`) while chunk i+1 computes.
+// d4 (optional): 4-bit results. The chunks then compute uint8 rows into
+// d_out, pack them into d4 and copy back d4's bytes; chunk boundaries fall on
+// even elements so no byte is shared by two chunks.
 static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq, const uint8_t *bc,
                            const int64_t *oc, int64_t nc, int k, int dtype, void *out_host, void *d_out,
-                           blg_search *s) {
+                           blg_search *s, void *d4) {
     const bool surv = k >= 0 && c->sched != BLG_SCHED_PLAIN;      // the survivor kernels run (search_run)
     int rc = search_upload_queries(c, bq, oq, nq, s);
     if (!rc) rc = search_upload_choices(c, bc, oc, nc, s, surv ? NEED_SORTED : NEED_TT);
@@ -1088,6 +1105,13 @@ static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int
     } else {
         const int n8 = (int)std::min<int64_t>(8, nq);
         for (int i = 1; i <= n8; i++) cut.push_back(nq * i / n8);
+    }
+    if (d4 && (nc & 1)) {                               // even element boundaries: even rows
+        std::vector<int64_t> even{0};
+        for (size_t i = 1; i + 1 < cut.size(); i++)
+            if ((cut[i] & ~int64_t(1)) > even.back()) even.push_back(cut[i] & ~int64_t(1));
+        even.push_back(nq);
+        cut.swap(even);
     }
     const int nch = (int)cut.size() - 1;
     std::vector<cudaEvent_t> ev(nch + 1, nullptr);
@@ -1106,6 +1130,7 @@ static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int
             const int64_t q0 = cut[ch], q1 = cut[ch + 1];
             rc = search_build_classes(c, oq, q0, q1, s);
             if (!rc) rc = search_run(c, s, k, dtype, d_out, q0, q1);
+            if (!rc && d4) rc = pack_u4(c, d_out, q0 * nc, q1 * nc, d4);
             if (!rc && cudaEventRecord(ev[ch], c->stream) != cudaSuccess) rc = fail(c, BLG_ERR_CUDA, "event");
             // exact runs: the host sorts the choices for the prefix-reuse
             // kernel while the first chunk computes on the tile-transposed
@@ -1116,8 +1141,9 @@ static int cdist_pipelined(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int
         if (ch >= 1) {
             const int64_t q0 = cut[ch - 1], q1 = cut[ch];
             if (cudaStreamWaitEvent(c->down, ev[ch - 1], 0) != cudaSuccess) { rc = fail(c, BLG_ERR_CUDA, "wait"); break; }
-            cudaError_t e = cudaMemcpyAsync((uint8_t *)out_host + q0 * row, (uint8_t *)d_out + q0 * row,
-                                            (size_t)(q1 - q0) * row, cudaMemcpyDeviceToHost, c->down);
+            const int64_t b0 = d4 ? q0 * nc / 2 : q0 * (int64_t)row, b1 = d4 ? (q1 * nc + 1) / 2 : q1 * (int64_t)row;
+            cudaError_t e = cudaMemcpyAsync((uint8_t *)out_host + b0, (uint8_t *)(d4 ? d4 : d_out) + b0,
+                                            (size_t)(b1 - b0), cudaMemcpyDeviceToHost, c->down);
             if (e != cudaSuccess) rc = cuda_fail(c, e, "D2H results");
         }
     }
@@ -1868,7 +1894,15 @@ int blg_pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uin
 int blg_pairs_run(blg_ctx *c, blg_pairs *p, int32_t max_dist, int32_t dtype, void *d_out) {
     ENTER(c);
     if (!p) return fail(c, BLG_ERR_ARG, "null pairs");
-    return pairs_run(c, p, max_dist, dtype, d_out);
+    if (dtype != BLG_UINT4) return pairs_run(c, p, max_dist, dtype, d_out);
+    if (p->n == 0) return BLG_OK;
+    if (!d_out) return fail(c, BLG_ERR_ARG, "null output");
+    void *d8 = nullptr;                                 // uint8 results, then packed into d_out
+    CK(dev_alloc(c, &d8, (size_t)p->n), "cudaMallocAsync(uint8 results)");
+    int rc = pairs_run(c, p, max_dist, BLG_UINT8, d8);
+    if (!rc) rc = pack_u4(c, d8, 0, p->n, d_out);
+    dev_free(c, d8);
+    return rc;
 }
 
 int blg_pairs_run_logged(blg_ctx *c, blg_pairs *p, int32_t max_dist, int32_t dtype, void *d_out,
@@ -2020,7 +2054,16 @@ int blg_search_upload(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t 
 int blg_search_run(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t dtype, void *d_out) {
     ENTER(c);
     if (!s) return fail(c, BLG_ERR_ARG, "null search");
-    return search_run(c, s, max_dist, dtype, d_out);
+    if (dtype != BLG_UINT4) return search_run(c, s, max_dist, dtype, d_out);
+    const int64_t n = s->nq * s->nc;
+    if (n == 0) return BLG_OK;
+    if (!d_out) return fail(c, BLG_ERR_ARG, "null output");
+    void *d8 = nullptr;                                 // uint8 results, then packed into d_out
+    CK(dev_alloc(c, &d8, (size_t)n), "cudaMallocAsync(uint8 results)");
+    int rc = search_run(c, s, max_dist, BLG_UINT8, d8);
+    if (!rc) rc = pack_u4(c, d8, 0, n, d_out);
+    dev_free(c, d8);
+    return rc;
 }
 
 void blg_search_free(blg_ctx *c, blg_search *s) {
@@ -2035,17 +2078,23 @@ int blg_pairwise(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uint8_t
                  const int64_t *ob, int64_t n, int32_t max_dist, int32_t dtype, void *out_host,
                  void **out_device) {
     ENTER(c);
-    if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
+    if (!dtype_ok_out(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16, uint8 or uint4");
     if (n < 0) return fail(c, BLG_ERR_ARG, "negative count");
     if (!out_device && n > 0 && !out_host) return fail(c, BLG_ERR_ARG, "null output");
-    const size_t obytes = dtype_size(dtype) * (size_t)n;
-    void *d_out = nullptr;
+    const bool u4 = dtype == BLG_UINT4;
+    const size_t obytes = out_bytes(dtype, n);
+    void *d_out = nullptr, *d8 = nullptr;
     CK(dev_alloc(c, &d_out, obytes), "cudaMallocAsync(out)");
+    if (u4 && dev_alloc(c, &d8, (size_t)n) != cudaSuccess) {   // uint8 results before packing
+        dev_free(c, d_out);
+        return fail(c, BLG_ERR_ALLOC, "cudaMallocAsync(uint8 results)");
+    }
     blg_pairs p;
     int rc = check_offsets_host(c, oa, n);
     if (!rc) rc = check_offsets_host(c, ob, n);
-    // host results of a large set: chunks overlap copies and kernels
-    const bool pipe = !rc && !out_device && n >= (1 << 18);
+    // host results of a large set: chunks overlap copies and kernels (4-bit
+    // results: one pass, their copy back is small)
+    const bool pipe = !rc && !out_device && !u4 && n >= (1 << 18);
     if (pipe) {
         rc = alloc_strings(c, ba, oa, n, p.a);
         if (!rc) rc = alloc_strings(c, bb, ob, n, p.b);
@@ -2054,13 +2103,15 @@ int blg_pairwise(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uint8_t
         if (!rc) rc = pairs_classify(c, oa, ob, n, &p);
         if (!rc) rc = upload_strings(c, ba, oa, n, p.a);
         if (!rc) rc = upload_strings(c, bb, ob, n, p.b);
-        if (!rc) rc = pairs_run(c, &p, max_dist, dtype, d_out);
+        if (!rc) rc = pairs_run(c, &p, max_dist, u4 ? BLG_UINT8 : dtype, u4 ? d8 : d_out);
+        if (!rc && u4 && n > 0) rc = pack_u4(c, d8, 0, n, d_out);
     }
     if (!rc && !pipe && !out_device && n > 0) {
         cudaError_t e = cudaMemcpyAsync(out_host, d_out, obytes, cudaMemcpyDeviceToHost, c->stream);
         if (e != cudaSuccess) rc = cuda_fail(c, e, "D2H results");
     }
     pairs_release(c, &p);
+    dev_free(c, d8);
     if (rc || !out_device) dev_free(c, d_out);
     const int rc2 = sync_and_status(c);
     if (rc) return rc;
@@ -2076,30 +2127,40 @@ int blg_cdist(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t nq, cons
               const int64_t *oc, int64_t nc, int32_t max_dist, int32_t dtype, void *out_host,
               void **out_device) {
     ENTER(c);
-    if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
+    if (!dtype_ok_out(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16, uint8 or uint4");
     if (nq < 0 || nc < 0) return fail(c, BLG_ERR_ARG, "negative count");
-    const size_t obytes = dtype_size(dtype) * (size_t)nq * (size_t)nc;
+    const bool u4 = dtype == BLG_UINT4;
+    const int64_t n = nq * nc;
+    const size_t obytes = out_bytes(dtype, n);
     if (!out_device && obytes > 0 && !out_host) return fail(c, BLG_ERR_ARG, "null output");
-    void *d_out = nullptr;
+    void *d_out = nullptr, *d8 = nullptr;
     CK(dev_alloc(c, &d_out, obytes), "cudaMallocAsync(out)");
+    if (u4 && dev_alloc(c, &d8, (size_t)n) != cudaSuccess) {   // uint8 results before packing
+        dev_free(c, d_out);
+        return fail(c, BLG_ERR_ALLOC, "cudaMallocAsync(uint8 results)");
+    }
     blg_search s;
     int rc = BLG_OK;
     if (nq > 0 && nc > 0) {
-        // a result matrix of 64 MiB or more going to the host: query chunks,
-        // each chunk's rows copied back while the next chunk computes
-        const bool pipe = !out_device && nq >= 2 && obytes >= (64u << 20);
+        // a result matrix of 64 MiB or more going to the host (32 MiB of
+        // 4-bit results): query chunks, each chunk's rows copied back while
+        // the next chunk computes
+        const bool pipe = !out_device && nq >= 2 && obytes >= (u4 ? (32u << 20) : (64u << 20));
         if (!pipe) {
             rc = search_upload(c, bq, oq, nq, bc, oc, nc, &s);
-            if (!rc) rc = search_run(c, &s, max_dist, dtype, d_out);
+            if (!rc) rc = search_run(c, &s, max_dist, u4 ? BLG_UINT8 : dtype, u4 ? d8 : d_out);
+            if (!rc && u4) rc = pack_u4(c, d8, 0, n, d_out);
             if (!rc && !out_device) {
                 cudaError_t e = cudaMemcpyAsync(out_host, d_out, obytes, cudaMemcpyDeviceToHost, c->stream);
                 if (e != cudaSuccess) rc = cuda_fail(c, e, "D2H results");
             }
         } else {
-            rc = cdist_pipelined(c, bq, oq, nq, bc, oc, nc, max_dist, dtype, out_host, d_out, &s);
+            rc = cdist_pipelined(c, bq, oq, nq, bc, oc, nc, max_dist, u4 ? BLG_UINT8 : dtype, out_host,
+                                 u4 ? d8 : d_out, &s, u4 ? d_out : nullptr);
         }
         search_release(c, &s);
     }
+    dev_free(c, d8);
     if (rc || !out_device) dev_free(c, d_out);
     const int rc2 = sync_and_status(c);
     if (rc) return rc;

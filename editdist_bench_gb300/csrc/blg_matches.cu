@@ -195,4 +195,52 @@ cudaError_t launch_match_compact(cudaStream_t st, int sms, int dtype, const void
     return match_compact_t<int32_t>(st, sms, dense, n, k, counts, total, nc, row0, out, capacity, emit);
 }
 
+// ---------------------------------------------------- 4-bit packed results --
+// Results e0 .. e1-1 of a uint8 result array, each saturated at 15, two per
+// byte: element e goes to byte e / 2, the low nibble for even e. e0 is even,
+// so every output byte comes from two elements of this range (the last one
+// has a zero high nibble when e1 is odd). One thread per 16 output bytes:
+// two 16-byte loads, one 16-byte store where the addresses line up, else
+// byte by byte.
+__device__ __forceinline__ uint32_t nibble_pack4(uint32_t x) {    // 4 bytes -> 2 bytes (low 16 bits)
+    x = __vminu4(x, 0x0f0f0f0fu);
+    const uint32_t y = (x & 0x000f000fu) | ((x >> 4) & 0x00f000f0u);
+    return __byte_perm(y, 0u, 0x4420);                             // bytes 0 and 2
+}
+
+__global__ void __launch_bounds__(256) k_pack_nibbles(const uint8_t *src, int64_t e0, int64_t e1, uint8_t *dst) {
+    const int64_t b0 = e0 >> 1, b1 = (e1 + 1) >> 1;              // output bytes [b0, b1)
+    const int64_t nb = b1 - b0;
+    const bool vec = ((reinterpret_cast<uintptr_t>(src + e0) | reinterpret_cast<uintptr_t>(dst + b0)) & 15) == 0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t * 16 < nb; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o = b0 + t * 16;                             // first output byte of this thread
+        if (vec && o + 16 <= b1 && 2 * (o + 16) <= e1) {
+            const uint4 a = *reinterpret_cast<const uint4 *>(src + 2 * o);
+            const uint4 b = *reinterpret_cast<const uint4 *>(src + 2 * o + 16);
+            uint4 r;
+            r.x = nibble_pack4(a.x) | (nibble_pack4(a.y) << 16);
+            r.y = nibble_pack4(a.z) | (nibble_pack4(a.w) << 16);
+            r.z = nibble_pack4(b.x) | (nibble_pack4(b.y) << 16);
+            r.w = nibble_pack4(b.z) | (nibble_pack4(b.w) << 16);
+            *reinterpret_cast<uint4 *>(dst + o) = r;
+        } else {
+            for (int64_t q = o; q < b1 && q < o + 16; q++) {
+                const uint32_t lo = min((uint32_t)src[2 * q], 15u);
+                const uint32_t hi = 2 * q + 1 < e1 ? min((uint32_t)src[2 * q + 1], 15u) : 0u;
+                dst[q] = (uint8_t)(lo | (hi << 4));
+            }
+        }
+    }
+}
+
+cudaError_t launch_pack_nibbles(cudaStream_t st, int sms, const uint8_t *src, int64_t e0, int64_t e1, uint8_t *dst) {
+    if (e1 <= e0) return cudaSuccess;
+    if (e0 & 1) return cudaErrorInvalidValue;
+    const int64_t threads = ((e1 - e0 + 1) / 2 + 15) / 16;
+    const int grid = (int)std::min<int64_t>((threads + 255) / 256, (int64_t)sms * 16);
+    k_pack_nibbles<<<grid, 256, 0, st>>>(src, e0, e1, dst);
+    return cudaGetLastError();
+}
+
 }  // namespace blg
+

@@ -99,6 +99,46 @@ def cdist_packed(pq, pc, max_dist=None, dtype=np.int32, return_device: bool = Fa
     return out
 
 
+# ---- 4-bit results (BLG_UINT4): two per byte, saturating at 15; exact for
+#      max_dist <= 14. Half the bytes of uint8 cross from the device.
+def unpack_u4(packed: np.ndarray, n: int) -> np.ndarray:
+    """uint8[n] from 4-bit results packed two per byte (low nibble first)."""
+    p = np.asarray(packed, dtype=np.uint8)
+    out = np.empty(2 * len(p), dtype=np.uint8)
+    out[0::2] = p & 15
+    out[1::2] = p >> 4
+    return out[:n]
+
+
+def pairwise_u4_packed(pa, pb, max_dist=None) -> np.ndarray:
+    """pairwise_packed with 4-bit results: uint8[(n + 1) // 2], two per byte."""
+    (ba, oa), (bb, ob) = _packed(pa), _packed(pb)
+    n = len(oa) - 1
+    if len(ob) - 1 != n:
+        raise ValueError(f"length mismatch: {n} vs {len(ob) - 1}")
+    k = check_k(max_dist)
+    ctx = _lib.context()
+    out = np.zeros(max(1, (n + 1) // 2), dtype=np.uint8)
+    if n:
+        ctx.check(ctx.lib.blg_pairwise(ctx.h, ba.ctypes.data, oa.ctypes.data, bb.ctypes.data, ob.ctypes.data, n, k,
+                                       _lib.UINT4, out.ctypes.data, None), "pairwise")
+    return out[:(n + 1) // 2]
+
+
+def cdist_u4_packed(pq, pc, max_dist=None) -> np.ndarray:
+    """cdist_packed with 4-bit results: uint8[(nq * nc + 1) // 2], row-major,
+    two results per byte."""
+    (bq, oq), (bc, oc) = _packed(pq), _packed(pc)
+    nq, nc = len(oq) - 1, len(oc) - 1
+    k = check_k(max_dist)
+    ctx = _lib.context()
+    out = np.zeros(max(1, (nq * nc + 1) // 2), dtype=np.uint8)
+    if nq and nc:
+        ctx.check(ctx.lib.blg_cdist(ctx.h, bq.ctypes.data, oq.ctypes.data, nq, bc.ctypes.data, oc.ctypes.data, nc,
+                                    k, _lib.UINT4, out.ctypes.data, None), "cdist")
+    return out[:(nq * nc + 1) // 2]
+
+
 # one record of blg_cdist_matches / blg_search_matches (include/bitlev_gb300.h: blg_match)
 MATCH_DTYPE = np.dtype([("query", "<i8"), ("choice", "<i8"), ("dist", "<i4"), ("reserved", "<i4")])
 

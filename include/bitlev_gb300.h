@@ -45,6 +45,14 @@ extern "C" {
 #define BLG_INT32 0
 #define BLG_UINT16 1
 #define BLG_UINT8 2
+/* 4-bit results, two per byte (element 2i in the low nibble of byte i, 2i+1
+ * in the high nibble), saturating at 15: for max_dist <= 14 every result is
+ * exact, and the device -> host copy is half of uint8's. No counterpart in
+ * the reference, which names narrower results as the way to cut the search's
+ * result stream (README.md:319-321). Accepted by blg_pairwise, blg_cdist,
+ * blg_pairs_run and blg_search_run; an output of n results is (n + 1) / 2
+ * bytes. */
+#define BLG_UINT4 3
 
 typedef struct blg_ctx blg_ctx;
 typedef struct blg_pairs blg_pairs;   /* resident pairs  (bench/cudamyers.py:83-114 PairsState) */
