@@ -862,11 +862,13 @@ def run_ours(args, ranks: Ranks):
 
     # e2e through the C-ABI with pinned host buffers
     pin = Pinned(ctx)
-    bench.e2e_setup(pin)
-    e2e = e2e_leg(bench, pin, min(args.steps, 10), args.warmup)
-    e2e["value"] = bench.pairs * ranks.world / (ranks.max(bench.pairs / e2e["value"]))
-    matches = matches_leg(bench, ctx, pin, flush, args)
-    e2e_list = list_leg(bench) if ranks.world == 1 and not args.no_suite else None
+    e2e = matches = e2e_list = None
+    if not args.kernel_only:
+        bench.e2e_setup(pin)
+        e2e = e2e_leg(bench, pin, min(args.steps, 10), args.warmup)
+        e2e["value"] = bench.pairs * ranks.world / (ranks.max(bench.pairs / e2e["value"]))
+        matches = matches_leg(bench, ctx, pin, flush, args)
+        e2e_list = list_leg(bench) if ranks.world == 1 and not args.no_suite else None
 
     result = {
         "metric": "pairs/s", "value": value, "unit": "pairs/s", "n_gpus": ranks.world,
@@ -1043,6 +1045,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of oracle work per leg")
     ap.add_argument("--suite-cpu-budget", type=float, default=3.0,
                     help="seconds of oracle work per leg for the other configurations")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="skip the end-to-end, matches and list legs (profiling runs)")
     ap.add_argument("--no-suite", action="store_true",
                     help="report the headline configuration only (not the other four under runs)")
     ap.add_argument("--nq", type=int, default=None, help="override the query count (profiling)")

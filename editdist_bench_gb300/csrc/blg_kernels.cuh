@@ -671,7 +671,9 @@ __device__ __forceinline__ uint64_t gram_sketch(const uint8_t *p, int m) {
 // scheduler network's similarity feature, and an exact filter: a pair whose
 // bound exceeds max_dist has distance > max_dist.
 __device__ __forceinline__ uint4 gram_counts(const uint8_t *p, int m) {
-    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+    // plain byte adds into l0..l3 (a byte cannot pass 255 within 252 grams),
+    // folded into the saturating totals c0..c3 every 252 bytes and at the end
+    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0, l0 = 0, l1 = 0, l2 = 0, l3 = 0;
     uint32_t g = 0;
     TextScan ts;
     ts.init(p);
@@ -684,15 +686,19 @@ __device__ __forceinline__ uint4 gram_counts(const uint8_t *p, int m) {
                 if (i + b >= 3) {
                     const uint32_t h = (g * 0x9E3779B1u) >> 28;    // bin 0..15
                     const uint32_t add = 1u << (8 * (h & 3u)), word = h >> 2;
-                    c0 = word == 0 ? __vaddus4(c0, add) : c0;
-                    c1 = word == 1 ? __vaddus4(c1, add) : c1;
-                    c2 = word == 2 ? __vaddus4(c2, add) : c2;
-                    c3 = word == 3 ? __vaddus4(c3, add) : c3;
+                    l0 += word == 0 ? add : 0u;
+                    l1 += word == 1 ? add : 0u;
+                    l2 += word == 2 ? add : 0u;
+                    l3 += word == 3 ? add : 0u;
                 }
             }
         }
+        if (i % 252 == 248) {
+            c0 = __vaddus4(c0, l0); c1 = __vaddus4(c1, l1); c2 = __vaddus4(c2, l2); c3 = __vaddus4(c3, l3);
+            l0 = l1 = l2 = l3 = 0;
+        }
     }
-    return make_uint4(c0, c1, c2, c3);
+    return make_uint4(__vaddus4(c0, l0), __vaddus4(c1, l1), __vaddus4(c2, l2), __vaddus4(c3, l3));
 }
 
 // Sum over the 16 bins of |count(x) - count(y)| (8 x gram_bound).
