@@ -59,7 +59,7 @@ int64_t match_blocks(int64_t n);
 cudaError_t launch_pack_nibbles(cudaStream_t st, int sms, const uint8_t *src, int64_t e0, int64_t e1, uint8_t *dst);
 cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, const DevStrings &A,
                               const DevStrings &B, int tile_pairs, int k, int dtype, void *out, const LongQueue &q,
-                              uint32_t *status, int32_t wait_polls);
+                              uint32_t *status, int32_t wait_polls, bool trusted);
 cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, bool band, const DevStrings &A,
                               const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
                               bool lengap_key, uint32_t *status);
@@ -120,6 +120,7 @@ struct blg_pairs {
     int64_t n = 0;
     int64_t cap[kLongClasses] = {0, 0, 0, 0, 0};
     int64_t short_pairs = 0;      // pairs whose shorter string is at most 32 bytes
+    bool trusted = false;         // the host pass found every offset pair in order (kernels skip their checks)
     int64_t len_max_side = 0;     // total bytes of the larger side (a or b)
     void *q_items = nullptr;      // all class regions, one allocation
     int32_t *q_ctr = nullptr;     // counts[5], heads[5]
@@ -430,14 +431,16 @@ static int pairs_classify(blg_ctx *c, const int64_t *oa, const int64_t *ob, int6
     // the pass reads 16 bytes of offsets per pair: large sets are split
     // over host threads
     const int nt = n >= (1 << 17) ? HostPool::get().size() : 1;
-    std::vector<std::array<int64_t, kLongClasses + 2>> part(nt);
+    // per thread: class counts, short pairs, and whether an offset pair is out of order
+    std::vector<std::array<int64_t, kLongClasses + 3>> part(nt);
     auto work = [&](int t) {
-        std::array<int64_t, kLongClasses + 2> h{};
+        std::array<int64_t, kLongClasses + 3> h{};
         const int64_t i0 = n * t / nt, i1 = n * (t + 1) / nt;
-        int64_t shorts = 0;
+        int64_t shorts = 0, bad = 0;
         for (int64_t i = i0; i < i1; i++) {                  // branch-free, vectorisable
             const int64_t la = oa[i + 1] - oa[i], lb = ob[i + 1] - ob[i];
             shorts += (la <= 32) | (lb <= 32);
+            bad |= (la < 0) | (lb < 0) | (la > INT32_MAX) | (lb > INT32_MAX);
         }
         if (shorts < i1 - i0) {
             for (int64_t i = i0; i < i1; i++) {
@@ -449,15 +452,21 @@ static int pairs_classify(blg_ctx *c, const int64_t *oa, const int64_t *ob, int6
             }
         }
         h[kLongClasses + 1] = shorts;
+        h[kLongClasses + 2] = bad;
         part[t] = h;
     };
     if (nt == 1) work(0);
     else HostPool::get().run(nt, work);
     p->short_pairs = 0;
+    bool bad = false;
     for (int t = 0; t < nt; t++) {
         for (int j = 0; j <= kLongClasses; j++) hist[j] += part[t][j];
         p->short_pairs += part[t][kLongClasses + 1];
+        bad |= part[t][kLongClasses + 2] != 0;
     }
+    // off[0] >= 0 and off[n] >= off[0] were checked above: with every pair in
+    // order, every string lies inside the uploaded buffer
+    p->trusted = !bad;
     int64_t total = 0, above = hist[kLongClasses];
     for (int j = kLongClasses - 1; j >= 0; j--) {
         above += hist[j];
@@ -583,7 +592,7 @@ static int pairs_run_direct(blg_ctx *c, blg_pairs *p, const DevStrings &A, const
         const int tile = avg <= 33.0 ? 512 : std::max(32, (int)(17000.0 / avg) & ~31);
         CK(launch(c, "pairs_tile", [&] {
                return launch_pairs_tile(c->stream, c->sms, c->tune.tile_buffers, hask, A, B, tile, k, dtype, d_out, q,
-                                        c->d_status, c->fault_wait_polls);
+                                        c->d_status, c->fault_wait_polls, p->trusted);
            }), "pairs_tile");
     } else {
         CK(launch(c, "pairs_staged", [&] {
@@ -1903,6 +1912,9 @@ int blg_pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uin
     blg_pairs *p = new (std::nothrow) blg_pairs();
     if (!p) return fail(c, BLG_ERR_ALLOC, "host allocation");
     int rc = pairs_upload(c, ba, oa, bb, ob, n, p);
+    // the copies complete before the call returns: the device copy is the
+    // data the host pass checked, whatever the caller does with its buffers
+    if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = fail(c, BLG_ERR_CUDA, "upload");
     if (rc) {
         pairs_release(c, p);
         delete p;

@@ -290,10 +290,14 @@ __device__ __forceinline__ void tile_issue(TS &S, int buf, const DevStrings &A, 
     if (lb) bulk_g2s(S.stage[buf][1] + 16, B.buf + S.span_lo[buf][1], lb, &S.bar[buf]);
 }
 
-// Validated view of string i from prefetched offsets (o0, o1).
+// Validated view of string i from prefetched offsets (o0, o1). TRUST: the
+// host's pass over the offsets found every pair in order (and the set's
+// first and last offsets bound the uploaded buffer), so the checks are left
+// out.
+template <bool TRUST>
 __device__ __forceinline__ const uint8_t *string_from(const DevStrings &S, int64_t o0, int64_t o1, int &len,
                                                       uint32_t *status) {
-    if (o0 < S.base || o1 < o0 || o1 - S.base > S.bytes || o1 - o0 > 0x7fffffff) {
+    if (!TRUST && (o0 < S.base || o1 < o0 || o1 - S.base > S.bytes || o1 - o0 > 0x7fffffff)) {
         atomicOr(status, ST_BAD_OFFSETS);
         len = 0;
         return S.buf;
@@ -316,7 +320,7 @@ __device__ __forceinline__ void load_offs(PairOffs &o, const DevStrings &A, cons
     }
 }
 
-template <bool HASK, int NBUF>
+template <bool HASK, int NBUF, bool TRUST>
 __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : 3)
     k_pairs_tile(DevStrings A, DevStrings B, int P, int k, int dtype, void *out, LongQueue q, uint32_t *status,
                  uint32_t unit, uint32_t wait_polls) {
@@ -392,8 +396,8 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : 3)
         auto classify = [&](const PairOffs &o, int j, int &key, int &rank, uint2 &ent) {
             const int64_t i = t0 + j;
             int la, lb;
-            const uint8_t *ga = string_from(A, o.a0, o.a1, la, status);
-            const uint8_t *gb = string_from(B, o.b0, o.b1, lb, status);
+            const uint8_t *ga = string_from<TRUST>(A, o.a0, o.a1, la, status);
+            const uint8_t *gb = string_from<TRUST>(B, o.b0, o.b1, lb, status);
             const int64_t ra = ga - A.buf, rb = gb - B.buf;
             const bool sa = alo >= 0 && ra >= alo && ra + la <= ahi;
             const bool sb = blo >= 0 && rb >= blo && rb + lb <= bhi;
@@ -518,20 +522,29 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : 3)
 }
 
 // ------------------------------------------------------------- launcher --
-template <bool HASK, int NBUF>
+template <bool HASK, int NBUF, bool TRUST>
 static cudaError_t launch_tile(cudaStream_t st, int sms, const DevStrings &A, const DevStrings &B, int P, int k,
                                int dtype, void *out, const LongQueue &q, uint32_t *status, uint32_t polls) {
     const int64_t ntiles = (A.n + P - 1) / P;
     const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sms * (NBUF == 2 ? 2 : 3));
     const size_t smem = sizeof(TileShared<NBUF>);
-    cudaFuncSetAttribute(k_pairs_tile<HASK, NBUF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_pairs_tile<HASK, NBUF><<<grid, kTileThreads, smem, st>>>(A, B, P, k, dtype, out, q, status, 1u, polls);
+    cudaFuncSetAttribute(k_pairs_tile<HASK, NBUF, TRUST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_pairs_tile<HASK, NBUF, TRUST><<<grid, kTileThreads, smem, st>>>(A, B, P, k, dtype, out, q, status, 1u, polls);
     return cudaGetLastError();
 }
 
+template <bool HASK, int NBUF>
+static cudaError_t launch_tile_t(bool trusted, cudaStream_t st, int sms, const DevStrings &A, const DevStrings &B,
+                                 int P, int k, int dtype, void *out, const LongQueue &q, uint32_t *status,
+                                 uint32_t polls) {
+    return trusted ? launch_tile<HASK, NBUF, true>(st, sms, A, B, P, k, dtype, out, q, status, polls)
+                   : launch_tile<HASK, NBUF, false>(st, sms, A, B, P, k, dtype, out, q, status, polls);
+}
+
+// trusted: the offsets were checked on the host (every pair in order).
 cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, const DevStrings &A,
                               const DevStrings &B, int tile_pairs, int k, int dtype, void *out, const LongQueue &q,
-                              uint32_t *status, int32_t wait_polls) {
+                              uint32_t *status, int32_t wait_polls, bool trusted) {
     if (A.n <= 0) return cudaSuccess;
     const uint32_t polls = wait_polls < 0 ? kMbarPolls : (uint32_t)wait_polls;
     int P = tile_pairs;
@@ -539,10 +552,10 @@ cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, 
     if (P < 32) P = 32;
     P &= ~3;                                                // 4-aligned tiles keep the vector stores aligned
     if (buffers == 1)
-        return hask ? launch_tile<true, 1>(st, sms, A, B, P, k, dtype, out, q, status, polls)
-                    : launch_tile<false, 1>(st, sms, A, B, P, k, dtype, out, q, status, polls);
-    return hask ? launch_tile<true, 2>(st, sms, A, B, P, k, dtype, out, q, status, polls)
-                : launch_tile<false, 2>(st, sms, A, B, P, k, dtype, out, q, status, polls);
+        return hask ? launch_tile_t<true, 1>(trusted, st, sms, A, B, P, k, dtype, out, q, status, polls)
+                    : launch_tile_t<false, 1>(trusted, st, sms, A, B, P, k, dtype, out, q, status, polls);
+    return hask ? launch_tile_t<true, 2>(trusted, st, sms, A, B, P, k, dtype, out, q, status, polls)
+                : launch_tile_t<false, 2>(trusted, st, sms, A, B, P, k, dtype, out, q, status, polls);
 }
 
 }  // namespace blg
