@@ -28,14 +28,48 @@
 namespace blg {
 
 
-// sketch[i] = gram_sketch(string i), counts[i] = gram_counts(string i)
+// sketch[i] = gram_sketch(string i), counts[i] = gram_counts(string i),
+// one warp per string: lane l takes the 4-grams starting at l, l + 32, ...
+// (one unaligned 4-byte read each, consecutive across the warp), the 16 bin
+// counts are summed by one ballot per bin, the sketch bits by an OR over the
+// warp. The values equal the per-thread functions' (the same grams, hash and
+// saturation at 255).
 __global__ void __launch_bounds__(256) k_sketch_strings(DevStrings S, uint64_t *sketch, uint4 *counts,
                                                         uint32_t *status) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < S.n; i += nwarps) {
         int n;
         const uint8_t *p = string_at(S, i, n, status);
-        sketch[i] = gram_sketch(p, n);
-        counts[i] = gram_counts(p, n);
+        uint32_t sk_lo = 0, sk_hi = 0, cnt = 0;              // lane b < 16 counts bin b
+        for (int s0 = 0; s0 + 3 < n; s0 += 32) {
+            const int s = s0 + lane;                          // the gram of bytes s .. s+3
+            const bool act = s + 3 < n;
+            const uint32_t g = act ? __byte_perm(load4(p + s), 0u, 0x0123) : 0u;   // b[s] << 24 | .. | b[s+3]
+            const uint32_t h = g * 0x9E3779B1u;
+            const uint32_t bin = act ? (h >> 28) : 16u;
+            if (act && s + 3 < kSketchWindow) {
+                const uint32_t bit = h >> 26;
+                if (bit < 32) sk_lo |= 1u << bit;
+                else sk_hi |= 1u << (bit - 32);
+            }
+#pragma unroll
+            for (uint32_t b = 0; b < 16; b++) {
+                const unsigned m = __ballot_sync(kFull, bin == b);
+                if ((uint32_t)lane == b) cnt += __popc(m);
+            }
+        }
+        sk_lo = __reduce_or_sync(kFull, sk_lo);
+        sk_hi = __reduce_or_sync(kFull, sk_hi);
+        uint32_t v = (lane < 16 ? min(cnt, 255u) : 0u) << (8 * (lane & 3));   // byte lane & 3 of word lane >> 2
+        v |= __shfl_xor_sync(kFull, v, 1);
+        v |= __shfl_xor_sync(kFull, v, 2);
+        const uint32_t w0 = __shfl_sync(kFull, v, 0), w1 = __shfl_sync(kFull, v, 4), w2 = __shfl_sync(kFull, v, 8),
+                       w3 = __shfl_sync(kFull, v, 12);
+        if (lane == 0) {
+            sketch[i] = ((uint64_t)sk_hi << 32) | sk_lo;
+            counts[i] = make_uint4(w0, w1, w2, w3);
+        }
     }
 }
 
@@ -91,7 +125,7 @@ __global__ void __launch_bounds__(256) k_search_lpt(DevStrings CS, const int32_t
 cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S, uint64_t *sketch, uint4 *counts,
                                   uint32_t *status) {
     if (S.n <= 0) return cudaSuccess;
-    const int grid = (int)std::min<int64_t>((S.n + 255) / 256, (int64_t)sms * 8);
+    const int grid = (int)std::min<int64_t>((S.n + 7) / 8, (int64_t)sms * 8);     // a warp per string
     k_sketch_strings<<<grid, 256, 0, st>>>(S, sketch, counts, status);
     return cudaGetLastError();
 }

@@ -324,3 +324,31 @@ def test_problem_batch_graph(gpu):
     got = gpu.cdist_batch(probs[:3], return_device=False)
     for (pq, pc, k, dt), o in zip(probs[:3], got):
         np.testing.assert_array_equal(o, oracle.saturate(oracle.cross(pq, pc, k), dt))
+
+
+def test_gram_filter_repeats_and_saturation(gpu):
+    """The survivor filter's 4-gram counts saturate at 255 per bin: long runs
+    of one symbol, periodic strings and their near-copies (distance small,
+    counts far past 255) must keep their exact thresholded distances."""
+    rng = np.random.default_rng(88)
+    base = [b"A" * 500, b"AC" * 250, b"ACGT" * 125, b"AAAAC" * 100, b"G" * 300 + b"T" * 200]
+    q = oracle.pack(base)
+    variants = []
+    for s in base:
+        for e in range(0, 10):
+            t = bytearray(s)
+            for _ in range(e):
+                i = int(rng.integers(0, len(t)))
+                op = int(rng.integers(0, 3))
+                if op == 0:
+                    t[i] = int(rng.choice(list(b"ACGT")))
+                elif op == 1:
+                    t.insert(i, int(rng.choice(list(b"ACGT"))))
+                elif len(t) > 1:
+                    del t[i]
+            variants.append(bytes(t))
+    c = W.concat(oracle.pack(variants), W.random_strings(rng, rng.integers(490, 510, 300)))
+    for k in (0, 3, 8, 31):
+        for dt in ("uint8", "int32"):
+            np.testing.assert_array_equal(gpu.cdist_packed(q, c, max_dist=k, dtype=dt),
+                                          oracle.saturate(oracle.cross(q, c, k), dt), err_msg=f"k={k} {dt}")
