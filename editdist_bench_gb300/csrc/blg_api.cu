@@ -90,7 +90,9 @@ cudaError_t launch_search_lpt(cudaStream_t st, int sms, int ctas_per_sm, int job
                               const int32_t *perm, const uint64_t *csk, const uint64_t *qsk, const uint4 *ccnt,
                               const uint4 *qcnt, const SearchClass &cls, const int32_t *lo, const int32_t *hi,
                               const int64_t *tile_start, int32_t *work, const uint8_t *keytab, int64_t keystride, int k,
-                              int dtype, void *out, int64_t nc, const SurvRows *rows, uint32_t *status);
+                              int dtype, void *out, int64_t nc, const SurvRows *rows, const DeferQueue &dq,
+                              uint32_t *status);
+cudaError_t launch_band_resume(cudaStream_t st, int sms, const DeferQueue &dq);
 cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
                              int64_t min_len, int64_t n_len, int k, int tile, int32_t *lo, int32_t *hi,
                              int64_t *tile_start, int32_t *work);
@@ -1227,6 +1229,31 @@ static int survivor_job_size(blg_ctx *c, const blg_search *s, const blg_search::
     return job;
 }
 
+// The context's queue of deferred banded survivors (allocated on first use;
+// an allocation failure leaves it off and every survivor finishes in its job).
+static DeferQueue defer_queue(blg_ctx *c) {
+    if (c->defer_cap <= 0) return DeferQueue{};
+    if (!c->defer_items && !c->defer_failed) {
+        void *items = nullptr, *count = nullptr;
+        if (cudaMalloc(&items, sizeof(DeferItem) * (size_t)kDeferCap) != cudaSuccess ||
+            cudaMalloc(&count, sizeof(unsigned long long)) != cudaSuccess) {
+            cudaGetLastError();
+            if (items) cudaFree(items);
+            c->defer_failed = true;
+        } else {
+            c->defer_items = items;
+            c->defer_count = count;
+        }
+    }
+    DeferQueue q;
+    if (c->defer_items) {
+        q.items = (DeferItem *)c->defer_items;
+        q.count = (unsigned long long *)c->defer_count;
+        q.cap = std::min(c->defer_cap, kDeferCap);
+    }
+    return q;
+}
+
 static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, int64_t q0, int64_t q1) {
     if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
     if (s->nq == 0 || s->nc == 0) return BLG_OK;
@@ -1246,6 +1273,15 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
         CK(launch(c, "build_peq", [&] {
                return launch_build_peq(c->stream, s->q.d, k_.qidx, k_.nq, k_.nw, k_.peq, c->d_status);
            }), "build_peq");
+    // survivors still in the band after a few columns leave their jobs for one resume pass
+    DeferQueue dq;
+    bool any_lpt = false;
+    if (surv && k <= 31)
+        for (auto &k_ : s->cls) any_lpt |= !k_.lanes && k_.nq > 0;
+    if (any_lpt) {
+        dq = defer_queue(c);
+        if (dq.items) CK(cudaMemsetAsync(dq.count, 0, sizeof(unsigned long long), c->stream), "reset defer queue");
+    }
     for (auto &k_ : s->cls) {
         SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
         if (surv && !k_.lanes) {
@@ -1281,7 +1317,7 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
                        return launch_search_lpt(c->stream, c->sms, c->tune.lpt_ctas, job, k_.nw, s->cs.d,
                                                 s->perm, s->csk, s->qsk, s->ccnt, s->qcnt, sc, k_.lo,
                                                 k_.hi, k_.tile_start, k_.work, keytab, keystride, k, dtype, d_out, s->nc,
-                                                nullptr, c->d_status);
+                                                nullptr, dq, c->d_status);
                    }), "search_lpt");
                 dev_free(c, keytab);
             } else {
@@ -1318,6 +1354,7 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
             }
         }
     }
+    if (dq.items) CK(launch(c, "band_resume", [&] { return launch_band_resume(c->stream, c->sms, dq); }), "band_resume");
     return BLG_OK;
 }
 
@@ -1544,10 +1581,11 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
 static int batch_run(blg_ctx *c, blg_batch *b) {
     if (!b->exec) {
         const bool prof = c->prof;
+        const DeferQueue dq = defer_queue(c);  // allocated before the capture
         c->prof = false;                      // no per-launch events inside a capture
         const int64_t before = c->launches;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "begin capture");
-        BatchPlan plan{b->d_jobs, b->njobs, b->nbanded, b->d_qprefix, b->d_job_tiles, b->d_tile_base, b->d_work};
+        BatchPlan plan{b->d_jobs, b->njobs, b->nbanded, b->d_qprefix, b->d_job_tiles, b->d_tile_base, b->d_work, dq};
         cudaError_t e = launch_batch(c->stream, c->sms, plan, b->d_fills, b->nfill, b->max_fill, b->total_queries,
                                      c->d_status);
         int rc = e == cudaSuccess ? BLG_OK : cuda_fail(c, e, "batch launch");
@@ -1562,7 +1600,9 @@ static int batch_run(blg_ctx *c, blg_batch *b) {
         if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_fail(c, e, "graph instantiate"); }
         b->graph = g;
         b->graph_kernels = (b->nfill > 0 ? 1 : 0) +
-                           (b->njobs > 0 ? 3 + (b->nbanded > 0 ? 1 : 0) + (b->nbanded < b->njobs ? 1 : 0) : 0) +
+                           (b->njobs > 0 ? 3 + (b->nbanded > 0 ? (dq.items ? 2 : 1) : 0) +
+                                               (b->nbanded < b->njobs ? 1 : 0)
+                                         : 0) +
                            (c->launches - before);
         c->launches = before;
     }
@@ -1887,6 +1927,8 @@ void blg_destroy(blg_ctx *c) {
     sched_model_free(c->model);
     c->model = nullptr;
     if (c->d_status) cudaFree(c->d_status);
+    if (c->defer_items) cudaFree(c->defer_items);
+    if (c->defer_count) cudaFree(c->defer_count);
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
     if (c->stage_done) cudaEventDestroy(c->stage_done);
@@ -2100,7 +2142,7 @@ int blg_sched_train_search(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t 
                return launch_search_lpt(c->stream, c->sms, c->tune.lpt_ctas, job, k_.nw, s->cs.d, s->perm,
                                         s->csk, s->qsk, s->ccnt, s->qcnt, sc, k_.lo, k_.hi,
                                         k_.tile_start, k_.work, nullptr, 0, max_dist, BLG_UINT8, out, s->nc, &R,
-                                        c->d_status);
+                                        DeferQueue{}, c->d_status);
            }), "search_lpt_logged");
     }
     int64_t rows = 0;
@@ -2504,6 +2546,13 @@ int blg_set_fault_injection(blg_ctx *c, int64_t alloc_fail_after, int32_t wait_p
     ENTER(c);
     c->fault_alloc_after = alloc_fail_after < 0 ? -1 : alloc_fail_after;
     c->fault_wait_polls = wait_polls < 0 ? -1 : wait_polls;
+    return BLG_OK;
+}
+
+int blg_set_defer_capacity(blg_ctx *c, int32_t cap) {
+    ENTER(c);
+    if (cap < 0) return fail(c, BLG_ERR_ARG, "defer capacity must be >= 0");
+    c->defer_cap = std::min(cap, kDeferCap);
     return BLG_OK;
 }
 

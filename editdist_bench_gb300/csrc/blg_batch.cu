@@ -3,11 +3,15 @@
 // A batch is a set of problems, each with its own queries, choices, max_dist,
 // output dtype and device output. Every problem keeps the layout of a
 // resident search (length-sorted choices, per-query Peq tables); a "job" is
-// one (problem, query word-class). Five kernels run the whole batch:
+// one (problem, query word-class). These kernels run the whole batch:
 //   k_batch_fill    max_dist+1 into every thresholded problem's output
 //   k_batch_peq     one CTA per (job, query): the query's Peq table
 //   k_batch_plan    one block per job: survivor ranges and tile prefix
 //   k_batch_scan    job tile prefix (the global tile space)
+//   k_batch_lpt     persistent: banded jobs (max_dist <= 31), 4096-survivor
+//                   units run longest-first; survivors still in the band
+//                   after a few columns are queued for
+//   k_band_resume   a thread per queued survivor, from its saved state
 //   k_batch_search  persistent: every CTA pulls (job, query, 1024-survivor)
 //                   tiles from one device counter until the space is done
 // The host captures them once into a CUDA graph and replays it per run.
@@ -15,6 +19,8 @@
 #include "blg_kernels.cuh"
 
 namespace blg {
+
+cudaError_t launch_band_resume(cudaStream_t st, int sms, const DeferQueue &dq);
 
 // Peq staging of the persistent kernel: [256][NW] u64, or the banded padded
 // halves [256][2*NW + 6] u32, whichever is larger for NW = kBatchMaxWords.
@@ -109,7 +115,12 @@ __global__ void __launch_bounds__(1024) k_batch_plan(BatchPlan plan) {
 __global__ void __launch_bounds__(1024) k_batch_scan(BatchPlan plan) {
     __shared__ int64_t s_sum[1024];
     __shared__ int64_t s_carry;
-    if (threadIdx.x == 0) { s_carry = 0; plan.work[0] = 0; plan.work[1] = 0; }
+    if (threadIdx.x == 0) {
+        s_carry = 0;
+        plan.work[0] = 0;
+        plan.work[1] = 0;
+        if (plan.defer.items) *plan.defer.count = 0;
+    }
     __syncthreads();
     for (int base = 0; base < plan.njobs; base += 1024) {
         const int j = base + threadIdx.x;
@@ -176,8 +187,8 @@ __global__ void __launch_bounds__(256) k_batch_lpt(BatchPlan plan, uint32_t *sta
         const int64_t s0 = job.lo[qi] + (lt - job.tile_start[qi]) * job.tile;
         const int cnt = (int)min((int64_t)job.tile, (int64_t)job.hi[qi] - s0);
         lpt_job(S, job.CS, job.perm, job.csk, job.ccnt, job.qsk[row], job.qcnt[row], s_rows, 2 * job.nw + 6,
-                job.cls.qlen[qi], row, s0, cnt, job.k, nullptr, job.dtype, job.out, job.nc, status, u,
-                [](int64_t, int, int, uint32_t) {});
+                job.cls.qlen[qi], row, s0, cnt, job.k, nullptr, job.dtype, job.out, job.nc, plan.defer,
+                job.cls.peq + (size_t)qi * 256 * job.nw, job.nw, status, u, [](int64_t, int, int, uint32_t) {});
     }
 }
 
@@ -239,7 +250,13 @@ cudaError_t launch_batch(cudaStream_t st, int sms, const BatchPlan &plan, const 
         k_batch_peq<<<(unsigned)total_queries, 256, 256 * kBatchMaxWords * 8, st>>>(plan, status);
         k_batch_plan<<<plan.njobs, 1024, 0, st>>>(plan);
         k_batch_scan<<<1, 1024, 0, st>>>(plan);
-        if (plan.nbanded > 0) k_batch_lpt<<<sms * 4, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
+        if (plan.nbanded > 0) {
+            k_batch_lpt<<<sms * 4, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
+            if (plan.defer.items) {
+                const cudaError_t e = launch_band_resume(st, sms, plan.defer);
+                if (e != cudaSuccess) return e;
+            }
+        }
         if (plan.nbanded < plan.njobs) k_batch_search<<<sms * 3, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
     }
     return cudaGetLastError();

@@ -44,6 +44,7 @@ struct BatchPlan {
     int64_t *job_tiles;        // [njobs]
     int64_t *tile_base;        // [njobs + 1]
     int32_t *work;             // persistent-kernel counters: [0] banded jobs, [1] the others
+    DeferQueue defer;          // banded survivors left for the resume pass (items null: none)
 };
 
 cudaError_t batch_set_attributes();

@@ -202,23 +202,40 @@ BLG_HD int popc32(uint32_t x) {
 #endif
 }
 
-// text(j) returns text byte j (0-based, called once per j in order);
-// eqw(c, p0) returns the window's match bits for byte c, where p0 is the
-// 0-based pattern index of window bit 0 (positions < 0 or >= m give no
-// bits). Caller guarantees 1 <= m, |n - m| <= k <= 31. Returns min(d, k+1);
-// *cols_out = text columns processed.
-template <typename TextFn, typename EqW>
-BLG_HD int band_core(int m, int n, int k, TextFn text, EqW eqw, Units u, int *cols_out) {
-    (void)u;                                                 // plain shifts here (see the column step)
-    const BandGeom bg = band_geom(m, n, k);
+// The banded loop's state before text column j: the window's vertical
+// deltas and D' of its top row. A run may stop at any column and resume
+// from the state later with the same results (band_steps).
+struct BandState {
+    uint32_t pv, mv;
+    int A, j;
+};
+
+BLG_HD BandState band_start(const BandGeom &bg) {
     const int nv = bg.dhi + 1;                               // virtual rows -dhi .. 0 at column 0
-    uint32_t mv = nv >= 32 ? 0xffffffffu : ((1u << nv) - 1u);
-    uint32_t pv = ~mv;
-    int A = bg.dhi;                                          // D'[top window row][current column]
-    for (int j = 0; j < n; j++) {
+    BandState s;
+    s.mv = nv >= 32 ? 0xffffffffu : ((1u << nv) - 1u);
+    s.pv = ~s.mv;
+    s.A = bg.dhi;                                            // D'[top window row][current column]
+    s.j = 0;
+    return s;
+}
+
+// Text columns s.j .. j_end - 1. text(j) returns text byte j (called once per
+// j in order); eqw(c, p0) returns the window's match bits for byte c, where
+// p0 is the 0-based pattern index of window bit 0 (positions < 0 or >= m
+// give no bits). Returns true when the exit fired (s.j = that column);
+// otherwise s holds the state before column j_end.
+template <typename TextFn, typename EqW>
+BLG_HD bool band_steps(int k, const BandGeom &bg, BandState &s, int j_end, TextFn text, EqW eqw) {
+    uint32_t pv = s.pv, mv = s.mv;
+    int A = s.A;
+    for (int j = s.j; j < j_end; j++) {
         if ((j & 3) == 0 && j > 0 && A - popc32(mv & bg.band) > k) {   // every band cell > k
-            if (cols_out) *cols_out = j;
-            return k + 1;
+            s.pv = pv;
+            s.mv = mv;
+            s.A = A;
+            s.j = j;
+            return true;
         }
         const uint32_t c = text(j);
         // column j's deltas re-indexed one row down; the new bottom row enters with +1
@@ -237,10 +254,29 @@ BLG_HD int band_core(int m, int n, int k, TextFn text, EqW eqw, Units u, int *co
         mv = phs & xv;
         A += 1 + (int)(pv & 1u) - (int)(mv & 1u);
     }
-    if (cols_out) *cols_out = n;
+    s.pv = pv;
+    s.mv = mv;
+    s.A = A;
+    s.j = j_end;
+    return false;
+}
+
+// min(d, k+1) from the state after the last text column.
+BLG_HD int band_finish(int k, const BandGeom &bg, const BandState &s) {
     const uint32_t ms = (bg.s >= 31 ? 0xffffffffu : ((2u << bg.s) - 1u)) & ~1u;   // bits 1..s
-    const int d = A + popc32(pv & ms) - popc32(mv & ms);
-    return cap_k(d, k);
+    return cap_k(s.A + popc32(s.pv & ms) - popc32(s.mv & ms), k);
+}
+
+// The whole banded run. Caller guarantees 1 <= m, |n - m| <= k <= 31.
+// Returns min(d, k+1); *cols_out = text columns processed.
+template <typename TextFn, typename EqW>
+BLG_HD int band_core(int m, int n, int k, TextFn text, EqW eqw, Units u, int *cols_out) {
+    (void)u;                                                 // plain shifts here (see the column step)
+    const BandGeom bg = band_geom(m, n, k);
+    BandState s = band_start(bg);
+    const bool exited = band_steps(k, bg, s, n, text, eqw);
+    if (cols_out) *cols_out = s.j;
+    return exited ? k + 1 : band_finish(k, bg, s);
 }
 
 // ---- host-side reference of the per-pair device logic ------------------

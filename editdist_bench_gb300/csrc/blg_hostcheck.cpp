@@ -227,6 +227,38 @@ extern "C" int blg_host_band_query(const uint8_t *q, int m, const uint8_t *t, in
     return band_core(m, n, k, text, eqw, u, nullptr);
 }
 
+// The search's banded run stopped after `stop` columns (a multiple of 4) and
+// resumed from its saved state with fresh text and window readers, the
+// window bits taken from the unpadded Peq words as the resume pass reads
+// them (32-bit halves p0 >> 5 and the next, zero outside the pattern).
+extern "C" int blg_host_band_resume(const uint8_t *q, int m, const uint8_t *t, int n, int k, int stop) {
+    if (k < 0 || k > 31 || stop < 0 || (stop & 3)) return -1;
+    if (m == 0) return cap_k(n, k);
+    if ((n > m ? n - m : m - n) > k) return k + 1;
+    Pattern P(q, m);
+    const int nw = (m + 63) / 64;
+    auto half = [&](uint32_t c, int r) -> uint32_t {
+        if (r < 0 || r >= 2 * nw) return 0u;
+        const uint64_t w = P.eq((uint8_t)c, r >> 1);
+        return (r & 1) ? (uint32_t)(w >> 32) : (uint32_t)w;
+    };
+    auto eqw = [&](uint32_t c, int p0) -> uint32_t {
+        const int r = p0 >> 5, s = p0 & 31;
+        const uint32_t lo = half(c, r), hi = half(c, r + 1);
+        return s == 0 ? lo : (lo >> s) | (hi << (32 - s));
+    };
+    const BandGeom bg = band_geom(m, n, k);
+    BandState s = band_start(bg);
+    auto text1 = [&](int j) -> uint32_t { return t[j]; };
+    if (band_steps(k, bg, s, stop < n ? stop : n, text1, eqw)) return k + 1;
+    const BandState saved = s;                          // what the queue item carries
+    BandState r = saved;
+    const uint8_t *rest = t + saved.j;
+    auto text2 = [&](int j) -> uint32_t { return rest[j - saved.j]; };
+    if (band_steps(k, bg, r, n, text2, eqw)) return k + 1;
+    return band_finish(k, bg, r);
+}
+
 extern "C" int blg_host_store(int d, int dtype) {
     if (dtype == DT_UINT8) return (int)saturate_u8(d);
     if (dtype == DT_UINT16) return (int)saturate_u16(d);

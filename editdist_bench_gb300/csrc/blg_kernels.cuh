@@ -607,6 +607,17 @@ __device__ __forceinline__ uint32_t band_row_bits(const uint32_t *row, int p0) {
     return __funnelshift_r(row[P >> 5], row[(P >> 5) + 1], (uint32_t)(P & 31));
 }
 
+// The same window bits from an unpadded [256][nw] u64 Peq row in global
+// memory (row = table + byte * nw): halves p0 >> 5 and the next one, zero
+// outside the row (p0 >= -32 may be negative).
+__device__ __forceinline__ uint32_t peq_window(const uint64_t *row, int nw, int p0) {
+    const uint32_t *h = reinterpret_cast<const uint32_t *>(row);
+    const int r = p0 >> 5;
+    const uint32_t lo = (unsigned)r < (unsigned)(2 * nw) ? __ldg(h + r) : 0u;
+    const uint32_t hi = (unsigned)(r + 1) < (unsigned)(2 * nw) ? __ldg(h + r + 1) : 0u;
+    return __funnelshift_r(lo, hi, (uint32_t)(p0 & 31));
+}
+
 // Stage a [256][nw] u64 Peq table as padded halves (stride 2*nw + 6).
 __device__ __forceinline__ void stage_band_rows(const uint64_t *src, int nw, uint32_t *dst) {
     const int stride = 2 * nw + 6;
@@ -734,16 +745,24 @@ __device__ __forceinline__ int upper_index(const int64_t *pre, int n, int64_t x)
     return a;
 }
 
+// Columns a job runs per survivor when it may defer: unrelated pairs that
+// pass the 4-gram bound leave the band within about 2k + 2 columns.
+__device__ __forceinline__ int defer_columns(int k) { return 4 * (k + 4); }
+
 // Called by all 256 threads of the CTA; `log(sidx, n, cols, gd)` sees every
 // solved survivor (gd: its 4-gram count distance). Survivors whose 4-gram
 // bound already exceeds k are not listed: their output keeps the k+1 fill.
 // With the learned schedule, `keyrow` is the query's key table indexed by
-// (length gap + k, 4-gram count distance 0..8k).
+// (length gap + k, 4-gram count distance 0..8k). With a defer queue, a
+// survivor still inside the band after defer_columns(k) columns is queued
+// with its state (`peq`: the query's [256][nw] table, which the resume pass
+// reads) and not logged.
 template <typename LogFn>
 __device__ __forceinline__ void lpt_job(LptShared &S, const DevStrings &CS, const int32_t *perm, const uint64_t *csk,
                                         const uint4 *ccnt, uint64_t qs, uint4 qc, const uint32_t *rows, int stride,
                                         int m, int64_t row, int64_t s0, int cnt, int k, const uint8_t *keyrow,
-                                        int dtype, void *out, int64_t nc, uint32_t *status, Units u, LogFn log) {
+                                        int dtype, void *out, int64_t nc, const DeferQueue &dq, const uint64_t *peq,
+                                        int nw, uint32_t *status, Units u, LogFn log) {
     constexpr int kPer = kSurvJob / 256;
     const int tid = threadIdx.x, lane = tid & 31;
     S.cnt[tid] = 0;
@@ -802,17 +821,85 @@ __device__ __forceinline__ void lpt_job(LptShared &S, const DevStrings &CS, cons
             const int64_t sidx = s0 + S.list[e];
             int n;
             const uint8_t *tp = string_at(CS, sidx, n, status);
-            int d, cols = 0;
+            int d = 0, cols = 0;
+            bool deferred = false;
             if (m == 0) d = cap_k(n, k);
             else if ((n > m ? n - m : m - n) > k) d = k + 1;
-            else d = band_distance(m, tp, n, k,
-                                   [&](uint32_t ch, int p0) { return band_row_bits(rows + ch * stride, p0); }, u,
-                                   &cols);
-            if (d <= k) store1(out, dtype, row * nc + perm[sidx], d);
-            log(sidx, n, cols, gram_dist(qc, ccnt[sidx]));
+            else {
+                const BandGeom bg = band_geom(m, n, k);
+                BandState bs = band_start(bg);
+                TextScan ts;
+                ts.init(tp);
+                uint32_t w4 = 0;
+                auto text = [&](int j) -> uint32_t {
+                    if ((j & 3) == 0) w4 = ts.next4();
+                    const uint32_t c = w4 & 0xffu;
+                    w4 >>= 8;
+                    return c;
+                };
+                auto eqw = [&](uint32_t ch, int p0) { return band_row_bits(rows + ch * stride, p0); };
+                const int first = dq.items ? min(n, defer_columns(k)) : n;
+                bool exited = band_steps(k, bg, bs, first, text, eqw);
+                if (!exited && first < n) {
+                    const unsigned long long slot = atomicAdd(dq.count, 1ull);
+                    if (slot < (unsigned long long)dq.cap) {
+                        DeferItem it;
+                        it.txt = tp;
+                        it.peq = peq;
+                        it.out = out;
+                        it.oidx = row * nc + perm[sidx];
+                        it.n = n;
+                        it.m = m;
+                        it.A = bs.A;
+                        it.j = bs.j;
+                        it.pv = bs.pv;
+                        it.mv = bs.mv;
+                        it.k = (uint8_t)k;
+                        it.nw = (uint8_t)nw;
+                        it.dtype = (uint8_t)dtype;
+                        dq.items[slot] = it;
+                        deferred = true;                      // the resume pass stores its result
+                    } else {
+                        exited = band_steps(k, bg, bs, n, text, eqw);
+                    }
+                }
+                d = exited ? k + 1 : band_finish(k, bg, bs);
+                cols = bs.j;
+            }
+            if (!deferred) {
+                if (d <= k) store1(out, dtype, row * nc + perm[sidx], d);
+                log(sidx, n, cols, gram_dist(qc, ccnt[sidx]));
+            }
         }
     }
     __syncthreads();
+}
+
+// Finishes the deferred survivors: one thread per item from its saved
+// column state, the pattern's window bits read from its Peq table in global
+// memory; results <= k are stored (the output holds k+1).
+__device__ __forceinline__ void band_resume_item(const DeferItem &it) {
+    const int k = it.k, nw = it.nw;
+    const BandGeom bg = band_geom(it.m, it.n, k);
+    BandState bs;
+    bs.pv = it.pv;
+    bs.mv = it.mv;
+    bs.A = it.A;
+    bs.j = it.j;
+    TextScan ts;
+    ts.init(it.txt + it.j);                                   // it.j is a multiple of 4
+    uint32_t w4 = 0;
+    auto text = [&](int j) -> uint32_t {
+        if ((j & 3) == 0) w4 = ts.next4();
+        const uint32_t c = w4 & 0xffu;
+        w4 >>= 8;
+        return c;
+    };
+    const uint64_t *peq = it.peq;
+    const bool exited = band_steps(k, bg, bs, it.n, text,
+                                   [&](uint32_t ch, int p0) { return peq_window(peq + ch * nw, nw, p0); });
+    const int d = exited ? k + 1 : band_finish(k, bg, bs);
+    if (d <= k) store1(it.out, it.dtype, it.oidx, d);
 }
 
 }  // namespace blg

@@ -15,7 +15,13 @@
 //   2. counting-sorts the job by key in shared memory, most expensive first;
 //   3. lets its warps pull 32-survivor chunks from a shared counter in that
 //      order (longest processing time first), so the expensive pairs start
-//      early and cheap ones fill the gaps.
+//      early and cheap ones fill the gaps;
+//   4. runs each survivor for at most 4 (k + 4) columns: unrelated pairs
+//      leave the band by then, and the rest (near-copies, which run the whole
+//      text, a few per job) are queued with their column state. One resume
+//      launch after all jobs finishes them 32 to a warp; left in their jobs
+//      they would run on a few lanes of one warp while the CTA's other
+//      warps wait for them at the job's last barrier.
 // Only results <= k are written; the output was filled with k+1 before.
 // The job body (lpt_job) is shared with the multi-problem batch kernel.
 #include <cuda_fp16.h>
@@ -79,8 +85,8 @@ __global__ void __launch_bounds__(256) k_search_lpt(DevStrings CS, const int32_t
                                                     SearchClass cls, const int32_t *lo,
                                                     const int32_t *hi, const int64_t *tile_start, int32_t *work,
                                                     const uint8_t *keytab, int64_t keystride, int k, int dtype,
-                                                    void *out, int64_t nc, int jobsz, SurvRows rows, uint32_t *status,
-                                                    uint32_t unit) {
+                                                    void *out, int64_t nc, int jobsz, SurvRows rows, DeferQueue dq,
+                                                    uint32_t *status, uint32_t unit) {
     extern __shared__ uint32_t s_rows[];              // the query's padded Peq halves (banded layout)
     __shared__ LptShared S;
     const Units u{unit, unit + unit};
@@ -103,7 +109,8 @@ __global__ void __launch_bounds__(256) k_search_lpt(DevStrings CS, const int32_t
         const int64_t s0 = lo[qi] + (job - tile_start[qi]) * jobsz;
         const int cnt = (int)min((int64_t)jobsz, (int64_t)hi[qi] - s0);
         lpt_job(S, CS, perm, csk, ccnt, qs, qcnt[row], s_rows, 2 * NW + 6, m, row, s0, cnt, k,
-                keytab ? keytab + qi * keystride : nullptr, dtype, out, nc, status, u,
+                keytab ? keytab + qi * keystride : nullptr, dtype, out, nc, dq, cls.peq + (size_t)qi * 256 * NW, NW,
+                status, u,
                 [&](int64_t sidx, int n, int cols, uint32_t gd) {
                     if (!LOG || m == 0 || n == 0 || (sidx % rows.stride) != 0) return;
                     const int64_t at = atomicAdd((unsigned long long *)rows.count, 1ull);
@@ -121,7 +128,22 @@ __global__ void __launch_bounds__(256) k_search_lpt(DevStrings CS, const int32_t
     }
 }
 
+// The resume pass of the deferred survivors (all query classes of a run, or
+// every banded problem of a batch): a thread per item.
+__global__ void __launch_bounds__(256) k_band_resume(DeferQueue dq) {
+    const unsigned long long claimed = *dq.count;
+    const uint32_t total = claimed < (unsigned long long)dq.cap ? (uint32_t)claimed : (uint32_t)dq.cap;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
+        band_resume_item(dq.items[i]);
+}
+
 // ------------------------------------------------------------- launchers --
+cudaError_t launch_band_resume(cudaStream_t st, int sms, const DeferQueue &dq) {
+    if (!dq.items) return cudaSuccess;
+    k_band_resume<<<sms * 4, 256, 0, st>>>(dq);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S, uint64_t *sketch, uint4 *counts,
                                   uint32_t *status) {
     if (S.n <= 0) return cudaSuccess;
@@ -135,17 +157,18 @@ static cudaError_t launch_lpt_nw(cudaStream_t st, int grid, const DevStrings &CS
                                  const uint64_t *csk, const uint64_t *qsk, const uint4 *ccnt, const uint4 *qcnt,
                                  const SearchClass &cls, const int32_t *lo, const int32_t *hi, const int64_t *tile_start, int32_t *work, const uint8_t *keytab,
                                  int64_t keystride, int k, int dtype, void *out, int64_t nc, int jobsz,
-                                 const SurvRows *rows, uint32_t *status) {
+                                 const SurvRows *rows, const DeferQueue &dq, uint32_t *status) {
     const size_t smem = (size_t)256 * (2 * NW + 6) * sizeof(uint32_t);
     if (rows) {
         cudaFuncSetAttribute(k_search_lpt<NW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_search_lpt<NW, true><<<grid, 256, smem, st>>>(CS, perm, csk, qsk, ccnt, qcnt, cls, lo, hi, tile_start, work, keytab,
-                                                        keystride, k, dtype, out, nc, jobsz, *rows, status, 1u);
+                                                        keystride, k, dtype, out, nc, jobsz, *rows, DeferQueue{},
+                                                        status, 1u);
     } else {
         const SurvRows none{nullptr, nullptr, 0, nullptr, 1};
         cudaFuncSetAttribute(k_search_lpt<NW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_search_lpt<NW, false><<<grid, 256, smem, st>>>(CS, perm, csk, qsk, ccnt, qcnt, cls, lo, hi, tile_start, work, keytab,
-                                                         keystride, k, dtype, out, nc, jobsz, none, status, 1u);
+                                                         keystride, k, dtype, out, nc, jobsz, none, dq, status, 1u);
     }
     return cudaGetLastError();
 }
@@ -155,13 +178,13 @@ cudaError_t launch_search_lpt(cudaStream_t st, int sms, int ctas_per_sm, int job
                               const uint4 *qcnt, const SearchClass &cls, const int32_t *lo, const int32_t *hi,
                               const int64_t *tile_start, int32_t *work,
                               const uint8_t *keytab, int64_t keystride, int k, int dtype, void *out, int64_t nc,
-                              const SurvRows *rows, uint32_t *status) {
+                              const SurvRows *rows, const DeferQueue &dq, uint32_t *status) {
     if (cls.nq <= 0) return cudaSuccess;
     if (k < 0 || k > 31 || jobsz < 256 || jobsz > kSurvJob) return cudaErrorInvalidValue;
     const int grid = sms * std::max(1, std::min(ctas_per_sm, 8));
     switch (nw) {
 #define BLG_LPT(W) \
-    case W: return launch_lpt_nw<W>(st, grid, CS, perm, csk, qsk, ccnt, qcnt, cls, lo, hi, tile_start, work, keytab, keystride, k, dtype, out, nc, jobsz, rows, status);
+    case W: return launch_lpt_nw<W>(st, grid, CS, perm, csk, qsk, ccnt, qcnt, cls, lo, hi, tile_start, work, keytab, keystride, k, dtype, out, nc, jobsz, rows, dq, status);
     BLG_LPT(1) BLG_LPT(2) BLG_LPT(3) BLG_LPT(4) BLG_LPT(5) BLG_LPT(6) BLG_LPT(7) BLG_LPT(8)
 #undef BLG_LPT
     default: return cudaErrorInvalidValue;

@@ -70,6 +70,8 @@ def hostcheck():
                                 ctypes.c_int]
     L.blg_host_band_query.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
     L.blg_host_band_blocks.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
+    L.blg_host_band_resume.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int]
     return L
 
 
@@ -201,6 +203,31 @@ def test_band_matches_oracle(hostcheck, k):
         assert hostcheck.blg_host_band(a, len(a), b, len(b), 0, k) == want
         assert hostcheck.blg_host_band_query(a, len(a), b, len(b), k) == want
         assert hostcheck.blg_host_band_blocks(a, len(a), b, len(b), k) == want
+
+
+@pytest.mark.parametrize("k", [0, 4, 8, 31])
+def test_band_stop_and_resume(hostcheck, k):
+    """The thresholded search defers survivors still inside the band after
+    4 (k + 4) columns: the state saved there and resumed with the window bits
+    read from the unpadded Peq words gives the uninterrupted run's result,
+    at every stop column (before, at and past the text's end)."""
+    rng = random.Random(900 + k)
+    for _ in range(150):
+        m = rng.randrange(0, 300)
+        al = rng.choice([b"ACGT", b"ACGTN", bytes(range(256))])
+        a = bytes(rng.choice(al) for _ in range(m))
+        b = bytearray(a)
+        for _ in range(rng.randrange(0, 2 * k + 3)):
+            i = rng.randrange(len(b) + 1)
+            op = rng.randrange(3)
+            if op == 0 and i < len(b): b[i] = rng.choice(al)
+            elif op == 1: b.insert(i, rng.choice(al))
+            elif i < len(b): del b[i]
+        b = bytes(b)
+        want = _one(a, b, k)
+        assert hostcheck.blg_host_band_query(a, len(a), b, len(b), k) == want
+        for stop in (0, 4, 4 * (k + 4), 64, 4 * (len(b) // 4), len(b) + 4 - len(b) % 4 if len(b) % 4 else len(b)):
+            assert hostcheck.blg_host_band_resume(a, len(a), b, len(b), k, stop) == want, (a, b, k, stop)
 
 
 def _gram_counts(s: bytes) -> np.ndarray:
