@@ -819,8 +819,6 @@ def run_ours(args, ranks: Ranks):
         tune = gpu.autotune(os.path.join(tempfile.gettempdir(), f"blg_tune_{ranks.local}.txt"))
         tune["seconds"] = time.perf_counter() - t0
     gpu.set_schedule(args.schedule)
-    if args.defer_cap is not None:               # deferred banded survivors per run (0: off)
-        ctx.check(ctx.lib.blg_set_defer_capacity(ctx.h, args.defer_cap))
     bench = make_bench(args.config, args)
     p = ctypes.c_void_p()
     ctx.check(ctx.lib.blg_malloc(ctx.h, L2_FLUSH_BYTES, ctypes.byref(p)))
@@ -1058,8 +1056,6 @@ def main():
     ap.add_argument("--schedule", default="auto", choices=["auto", "plain", "learned", "lensort"],
                     help="work order of max_dist runs (results are identical)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
-    ap.add_argument("--defer-cap", type=int, default=None,
-                    help="banded survivors deferred to the resume pass per run (0: off; default 2^20)")
     ap.add_argument("--epochs", type=int, default=10, help="scheduler training epochs (learned)")
     ap.add_argument("--lr", type=float, default=0.02, help="scheduler learning rate (learned)")
     args = ap.parse_args()

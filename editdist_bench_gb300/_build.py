@@ -23,7 +23,7 @@ HOSTCHECK = os.path.join(HERE, "libblg_hostcheck.so")
 PROBE = os.path.join(HERE, "libblg_probe.so")
 
 CU_SOURCES = ["blg_api.cu", "blg_kernels.cu", "blg_noalloc.cu", "blg_pairs_sched.cu", "blg_mlp.cu", "blg_batch.cu",
-              "blg_pairs_tile.cu", "blg_search_lpt.cu", "blg_matches.cu"]
+              "blg_pairs_tile.cu", "blg_search_band.cu", "blg_matches.cu"]
 HEADERS = ["blg_device.cuh", "blg_internal.h", "blg_kernels.cuh", "blg_context.h", "blg_sched.h", "blg_batch.h", "blg_tma.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

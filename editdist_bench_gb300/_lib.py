@@ -69,7 +69,6 @@ SIGNATURES = [
     ("blg_autotune", ctypes.c_int, [_P, ctypes.c_char_p]),
     ("blg_get_tuning", ctypes.c_int, [_P, _P, ctypes.c_int]),
     ("blg_set_fault_injection", ctypes.c_int, [_P, _I64, _I32]),
-    ("blg_set_defer_capacity", ctypes.c_int, [_P, _I32]),
     ("blg_profile_enable", ctypes.c_int, [_P, ctypes.c_int]),
     ("blg_profile_report", ctypes.c_int, [_P, ctypes.c_char_p, _SZ]),
 ]

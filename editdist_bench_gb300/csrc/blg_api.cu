@@ -72,8 +72,6 @@ cudaError_t launch_solve_band(cudaStream_t st, int sms, int ctas_per_sm, const P
 int sched_model_ensure(blg_ctx *c, blg_sched_model **out);
 cudaError_t launch_mlp_keys(cudaStream_t st, int sms, const blg_sched_model *m, const blg::PairsPlan &plan,
                             bool band);
-cudaError_t launch_surv_keytab(cudaStream_t st, int sms, const blg_sched_model *m, const blg::SearchClass &cls, int k,
-                               uint8_t *keytab);
 cudaError_t launch_collect_rows(cudaStream_t st, int sms, const blg::PairsPlan &plan, const int32_t *cols,
                                 int64_t stride, int64_t max_rows, half *x, float *y, int64_t *n_rows);
 int sched_train_rows(blg_ctx *c, blg_sched_model *m, half *x, float *y, const int64_t *d_rows, int64_t rows,
@@ -86,13 +84,11 @@ cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &sr
                                   const int64_t *dst_off, uint8_t *dst, int64_t n, uint32_t *status);
 cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S, uint64_t *sketch, uint4 *counts,
                                   uint32_t *status);
-cudaError_t launch_search_lpt(cudaStream_t st, int sms, int ctas_per_sm, int jobsz, int nw, const DevStrings &CS,
-                              const int32_t *perm, const uint64_t *csk, const uint64_t *qsk, const uint4 *ccnt,
-                              const uint4 *qcnt, const SearchClass &cls, const int32_t *lo, const int32_t *hi,
-                              const int64_t *tile_start, int32_t *work, const uint8_t *keytab, int64_t keystride, int k,
-                              int dtype, void *out, int64_t nc, const SurvRows *rows, const DeferQueue &dq,
-                              uint32_t *status);
-cudaError_t launch_band_resume(cudaStream_t st, int sms, const DeferQueue &dq);
+cudaError_t launch_search_band(cudaStream_t st, int sms, int ctas_per_sm, int jobsz, int ncls,
+                               const SearchClass *cls, const int32_t *const *lo, const int32_t *const *hi,
+                               const int64_t *const *tile_start, int32_t *work, const DevStrings &CS,
+                               const int32_t *perm, const uint4 *ccnt, const uint4 *qcnt, int k, int dtype, void *out,
+                               int64_t nc, const SurvRows *rows, uint32_t *status);
 cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
                              int64_t min_len, int64_t n_len, int k, int tile, int32_t *lo, int32_t *hi,
                              int64_t *tile_start, int32_t *work);
@@ -1210,48 +1206,26 @@ static int pick_qpb(blg_ctx *c, int nw, int nq_cls, int64_t nc) {
 
 // Launch the current classes' kernels; the max_dist fill covers rows [q0, q1)
 // (all rows by default: the classes hold every query).
-// Survivors per job of the thresholded search for one class: the tuned size,
-// halved (down to 1024) while the class would have fewer than 4 jobs per CTA
-// of the persistent grid, so small searches still spread over the GPU. The
+// Survivors per job of the thresholded search: the tuned size, halved
+// (down to 1024) while the run would have fewer than 4 jobs per warp of the
+// persistent grid, so small searches still spread over the GPU. The
 // survivor count comes from the host copies of the length histogram.
-static int survivor_job_size(blg_ctx *c, const blg_search *s, const blg_search::Cls &k_, int k) {
+static int survivor_job_size(blg_ctx *c, const blg_search *s, int k) {
     int64_t total = 0;
     const int64_t nl = s->n_len;
-    for (int32_t m : k_.h_qlen) {
-        int64_t a = m - k - s->min_len, b = m + k - s->min_len + 1;
-        a = std::max<int64_t>(0, std::min(a, nl));
-        b = std::max<int64_t>(0, std::min(b, nl));
-        if (b > a) total += s->h_lstart[b] - s->h_lstart[a];
-    }
-    const int64_t ctas = (int64_t)c->sms * c->tune.lpt_ctas;
-    int job = c->tune.lpt_job;
-    while (job > 1024 && total < 4 * ctas * (int64_t)job) job >>= 1;
-    return job;
-}
-
-// The context's queue of deferred banded survivors (allocated on first use;
-// an allocation failure leaves it off and every survivor finishes in its job).
-static DeferQueue defer_queue(blg_ctx *c) {
-    if (c->defer_cap <= 0) return DeferQueue{};
-    if (!c->defer_items && !c->defer_failed) {
-        void *items = nullptr, *count = nullptr;
-        if (cudaMalloc(&items, sizeof(DeferItem) * (size_t)kDeferCap) != cudaSuccess ||
-            cudaMalloc(&count, sizeof(unsigned long long)) != cudaSuccess) {
-            cudaGetLastError();
-            if (items) cudaFree(items);
-            c->defer_failed = true;
-        } else {
-            c->defer_items = items;
-            c->defer_count = count;
+    for (auto &k_ : s->cls) {
+        if (k_.lanes) continue;
+        for (int32_t m : k_.h_qlen) {
+            int64_t a = m - k - s->min_len, b = m + k - s->min_len + 1;
+            a = std::max<int64_t>(0, std::min(a, nl));
+            b = std::max<int64_t>(0, std::min(b, nl));
+            if (b > a) total += s->h_lstart[b] - s->h_lstart[a];
         }
     }
-    DeferQueue q;
-    if (c->defer_items) {
-        q.items = (DeferItem *)c->defer_items;
-        q.count = (unsigned long long *)c->defer_count;
-        q.cap = std::min(c->defer_cap, kDeferCap);
-    }
-    return q;
+    const int64_t warps = (int64_t)c->sms * c->tune.lpt_ctas * 8;
+    int job = c->tune.lpt_job;
+    while (job > 1024 && total < 4 * warps * (int64_t)job) job >>= 1;
+    return job;
 }
 
 static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, int64_t q0, int64_t q1) {
@@ -1273,53 +1247,30 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
         CK(launch(c, "build_peq", [&] {
                return launch_build_peq(c->stream, s->q.d, k_.qidx, k_.nq, k_.nw, k_.peq, c->d_status);
            }), "build_peq");
-    // survivors still in the band after a few columns leave their jobs for one resume pass
-    DeferQueue dq;
-    bool any_lpt = false;
-    if (surv && k <= 31)
-        for (auto &k_ : s->cls) any_lpt |= !k_.lanes && k_.nq > 0;
-    if (any_lpt) {
-        dq = defer_queue(c);
-        if (dq.items) CK(cudaMemsetAsync(dq.count, 0, sizeof(unsigned long long), c->stream), "reset defer queue");
-    }
+    // max_dist <= 31: the sequential classes' survivors in one launch
+    const bool band = surv && k <= 31;
+    const int band_job = band ? survivor_job_size(c, s, k) : 0;
+    SearchClass bcls[kSurvClasses];
+    const int32_t *blo[kSurvClasses], *bhi[kSurvClasses];
+    const int64_t *bts[kSurvClasses];
+    int32_t *bwork = nullptr;
+    int nb = 0;
     for (auto &k_ : s->cls) {
         SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
         if (surv && !k_.lanes) {
-            // max_dist <= 31: jobs of 4096 survivors ordered by predicted cost
-            const bool lpt = k <= 31;
-            const int job = lpt ? survivor_job_size(c, s, k_, k) : 1024;
+            const int job = band ? band_job : 1024;
             CK(launch(c, "surv_plan", [&] {
                    return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, k, job,
                                            k_.lo, k_.hi, k_.tile_start, k_.work);
                }), "surv_plan");
-            if (lpt) {
-                // survivor keys: the sketch distance (auto), the network's
-                // per-query table (learned), or one table of the length
-                // difference alone, shared by every query (lensort)
-                uint8_t *keytab = nullptr;
-                int64_t keystride = 0;
-                const int E = (2 * k + 1) * (8 * k + 1);   // (length gap, 4-gram count distance)
-                if (c->sched == BLG_SCHED_LEARNED && c->model && sched_model_trained(c->model)) {
-                    CK(dev_alloc(c, (void **)&keytab, (size_t)k_.nq * E), "cudaMallocAsync(keytab)");
-                    keystride = E;
-                    CK(launch(c, "sched_keytab", [&] { return launch_surv_keytab(c->stream, c->sms, c->model, sc, k, keytab); }),
-                       "sched_keytab");
-                } else if (c->sched == BLG_SCHED_LENSORT) {
-                    CK(dev_alloc(c, (void **)&keytab, (size_t)E), "cudaMallocAsync(keytab)");
-                    std::vector<uint8_t> tab((size_t)E);
-                    for (int g = 0; g <= 2 * k; g++)              // g = length gap + k: equal lengths first
-                        for (int d = 0; d <= 8 * k; d++)
-                            tab[(size_t)g * (8 * k + 1) + d] = (uint8_t)(255 - 8 * std::abs(g - k));
-                    CK(cudaMemcpyAsync(keytab, tab.data(), (size_t)E, cudaMemcpyHostToDevice, c->stream), "H2D keytab");
-                    CK(cudaStreamSynchronize(c->stream), "sync keytab");   // the host table is pageable
-                }
-                CK(launch(c, "search_lpt", [&] {
-                       return launch_search_lpt(c->stream, c->sms, c->tune.lpt_ctas, job, k_.nw, s->cs.d,
-                                                s->perm, s->csk, s->qsk, s->ccnt, s->qcnt, sc, k_.lo,
-                                                k_.hi, k_.tile_start, k_.work, keytab, keystride, k, dtype, d_out, s->nc,
-                                                nullptr, dq, c->d_status);
-                   }), "search_lpt");
-                dev_free(c, keytab);
+            if (band) {
+                if (nb == kSurvClasses) return fail(c, BLG_ERR_ARG, "too many query classes");
+                bcls[nb] = sc;
+                blo[nb] = k_.lo;
+                bhi[nb] = k_.hi;
+                bts[nb] = k_.tile_start;
+                if (!bwork) bwork = k_.work;        // cleared by this class's plan
+                nb++;
             } else {
                 CK(launch(c, "search_surv", [&] {
                        return launch_search_surv(c->stream, c->sms, k_.nw, s->cs.d, s->perm, sc, k_.lo, k_.hi,
@@ -1354,7 +1305,12 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
             }
         }
     }
-    if (dq.items) CK(launch(c, "band_resume", [&] { return launch_band_resume(c->stream, c->sms, dq); }), "band_resume");
+    if (nb > 0)
+        CK(launch(c, "search_band", [&] {
+               return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, band_job, nb, bcls, blo, bhi, bts, bwork,
+                                         s->cs.d, s->perm, s->ccnt, s->qcnt, k, dtype, d_out, s->nc, nullptr,
+                                         c->d_status);
+           }), "search_band");
     return BLG_OK;
 }
 
@@ -1581,11 +1537,10 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
 static int batch_run(blg_ctx *c, blg_batch *b) {
     if (!b->exec) {
         const bool prof = c->prof;
-        const DeferQueue dq = defer_queue(c);  // allocated before the capture
         c->prof = false;                      // no per-launch events inside a capture
         const int64_t before = c->launches;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "begin capture");
-        BatchPlan plan{b->d_jobs, b->njobs, b->nbanded, b->d_qprefix, b->d_job_tiles, b->d_tile_base, b->d_work, dq};
+        BatchPlan plan{b->d_jobs, b->njobs, b->nbanded, b->d_qprefix, b->d_job_tiles, b->d_tile_base, b->d_work};
         cudaError_t e = launch_batch(c->stream, c->sms, plan, b->d_fills, b->nfill, b->max_fill, b->total_queries,
                                      c->d_status);
         int rc = e == cudaSuccess ? BLG_OK : cuda_fail(c, e, "batch launch");
@@ -1600,9 +1555,7 @@ static int batch_run(blg_ctx *c, blg_batch *b) {
         if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_fail(c, e, "graph instantiate"); }
         b->graph = g;
         b->graph_kernels = (b->nfill > 0 ? 1 : 0) +
-                           (b->njobs > 0 ? 3 + (b->nbanded > 0 ? (dq.items ? 2 : 1) : 0) +
-                                               (b->nbanded < b->njobs ? 1 : 0)
-                                         : 0) +
+                           (b->njobs > 0 ? 3 + (b->nbanded > 0 ? 1 : 0) + (b->nbanded < b->njobs ? 1 : 0) : 0) +
                            (c->launches - before);
         c->launches = before;
     }
@@ -1927,8 +1880,6 @@ void blg_destroy(blg_ctx *c) {
     sched_model_free(c->model);
     c->model = nullptr;
     if (c->d_status) cudaFree(c->d_status);
-    if (c->defer_items) cudaFree(c->defer_items);
-    if (c->defer_count) cudaFree(c->defer_count);
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
     if (c->stage_done) cudaEventDestroy(c->stage_done);
@@ -2130,21 +2081,30 @@ int blg_sched_train_search(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t 
     CK(cudaMemsetAsync(nrows, 0, sizeof(int64_t), c->stream), "memset");
     SurvRows R{(half *)x, (float *)y, max_rows, (int64_t *)nrows,
                (int)std::min<int64_t>(INT32_MAX, std::max<int64_t>(1, (survivors + max_rows - 1) / max_rows))};
+    const int job = survivor_job_size(c, s, max_dist);
+    SearchClass bcls[kSurvClasses];
+    const int32_t *blo[kSurvClasses], *bhi[kSurvClasses];
+    const int64_t *bts[kSurvClasses];
+    int32_t *bwork = nullptr;
+    int nb = 0;
     for (auto &k_ : s->cls) {
-        if (k_.lanes) continue;
+        if (k_.lanes || nb == kSurvClasses) continue;
         SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
-        const int job = survivor_job_size(c, s, k_, max_dist);
         CK(launch(c, "surv_plan", [&] {
                return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, max_dist, job, k_.lo, k_.hi,
                                        k_.tile_start, k_.work);
            }), "surv_plan");
-        CK(launch(c, "search_lpt_logged", [&] {
-               return launch_search_lpt(c->stream, c->sms, c->tune.lpt_ctas, job, k_.nw, s->cs.d, s->perm,
-                                        s->csk, s->qsk, s->ccnt, s->qcnt, sc, k_.lo, k_.hi,
-                                        k_.tile_start, k_.work, nullptr, 0, max_dist, BLG_UINT8, out, s->nc, &R,
-                                        DeferQueue{}, c->d_status);
-           }), "search_lpt_logged");
+        bcls[nb] = sc;
+        blo[nb] = k_.lo;
+        bhi[nb] = k_.hi;
+        bts[nb] = k_.tile_start;
+        if (!bwork) bwork = k_.work;
+        nb++;
     }
+    CK(launch(c, "search_band_logged", [&] {
+           return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, job, nb, bcls, blo, bhi, bts, bwork, s->cs.d,
+                                     s->perm, s->ccnt, s->qcnt, max_dist, BLG_UINT8, out, s->nc, &R, c->d_status);
+       }), "search_band_logged");
     int64_t rows = 0;
     CK(cudaMemcpyAsync(&rows, nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream), "D2H rows");
     CK(cudaStreamSynchronize(c->stream), "sync");
@@ -2546,13 +2506,6 @@ int blg_set_fault_injection(blg_ctx *c, int64_t alloc_fail_after, int32_t wait_p
     ENTER(c);
     c->fault_alloc_after = alloc_fail_after < 0 ? -1 : alloc_fail_after;
     c->fault_wait_polls = wait_polls < 0 ? -1 : wait_polls;
-    return BLG_OK;
-}
-
-int blg_set_defer_capacity(blg_ctx *c, int32_t cap) {
-    ENTER(c);
-    if (cap < 0) return fail(c, BLG_ERR_ARG, "defer capacity must be >= 0");
-    c->defer_cap = std::min(cap, kDeferCap);
     return BLG_OK;
 }
 

@@ -8,10 +8,9 @@
 //   k_batch_peq     one CTA per (job, query): the query's Peq table
 //   k_batch_plan    one block per job: survivor ranges and tile prefix
 //   k_batch_scan    job tile prefix (the global tile space)
-//   k_batch_lpt     persistent: banded jobs (max_dist <= 31), 4096-survivor
-//                   units run longest-first; survivors still in the band
-//                   after a few columns are queued for
-//   k_band_resume   a thread per queued survivor, from its saved state
+//   k_batch_band    persistent warps: banded jobs (max_dist <= 31), units of
+//                   survivors of one query filtered by the 4-gram bound and
+//                   solved with lanes refilled between rounds (survivor_warp)
 //   k_batch_search  persistent: every CTA pulls (job, query, 1024-survivor)
 //                   tiles from one device counter until the space is done
 // The host captures them once into a CUDA graph and replays it per run.
@@ -20,12 +19,9 @@
 
 namespace blg {
 
-cudaError_t launch_band_resume(cudaStream_t st, int sms, const DeferQueue &dq);
-
-// Peq staging of the persistent kernel: [256][NW] u64, or the banded padded
-// halves [256][2*NW + 6] u32, whichever is larger for NW = kBatchMaxWords.
-constexpr int kBatchSearchSmem = 256 * (2 * kBatchMaxWords + 6) * 4 > 256 * kBatchMaxWords * 8
-                                     ? 256 * (2 * kBatchMaxWords + 6) * 4 : 256 * kBatchMaxWords * 8;
+// Peq staging of the exact / wide-threshold kernel: [256][NW] u64 for NW =
+// kBatchMaxWords.
+constexpr int kBatchSearchSmem = 256 * kBatchMaxWords * 8;
 
 // out[0..n) = v (dtype-sized) by this thread's share (tid of stride).
 __device__ __forceinline__ void fill_share(void *out, int64_t n, int dtype, uint32_t v, int64_t tid,
@@ -119,7 +115,6 @@ __global__ void __launch_bounds__(1024) k_batch_scan(BatchPlan plan) {
         s_carry = 0;
         plan.work[0] = 0;
         plan.work[1] = 0;
-        if (plan.defer.items) *plan.defer.count = 0;
     }
     __syncthreads();
     for (int base = 0; base < plan.njobs; base += 1024) {
@@ -161,35 +156,43 @@ __device__ __forceinline__ void batch_tile(const BatchJob &job, const uint64_t *
     }
 }
 
-// Banded jobs (0 <= k <= 31): persistent CTAs pull (job, query, 4096-survivor)
-// units of the banded part of the tile space and run them longest-first.
-__global__ void __launch_bounds__(256) k_batch_lpt(BatchPlan plan, uint32_t *status, uint32_t unit) {
-    extern __shared__ uint32_t s_rows[];
-    __shared__ LptShared S;
-    const Units u{unit, unit + unit};
+// Banded jobs (0 <= k <= 31): persistent warps pull (job, query, survivor
+// unit) tiles of the banded part of the tile space.
+__global__ void __launch_bounds__(256) k_batch_band(BatchPlan plan, uint32_t *status) {
+    __shared__ SurvJob s_job[8];
+    __shared__ int32_t s_pend[8][kSurvPend];
+    __shared__ uint16_t s_pgd[8][kSurvPend];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t total = plan.tile_base[plan.nbanded];
-    int cur_j = -1, cur_q = -1;
-    while (true) {
-        if (threadIdx.x == 0) S.job = atomicAdd(&plan.work[0], 1);
-        __syncthreads();
-        const int64_t tile = S.job;
-        if (tile >= total) break;
-        const int j = upper_index(plan.tile_base, plan.nbanded, tile);
-        const BatchJob &job = plan.jobs[j];
-        const int64_t lt = tile - plan.tile_base[j];
-        const int qi = upper_index(job.tile_start, job.cls.nq, lt);
-        if (j != cur_j || qi != cur_q) {
-            stage_band_rows(job.cls.peq + (size_t)qi * 256 * job.nw, job.nw, s_rows);
-            cur_j = j;
-            cur_q = qi;
+    auto next_job = [&](SurvJob &J) -> bool {
+        int64_t tile = 0;
+        if (lane == 0) tile = atomicAdd(&plan.work[0], 1);
+        tile = __shfl_sync(kFull, tile, 0);
+        if (tile >= total) return false;
+        if (lane == 0) {
+            const int j = upper_index(plan.tile_base, plan.nbanded, tile);
+            const BatchJob &job = plan.jobs[j];
+            const int64_t lt = tile - plan.tile_base[j];
+            const int qi = upper_index(job.tile_start, job.cls.nq, lt);
+            const int64_t row = job.cls.qidx[qi];
+            J.CS = job.CS;
+            J.perm = job.perm;
+            J.ccnt = job.ccnt;
+            J.peq = job.cls.peq + (size_t)qi * 256 * job.nw;
+            J.out = job.out;
+            J.row = row;
+            J.nc = job.nc;
+            J.s = job.lo[qi] + (lt - job.tile_start[qi]) * job.tile;
+            J.s1 = min(J.s + job.tile, (int64_t)job.hi[qi]);
+            J.qc = job.qcnt[row];
+            J.m = job.cls.qlen[qi];
+            J.nw = job.nw;
+            J.k = job.k;
+            J.dtype = job.dtype;
         }
-        const int64_t row = job.cls.qidx[qi];
-        const int64_t s0 = job.lo[qi] + (lt - job.tile_start[qi]) * job.tile;
-        const int cnt = (int)min((int64_t)job.tile, (int64_t)job.hi[qi] - s0);
-        lpt_job(S, job.CS, job.perm, job.csk, job.ccnt, job.qsk[row], job.qcnt[row], s_rows, 2 * job.nw + 6,
-                job.cls.qlen[qi], row, s0, cnt, job.k, nullptr, job.dtype, job.out, job.nc, plan.defer,
-                job.cls.peq + (size_t)qi * 256 * job.nw, job.nw, status, u, [](int64_t, int, int, uint32_t) {});
-    }
+        return true;
+    };
+    survivor_warp(s_job[w], next_job, s_pend[w], s_pgd[w], status, [](int64_t, int, int, int, uint32_t) {});
 }
 
 // The other jobs (exact, or max_dist > 31): 1024-choice tiles, 4 per thread.
@@ -232,8 +235,6 @@ cudaError_t batch_set_attributes() {
                                          256 * kBatchMaxWords * 8);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_batch_search, cudaFuncAttributeMaxDynamicSharedMemorySize, kBatchSearchSmem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch_lpt, cudaFuncAttributeMaxDynamicSharedMemorySize, kBatchSearchSmem);
     return e;
 }
 
@@ -250,13 +251,7 @@ cudaError_t launch_batch(cudaStream_t st, int sms, const BatchPlan &plan, const 
         k_batch_peq<<<(unsigned)total_queries, 256, 256 * kBatchMaxWords * 8, st>>>(plan, status);
         k_batch_plan<<<plan.njobs, 1024, 0, st>>>(plan);
         k_batch_scan<<<1, 1024, 0, st>>>(plan);
-        if (plan.nbanded > 0) {
-            k_batch_lpt<<<sms * 4, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
-            if (plan.defer.items) {
-                const cudaError_t e = launch_band_resume(st, sms, plan.defer);
-                if (e != cudaSuccess) return e;
-            }
-        }
+        if (plan.nbanded > 0) k_batch_band<<<sms * 4, 256, 0, st>>>(plan, status);
         if (plan.nbanded < plan.njobs) k_batch_search<<<sms * 3, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
     }
     return cudaGetLastError();

@@ -21,7 +21,7 @@ struct BatchJob {
     int64_t *tile_start;       // tile prefix per query (nq + 1)
     int64_t nc;
     int k, dtype, nw;
-    int tile;                  // survivors per work unit: 4096 (banded, longest-first jobs) or 1024
+    int tile;                  // survivors per work unit: 4096 (banded survivor jobs) or 1024
     const uint64_t *csk;       // 4-gram sketches of the sorted choices
     const uint64_t *qsk;       // 4-gram sketches of the queries (by query row)
     const uint4 *ccnt;         // binned 4-gram counts of the sorted choices
@@ -39,12 +39,11 @@ struct BatchFill {
 struct BatchPlan {
     const BatchJob *jobs;      // device array; banded jobs (0 <= k <= 31) first
     int njobs;
-    int nbanded;               // jobs [0, nbanded) run as longest-first jobs (k_batch_lpt)
+    int nbanded;               // jobs [0, nbanded) run in the banded survivor kernel (k_batch_band)
     const int64_t *q_prefix;   // [njobs + 1] queries before each job (Peq build CTAs)
     int64_t *job_tiles;        // [njobs]
     int64_t *tile_base;        // [njobs + 1]
     int32_t *work;             // persistent-kernel counters: [0] banded jobs, [1] the others
-    DeferQueue defer;          // banded survivors left for the resume pass (items null: none)
 };
 
 cudaError_t batch_set_attributes();

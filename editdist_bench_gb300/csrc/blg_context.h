@@ -47,12 +47,6 @@ struct blg_ctx {
     int32_t fault_wait_polls = -1;
     // pinned host staging for arrays the host builds and copies (grown on
     // demand; stage_done marks the end of the last copy out of it)
-    // the queue of banded survivors deferred by the thresholded-search jobs
-    // (blg::DeferQueue; allocated on first use, never if that failed once)
-    void *defer_items = nullptr;
-    void *defer_count = nullptr;
-    bool defer_failed = false;
-    int32_t defer_cap = 1 << 20;      // items per run (blg_set_defer_capacity; 0: off)
     void *stage = nullptr;
     size_t stage_bytes = 0;
     cudaEvent_t stage_done = nullptr;

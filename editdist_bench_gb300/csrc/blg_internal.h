@@ -98,31 +98,9 @@ struct PrefixChoices {
     int ck[kPfxCheckpoints] = {0, 0};
 };
 
-// Banded survivors deferred by the thresholded-search jobs. A job runs every
-// listed survivor for a few columns only; the ones still inside the band
-// then (mostly near-copies of the query, which run the whole text) are
-// queued with their column state and finished by one resume pass, where
-// they fill whole warps instead of holding one job's warp while the rest
-// of its CTA waits. A full queue makes the job finish the survivor itself.
-struct DeferItem {
-    const uint8_t *txt;      // the choice (text), from byte 0
-    const uint64_t *peq;     // the query's Peq table [256][nw]
-    void *out;               // output base
-    int64_t oidx;            // output element
-    int32_t n, m;            // text and pattern lengths
-    int32_t A, j;            // BandState: D' of the window's top row, next column
-    uint32_t pv, mv;         // BandState: vertical deltas
-    uint8_t k, nw, dtype, pad[5];
-};
-static_assert(sizeof(DeferItem) == 64, "one item per 64-byte line");
-
-constexpr int32_t kDeferCap = 1 << 20;
-
-struct DeferQueue {
-    DeferItem *items = nullptr;   // null: no deferral (every survivor finishes in its job)
-    unsigned long long *count = nullptr;   // items claimed (may exceed cap; claims past cap are not written)
-    int32_t cap = 0;
-};
+// Query word classes of the sequential search kernels (patterns of 1..8
+// 64-bit words); longer queries run lane-spread.
+constexpr int kSurvClasses = 8;
 
 // Per-query-class search launch description.
 struct SearchClass {

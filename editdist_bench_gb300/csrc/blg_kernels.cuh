@@ -717,22 +717,34 @@ __device__ __forceinline__ uint32_t gram_dist(uint4 a, uint4 b) {
     return __vsadu4(a.x, b.x) + __vsadu4(a.y, b.y) + __vsadu4(a.z, b.z) + __vsadu4(a.w, b.w);
 }
 
-// ---------------------------------- thresholded search: longest-first jobs --
-// A job is up to kSurvJob survivors (choices within max_dist k <= 31 in length)
-// of one query, whose banded Peq rows are in shared memory. Every survivor
-// gets a predicted-cost key (the query/choice sketch distance, or a row of the
-// learned scheduler's key table indexed by (length gap, sketch distance)),
-// the job is counting-sorted by key in shared memory, most expensive first,
-// and warps pull 32-survivor chunks in that order from a shared counter.
-// Results <= k are stored (the output holds k+1 already).
-constexpr int kSurvJob = 4096;
+// -------------------------------- thresholded search: filter and band solve --
+// The survivors of a query (choices within max_dist k <= 31 of its length, a
+// contiguous range of the length-sorted choices) go through the 4-gram count
+// bound, and the ones it does not rule out through the banded loop, one lane
+// per survivor. Their costs differ by two orders of magnitude: most leave
+// the band within 2k + 2 columns, near-copies of the query run the whole
+// text. So warps run without CTA barriers and their lanes advance in rounds
+// of kSurvRound columns; between rounds the warp hands the passers it has
+// found to the lanes whose survivor finished, scanning further survivors
+// (128 per step, four independent count loads per lane) while lanes are
+// free. The window bits come from the query's Peq table in global memory
+// (L1-resident while a warp works on the query). Results <= k are stored
+// (the output holds k+1 already).
+constexpr int kSurvRound = 32;         // text columns per round
+constexpr int kSurvPend = 128;         // passers one scan step can buffer
 
-struct LptShared {
-    uint16_t list[kSurvJob];
-    int cnt[256], start[256];
-    int64_t job;
-    int next;
-    int listed;            // survivors that passed the 4-gram bound
+// One query's survivor range, read by all lanes of a warp (kept in shared
+// memory: warp-uniform values that would otherwise take registers).
+struct SurvJob {
+    DevStrings CS;                     // the problem's length-sorted choices
+    const int32_t *perm;               // sorted -> original choice index
+    const uint4 *ccnt;                 // binned 4-gram counts of the sorted choices
+    const uint64_t *peq;               // the query's Peq table [256][nw]
+    void *out;
+    int64_t row, nc;                   // the query's output row, row length
+    int64_t s, s1;                     // next and end survivor (sorted choice index)
+    uint4 qc;                          // the query's binned 4-gram counts
+    int m, nw, k, dtype;
 };
 
 // largest j in [0, n) with pre[j] <= x (pre non-decreasing, pre[0] <= x)
@@ -745,161 +757,134 @@ __device__ __forceinline__ int upper_index(const int64_t *pre, int n, int64_t x)
     return a;
 }
 
-// Columns a job runs per survivor when it may defer: unrelated pairs that
-// pass the 4-gram bound leave the band within about 2k + 2 columns.
-__device__ __forceinline__ int defer_columns(int k) { return 4 * (k + 4); }
-
-// Called by all 256 threads of the CTA; `log(sidx, n, cols, gd)` sees every
-// solved survivor (gd: its 4-gram count distance). Survivors whose 4-gram
-// bound already exceeds k are not listed: their output keeps the k+1 fill.
-// With the learned schedule, `keyrow` is the query's key table indexed by
-// (length gap + k, 4-gram count distance 0..8k). With a defer queue, a
-// survivor still inside the band after defer_columns(k) columns is queued
-// with its state (`peq`: the query's [256][nw] table, which the resume pass
-// reads) and not logged.
-template <typename LogFn>
-__device__ __forceinline__ void lpt_job(LptShared &S, const DevStrings &CS, const int32_t *perm, const uint64_t *csk,
-                                        const uint4 *ccnt, uint64_t qs, uint4 qc, const uint32_t *rows, int stride,
-                                        int m, int64_t row, int64_t s0, int cnt, int k, const uint8_t *keyrow,
-                                        int dtype, void *out, int64_t nc, const DeferQueue &dq, const uint64_t *peq,
-                                        int nw, uint32_t *status, Units u, LogFn log) {
-    constexpr int kPer = kSurvJob / 256;
-    const int tid = threadIdx.x, lane = tid & 31;
-    S.cnt[tid] = 0;
-    if (tid == 0) S.next = 0;
-    __syncthreads();
-    int key[kPer], rank[kPer];
-    const uint32_t gmax = 8u * (uint32_t)k;
-#pragma unroll
-    for (int r = 0; r < kPer; r++) {
-        const int l = tid + 256 * r;
-        key[r] = -1;
-        if (l < cnt) {
-            const int64_t sidx = s0 + l;
-            const uint32_t gd = gram_dist(qc, ccnt[sidx]);
-            if (gd <= gmax) {                                 // else the bound alone proves d > k
-                if (keyrow) {
-                    int g = (int)(CS.off[sidx + 1] - CS.off[sidx]) - m + k;
-                    g = g < 0 ? 0 : (g > 2 * k ? 2 * k : g);
-                    key[r] = keyrow[g * (8 * k + 1) + (gd > gmax ? gmax : gd)];
-                } else {
-                    key[r] = kSketchWindow - __popcll(qs ^ csk[sidx]);   // near-copies (low distance) run longest
-                }
-                rank[r] = atomicAdd(&S.cnt[key[r]], 1);
-            }
-        }
-    }
-    __syncthreads();
-    if (tid < 32) {                                           // bucket starts, largest key first
-        int v[8], sum = 0;
-#pragma unroll
-        for (int q = 0; q < 8; q++) { v[q] = S.cnt[255 - (tid * 8 + q)]; sum += v[q]; }
-        int incl = sum;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int x = __shfl_up_sync(kFull, incl, o);
-            if (tid >= o) incl += x;
-        }
-        int run = incl - sum;
-#pragma unroll
-        for (int q = 0; q < 8; q++) { S.start[255 - (tid * 8 + q)] = run; run += v[q]; }
-        if (tid == 31) S.listed = incl;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < kPer; r++)
-        if (key[r] >= 0) S.list[S.start[key[r]] + rank[r]] = (uint16_t)(tid + 256 * r);
-    __syncthreads();
-    const int listed = S.listed;
+// Called by every lane of a warp. next_job(J) fills the warp's job (every
+// lane calls it; lane 0 writes J) and returns false when none is left.
+// s_pend: the warp's kSurvPend passer slots (sorted choice index), s_pgd
+// their 4-gram count distances. log(sidx, m, n, cols, gd) sees every
+// survivor the banded loop finished.
+template <typename NextJob, typename LogFn>
+__device__ __forceinline__ void survivor_warp(SurvJob &J, NextJob next_job, int32_t *s_pend, uint16_t *s_pgd,
+                                              uint32_t *status, LogFn log) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    bool have_job = false, jobs_done = false;
+    int pend = 0;                                          // warp-uniform
+    // this lane's survivor
+    bool busy = false;
+    TextScan ts{};
+    uint32_t w4 = 0;
+    const uint64_t *peq = nullptr;
+    void *out = nullptr;
+    int64_t oidx = 0;
+    int n = 0, m = 0, nw = 1, k = 0, dtype = 0, sidx = 0;
+    uint32_t gd = 0;
+    BandGeom bg{};
+    BandState bs{};
     while (true) {
-        int c = 0;
-        if (lane == 0) c = atomicAdd(&S.next, 1);
-        c = __shfl_sync(kFull, c, 0);
-        if (c * 32 >= listed) break;
-        const int e = c * 32 + lane;
-        if (e < listed) {
-            const int64_t sidx = s0 + S.list[e];
-            int n;
-            const uint8_t *tp = string_at(CS, sidx, n, status);
-            int d = 0, cols = 0;
-            bool deferred = false;
-            if (m == 0) d = cap_k(n, k);
-            else if ((n > m ? n - m : m - n) > k) d = k + 1;
-            else {
-                const BandGeom bg = band_geom(m, n, k);
-                BandState bs = band_start(bg);
-                TextScan ts;
-                ts.init(tp);
-                uint32_t w4 = 0;
-                auto text = [&](int j) -> uint32_t {
-                    if ((j & 3) == 0) w4 = ts.next4();
-                    const uint32_t c = w4 & 0xffu;
-                    w4 >>= 8;
-                    return c;
-                };
-                auto eqw = [&](uint32_t ch, int p0) { return band_row_bits(rows + ch * stride, p0); };
-                const int first = dq.items ? min(n, defer_columns(k)) : n;
-                bool exited = band_steps(k, bg, bs, first, text, eqw);
-                if (!exited && first < n) {
-                    const unsigned long long slot = atomicAdd(dq.count, 1ull);
-                    if (slot < (unsigned long long)dq.cap) {
-                        DeferItem it;
-                        it.txt = tp;
-                        it.peq = peq;
-                        it.out = out;
-                        it.oidx = row * nc + perm[sidx];
-                        it.n = n;
-                        it.m = m;
-                        it.A = bs.A;
-                        it.j = bs.j;
-                        it.pv = bs.pv;
-                        it.mv = bs.mv;
-                        it.k = (uint8_t)k;
-                        it.nw = (uint8_t)nw;
-                        it.dtype = (uint8_t)dtype;
-                        dq.items[slot] = it;
-                        deferred = true;                      // the resume pass stores its result
-                    } else {
-                        exited = band_steps(k, bg, bs, n, text, eqw);
+        unsigned freem = __ballot_sync(kFull, !busy);
+        while (freem) {
+            if (pend == 0) {
+                if (!have_job || J.s >= J.s1) {
+                    if (jobs_done) break;
+                    have_job = next_job(J);
+                    __syncwarp();
+                    if (!have_job) {
+                        jobs_done = true;
+                        break;
+                    }
+                    if (J.m == 0) {                        // empty query: d = n for every survivor
+                        for (int64_t x = J.s + lane; x < J.s1; x += 32) {
+                            int nn;
+                            string_at(J.CS, x, nn, status);
+                            store1(J.out, J.dtype, J.row * J.nc + J.perm[x], cap_k(nn, J.k));
+                        }
+                        __syncwarp();
+                        if (lane == 0) J.s = J.s1;
+                        __syncwarp();
+                        continue;
                     }
                 }
-                d = exited ? k + 1 : band_finish(k, bg, bs);
-                cols = bs.j;
+                // scan 128 survivors: four independent count loads per lane
+                const int64_t base = J.s, s1 = J.s1;
+                const uint4 qc = J.qc;
+                const uint32_t gmax = 8u * (uint32_t)J.k;
+                uint4 c[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int64_t x = base + i * 32 + lane;
+                    c[i] = x < s1 ? __ldg(J.ccnt + x) : make_uint4(0, 0, 0, 0);
+                }
+                uint32_t g[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) g[i] = base + i * 32 + lane < s1 ? gram_dist(qc, c[i]) : 0xffffffffu;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const bool pass = g[i] <= gmax;        // else the bound alone proves d > k
+                    const unsigned pm = __ballot_sync(kFull, pass);
+                    if (pass) {
+                        const int at = pend + __popc(pm & lt);
+                        s_pend[at] = (int32_t)(base + i * 32 + lane);
+                        s_pgd[at] = (uint16_t)g[i];
+                    }
+                    pend += __popc(pm);
+                }
+                __syncwarp();
+                if (lane == 0) J.s = base + 4 * 32;
+                __syncwarp();
+                continue;
             }
-            if (!deferred) {
-                if (d <= k) store1(out, dtype, row * nc + perm[sidx], d);
-                log(sidx, n, cols, gram_dist(qc, ccnt[sidx]));
+            // hand buffered passers to free lanes, from the end of the buffer
+            const int take = min(pend, __popc(freem));
+            const int r = __popc(freem & lt);
+            if (!busy && r < take) {
+                const int e = pend - take + r;
+                sidx = s_pend[e];
+                gd = s_pgd[e];
+                const uint8_t *t = string_at(J.CS, sidx, n, status);
+                m = J.m;
+                k = J.k;
+                dtype = J.dtype;
+                out = J.out;
+                peq = J.peq;
+                nw = J.nw;
+                oidx = J.row * J.nc + J.perm[sidx];
+                if ((n > m ? n - m : m - n) > k) {
+                    // outside the length window: the output keeps its k+1
+                } else {
+                    bg = band_geom(m, n, k);
+                    bs = band_start(bg);
+                    ts.init(t);
+                    w4 = 0;
+                    busy = true;
+                }
+            }
+            pend -= take;
+            __syncwarp();
+            freem = __ballot_sync(kFull, !busy);
+        }
+        if (!__any_sync(kFull, busy)) {
+            if (jobs_done && pend == 0) break;
+            continue;
+        }
+        if (busy) {
+            auto text = [&](int j) -> uint32_t {
+                if ((j & 3) == 0) w4 = ts.next4();
+                const uint32_t c = w4 & 0xffu;
+                w4 >>= 8;
+                return c;
+            };
+            const uint64_t *pq = peq;
+            const int nwl = nw;
+            auto eqw = [&](uint32_t c, int p0) { return peq_window(pq + c * nwl, nwl, p0); };
+            const bool exited = band_steps(k, bg, bs, min(n, bs.j + kSurvRound), text, eqw);
+            if (exited || bs.j == n) {
+                const int d = exited ? k + 1 : band_finish(k, bg, bs);
+                if (d <= k) store1(out, dtype, oidx, d);
+                log((int64_t)sidx, m, n, bs.j, gd);
+                busy = false;
             }
         }
     }
-    __syncthreads();
-}
-
-// Finishes the deferred survivors: one thread per item from its saved
-// column state, the pattern's window bits read from its Peq table in global
-// memory; results <= k are stored (the output holds k+1).
-__device__ __forceinline__ void band_resume_item(const DeferItem &it) {
-    const int k = it.k, nw = it.nw;
-    const BandGeom bg = band_geom(it.m, it.n, k);
-    BandState bs;
-    bs.pv = it.pv;
-    bs.mv = it.mv;
-    bs.A = it.A;
-    bs.j = it.j;
-    TextScan ts;
-    ts.init(it.txt + it.j);                                   // it.j is a multiple of 4
-    uint32_t w4 = 0;
-    auto text = [&](int j) -> uint32_t {
-        if ((j & 3) == 0) w4 = ts.next4();
-        const uint32_t c = w4 & 0xffu;
-        w4 >>= 8;
-        return c;
-    };
-    const uint64_t *peq = it.peq;
-    const bool exited = band_steps(k, bg, bs, it.n, text,
-                                   [&](uint32_t ch, int p0) { return peq_window(peq + ch * nw, nw, p0); });
-    const int d = exited ? k + 1 : band_finish(k, bg, bs);
-    if (d <= k) store1(it.out, it.dtype, it.oidx, d);
 }
 
 }  // namespace blg

@@ -274,50 +274,6 @@ __global__ void __launch_bounds__(256) k_mlp_keys(const half *w16, PairsPlan pla
     }
 }
 
-// Survivor key table of a thresholded search: for every query of the class
-// and every (length gap g = n - m + k in 0..2k, 4-gram count distance gd in
-// 0..8k: survivors with a larger one are filtered out before) the network's
-// predicted work, as a cost bucket. The search's features are (m, n, m, n,
-// n - m, gd / 8 = the 4-gram count lower bound, k): the query is the pattern
-// whatever its length, with no trimming. One CTA per query, two table
-// entries per thread.
-__device__ __forceinline__ void search_features(int m, int n, int gd, int k, float (&x)[8]) {
-    x[0] = (float)m * (1.f / 256.f);
-    x[1] = (float)n * (1.f / 256.f);
-    x[2] = x[0];
-    x[3] = x[1];
-    x[4] = (float)(n - m) * (1.f / 16.f);
-    x[5] = (float)gd * (1.f / 128.f);
-    x[6] = (float)k * (1.f / 16.f);
-    x[7] = 1.f;
-}
-
-__device__ __forceinline__ uint8_t work_bucket(float y, int n) {
-    y = y < 0.f ? 0.f : (y > 1.f ? 1.f : y);
-    const int b = (int)(__log2f(y * (float)n + 16.f) * 8.f) + 1;
-    return (uint8_t)(b < 0 ? 0 : (b > kCostBuckets - 1 ? kCostBuckets - 1 : b));
-}
-
-__global__ void __launch_bounds__(256) k_surv_keytab(const half *w16, SearchClass cls, int k, uint8_t *keytab) {
-    __shared__ __align__(16) float w[kInfFloats];
-    load_inference_weights(w16, w);
-    __syncthreads();
-    const int D = 8 * k + 1, E = (2 * k + 1) * D;
-    for (int qi = blockIdx.x; qi < cls.nq; qi += gridDim.x) {
-        const int m = cls.qlen[qi];
-        for (int e0 = threadIdx.x; e0 < E; e0 += 2 * blockDim.x) {
-            const int e1 = e0 + blockDim.x;
-            const int n0 = m - k + e0 / D, n1 = m - k + e1 / D;
-            float x0[8], x1[8], y0, y1;
-            search_features(m, n0 < 0 ? 0 : n0, e0 % D, k, x0);
-            search_features(m, n1 < 0 ? 0 : n1, e1 % D, k, x1);
-            mlp_forward2(w, x0, x1, y0, y1);
-            keytab[(size_t)qi * E + e0] = n0 <= 0 ? 0 : work_bucket(y0, n0);
-            if (e1 < E) keytab[(size_t)qi * E + e1] = n1 <= 0 ? 0 : work_bucket(y1, n1);
-        }
-    }
-}
-
 // Predictions for given rows (diagnostics and tests).
 __global__ void __launch_bounds__(256) k_mlp_predict(const half *w16, const half *x, int64_t rows, float *out) {
     __shared__ float w[kParams];
@@ -403,13 +359,6 @@ static int set_weights(blg_ctx *c, blg_sched_model *m, const std::vector<float> 
 // Host-side pieces the runtime (blg_api.cu) calls.
 cudaError_t launch_mlp_keys(cudaStream_t st, int sms, const blg_sched_model *m, const PairsPlan &plan, bool band) {
     k_mlp_keys<<<sms * 4, 256, 0, st>>>(m->w16, plan, band ? 1 : 0);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_surv_keytab(cudaStream_t st, int sms, const blg_sched_model *m, const SearchClass &cls, int k,
-                               uint8_t *keytab) {
-    if (cls.nq <= 0) return cudaSuccess;
-    k_surv_keytab<<<std::min(cls.nq, sms * 8), 256, 0, st>>>(m->w16, cls, k, keytab);
     return cudaGetLastError();
 }
 

@@ -269,16 +269,6 @@ int blg_synchronize(blg_ctx *ctx);
  * Nothing here faults, traps or hangs the GPU; the context stays usable. */
 int blg_set_fault_injection(blg_ctx *ctx, int64_t alloc_fail_after, int32_t wait_polls);
 
-/* Deferral of long banded survivors in thresholded searches (max_dist <= 31,
- * the longest-first survivor kernels and the multi-problem batch): a job
- * runs each survivor for 4 (max_dist + 4) columns, queues the ones still
- * inside the band with their column state, and one resume launch finishes
- * them, 32 to a warp. `cap` bounds the queue per run (at most 2^20, the
- * default); survivors past it finish inside their jobs; 0 turns deferral
- * off. Results never depend on it, only time. A batch's captured graph keeps
- * the setting it was captured with. No counterpart in the reference. */
-int blg_set_defer_capacity(blg_ctx *ctx, int32_t cap);
-
 /* Timing on the context's stream with CUDA events (ms between start/stop). */
 int blg_timer_start(blg_ctx *ctx);
 int blg_timer_stop(blg_ctx *ctx, float *ms);

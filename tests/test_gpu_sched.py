@@ -167,29 +167,14 @@ def test_trained_network_order_against_no_network(gpu):
     assert t["learned"] * 1.1 < t["no network"]
 
 
-def _lpt_ms(ctx, s, out, k, runs=3):
-    buf = ctypes.create_string_buffer(8192)
-    s.run(out, max_dist=k)
-    ctx.check(ctx.lib.blg_synchronize(ctx.h))
-    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 1))
-    for _ in range(runs):
-        s.run(out, max_dist=k)
-    ctx.check(ctx.lib.blg_profile_report(ctx.h, buf, 8192))
-    ctx.check(ctx.lib.blg_profile_enable(ctx.h, 0))
-    rows = dict((l.split()[0], float(l.split()[2])) for l in buf.value.decode().splitlines())
-    return rows["search_lpt"] / runs
-
-
-def test_learned_search_order_gain_and_exactness(gpu):
+def test_search_training_and_schedules_exact(gpu):
     """Thresholded search (lengths 100..256, 5% planted near-copies, k = 4):
-    the network trained on the survivor kernel's own logged rows orders each
-    job longest-predicted-first. Results equal the oracle under every order.
-    The survivor kernel first drops every survivor whose 4-gram count bound
-    exceeds k (exact: the bound never exceeds the distance); what remains is
-    mostly the planted near-copies, which all run long, so no order has much
-    left to gain. The times of the learned order, the automatic (sketch
-    distance) order, lensort and no network are printed, and the learned
-    order must cost no more than 25% over the best of them."""
+    the network trains on the survivor kernel's own logged rows (features and
+    exit columns), and every schedule -- the learned one with the trained
+    and with a zero network, auto, lensort -- gives the oracle's results.
+    The search itself has no work order left to choose (its warps hand each
+    lane the next filtered survivor as the last one finishes), so the
+    schedules run the same kernel."""
     ctx = _lib.context()
     tr = W.config4(nq=32, nc=1 << 17, seed=2004)
     ts = gpu.SearchBatch(tr.q, tr.c)
@@ -198,28 +183,23 @@ def test_learned_search_order_gain_and_exactness(gpu):
     assert np.isfinite(loss.value)
     trained = np.empty(P, dtype=np.float32)
     ctx.check(ctx.lib.blg_sched_get_weights(ctx.h, trained.ctypes.data, P))
+    assert np.abs(trained).sum() > 0
     w = W.config4(nq=128, nc=1 << 17, seed=1004)
     s = gpu.SearchBatch(w.q, w.c)
-    out = s.alloc("uint8")
     rows = [0, 1, 63, 127]
     want = oracle.saturate(oracle.cross(W.take(w.q, rows), w.c, 4, threads=8), "uint8")
-    t, got = {}, {}
+    got = {}
     try:
         gpu.set_schedule("learned")
-        t["learned"] = _lpt_ms(ctx, s, out, 4)
-        got["learned"] = out.get()
+        got["learned"] = s.run(s.alloc("uint8"), max_dist=4).get()
         _set(ctx, np.zeros(P, dtype=np.float32))
-        t["no network"] = _lpt_ms(ctx, s, out, 4)
-        got["no network"] = out.get()
+        got["no network"] = s.run(s.alloc("uint8"), max_dist=4).get()
         _set(ctx, trained)
         for sched in ("auto", "lensort"):
             gpu.set_schedule(sched)
-            t[sched] = _lpt_ms(ctx, s, out, 4)
-            got[sched] = out.get()
+            got[sched] = s.run(s.alloc("uint8"), max_dist=4).get()
     finally:
         gpu.set_schedule("auto")
     np.testing.assert_array_equal(got["learned"][rows], want)
     for name in got:
         np.testing.assert_array_equal(got[name], got["learned"], err_msg=name)
-    print("survivor kernel (ms): " + ", ".join(f"{k} {v:.3f}" for k, v in t.items()))
-    assert t["learned"] <= 1.25 * min(t.values())
