@@ -84,14 +84,11 @@ cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &sr
                                   const int64_t *dst_off, uint8_t *dst, int64_t n, uint32_t *status);
 cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S, uint64_t *sketch, uint4 *counts,
                                   uint32_t *status);
-cudaError_t launch_search_band(cudaStream_t st, int sms, int ctas_per_sm, int jobsz, int ncls,
-                               const SearchClass *cls, const int32_t *const *lo, const int32_t *const *hi,
-                               const int64_t *const *tile_start, int32_t *work, const DevStrings &CS,
-                               const int32_t *perm, const uint4 *ccnt, const uint4 *qcnt, int k, int dtype, void *out,
-                               int64_t nc, const SurvRows *rows, uint32_t *status);
-cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
-                             int64_t min_len, int64_t n_len, int k, int tile, int32_t *lo, int32_t *hi,
-                             int64_t *tile_start, int32_t *work);
+cudaError_t launch_search_band(cudaStream_t st, int sms, int ctas_per_sm, int round, int jobsz, const SurvClasses &C,
+                               const DevStrings &CS, const int32_t *perm, const uint4 *ccnt, const uint4 *qcnt, int k,
+                               int dtype, void *out, int64_t nc, const SurvRows *rows, uint32_t *status);
+cudaError_t launch_surv_plan(cudaStream_t st, const SurvClasses &C, const int64_t *lstart, int64_t min_len,
+                             int64_t n_len, int k, int tile);
 cudaError_t launch_search_surv(cudaStream_t st, int sms, int nw, const DevStrings &CS, const int32_t *perm,
                                const SearchClass &cls, const int32_t *lo, const int32_t *hi,
                                const int64_t *tile_start, int32_t *work, int k, int dtype, void *out,
@@ -549,14 +546,15 @@ static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, const DevStrings &A, co
     CK(launch(c, "pairs_order", [&] { return launch_order(c->stream, c->sms, plan); }), "pairs_order");
     bool any_long = false;
     for (int j = 1; j < kPairClasses; j++) any_long |= p->pcap[j] > 0;
-    if (band)
+    if (band) {
         CK(launch(c, "pairs_band", [&] {
                return launch_solve_band(c->stream, c->sms, c->tune.band_ctas, plan, k, dtype, d_out, exit_log);
            }), "pairs_band");
-    else
+    } else {
         CK(launch(c, "pairs_solve", [&] {
                return launch_solve(c->stream, c->sms, hask, plan, k, dtype, d_out, exit_log, any_long);
            }), "pairs_solve");
+    }
     return BLG_OK;
 }
 
@@ -775,7 +773,12 @@ static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64
         CK(cudaMemcpyAsync(kk.qidx, both.data(), sizeof(int32_t) * 2 * nq, cudaMemcpyHostToDevice, c->stream),
            "H2D class queries");
     }
-    // the host vectors above are pageable: the copies completed before return
+    // the host vectors above are pageable: the copies completed before return.
+    // Peq tables once per class set: every run of these queries reads them.
+    for (auto &k_ : s->cls)
+        CK(launch(c, "build_peq", [&] {
+               return launch_build_peq(c->stream, s->q.d, k_.qidx, k_.nq, k_.nw, k_.peq, c->d_status);
+           }), "build_peq");
     return BLG_OK;
 }
 
@@ -1228,6 +1231,22 @@ static int survivor_job_size(blg_ctx *c, const blg_search *s, int k) {
     return job;
 }
 
+// The sequential (not lane-spread) query classes of a search, for the
+// survivor plan and kernels.
+static SurvClasses seq_classes(blg_search *s) {
+    SurvClasses C;
+    for (auto &k_ : s->cls) {
+        if (k_.lanes || C.n == kSurvClasses) continue;
+        C.cls[C.n] = SearchClass{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
+        C.lo[C.n] = k_.lo;
+        C.hi[C.n] = k_.hi;
+        C.tile_start[C.n] = k_.tile_start;
+        C.work[C.n] = k_.work;
+        C.n++;
+    }
+    return C;
+}
+
 static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, int64_t q0, int64_t q1) {
     if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
     if (s->nq == 0 || s->nc == 0) return BLG_OK;
@@ -1243,42 +1262,33 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
                                   (q1 - q0) * s->nc, dtype, fillv);
            }), "fill");
     }
-    for (auto &k_ : s->cls)
-        CK(launch(c, "build_peq", [&] {
-               return launch_build_peq(c->stream, s->q.d, k_.qidx, k_.nq, k_.nw, k_.peq, c->d_status);
-           }), "build_peq");
-    // max_dist <= 31: the sequential classes' survivors in one launch
-    const bool band = surv && k <= 31;
-    const int band_job = band ? survivor_job_size(c, s, k) : 0;
-    SearchClass bcls[kSurvClasses];
-    const int32_t *blo[kSurvClasses], *bhi[kSurvClasses];
-    const int64_t *bts[kSurvClasses];
-    int32_t *bwork = nullptr;
-    int nb = 0;
+    if (surv) {
+        // the sequential classes' survivor plans in one launch; max_dist <=
+        // 31: their survivors in one more (lanes refilled as survivors finish)
+        const SurvClasses C = seq_classes(s);
+        const bool band = k <= 31;
+        const int job = band ? survivor_job_size(c, s, k) : 1024;
+        CK(launch(c, "surv_plan", [&] {
+               return launch_surv_plan(c->stream, C, s->lstart, s->min_len, s->n_len, k, job);
+           }), "surv_plan");
+        if (band) {
+            CK(launch(c, "search_band", [&] {
+                   return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, c->tune.surv_round, job, C, s->cs.d,
+                                             s->perm, s->ccnt,
+                                             s->qcnt, k, dtype, d_out, s->nc, nullptr, c->d_status);
+               }), "search_band");
+        } else {
+            for (int i = 0; i < C.n; i++)
+                CK(launch(c, "search_surv", [&] {
+                       return launch_search_surv(c->stream, c->sms, C.cls[i].nw, s->cs.d, s->perm, C.cls[i], C.lo[i],
+                                                 C.hi[i], C.tile_start[i], C.work[i], k, dtype, d_out, s->nc,
+                                                 c->d_status);
+                   }), "search_surv");
+        }
+    }
     for (auto &k_ : s->cls) {
         SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
-        if (surv && !k_.lanes) {
-            const int job = band ? band_job : 1024;
-            CK(launch(c, "surv_plan", [&] {
-                   return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, k, job,
-                                           k_.lo, k_.hi, k_.tile_start, k_.work);
-               }), "surv_plan");
-            if (band) {
-                if (nb == kSurvClasses) return fail(c, BLG_ERR_ARG, "too many query classes");
-                bcls[nb] = sc;
-                blo[nb] = k_.lo;
-                bhi[nb] = k_.hi;
-                bts[nb] = k_.tile_start;
-                if (!bwork) bwork = k_.work;        // cleared by this class's plan
-                nb++;
-            } else {
-                CK(launch(c, "search_surv", [&] {
-                       return launch_search_surv(c->stream, c->sms, k_.nw, s->cs.d, s->perm, sc, k_.lo, k_.hi,
-                                                 k_.tile_start, k_.work, k, dtype, d_out, s->nc, c->d_status);
-                   }), "search_surv");
-            }
-            continue;
-        }
+        if (surv && !k_.lanes) continue;
         if (k_.lanes) {
             CK(launch(c, "search_lanes", [&] {
                    return launch_search_lanes(c->stream, hask, s->c.d, sc, k_.nw, k, dtype, d_out,
@@ -1305,12 +1315,6 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
             }
         }
     }
-    if (nb > 0)
-        CK(launch(c, "search_band", [&] {
-               return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, band_job, nb, bcls, blo, bhi, bts, bwork,
-                                         s->cs.d, s->perm, s->ccnt, s->qcnt, k, dtype, d_out, s->nc, nullptr,
-                                         c->d_status);
-           }), "search_band");
     return BLG_OK;
 }
 
@@ -1406,12 +1410,12 @@ struct blg_batch {
     std::vector<int> regular;         // problems outside the persistent kernel (long queries)
     BatchJob *d_jobs = nullptr;
     int njobs = 0;
-    int64_t *d_qprefix = nullptr, *d_job_tiles = nullptr, *d_tile_base = nullptr;
+    int64_t *d_job_tiles = nullptr, *d_tile_base = nullptr;
     int32_t *d_work = nullptr;
     int nbanded = 0;
     BatchFill *d_fills = nullptr;
     int nfill = 0;
-    int64_t max_fill = 0, total_queries = 0, pairs = 0;
+    int64_t max_fill = 0, pairs = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int64_t graph_kernels = 0;
@@ -1425,7 +1429,6 @@ static void batch_release(blg_ctx *c, blg_batch *b) {
     }
     b->probs.clear();
     dev_free(c, b->d_jobs);
-    dev_free(c, b->d_qprefix);
     dev_free(c, b->d_job_tiles);
     dev_free(c, b->d_tile_base);
     dev_free(c, b->d_work);
@@ -1440,7 +1443,6 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
     if (nprob < 0 || (nprob > 0 && !pr)) return fail(c, BLG_ERR_ARG, "bad problem list");
     std::vector<BatchJob> jobs;
     std::vector<BatchFill> fills;
-    std::vector<int64_t> qprefix(1, 0);
     // one pinned region per problem for its permutation, reserved up front
     size_t stage_words = 0;
     for (int i = 0; i < nprob; i++)
@@ -1475,7 +1477,6 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
         }
         for (auto &cl : s->cls) {
             BatchJob j{};
-            j.Q = s->q.d;
             j.CS = s->cs.d;
             j.perm = s->perm;
             j.lstart = s->lstart;
@@ -1489,14 +1490,13 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
             j.k = k;
             j.dtype = p.dtype;
             j.nw = cl.nw;
-            j.tile = (k >= 0 && k <= 31) ? 4096 : 1024;   // longest-first jobs of the banded kernel
+            j.tile = 1024;                      // survivors per work unit (config 5: 0.99 ms per step; 1.30 with 4096)
             j.csk = s->csk;
             j.qsk = s->qsk;
             j.ccnt = s->ccnt;
             j.qcnt = s->qcnt;
             j.out = p.d_out;
             jobs.push_back(j);
-            qprefix.push_back(qprefix.back() + cl.nq);
         }
         if (k >= 0) {
             const uint32_t v = (uint32_t)(p.dtype == BLG_UINT8 ? std::min(k + 1, 255)
@@ -1505,20 +1505,14 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
             b->max_fill = std::max(b->max_fill, p.nq * p.nc * (int64_t)dtype_size(p.dtype));
         }
     }
-    // banded jobs first (they run in their own persistent kernel); the Peq
-    // prefix follows the job order
+    // banded jobs first (they run in their own persistent kernel)
     std::stable_partition(jobs.begin(), jobs.end(), [](const BatchJob &j) { return j.k >= 0 && j.k <= 31; });
     b->nbanded = (int)std::count_if(jobs.begin(), jobs.end(), [](const BatchJob &j) { return j.k >= 0 && j.k <= 31; });
-    qprefix.assign(1, 0);
-    for (const BatchJob &j : jobs) qprefix.push_back(qprefix.back() + j.cls.nq);
     b->njobs = (int)jobs.size();
     b->nfill = (int)fills.size();
-    b->total_queries = qprefix.back();
     if (b->njobs > 0) {
         CK(dev_alloc(c, (void **)&b->d_jobs, sizeof(BatchJob) * jobs.size()), "alloc jobs");
         CK(cudaMemcpyAsync(b->d_jobs, jobs.data(), sizeof(BatchJob) * jobs.size(), cudaMemcpyHostToDevice, c->stream), "H2D jobs");
-        CK(dev_alloc(c, (void **)&b->d_qprefix, sizeof(int64_t) * qprefix.size()), "alloc qprefix");
-        CK(cudaMemcpyAsync(b->d_qprefix, qprefix.data(), sizeof(int64_t) * qprefix.size(), cudaMemcpyHostToDevice, c->stream), "H2D qprefix");
         CK(dev_alloc(c, (void **)&b->d_job_tiles, sizeof(int64_t) * jobs.size()), "alloc job tiles");
         CK(dev_alloc(c, (void **)&b->d_tile_base, sizeof(int64_t) * (jobs.size() + 1)), "alloc tile base");
         CK(dev_alloc(c, (void **)&b->d_work, 2 * sizeof(int32_t)), "alloc work");
@@ -1540,9 +1534,8 @@ static int batch_run(blg_ctx *c, blg_batch *b) {
         c->prof = false;                      // no per-launch events inside a capture
         const int64_t before = c->launches;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "begin capture");
-        BatchPlan plan{b->d_jobs, b->njobs, b->nbanded, b->d_qprefix, b->d_job_tiles, b->d_tile_base, b->d_work};
-        cudaError_t e = launch_batch(c->stream, c->sms, plan, b->d_fills, b->nfill, b->max_fill, b->total_queries,
-                                     c->d_status);
+        BatchPlan plan{b->d_jobs, b->njobs, b->nbanded, b->d_job_tiles, b->d_tile_base, b->d_work};
+        cudaError_t e = launch_batch(c->stream, c->sms, plan, b->d_fills, b->nfill, b->max_fill, c->d_status);
         int rc = e == cudaSuccess ? BLG_OK : cuda_fail(c, e, "batch launch");
         for (int i : b->regular)
             if (!rc) rc = search_run(c, b->probs[i], b->kk[i], b->dt[i], b->outs[i]);
@@ -1555,7 +1548,7 @@ static int batch_run(blg_ctx *c, blg_batch *b) {
         if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_fail(c, e, "graph instantiate"); }
         b->graph = g;
         b->graph_kernels = (b->nfill > 0 ? 1 : 0) +
-                           (b->njobs > 0 ? 3 + (b->nbanded > 0 ? 1 : 0) + (b->nbanded < b->njobs ? 1 : 0) : 0) +
+                           (b->njobs > 0 ? 2 + (b->nbanded > 0 ? 1 : 0) + (b->nbanded < b->njobs ? 1 : 0) : 0) +
                            (c->launches - before);
         c->launches = before;
     }
@@ -1698,17 +1691,25 @@ static int tune_threshold_search(blg_ctx *c) {
     // The job size stays at its maximum, 4096: on 1024 x 2^20 it measured 8%
     // faster than 2048, while a search of this size cannot tell them apart;
     // smaller searches get smaller jobs at run time (survivor_job_size).
+    // CTAs per SM x columns per lane round
     float best_ms = 1e30f;
-    int best_ctas = c->tune.lpt_ctas;
+    int best_ctas = c->tune.lpt_ctas, best_round = c->tune.surv_round;
     c->tune.lpt_job = 4096;
-    for (int ctas : {2, 3, 4}) {
-        if (rc) break;
-        c->tune.lpt_ctas = ctas;
-        float ms = 0.f;
-        rc = time_best(c, 5, [&] { return search_run(c, &s, 4, BLG_UINT8, out); }, &ms);
-        if (!rc && ms < best_ms) { best_ms = ms; best_ctas = ctas; }
-    }
+    for (int ctas : {2, 3, 4})
+        for (int round : {8, 16, 32}) {
+            if (rc) break;
+            c->tune.lpt_ctas = ctas;
+            c->tune.surv_round = round;
+            float ms = 0.f;
+            rc = time_best(c, 5, [&] { return search_run(c, &s, 4, BLG_UINT8, out); }, &ms);
+            if (!rc && ms < best_ms) {
+                best_ms = ms;
+                best_ctas = ctas;
+                best_round = round;
+            }
+        }
     c->tune.lpt_ctas = best_ctas;
+    c->tune.surv_round = best_round;
     dev_free(c, out);
     search_release(c, &s);
     return rc;
@@ -1778,7 +1779,7 @@ static std::string tuning_header(blg_ctx *c) {
     std::string name = prop.name;
     for (auto &ch : name)
         if (ch == ' ') ch = '_';
-    return "BLGTUNE4 " + name + " sm" + std::to_string(prop.major * 10 + prop.minor) + " " + std::to_string(c->sms) +
+    return "BLGTUNE5 " + name + " sm" + std::to_string(prop.major * 10 + prop.minor) + " " + std::to_string(c->sms) +
            " " + std::to_string(blg_version());
 }
 
@@ -1799,11 +1800,12 @@ static bool tuning_load(blg_ctx *c, const char *path) {
             if (w >= 1 && w <= 8 && v >= 0 && v <= 4096) { t.qpb[w] = v; fields++; }
         } else if (k == "lpt_ctas" && v >= 1 && v <= 8) { t.lpt_ctas = v; fields++; }
         else if (k == "lpt_job" && v >= 256 && v <= 4096) { t.lpt_job = v; fields++; }
+        else if (k == "surv_round" && (v == 8 || v == 16 || v == 32)) { t.surv_round = v; fields++; }
         else if (k == "band_ctas" && v >= 1 && v <= 3) { t.band_ctas = v; fields++; }
         else if (k == "tile_buffers" && v >= 1 && v <= 2) { t.tile_buffers = v; fields++; }
     }
     fclose(f);
-    if (!ok || fields < 12) return false;
+    if (!ok || fields < 13) return false;
     t.tuned = 2;                                        // loaded from the cache
     c->tune = t;
     return true;
@@ -1814,8 +1816,8 @@ static void tuning_save(blg_ctx *c, const char *path) {
     if (!f) return;
     fprintf(f, "%s\n", tuning_header(c).c_str());
     for (int w = 1; w <= 8; w++) fprintf(f, "qpb%d %d\n", w, c->tune.qpb[w]);
-    fprintf(f, "lpt_ctas %d\nlpt_job %d\nband_ctas %d\ntile_buffers %d\n", c->tune.lpt_ctas, c->tune.lpt_job,
-            c->tune.band_ctas, c->tune.tile_buffers);
+    fprintf(f, "lpt_ctas %d\nlpt_job %d\nsurv_round %d\nband_ctas %d\ntile_buffers %d\n", c->tune.lpt_ctas,
+            c->tune.lpt_job, c->tune.surv_round, c->tune.band_ctas, c->tune.tile_buffers);
     fclose(f);
 }
 
@@ -2055,20 +2057,15 @@ int blg_sched_train_search(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t 
     int rc = sched_model_ensure(c, &m);
     if (rc) return rc;
     // survivors of every sequential class (host estimate from the plans, for the row spacing)
-    for (auto &k_ : s->cls)
-        CK(launch(c, "build_peq", [&] {
-               return launch_build_peq(c->stream, s->q.d, k_.qidx, k_.nq, k_.nw, k_.peq, c->d_status);
-           }), "build_peq");
+    const SurvClasses C = seq_classes(s);
+    CK(launch(c, "surv_plan", [&] {
+           return launch_surv_plan(c->stream, C, s->lstart, s->min_len, s->n_len, max_dist, 1);
+       }), "surv_plan");
     int64_t survivors = 0;
-    for (auto &k_ : s->cls) {
-        if (k_.lanes) continue;
-        SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
-        CK(launch(c, "surv_plan", [&] {
-               return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, max_dist, 1, k_.lo, k_.hi,
-                                       k_.tile_start, k_.work);
-           }), "surv_plan");
+    for (int i = 0; i < C.n; i++) {
         int64_t t = 0;
-        CK(cudaMemcpyAsync(&t, k_.tile_start + k_.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream), "D2H");
+        CK(cudaMemcpyAsync(&t, C.tile_start[i] + C.cls[i].nq, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream),
+           "D2H");
         CK(cudaStreamSynchronize(c->stream), "sync");
         survivors += t;
     }
@@ -2082,28 +2079,13 @@ int blg_sched_train_search(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t 
     SurvRows R{(half *)x, (float *)y, max_rows, (int64_t *)nrows,
                (int)std::min<int64_t>(INT32_MAX, std::max<int64_t>(1, (survivors + max_rows - 1) / max_rows))};
     const int job = survivor_job_size(c, s, max_dist);
-    SearchClass bcls[kSurvClasses];
-    const int32_t *blo[kSurvClasses], *bhi[kSurvClasses];
-    const int64_t *bts[kSurvClasses];
-    int32_t *bwork = nullptr;
-    int nb = 0;
-    for (auto &k_ : s->cls) {
-        if (k_.lanes || nb == kSurvClasses) continue;
-        SearchClass sc{k_.nw, k_.nq, k_.qidx, k_.qlen, k_.peq};
-        CK(launch(c, "surv_plan", [&] {
-               return launch_surv_plan(c->stream, sc, s->lstart, s->min_len, s->n_len, max_dist, job, k_.lo, k_.hi,
-                                       k_.tile_start, k_.work);
-           }), "surv_plan");
-        bcls[nb] = sc;
-        blo[nb] = k_.lo;
-        bhi[nb] = k_.hi;
-        bts[nb] = k_.tile_start;
-        if (!bwork) bwork = k_.work;
-        nb++;
-    }
+    CK(launch(c, "surv_plan", [&] {
+           return launch_surv_plan(c->stream, C, s->lstart, s->min_len, s->n_len, max_dist, job);
+       }), "surv_plan");
     CK(launch(c, "search_band_logged", [&] {
-           return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, job, nb, bcls, blo, bhi, bts, bwork, s->cs.d,
-                                     s->perm, s->ccnt, s->qcnt, max_dist, BLG_UINT8, out, s->nc, &R, c->d_status);
+           return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, c->tune.surv_round, job, C, s->cs.d, s->perm,
+                                     s->ccnt, s->qcnt,
+                                     max_dist, BLG_UINT8, out, s->nc, &R, c->d_status);
        }), "search_band_logged");
     int64_t rows = 0;
     CK(cudaMemcpyAsync(&rows, nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream), "D2H rows");
@@ -2485,13 +2467,14 @@ int blg_autotune(blg_ctx *c, const char *cache_path) {
 
 int blg_get_tuning(blg_ctx *c, int32_t *values, int n) {
     ENTER(c);
-    if (!values || n < 13) return fail(c, BLG_ERR_ARG, "need 13 values");
+    if (!values || n < 14) return fail(c, BLG_ERR_ARG, "need 14 values");
     for (int w = 1; w <= 8; w++) values[w - 1] = c->tune.qpb[w];
     values[8] = c->tune.lpt_ctas;
     values[9] = c->tune.lpt_job;
     values[10] = c->tune.band_ctas;
     values[11] = c->tune.tuned;
     values[12] = c->tune.tile_buffers;
+    values[13] = c->tune.surv_round;
     return BLG_OK;
 }
 

@@ -5,7 +5,6 @@
 // resident search (length-sorted choices, per-query Peq tables); a "job" is
 // one (problem, query word-class). These kernels run the whole batch:
 //   k_batch_fill    max_dist+1 into every thresholded problem's output
-//   k_batch_peq     one CTA per (job, query): the query's Peq table
 //   k_batch_plan    one block per job: survivor ranges and tile prefix
 //   k_batch_scan    job tile prefix (the global tile space)
 //   k_batch_band    persistent warps: banded jobs (max_dist <= 31), units of
@@ -51,16 +50,6 @@ __global__ void __launch_bounds__(256) k_batch_fill(const BatchFill *fills) {
     const BatchFill f = fills[blockIdx.y];
     fill_share(f.out, f.n, f.dtype, f.value, (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
                (int64_t)gridDim.x * blockDim.x);
-}
-
-__global__ void __launch_bounds__(256) k_batch_peq(BatchPlan plan, uint32_t *status) {
-    extern __shared__ uint64_t tab[];
-    const int j = upper_index(plan.q_prefix, plan.njobs, blockIdx.x);
-    const BatchJob &job = plan.jobs[j];
-    const int qi = (int)(blockIdx.x - plan.q_prefix[j]);
-    int m;
-    const uint8_t *p = string_at(job.Q, job.cls.qidx[qi], m, status);
-    build_peq_block(p, m, job.nw, tab, const_cast<uint64_t *>(job.cls.peq) + (size_t)qi * 256 * job.nw);
 }
 
 // One block per job: survivor range of every query (all choices for exact
@@ -158,8 +147,10 @@ __device__ __forceinline__ void batch_tile(const BatchJob &job, const uint64_t *
 
 // Banded jobs (0 <= k <= 31): persistent warps pull (job, query, survivor
 // unit) tiles of the banded part of the tile space.
+template <int R>
 __global__ void __launch_bounds__(256) k_batch_band(BatchPlan plan, uint32_t *status) {
-    __shared__ SurvJob s_job[8];
+    __shared__ __align__(16) unsigned char s_raw[8 * sizeof(SurvJob)];   // (no constructor runs on shared memory)
+    SurvJob *s_job = reinterpret_cast<SurvJob *>(s_raw);
     __shared__ int32_t s_pend[8][kSurvPend];
     __shared__ uint16_t s_pgd[8][kSurvPend];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -192,7 +183,7 @@ __global__ void __launch_bounds__(256) k_batch_band(BatchPlan plan, uint32_t *st
         }
         return true;
     };
-    survivor_warp(s_job[w], next_job, s_pend[w], s_pgd[w], status, [](int64_t, int, int, int, uint32_t) {});
+    survivor_warp<R>(s_job[w], next_job, s_pend[w], s_pgd[w], status, [](int64_t, int, int, int, uint32_t) {});
 }
 
 // The other jobs (exact, or max_dist > 31): 1024-choice tiles, 4 per thread.
@@ -231,27 +222,25 @@ __global__ void __launch_bounds__(256) k_batch_search(BatchPlan plan, uint32_t *
 }
 
 cudaError_t batch_set_attributes() {
-    cudaError_t e = cudaFuncSetAttribute(k_batch_peq, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         256 * kBatchMaxWords * 8);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch_search, cudaFuncAttributeMaxDynamicSharedMemorySize, kBatchSearchSmem);
-    return e;
+    return cudaFuncSetAttribute(k_batch_search, cudaFuncAttributeMaxDynamicSharedMemorySize, kBatchSearchSmem);
 }
 
-// The five launches of one batch run, on `st` (capturable: no allocation,
-// no attribute change, no synchronisation).
+// The launches of one batch run, on `st` (capturable: no allocation, no
+// attribute change, no synchronisation). The queries' Peq tables were built
+// at upload.
 cudaError_t launch_batch(cudaStream_t st, int sms, const BatchPlan &plan, const BatchFill *fills, int nfill,
-                         int64_t max_fill, int64_t total_queries, uint32_t *status) {
+                         int64_t max_fill, uint32_t *status) {
     if (nfill > 0) {
         int64_t bx = (max_fill / 16 + 255) / 256;
         bx = bx < 1 ? 1 : (bx > 1024 ? 1024 : bx);
         k_batch_fill<<<dim3((unsigned)bx, (unsigned)nfill), 256, 0, st>>>(fills);
     }
     if (plan.njobs > 0) {
-        k_batch_peq<<<(unsigned)total_queries, 256, 256 * kBatchMaxWords * 8, st>>>(plan, status);
         k_batch_plan<<<plan.njobs, 1024, 0, st>>>(plan);
         k_batch_scan<<<1, 1024, 0, st>>>(plan);
-        if (plan.nbanded > 0) k_batch_band<<<sms * 4, 256, 0, st>>>(plan, status);
+        // 32 columns per round: the batch's short strings mostly end within
+        // one (config 5: 1.38 ms per step, 1.70 with 16 columns, 1.72 with 8)
+        if (plan.nbanded > 0) k_batch_band<32><<<sms * 4, 256, 0, st>>>(plan, status);
         if (plan.nbanded < plan.njobs) k_batch_search<<<sms * 3, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
     }
     return cudaGetLastError();

@@ -11,7 +11,6 @@ constexpr int kBatchMaxWords = 4;   // batched queries up to 256 bytes; longer o
 
 // One (problem, query word-class): everything the persistent kernel needs.
 struct BatchJob {
-    DevStrings Q;              // the problem's queries
     DevStrings CS;             // its choices, length-sorted
     const int32_t *perm;       // sorted -> original choice index
     const int64_t *lstart;     // first sorted index per length
@@ -40,7 +39,6 @@ struct BatchPlan {
     const BatchJob *jobs;      // device array; banded jobs (0 <= k <= 31) first
     int njobs;
     int nbanded;               // jobs [0, nbanded) run in the banded survivor kernel (k_batch_band)
-    const int64_t *q_prefix;   // [njobs + 1] queries before each job (Peq build CTAs)
     int64_t *job_tiles;        // [njobs]
     int64_t *tile_base;        // [njobs + 1]
     int32_t *work;             // persistent-kernel counters: [0] banded jobs, [1] the others
@@ -48,6 +46,6 @@ struct BatchPlan {
 
 cudaError_t batch_set_attributes();
 cudaError_t launch_batch(cudaStream_t st, int sms, const BatchPlan &plan, const BatchFill *fills, int nfill,
-                         int64_t max_fill, int64_t total_queries, uint32_t *status);
+                         int64_t max_fill, uint32_t *status);
 
 }  // namespace blg

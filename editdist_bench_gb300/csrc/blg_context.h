@@ -15,6 +15,7 @@ struct blg_tuning {
     int qpb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};   // exact search: queries per CTA by query words (0: heuristic)
     int lpt_ctas = 4;                            // thresholded search: CTAs per SM
     int lpt_job = 4096;                          // thresholded search: survivors per job
+    int surv_round = 16;                         // thresholded search: columns per lane round (8, 16, 32)
     int band_ctas = 3;                           // banded pairs solver: CTAs per SM
     int tile_buffers = 2;                        // short-pair tile kernel: stage buffers (1: 3 CTAs/SM)
     int tuned = 0;

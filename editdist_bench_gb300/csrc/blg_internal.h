@@ -98,10 +98,6 @@ struct PrefixChoices {
     int ck[kPfxCheckpoints] = {0, 0};
 };
 
-// Query word classes of the sequential search kernels (patterns of 1..8
-// 64-bit words); longer queries run lane-spread.
-constexpr int kSurvClasses = 8;
-
 // Per-query-class search launch description.
 struct SearchClass {
     int nw;                 // pattern words (sequential kernels) or 0 for lane-spread
@@ -109,6 +105,20 @@ struct SearchClass {
     const int32_t *qidx;    // device: query row per class entry
     const int32_t *qlen;    // device: query length per class entry
     const uint64_t *peq;    // device: [nq][256][nw] Peq tables
+};
+
+// Query word classes of the sequential search kernels (patterns of 1..8
+// 64-bit words); longer queries run lane-spread. A thresholded run plans and
+// solves the survivors of all its sequential classes in one launch each.
+constexpr int kSurvClasses = 8;
+
+struct SurvClasses {
+    int n = 0;                                 // classes
+    SearchClass cls[kSurvClasses];
+    int32_t *lo[kSurvClasses];                 // survivor range per query
+    int32_t *hi[kSurvClasses];
+    int64_t *tile_start[kSurvClasses];         // job prefix per query (nq + 1)
+    int32_t *work[kSurvClasses];               // job counters (cleared by the plan)
 };
 
 }  // namespace blg

@@ -560,16 +560,25 @@ __global__ void __launch_bounds__(256) k_gather_strings(DevStrings src, const in
     }
 }
 
-// Per class: survivor range [lo, hi) of every query (queries sorted by
-// length), tile counts, and their exclusive prefix tile_start[0..nq]. One
-// block; the scan walks the queries 1024 at a time.
-__global__ void __launch_bounds__(1024) k_surv_plan(SearchClass cls, const int64_t *lstart, int64_t min_len,
-                                                    int64_t n_len, int k, int tile, int32_t *lo, int32_t *hi,
-                                                    int64_t *tile_start, int32_t *work) {
+// Per class (one block each): survivor range [lo, hi) of every query
+// (queries sorted by length), tile counts, and their exclusive prefix
+// tile_start[0..nq]; the class's work counter cleared. The scan walks the
+// queries 1024 at a time.
+__global__ void __launch_bounds__(1024) k_surv_plan(SurvClasses C, const int64_t *lstart, int64_t min_len,
+                                                    int64_t n_len, int k, int tile) {
+    __shared__ __align__(16) unsigned char s_raw[sizeof(SurvClasses)];   // (no constructor runs on shared memory)
+    SurvClasses &s_c = *reinterpret_cast<SurvClasses *>(s_raw);
     __shared__ int64_t s_sum[1024];
     __shared__ int64_t s_carry;
-    if (threadIdx.x == 0) { s_carry = 0; *work = 0; }
+    if (threadIdx.x == 0) {
+        s_c = C;
+        s_carry = 0;
+    }
     __syncthreads();
+    const SearchClass &cls = s_c.cls[blockIdx.x];
+    int32_t *lo = s_c.lo[blockIdx.x], *hi = s_c.hi[blockIdx.x];
+    int64_t *tile_start = s_c.tile_start[blockIdx.x];
+    if (threadIdx.x == 0) *s_c.work[blockIdx.x] = 0;
     for (int base = 0; base < cls.nq; base += 1024) {
         const int qi = base + threadIdx.x;
         int64_t tiles = 0;
@@ -871,11 +880,11 @@ cudaError_t launch_gather_strings(cudaStream_t st, int sms, const DevStrings &sr
     return cudaGetLastError();
 }
 
-cudaError_t launch_surv_plan(cudaStream_t st, const SearchClass &cls, const int64_t *lstart,
-                             int64_t min_len, int64_t n_len, int k, int tile, int32_t *lo, int32_t *hi,
-                             int64_t *tile_start, int32_t *work) {
-    if (cls.nq <= 0) return cudaSuccess;
-    k_surv_plan<<<1, 1024, 0, st>>>(cls, lstart, min_len, n_len, k, tile, lo, hi, tile_start, work);
+cudaError_t launch_surv_plan(cudaStream_t st, const SurvClasses &C, const int64_t *lstart, int64_t min_len,
+                             int64_t n_len, int k, int tile) {
+    if (C.n <= 0) return cudaSuccess;
+    if (C.n > kSurvClasses) return cudaErrorInvalidValue;
+    k_surv_plan<<<C.n, 1024, 0, st>>>(C, lstart, min_len, n_len, k, tile);
     return cudaGetLastError();
 }
 

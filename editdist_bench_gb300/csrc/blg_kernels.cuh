@@ -724,13 +724,13 @@ __device__ __forceinline__ uint32_t gram_dist(uint4 a, uint4 b) {
 // per survivor. Their costs differ by two orders of magnitude: most leave
 // the band within 2k + 2 columns, near-copies of the query run the whole
 // text. So warps run without CTA barriers and their lanes advance in rounds
-// of kSurvRound columns; between rounds the warp hands the passers it has
+// of R columns (a tuned launch shape: 8, 16 or 32); between rounds the warp
+// hands the passers it has
 // found to the lanes whose survivor finished, scanning further survivors
 // (128 per step, four independent count loads per lane) while lanes are
 // free. The window bits come from the query's Peq table in global memory
 // (L1-resident while a warp works on the query). Results <= k are stored
 // (the output holds k+1 already).
-constexpr int kSurvRound = 32;         // text columns per round
 constexpr int kSurvPend = 128;         // passers one scan step can buffer
 
 // One query's survivor range, read by all lanes of a warp (kept in shared
@@ -762,7 +762,7 @@ __device__ __forceinline__ int upper_index(const int64_t *pre, int n, int64_t x)
 // s_pend: the warp's kSurvPend passer slots (sorted choice index), s_pgd
 // their 4-gram count distances. log(sidx, m, n, cols, gd) sees every
 // survivor the banded loop finished.
-template <typename NextJob, typename LogFn>
+template <int R, typename NextJob, typename LogFn>
 __device__ __forceinline__ void survivor_warp(SurvJob &J, NextJob next_job, int32_t *s_pend, uint16_t *s_pgd,
                                               uint32_t *status, LogFn log) {
     const int lane = threadIdx.x & 31;
@@ -876,7 +876,7 @@ __device__ __forceinline__ void survivor_warp(SurvJob &J, NextJob next_job, int3
             const uint64_t *pq = peq;
             const int nwl = nw;
             auto eqw = [&](uint32_t c, int p0) { return peq_window(pq + c * nwl, nwl, p0); };
-            const bool exited = band_steps(k, bg, bs, min(n, bs.j + kSurvRound), text, eqw);
+            const bool exited = band_steps(k, bg, bs, min(n, bs.j + R), text, eqw);
             if (exited || bs.j == n) {
                 const int d = exited ? k + 1 : band_finish(k, bg, bs);
                 if (d <= k) store1(out, dtype, oidx, d);

@@ -22,10 +22,12 @@ namespace blg {
 
 // sketch[i] = gram_sketch(string i), counts[i] = gram_counts(string i),
 // one warp per string: lane l takes the 4-grams starting at l, l + 32, ...
-// (one unaligned 4-byte read each, consecutive across the warp), the 16 bin
-// counts are summed by one ballot per bin, the sketch bits by an OR over the
-// warp. The values equal the per-thread functions' (the same grams, hash and
-// saturation at 255).
+// (one unaligned 4-byte read each, consecutive across the warp) and counts
+// them in its own 16 byte counters (4 registers); every 255 steps, before a
+// lane counter can wrap, and at the end the counters are folded into
+// saturating totals, then summed over the warp with saturating byte adds.
+// The sketch bits are an OR over the warp. The values equal the per-thread
+// functions' (the same grams, hash and saturation at 255).
 __global__ void __launch_bounds__(256) k_sketch_strings(DevStrings S, uint64_t *sketch, uint4 *counts,
                                                         uint32_t *status) {
     const int lane = threadIdx.x & 31;
@@ -33,59 +35,55 @@ __global__ void __launch_bounds__(256) k_sketch_strings(DevStrings S, uint64_t *
     for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < S.n; i += nwarps) {
         int n;
         const uint8_t *p = string_at(S, i, n, status);
-        uint32_t sk_lo = 0, sk_hi = 0, cnt = 0;              // lane b < 16 counts bin b
-        for (int s0 = 0; s0 + 3 < n; s0 += 32) {
-            const int s = s0 + lane;                          // the gram of bytes s .. s+3
-            const bool act = s + 3 < n;
-            const uint32_t g = act ? __byte_perm(load4(p + s), 0u, 0x0123) : 0u;   // b[s] << 24 | .. | b[s+3]
-            const uint32_t h = g * 0x9E3779B1u;
-            const uint32_t bin = act ? (h >> 28) : 16u;
-            if (act && s + 3 < kSketchWindow) {
-                const uint32_t bit = h >> 26;
-                if (bit < 32) sk_lo |= 1u << bit;
-                else sk_hi |= 1u << (bit - 32);
+        uint32_t sk_lo = 0, sk_hi = 0;
+        uint32_t t[4] = {0, 0, 0, 0};                          // saturating totals, bins 4w .. 4w+3
+        for (int c0 = 0; c0 + 3 < n; c0 += 32 * 255) {
+            uint32_t c[4] = {0, 0, 0, 0};                      // this lane's counts of the chunk
+            const int c1 = min(n - 3, c0 + 32 * 255);          // grams starting before c1
+            for (int s = c0 + lane; s < c1; s += 32) {
+                const uint32_t g = __byte_perm(load4(p + s), 0u, 0x0123);   // b[s] << 24 | .. | b[s+3]
+                const uint32_t h = g * 0x9E3779B1u;
+                const uint32_t bin = h >> 28, inc = 1u << (8 * (bin & 3));
+#pragma unroll
+                for (int w = 0; w < 4; w++) c[w] += (bin >> 2) == (uint32_t)w ? inc : 0u;
+                if (s + 3 < kSketchWindow) {
+                    const uint32_t bit = h >> 26;
+                    if (bit < 32) sk_lo |= 1u << bit;
+                    else sk_hi |= 1u << (bit - 32);
+                }
             }
 #pragma unroll
-            for (uint32_t b = 0; b < 16; b++) {
-                const unsigned m = __ballot_sync(kFull, bin == b);
-                if ((uint32_t)lane == b) cnt += __popc(m);
-            }
+            for (int w = 0; w < 4; w++) t[w] = __vaddus4(t[w], c[w]);
         }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+            for (int w = 0; w < 4; w++) t[w] = __vaddus4(t[w], __shfl_xor_sync(kFull, t[w], off));
         sk_lo = __reduce_or_sync(kFull, sk_lo);
         sk_hi = __reduce_or_sync(kFull, sk_hi);
-        uint32_t v = (lane < 16 ? min(cnt, 255u) : 0u) << (8 * (lane & 3));   // byte lane & 3 of word lane >> 2
-        v |= __shfl_xor_sync(kFull, v, 1);
-        v |= __shfl_xor_sync(kFull, v, 2);
-        const uint32_t w0 = __shfl_sync(kFull, v, 0), w1 = __shfl_sync(kFull, v, 4), w2 = __shfl_sync(kFull, v, 8),
-                       w3 = __shfl_sync(kFull, v, 12);
         if (lane == 0) {
             sketch[i] = ((uint64_t)sk_hi << 32) | sk_lo;
-            counts[i] = make_uint4(w0, w1, w2, w3);
+            counts[i] = make_uint4(t[0], t[1], t[2], t[3]);
         }
     }
 }
 
-// Every non-lane-spread query class of one thresholded run in one launch.
-struct SurvClasses {
-    int n;                                     // classes
-    SearchClass cls[kSurvClasses];
-    const int32_t *lo[kSurvClasses];           // survivor range per query
-    const int32_t *hi[kSurvClasses];
-    const int64_t *tile_start[kSurvClasses];   // job prefix per query (nq + 1)
-};
-
-template <bool LOG>
+template <int R, bool LOG>
 __global__ void __launch_bounds__(256) k_search_band(DevStrings CS, const int32_t *perm, const uint4 *ccnt,
-                                                     const uint4 *qcnt, SurvClasses C, int32_t *work, int jobsz,
+                                                     const uint4 *qcnt, SurvClasses C, int jobsz,
                                                      int k, int dtype, void *out, int64_t nc, SurvRows rows,
                                                      uint32_t *status) {
-    __shared__ SurvClasses s_cls;
-    __shared__ SurvJob s_job[8];
+    // raw shared bytes: no constructor runs on shared memory
+    constexpr size_t kJobs = (sizeof(SurvClasses) + 15) & ~size_t(15);
+    __shared__ __align__(16) unsigned char s_raw[kJobs + 8 * sizeof(SurvJob)];
+    SurvClasses &s_cls = *reinterpret_cast<SurvClasses *>(s_raw);
+    SurvJob *s_job = reinterpret_cast<SurvJob *>(s_raw + kJobs);
     __shared__ int32_t s_pend[8][kSurvPend];
     __shared__ uint16_t s_pgd[8][kSurvPend];
     if (threadIdx.x == 0) s_cls = C;
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int32_t *work = s_cls.work[0];                 // one counter for the launch
     auto next_job = [&](SurvJob &J) -> bool {
         int job = 0;
         if (lane == 0) job = atomicAdd(work, 1);
@@ -120,7 +118,7 @@ __global__ void __launch_bounds__(256) k_search_band(DevStrings CS, const int32_
         }
         return true;
     };
-    survivor_warp(s_job[w], next_job, s_pend[w], s_pgd[w], status,
+    survivor_warp<R>(s_job[w], next_job, s_pend[w], s_pgd[w], status,
                   [&](int64_t sidx, int m, int n, int cols, uint32_t gd) {
                       if (!LOG || m == 0 || n == 0 || (sidx % rows.stride) != 0) return;
                       const int64_t at = atomicAdd((unsigned long long *)rows.count, 1ull);
@@ -146,32 +144,30 @@ cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S,
     return cudaGetLastError();
 }
 
-// `work` must be zero when the launch starts (the first class's survivor
-// plan clears it on the stream).
-cudaError_t launch_search_band(cudaStream_t st, int sms, int ctas_per_sm, int jobsz, int ncls,
-                               const SearchClass *cls, const int32_t *const *lo, const int32_t *const *hi,
-                               const int64_t *const *tile_start, int32_t *work, const DevStrings &CS,
-                               const int32_t *perm, const uint4 *ccnt, const uint4 *qcnt, int k, int dtype, void *out,
-                               int64_t nc, const SurvRows *rows, uint32_t *status) {
-    if (ncls <= 0) return cudaSuccess;
-    if (ncls > kSurvClasses || k < 0 || k > 31 || jobsz < 128) return cudaErrorInvalidValue;
-    SurvClasses C{};
-    C.n = ncls;
-    for (int c = 0; c < ncls; c++) {
-        C.cls[c] = cls[c];
-        C.lo[c] = lo[c];
-        C.hi[c] = hi[c];
-        C.tile_start[c] = tile_start[c];
-    }
-    const int grid = sms * std::max(1, std::min(ctas_per_sm, 8));
+template <int R>
+static void launch_band_r(cudaStream_t st, int grid, int jobsz, const SurvClasses &C, const DevStrings &CS,
+                          const int32_t *perm, const uint4 *ccnt, const uint4 *qcnt, int k, int dtype, void *out,
+                          int64_t nc, const SurvRows *rows, uint32_t *status) {
     if (rows) {
-        k_search_band<true><<<grid, 256, 0, st>>>(CS, perm, ccnt, qcnt, C, work, jobsz, k, dtype, out, nc, *rows,
-                                                   status);
+        k_search_band<R, true><<<grid, 256, 0, st>>>(CS, perm, ccnt, qcnt, C, jobsz, k, dtype, out, nc, *rows, status);
     } else {
         const SurvRows none{nullptr, nullptr, 0, nullptr, 1};
-        k_search_band<false><<<grid, 256, 0, st>>>(CS, perm, ccnt, qcnt, C, work, jobsz, k, dtype, out, nc, none,
-                                                    status);
+        k_search_band<R, false><<<grid, 256, 0, st>>>(CS, perm, ccnt, qcnt, C, jobsz, k, dtype, out, nc, none, status);
     }
+}
+
+// The job counter is C.work[0], zero when the launch starts (the plan
+// clears it on the stream). round: columns per round, 8, 16 or 32.
+cudaError_t launch_search_band(cudaStream_t st, int sms, int ctas_per_sm, int round, int jobsz, const SurvClasses &C,
+                               const DevStrings &CS, const int32_t *perm, const uint4 *ccnt, const uint4 *qcnt, int k,
+                               int dtype, void *out, int64_t nc, const SurvRows *rows, uint32_t *status) {
+    if (C.n <= 0) return cudaSuccess;
+    if (C.n > kSurvClasses || k < 0 || k > 31 || jobsz < 128) return cudaErrorInvalidValue;
+    const int grid = sms * std::max(1, std::min(ctas_per_sm, 8));
+    if (round == 8) launch_band_r<8>(st, grid, jobsz, C, CS, perm, ccnt, qcnt, k, dtype, out, nc, rows, status);
+    else if (round == 16) launch_band_r<16>(st, grid, jobsz, C, CS, perm, ccnt, qcnt, k, dtype, out, nc, rows, status);
+    else if (round == 32) launch_band_r<32>(st, grid, jobsz, C, CS, perm, ccnt, qcnt, k, dtype, out, nc, rows, status);
+    else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 
