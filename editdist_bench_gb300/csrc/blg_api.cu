@@ -67,7 +67,8 @@ cudaError_t launch_order(cudaStream_t st, int sms, const PairsPlan &plan);
 cudaError_t launch_solve(cudaStream_t st, int sms, bool hask, const PairsPlan &plan, int k, int dtype,
                          void *out, int32_t *exit_log, bool any_long);
 cudaError_t launch_solve_band(cudaStream_t st, int sms, int ctas_per_sm, const PairsPlan &plan, int k, int dtype, void *out,
-                              int32_t *exit_log);
+                              int32_t *exit_log, int variant, const uint32_t *alpha);
+cudaError_t launch_byte_presence(cudaStream_t st, int sms, const DevStrings &A, const DevStrings &B, uint32_t *mask);
 }  // namespace blg
 int sched_model_ensure(blg_ctx *c, blg_sched_model **out);
 cudaError_t launch_mlp_keys(cudaStream_t st, int sms, const blg_sched_model *m, const blg::PairsPlan &plan,
@@ -124,6 +125,10 @@ struct blg_pairs {
     void *plan_mem = nullptr;     // raw + sorted records, keys
     half *feat_mem = nullptr;     // feature rows (learned schedule)
     int32_t *plan_ctr = nullptr;  // count, head, hist, cursor
+    // the bytes the set uses (8 words) and their count on the host (-1: not
+    // known; the banded solver's one-row-per-byte variant needs at most 15)
+    uint32_t *d_alpha = nullptr;
+    int nsym = -1;
     // resident runs as a CUDA graph (pairs_run_graph): the launches of one
     // run, captured once its parameters repeat, replayed while they stay
     struct GraphKey {
@@ -547,8 +552,20 @@ static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, const DevStrings &A, co
     bool any_long = false;
     for (int j = 1; j < kPairClasses; j++) any_long |= p->pcap[j] > 0;
     if (band) {
+        // a resident set's alphabet is known from its upload; a pipeline chunk's
+        // is scanned on the stream and both variants launch (one returns at once)
+        if (!p->d_alpha) CK(dev_alloc(c, (void **)&p->d_alpha, 8 * sizeof(uint32_t)), "cudaMallocAsync(alphabet)");
+        int variant = -1;
+        if (p->nsym >= 0) {
+            variant = p->nsym <= kBandSymbols ? 1 : 0;
+        } else {
+            CK(cudaMemsetAsync(p->d_alpha, 0, 8 * sizeof(uint32_t), c->stream), "reset alphabet");
+            CK(launch(c, "byte_presence", [&] { return launch_byte_presence(c->stream, c->sms, A, B, p->d_alpha); }),
+               "byte_presence");
+        }
         CK(launch(c, "pairs_band", [&] {
-               return launch_solve_band(c->stream, c->sms, c->tune.band_ctas, plan, k, dtype, d_out, exit_log);
+               return launch_solve_band(c->stream, c->sms, c->tune.band_ctas, plan, k, dtype, d_out, exit_log, variant,
+                                        p->d_alpha);
            }), "pairs_band");
     } else {
         CK(launch(c, "pairs_solve", [&] {
@@ -703,6 +720,8 @@ static void pairs_release(blg_ctx *c, blg_pairs *p) {
     dev_free(c, p->plan_mem);
     dev_free(c, p->plan_ctr);
     dev_free(c, p->feat_mem);
+    dev_free(c, p->d_alpha);
+    p->d_alpha = nullptr;
     p->plan_mem = nullptr;
     p->plan_ctr = nullptr;
     p->feat_mem = nullptr;
@@ -1907,9 +1926,23 @@ int blg_pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uin
     blg_pairs *p = new (std::nothrow) blg_pairs();
     if (!p) return fail(c, BLG_ERR_ALLOC, "host allocation");
     int rc = pairs_upload(c, ba, oa, bb, ob, n, p);
+    // the bytes the set uses, once: they pick the banded solver's row layout
+    uint32_t alpha[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (!rc && n > 0) {
+        if (dev_alloc(c, (void **)&p->d_alpha, sizeof(alpha)) != cudaSuccess ||
+            cudaMemsetAsync(p->d_alpha, 0, sizeof(alpha), c->stream) != cudaSuccess ||
+            launch(c, "byte_presence", [&] { return launch_byte_presence(c->stream, c->sms, p->a.d, p->b.d, p->d_alpha); }) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(alpha, p->d_alpha, sizeof(alpha), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+            rc = fail(c, BLG_ERR_CUDA, "alphabet");
+    }
     // the copies complete before the call returns: the device copy is the
     // data the host pass checked, whatever the caller does with its buffers
     if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = fail(c, BLG_ERR_CUDA, "upload");
+    if (!rc && n > 0) {
+        p->nsym = 0;
+        for (uint32_t w : alpha) p->nsym += __builtin_popcount(w);
+    }
     if (rc) {
         pairs_release(c, p);
         delete p;

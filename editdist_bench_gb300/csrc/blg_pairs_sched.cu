@@ -17,6 +17,8 @@
 //   3. k_solve_word / k_solve_lanes consume the sorted records from device
 //      work counters, so a warp takes pairs of similar cost.
 // Which pairs are computed and their values never change: only the order.
+#include <algorithm>
+
 #include "blg_kernels.cuh"
 #include "blg_sched.h"
 
@@ -203,23 +205,65 @@ __global__ void __launch_bounds__(256) k_solve_lanes(PairsPlan plan, int k, int 
 
 // max_dist <= 31: every record (any pattern length) solved by the banded
 // loop, one thread per record. The window's match bits come from per-thread
-// nibble rows over a 64-position block of the pattern: rows 0..15 / 16..31
-// of a [row][thread] table hold, for each high / low nibble value, the
-// positions whose byte has it (bit i <-> position 32b - dhi + i in block b).
-// Columns 32b .. 32b+31 read their 32-bit windows out of the same block with
-// one funnel shift, so within a block the table is read-only and the match
-// loads stay off the column chain; every 32 columns the rows shift down by
-// 32 positions and the next 32 pattern bytes are entered. The [row][thread]
-// layout keeps every access bank-conflict free.
+// rows over a 64-position block of the pattern (bit i <-> position
+// 32b - dhi + i in block b), in a [row][thread] table (every access
+// bank-conflict free). Columns 32b .. 32b+31 read their 32-bit windows out
+// of the same block with one funnel shift, so within a block the table is
+// read-only and the match loads stay off the column chain; every 32 columns
+// the rows shift down by 32 positions and the next 32 pattern bytes are
+// entered. Two row layouts:
+//   SYM = false: nibble rows, 0..15 / 16..31 for each high / low nibble
+//     value; Eq(c) = row[c >> 4] & row[16 + (c & 15)], any byte alphabet,
+//     two row updates per pattern byte, 64 KB per CTA (3 CTAs per SM);
+//   SYM = true: when the pair set uses at most 15 distinct bytes, one row
+//     per byte (rank of the byte among the set's bytes; the bytes outside
+//     the set share row 15, which stays empty): one update per pattern
+//     byte, one row load per column, and 32 KB per CTA, so twice the warps
+//     per SM hide the latency of the lanes' string loads (the kernel's
+//     stall: each lane walks its own strings).
+// alpha: the set's bytes (8 words), or null when the host has chosen the
+// variant; given, each variant checks it and the one that does not apply
+// returns at once (one launch of each, no host round trip).
 constexpr int kBandThreads = 256;
+constexpr int kSymRows = kBandSymbols + 1;           // the last row stays empty
 
-template <bool LOG>
+template <bool LOG, bool SYM>
 __global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int k, int dtype, void *out,
-                                                             int32_t *exit_log, uint32_t unit) {
-    extern __shared__ uint2 s_rows2[];                      // [32 rows][kBandThreads] 64-bit rows
-    const Units u{unit, unit + unit};
+                                                             int32_t *exit_log, const uint32_t *alpha) {
+    constexpr int R = SYM ? kSymRows : 32;
+    extern __shared__ uint2 s_rows2[];                      // [R rows][kBandThreads] 64-bit rows
+    __shared__ uint8_t s_map[256];                          // byte -> row (SYM)
+    if (alpha) {
+        int total = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) total += __popc(__ldg(alpha + i));
+        if ((total <= kBandSymbols) != SYM) return;         // uniform: the other variant runs the set
+    }
+    if (SYM) {
+        const int b = threadIdx.x;                          // kBandThreads == 256: one byte per thread
+        const uint32_t w = __ldg(alpha + (b >> 5));
+        int rank = __popc(w & ((1u << (b & 31)) - 1u));
+        for (int i = 0; i < (b >> 5); i++) rank += __popc(__ldg(alpha + i));
+        s_map[b] = (uint8_t)(((w >> (b & 31)) & 1u) ? rank : kSymRows - 1);
+        __syncthreads();
+    }
     uint2 *tc = s_rows2 + threadIdx.x;                      // row r at tc[r * kBandThreads]
     const int lane = threadIdx.x & 31;
+    // pattern byte c at window bit `bitpos` of the block (0..63)
+    auto enter = [&](uint32_t c, int bitpos) {
+        const uint32_t bit = 1u << (bitpos & 31);
+        if (SYM) {
+            atomicOr(reinterpret_cast<uint32_t *>(tc + s_map[c] * kBandThreads) + (bitpos >> 5), bit);
+        } else {
+            atomicOr(reinterpret_cast<uint32_t *>(tc + (c >> 4) * kBandThreads) + (bitpos >> 5), bit);
+            atomicOr(reinterpret_cast<uint32_t *>(tc + (16 + (c & 15)) * kBandThreads) + (bitpos >> 5), bit);
+        }
+    };
+    auto rowbits = [&](uint32_t c) -> uint2 {
+        if (SYM) return tc[s_map[c] * kBandThreads];
+        const uint2 h = tc[(c >> 4) * kBandThreads], l = tc[(16 + (c & 15)) * kBandThreads];
+        return make_uint2(h.x & l.x, h.y & l.y);
+    };
     for (int cls = kPairClasses - 1; cls >= 0; cls--) {
         const int count = min(plan.count[cls], (int)plan.cap[cls]);
         while (true) {
@@ -238,7 +282,7 @@ __global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int
                 const BandGeom bg = band_geom(m, n, k);
                 const int dhi = bg.dhi;
 #pragma unroll
-                for (int r = 0; r < 32; r++) tc[r * kBandThreads] = make_uint2(0, 0);
+                for (int r = 0; r < R; r++) tc[r * kBandThreads] = make_uint2(0, 0);
                 // block 0: positions 0 .. min(m, 64 - dhi) - 1 at bits pos + dhi
                 const int first_end = min(m, 64 - dhi);
                 {
@@ -247,17 +291,8 @@ __global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int
                     for (int p = 0; p < first_end; p += 4) {
                         const uint32_t w4 = fs.next4();
 #pragma unroll
-                        for (int b = 0; b < 4; b++) {
-                            if (p + b < first_end) {
-                                const uint32_t c = (w4 >> (8 * b)) & 0xffu;
-                                const int bitpos = p + b + dhi;
-                                uint32_t *h = reinterpret_cast<uint32_t *>(tc + (c >> 4) * kBandThreads) + (bitpos >> 5);
-                                uint32_t *l = reinterpret_cast<uint32_t *>(tc + (16 + (c & 15)) * kBandThreads) + (bitpos >> 5);
-                                const uint32_t bit = 1u << (bitpos & 31);
-                                atomicOr(h, bit);
-                                atomicOr(l, bit);
-                            }
-                        }
+                        for (int b = 0; b < 4; b++)
+                            if (p + b < first_end) enter((w4 >> (8 * b)) & 0xffu, p + b + dhi);
                     }
                 }
                 // later blocks enter the positions from 64 - dhi on, 32 at a time
@@ -268,7 +303,7 @@ __global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int
                     const int j = p0 + dhi;
                     if ((j & 31) == 0 && j > 0) {               // warp-uniform: lanes share j
 #pragma unroll
-                        for (int r = 0; r < 32; r++) {
+                        for (int r = 0; r < R; r++) {
                             const uint32_t hi = tc[r * kBandThreads].y;
                             tc[r * kBandThreads] = make_uint2(hi, 0);
                         }
@@ -276,25 +311,56 @@ __global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int
                         for (int i = 0; i < cnt; i += 4) {
                             const uint32_t w4 = ps.next4();
 #pragma unroll
-                            for (int b = 0; b < 4; b++) {
-                                if (i + b < cnt) {
-                                    const uint32_t ch = (w4 >> (8 * b)) & 0xffu, bit = 1u << (i + b);
-                                    atomicOr(&tc[(ch >> 4) * kBandThreads].y, bit);
-                                    atomicOr(&tc[(16 + (ch & 15)) * kBandThreads].y, bit);
-                                }
-                            }
+                            for (int b = 0; b < 4; b++)
+                                if (i + b < cnt) enter((w4 >> (8 * b)) & 0xffu, 32 + i + b);
                         }
                         next_pos += cnt > 0 ? cnt : 0;
                     }
-                    const uint2 h = tc[(c >> 4) * kBandThreads], l = tc[(16 + (c & 15)) * kBandThreads];
-                    return __funnelshift_r(h.x & l.x, h.y & l.y, (uint32_t)(j & 31));
+                    const uint2 x = rowbits(c);
+                    return __funnelshift_r(x.x, x.y, (uint32_t)(j & 31));
                 };
-                d = band_distance(m, it.txt, n, k, eqw, u, LOG ? &cols : nullptr);
+                d = band_distance(m, it.txt, n, k, eqw, Units{1u, 2u}, LOG ? &cols : nullptr);
             }
             store1(out, dtype, it.idx, d);
             if (LOG) exit_log[it.idx] = cols;
         }
     }
+}
+
+// Bytes present in the strings of A and B (each over its own offset range):
+// 16-byte aligned loads, a block-wide bitmap in shared memory set at a
+// byte's first sighting in the block, OR-ed into `mask` (8 words, zero
+// before the launch).
+__device__ __forceinline__ void presence_scan(const DevStrings &S, uint32_t *s_m) {
+    if (S.n <= 0) return;
+    int64_t lo = S.off[0] - S.base, hi = S.off[S.n] - S.base;
+    lo = lo < 0 ? 0 : (lo > S.bytes ? S.bytes : lo);
+    hi = hi < lo ? lo : (hi > S.bytes ? S.bytes : hi);
+    const int64_t a0 = lo & ~int64_t(15);
+    const uint4 *v = reinterpret_cast<const uint4 *>(S.buf + a0);   // buf is 16-byte aligned, 16 bytes of slack
+    const int64_t nv = (hi - a0 + 15) >> 4;
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < nv; x += (int64_t)gridDim.x * blockDim.x) {
+        const uint4 q = __ldg(v + x);
+        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+        const int64_t p0 = a0 + 16 * x;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const int64_t p = p0 + i;
+            if (p < lo || p >= hi) continue;
+            const uint32_t c = (w[i >> 2] >> (8 * (i & 3))) & 0xffu, bit = 1u << (c & 31);
+            if (!(s_m[c >> 5] & bit)) atomicOr(&s_m[c >> 5], bit);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_byte_presence(DevStrings A, DevStrings B, uint32_t *mask) {
+    __shared__ uint32_t s_m[8];
+    if (threadIdx.x < 8) s_m[threadIdx.x] = 0;
+    __syncthreads();
+    presence_scan(A, s_m);
+    presence_scan(B, s_m);
+    __syncthreads();
+    if (threadIdx.x < 8 && s_m[threadIdx.x]) atomicOr(mask + threadIdx.x, s_m[threadIdx.x]);
 }
 
 // ------------------------------------------------------------- launchers --
@@ -317,18 +383,46 @@ cudaError_t launch_order(cudaStream_t st, int sms, const PairsPlan &plan) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_solve_band(cudaStream_t st, int sms, int ctas_per_sm, const PairsPlan &plan, int k, int dtype,
-                              void *out, int32_t *exit_log) {
-    // 64 KB of nibble rows per CTA: at most three CTAs per SM
-    const int grid = sms * (ctas_per_sm < 1 ? 1 : (ctas_per_sm > 3 ? 3 : ctas_per_sm));
-    const size_t smem = sizeof(uint2) * 32 * kBandThreads;
-    if (exit_log) {
-        cudaFuncSetAttribute(k_solve_band<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_solve_band<true><<<grid, kBandThreads, smem, st>>>(plan, k, dtype, out, exit_log, 1u);
-    } else {
-        cudaFuncSetAttribute(k_solve_band<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_solve_band<false><<<grid, kBandThreads, smem, st>>>(plan, k, dtype, out, nullptr, 1u);
+template <bool LOG, bool SYM>
+static cudaError_t launch_band_v(cudaStream_t st, int sms, int ctas_per_sm, const PairsPlan &plan, int k, int dtype,
+                                 void *out, int32_t *exit_log, const uint32_t *alpha) {
+    const size_t smem = sizeof(uint2) * (SYM ? kSymRows : 32) * kBandThreads;
+    cudaFuncSetAttribute(k_solve_band<LOG, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = ctas_per_sm;
+    if (SYM) {                                           // as many CTAs as fit: the point of the small rows
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_band<LOG, SYM>, kBandThreads, smem) !=
+                cudaSuccess || per_sm < 1)
+            per_sm = 1;
+    } else {                                             // 64 KB of nibble rows per CTA: at most three per SM
+        per_sm = per_sm < 1 ? 1 : (per_sm > 3 ? 3 : per_sm);
     }
+    k_solve_band<LOG, SYM><<<sms * per_sm, kBandThreads, smem, st>>>(plan, k, dtype, out, exit_log, alpha);
+    return cudaGetLastError();
+}
+
+// variant: 1 = one row per byte (the set's alphabet fits; `alpha` its bytes),
+// 0 = nibble rows, -1 = unknown: both launch and the alphabet in `alpha`
+// (computed on the stream before) picks the one that runs.
+cudaError_t launch_solve_band(cudaStream_t st, int sms, int ctas_per_sm, const PairsPlan &plan, int k, int dtype,
+                              void *out, int32_t *exit_log, int variant, const uint32_t *alpha) {
+    cudaError_t e = cudaSuccess;
+    if (variant != 0) {
+        e = exit_log ? launch_band_v<true, true>(st, sms, ctas_per_sm, plan, k, dtype, out, exit_log, alpha)
+                     : launch_band_v<false, true>(st, sms, ctas_per_sm, plan, k, dtype, out, exit_log, alpha);
+        if (e != cudaSuccess) return e;
+    }
+    if (variant != 1) {
+        const uint32_t *a = variant < 0 ? alpha : nullptr;
+        e = exit_log ? launch_band_v<true, false>(st, sms, ctas_per_sm, plan, k, dtype, out, exit_log, a)
+                     : launch_band_v<false, false>(st, sms, ctas_per_sm, plan, k, dtype, out, exit_log, a);
+    }
+    return e;
+}
+
+cudaError_t launch_byte_presence(cudaStream_t st, int sms, const DevStrings &A, const DevStrings &B, uint32_t *mask) {
+    const int64_t bytes = std::max<int64_t>(A.n > 0 ? 1 : 0, (A.bytes + B.bytes) / 16);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((bytes + 255) / 256, (int64_t)sms * 8));
+    k_byte_presence<<<grid, 256, 0, st>>>(A, B, mask);
     return cudaGetLastError();
 }
 
