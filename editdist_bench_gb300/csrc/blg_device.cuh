@@ -220,23 +220,18 @@ BLG_HD BandState band_start(const BandGeom &bg) {
     return s;
 }
 
-// Text columns s.j .. j_end - 1. text(j) returns text byte j (called once per
-// j in order); eqw(c, p0) returns the window's match bits for byte c, where
-// p0 is the 0-based pattern index of window bit 0 (positions < 0 or >= m
-// give no bits). Returns true when the exit fired (s.j = that column);
-// otherwise s holds the state before column j_end.
+// Text columns s.j .. j_end - 1; s.j is 0 or a multiple of 4. text(j)
+// returns text byte j (called once per j in order); eqw(c, p0) returns the
+// window's match bits for byte c, where p0 is the 0-based pattern index of
+// window bit 0 (positions < 0 or >= m give no bits). Returns true when the
+// exit fired (s.j = that column); otherwise s holds the state before column
+// j_end. The exit test runs before every 4th column; the main loop takes 4
+// columns per iteration, so the readers' per-column alignment tests fold.
 template <typename TextFn, typename EqW>
 BLG_HD bool band_steps(int k, const BandGeom &bg, BandState &s, int j_end, TextFn text, EqW eqw) {
     uint32_t pv = s.pv, mv = s.mv;
     int A = s.A;
-    for (int j = s.j; j < j_end; j++) {
-        if ((j & 3) == 0 && j > 0 && A - popc32(mv & bg.band) > k) {   // every band cell > k
-            s.pv = pv;
-            s.mv = mv;
-            s.A = A;
-            s.j = j;
-            return true;
-        }
+    auto column = [&](int j) {
         const uint32_t c = text(j);
         // column j's deltas re-indexed one row down; the new bottom row enters with +1
         // (plain shifts and add: the IMAD forms of the 32-bit step measured
@@ -253,11 +248,35 @@ BLG_HD bool band_steps(int k, const BandGeom &bg, BandState &s, int j_end, TextF
         pv = mhs | ~(xv | phs);
         mv = phs & xv;
         A += 1 + (int)(pv & 1u) - (int)(mv & 1u);
+    };
+    auto stop = [&](int j) {
+        s.pv = pv;
+        s.mv = mv;
+        s.A = A;
+        s.j = j;
+    };
+    int j = s.j;
+    for (; j + 4 <= j_end; j += 4) {
+#if defined(__CUDA_ARCH__)
+        __builtin_assume((j & 3) == 0);
+#endif
+        if (j > 0 && A - popc32(mv & bg.band) > k) {          // every band cell > k
+            stop(j);
+            return true;
+        }
+        column(j);
+        column(j + 1);
+        column(j + 2);
+        column(j + 3);
     }
-    s.pv = pv;
-    s.mv = mv;
-    s.A = A;
-    s.j = j_end;
+    for (; j < j_end; j++) {
+        if ((j & 3) == 0 && j > 0 && A - popc32(mv & bg.band) > k) {
+            stop(j);
+            return true;
+        }
+        column(j);
+    }
+    stop(j_end);
     return false;
 }
 
