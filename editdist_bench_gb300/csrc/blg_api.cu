@@ -59,7 +59,7 @@ int64_t match_blocks(int64_t n);
 cudaError_t launch_pack_nibbles(cudaStream_t st, int sms, const uint8_t *src, int64_t e0, int64_t e1, uint8_t *dst);
 cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, const DevStrings &A,
                               const DevStrings &B, int tile_pairs, int k, int dtype, void *out, const LongQueue &q,
-                              uint32_t *status, int32_t wait_polls, bool trusted);
+                              uint32_t *status, int32_t wait_polls, bool trusted, int variant, const uint32_t *alpha);
 cudaError_t launch_pairs_prep(cudaStream_t st, int grid, bool hask, bool feat, bool band, const DevStrings &A,
                               const DevStrings &B, int k, int dtype, void *out, const PairsPlan &plan,
                               bool lengap_key, uint32_t *status);
@@ -527,6 +527,24 @@ static PairsPlan plan_view(blg_pairs *p) {
     return pl;
 }
 
+// The row layout of the pairs kernels for strings A, B of set p: 1 = one
+// row per byte, 0 = nibble rows, from the alphabet a resident set's upload
+// found; -1 = unknown: the bytes of A and B are scanned into p->d_alpha on
+// the stream and both variants launch, the one that does not apply
+// returning at once.
+static int pairs_alphabet(blg_ctx *c, blg_pairs *p, const DevStrings &A, const DevStrings &B, int *variant) {
+    if (!p->d_alpha) CK(dev_alloc(c, (void **)&p->d_alpha, 8 * sizeof(uint32_t)), "cudaMallocAsync(alphabet)");
+    if (p->nsym >= 0) {
+        *variant = p->nsym <= kBandSymbols ? 1 : 0;
+        return BLG_OK;
+    }
+    *variant = -1;
+    CK(cudaMemsetAsync(p->d_alpha, 0, 8 * sizeof(uint32_t), c->stream), "reset alphabet");
+    CK(launch(c, "byte_presence", [&] { return launch_byte_presence(c->stream, c->sms, A, B, p->d_alpha); }),
+       "byte_presence");
+    return BLG_OK;
+}
+
 // prep -> order -> solve (every schedule but PLAIN). exit_log (optional,
 // device int32[n]) receives the columns each pair's column loop processed.
 static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, const DevStrings &A, const DevStrings &B, int k,
@@ -552,17 +570,9 @@ static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, const DevStrings &A, co
     bool any_long = false;
     for (int j = 1; j < kPairClasses; j++) any_long |= p->pcap[j] > 0;
     if (band) {
-        // a resident set's alphabet is known from its upload; a pipeline chunk's
-        // is scanned on the stream and both variants launch (one returns at once)
-        if (!p->d_alpha) CK(dev_alloc(c, (void **)&p->d_alpha, 8 * sizeof(uint32_t)), "cudaMallocAsync(alphabet)");
         int variant = -1;
-        if (p->nsym >= 0) {
-            variant = p->nsym <= kBandSymbols ? 1 : 0;
-        } else {
-            CK(cudaMemsetAsync(p->d_alpha, 0, 8 * sizeof(uint32_t), c->stream), "reset alphabet");
-            CK(launch(c, "byte_presence", [&] { return launch_byte_presence(c->stream, c->sms, A, B, p->d_alpha); }),
-               "byte_presence");
-        }
+        rc = pairs_alphabet(c, p, A, B, &variant);
+        if (rc) return rc;
         CK(launch(c, "pairs_band", [&] {
                return launch_solve_band(c->stream, c->sms, c->tune.band_ctas, plan, k, dtype, d_out, exit_log, variant,
                                         p->d_alpha);
@@ -599,13 +609,16 @@ static int pairs_run_direct(blg_ctx *c, blg_pairs *p, const DevStrings &A, const
     if (total > 0)
         CK(cudaMemsetAsync(p->q_ctr, 0, sizeof(int32_t) * 2 * kLongClasses, c->stream), "reset queue");
     if (use_tile) {
-        // 512 pairs per tile while each side averages <= 33 bytes; longer
+        // 512 pairs per tile while each side averages <= 32 bytes; longer
         // strings get smaller tiles so a tile's span still fits the stage
         const double avg = (double)p->len_max_side / (double)p->n;
-        const int tile = avg <= 33.0 ? 512 : std::max(32, (int)(17000.0 / avg) & ~31);
+        const int tile = avg <= 32.0 ? 512 : std::max(32, (int)(16384.0 / avg) & ~31);
+        int variant = -1;
+        int rc = pairs_alphabet(c, p, A, B, &variant);
+        if (rc) return rc;
         CK(launch(c, "pairs_tile", [&] {
                return launch_pairs_tile(c->stream, c->sms, c->tune.tile_buffers, hask, A, B, tile, k, dtype, d_out, q,
-                                        c->d_status, c->fault_wait_polls, p->trusted);
+                                        c->d_status, c->fault_wait_polls, p->trusted, variant, p->d_alpha);
            }), "pairs_tile");
     } else {
         CK(launch(c, "pairs_staged", [&] {

@@ -107,6 +107,11 @@ struct SearchClass {
     const uint64_t *peq;    // device: [nq][256][nw] Peq tables
 };
 
+// Pair sets using at most kBandSymbols distinct bytes run the pairs kernels'
+// one-row-per-byte pattern tables (row kBandSymbols stays empty for the
+// bytes outside the set); larger alphabets use nibble rows.
+constexpr int kBandSymbols = 15;
+
 // Query word classes of the sequential search kernels (patterns of 1..8
 // 64-bit words); longer queries run lane-spread. A thresholded run plans and
 // solves the survivors of all its sequential classes in one launch each.

@@ -87,6 +87,28 @@ __device__ __forceinline__ const uint8_t *string_at(const DevStrings &S, int64_t
     return S.buf + (o0 - S.base);
 }
 
+// ------------------------------------------------------- byte alphabets --
+// A set's bytes as an 8-word presence bitmap (k_byte_presence): its size,
+// and the byte -> row map of the one-row-per-byte pattern tables (bytes in
+// increasing order get rows 0, 1, ...; the rest row kBandSymbols). The map
+// is built by the whole block into shared memory.
+__device__ __forceinline__ int alpha_size(const uint32_t *alpha) {
+    int total = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) total += __popc(__ldg(alpha + i));
+    return total;
+}
+
+__device__ __forceinline__ void alpha_map(const uint32_t *alpha, uint8_t *map) {
+    for (int b = threadIdx.x; b < 256; b += blockDim.x) {
+        const uint32_t w = __ldg(alpha + (b >> 5));
+        int rank = __popc(w & ((1u << (b & 31)) - 1u));
+        for (int i = 0; i < (b >> 5); i++) rank += __popc(__ldg(alpha + i));
+        map[b] = (uint8_t)(((w >> (b & 31)) & 1u) ? rank : kBandSymbols);
+    }
+    __syncthreads();
+}
+
 // --------------------------------------------------------------- stores --
 __device__ __forceinline__ void store1(void *out, int dtype, int64_t i, int d) {
     if (dtype == DT_UINT8) reinterpret_cast<uint8_t *>(out)[i] = (uint8_t)saturate_u8(d);

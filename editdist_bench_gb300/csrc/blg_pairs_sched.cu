@@ -233,20 +233,8 @@ __global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int
     constexpr int R = SYM ? kSymRows : 32;
     extern __shared__ uint2 s_rows2[];                      // [R rows][kBandThreads] 64-bit rows
     __shared__ uint8_t s_map[256];                          // byte -> row (SYM)
-    if (alpha) {
-        int total = 0;
-#pragma unroll
-        for (int i = 0; i < 8; i++) total += __popc(__ldg(alpha + i));
-        if ((total <= kBandSymbols) != SYM) return;         // uniform: the other variant runs the set
-    }
-    if (SYM) {
-        const int b = threadIdx.x;                          // kBandThreads == 256: one byte per thread
-        const uint32_t w = __ldg(alpha + (b >> 5));
-        int rank = __popc(w & ((1u << (b & 31)) - 1u));
-        for (int i = 0; i < (b >> 5); i++) rank += __popc(__ldg(alpha + i));
-        s_map[b] = (uint8_t)(((w >> (b & 31)) & 1u) ? rank : kSymRows - 1);
-        __syncthreads();
-    }
+    if (alpha && (alpha_size(alpha) <= kBandSymbols) != SYM) return;   // uniform: the other variant runs the set
+    if (SYM) alpha_map(alpha, s_map);
     uint2 *tc = s_rows2 + threadIdx.x;                      // row r at tc[r * kBandThreads]
     const int lane = threadIdx.x & 31;
     // pattern byte c at window bit `bitpos` of the block (0..63)

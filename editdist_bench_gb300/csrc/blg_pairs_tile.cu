@@ -19,9 +19,10 @@
 //     lane-spread consumer, the rest listed with their trimmed column count;
 //  3. a counting sort of the listed pairs by column count inside the CTA, so
 //     each warp takes 32 pairs of nearly equal work;
-//  4. solve: one 32-bit Myers/Hyyro word per pair, Eq from per-thread nibble
-//     tables, the final score read from the last column's vertical deltas
-//     (D[m][n] = n + popc(Pv) - popc(Mv) over the pattern rows);
+//  4. solve: one 32-bit Myers/Hyyro word per pair, Eq from per-thread rows
+//     (one per byte when the pair set uses at most 15 distinct bytes, else
+//     nibble rows), the final score read from the last column's vertical
+//     deltas (D[m][n] = n + popc(Pv) - popc(Mv) over the pattern rows);
 //  5. the tile's results leave as coalesced vector stores.
 #include <algorithm>
 
@@ -32,18 +33,19 @@ namespace blg {
 
 constexpr int kTileThreads = 256;
 constexpr int kTileMaxPairs = 512;
-constexpr int kTileCap = 17408;                  // rounded span bytes staged per side
+constexpr int kTileCap = 16896;                  // rounded span bytes staged per side (512 pairs of <= 33)
 constexpr int kTileSide = kTileCap + 48;         // 16 bytes of slack before, 32 after
 constexpr int kTileKeys = 64;                    // counting-sort keys: min(columns, 63)
 constexpr int32_t kNoStore = INT32_MIN;          // result slot filled by the long-pair consumer
 
 // NBUF = 2: the next tile's copy flies while this one computes (2 CTAs per
 // SM); NBUF = 1: one stage, the copy is issued when the tile is done and the
-// other CTAs of the SM (3 per SM) compute meanwhile.
-template <int NBUF>
+// other CTAs of the SM (3 per SM, 4 with one row per byte) compute meanwhile.
+template <int NBUF, bool SYM>
 struct __align__(16) TileShared {
     uint8_t stage[NBUF][2][kTileSide];            // [buffer][a|b]
-    uint32_t tab[32 * kTileThreads];              // nibble tables, row r of thread t at [r*256 + t]
+    uint32_t tab[(SYM ? 16 : 32) * kTileThreads]; // pattern rows, row r of thread t at [r*256 + t]
+    uint8_t map[SYM ? 256 : 4];                   // byte -> row (SYM)
     uint2 ent[kTileMaxPairs];                     // sorted work list
     int32_t res[kTileMaxPairs];
     int32_t hist[kTileKeys];
@@ -67,11 +69,49 @@ __device__ __forceinline__ void step32(uint32_t &pv, uint32_t &mv, uint32_t eq, 
     mv = phs & xv;
 }
 
-// Nibble tables of a pattern of m <= 32 bytes: row h (0..15) holds the
-// positions whose high nibble is h, row 16 + l those whose low nibble is l;
-// Eq(c) = row[c >> 4] & row[16 + (c & 15)].
-template <typename L>
-__device__ __forceinline__ void nib32_set(uint32_t *tc, const uint8_t *p, int m, bool set) {
+// Per-thread rows of a pattern of m <= 32 bytes (bit i <-> position i), in a
+// [row][thread] table. SYM = false: nibble rows, row h (0..15) holds the
+// positions whose high nibble is h, row 16 + l those whose low nibble is l,
+// Eq(c) = row[c >> 4] & row[16 + (c & 15)]. SYM = true: the pair set uses at
+// most 15 distinct bytes and row map[c] holds the positions of byte c (the
+// bytes outside the set map to row 15, which stays empty): one row update
+// per pattern byte, one row load per text column, half the table.
+template <bool SYM>
+struct Rows32 {
+    static constexpr int R = SYM ? 16 : 32;
+    uint32_t *tc;                                  // this thread's row 0
+    const uint8_t *map;
+    // position bit of byte c (one shared-memory atomic OR per row update
+    // instead of a load-or-store chain)
+    __device__ __forceinline__ void set(uint32_t c, uint32_t bit) const {
+        if (SYM) {
+            atomicOr(tc + map[c] * kTileThreads, bit);
+        } else {
+            atomicOr(tc + (c >> 4) * kTileThreads, bit);
+            atomicOr(tc + (16 + (c & 15)) * kTileThreads, bit);
+        }
+    }
+    __device__ __forceinline__ void clear_byte(uint32_t c) const {
+        if (SYM) {
+            tc[map[c] * kTileThreads] = 0;
+        } else {
+            tc[(c >> 4) * kTileThreads] = 0;
+            tc[(16 + (c & 15)) * kTileThreads] = 0;
+        }
+    }
+    __device__ __forceinline__ void clear_all() const {
+#pragma unroll
+        for (int r = 0; r < R; r++) tc[r * kTileThreads] = 0;
+    }
+    __device__ __forceinline__ uint32_t eq(uint32_t c) const {
+        if (SYM) return tc[map[c] * kTileThreads];
+        return tc[(c >> 4) * kTileThreads] & tc[(16 + (c & 15)) * kTileThreads];
+    }
+};
+
+// Rows of a pattern read through loader L: set, or clear the rows it touched.
+template <typename L, bool SYM>
+__device__ __forceinline__ void rows_pattern(const Rows32<SYM> &rw, const uint8_t *p, int m, bool set) {
     TextScanT<L> ps;
     ps.init(p);
     for (int i = 0; i < m; i += 4) {
@@ -80,22 +120,11 @@ __device__ __forceinline__ void nib32_set(uint32_t *tc, const uint8_t *p, int m,
         for (int b = 0; b < 4; b++) {
             if (i + b < m) {
                 const uint32_t c = (w4 >> (8 * b)) & 0xffu;
-                uint32_t *h = tc + (c >> 4) * kTileThreads, *l = tc + (16 + (c & 15)) * kTileThreads;
-                if (set) {
-                    const uint32_t bit = 1u << (i + b);
-                    *h |= bit;
-                    *l |= bit;
-                } else {
-                    *h = 0;
-                    *l = 0;
-                }
+                if (set) rw.set(c, 1u << (i + b));
+                else rw.clear_byte(c);
             }
         }
     }
-}
-
-__device__ __forceinline__ uint32_t nib32_eq(const uint32_t *tc, uint32_t c) {
-    return tc[(c >> 4) * kTileThreads] & tc[(16 + (c & 15)) * kTileThreads];
 }
 
 // ---- strings in the stage, addressed by byte offset from its 16-byte-aligned
@@ -168,14 +197,13 @@ __device__ __forceinline__ void stage_trim(const uint8_t *base, uint32_t &oa, in
     lb -= p + s;
 }
 
-// Nibble tables of a staged pattern: set its rows (one shared-memory atomic
-// OR per row update instead of a load-or-store chain), or clear them: all 32
-// rows with plain stores once the pattern has more than 4 bytes, else just
-// the rows it touched.
-__device__ __forceinline__ void stage_nib(uint32_t *tc, const uint8_t *base, uint32_t op, int m, bool set) {
-    if (!set && m > 4) {
-#pragma unroll
-        for (int r = 0; r < 32; r++) tc[r * kTileThreads] = 0;
+// Rows of a staged pattern: set them, or clear them: all rows with plain
+// stores once the pattern touches more rows than that, else just the rows it
+// touched.
+template <bool SYM>
+__device__ __forceinline__ void stage_rows(const Rows32<SYM> &rw, const uint8_t *base, uint32_t op, int m, bool set) {
+    if (!set && m > Rows32<SYM>::R / 8) {
+        rw.clear_all();
         return;
     }
     StageScan ps;
@@ -186,25 +214,18 @@ __device__ __forceinline__ void stage_nib(uint32_t *tc, const uint8_t *base, uin
         for (int b = 0; b < 4; b++) {
             if (i + b < m) {
                 const uint32_t c = (w4 >> (8 * b)) & 0xffu;
-                uint32_t *h = tc + (c >> 4) * kTileThreads, *l = tc + (16 + (c & 15)) * kTileThreads;
-                if (set) {
-                    const uint32_t bit = 1u << (i + b);
-                    atomicOr(h, bit);
-                    atomicOr(l, bit);
-                } else {
-                    *h = 0;
-                    *l = 0;
-                }
+                if (set) rw.set(c, 1u << (i + b));
+                else rw.clear_byte(c);
             }
         }
     }
 }
 
 // solve32 for a staged pair (pattern at op, text at ot).
-template <bool HASK>
-__device__ __forceinline__ int stage_solve32(uint32_t *tc, const uint8_t *base, uint32_t op, int m, uint32_t ot,
+template <bool HASK, bool SYM>
+__device__ __forceinline__ int stage_solve32(const Rows32<SYM> &rw, const uint8_t *base, uint32_t op, int m, uint32_t ot,
                                              int n, int k, Units u) {
-    stage_nib(tc, base, op, m, true);
+    stage_rows(rw, base, op, m, true);
     const uint32_t M = m >= 32 ? 0xffffffffu : ((1u << m) - 1u);
     uint32_t pv = 0xffffffffu, mv = 0;
     StageScan ts;
@@ -213,10 +234,10 @@ __device__ __forceinline__ int stage_solve32(uint32_t *tc, const uint8_t *base, 
     int j = 0;
     for (; j + 4 <= n; j += 4) {
         const uint32_t w4 = ts.next4();
-        step32(pv, mv, nib32_eq(tc, w4 & 0xffu), u);
-        step32(pv, mv, nib32_eq(tc, (w4 >> 8) & 0xffu), u);
-        step32(pv, mv, nib32_eq(tc, (w4 >> 16) & 0xffu), u);
-        step32(pv, mv, nib32_eq(tc, w4 >> 24), u);
+        step32(pv, mv, rw.eq(w4 & 0xffu), u);
+        step32(pv, mv, rw.eq((w4 >> 8) & 0xffu), u);
+        step32(pv, mv, rw.eq((w4 >> 16) & 0xffu), u);
+        step32(pv, mv, rw.eq(w4 >> 24), u);
         if (HASK && hopeless(j + 4 + popc32(pv & M) - popc32(mv & M), j + 3, n, k)) {
             dead = true;
             break;
@@ -224,19 +245,19 @@ __device__ __forceinline__ int stage_solve32(uint32_t *tc, const uint8_t *base, 
     }
     if (!dead && j < n) {
         uint32_t w4 = ts.next4();
-        for (; j < n; j++, w4 >>= 8) step32(pv, mv, nib32_eq(tc, w4 & 0xffu), u);
+        for (; j < n; j++, w4 >>= 8) step32(pv, mv, rw.eq(w4 & 0xffu), u);
     }
-    stage_nib(tc, base, op, m, false);
+    stage_rows(rw, base, op, m, false);
     if (dead) return k + 1;
     const int d = n + popc32(pv & M) - popc32(mv & M);
     return HASK ? cap_k(d, k) : d;
 }
 
 // d(p, t) for 1 <= m <= 32, m <= n; min(d, k+1) when HASK.
-template <bool HASK, typename L>
-__device__ __forceinline__ int solve32(uint32_t *tc, const uint8_t *p, int m, const uint8_t *t, int n, int k,
+template <bool HASK, typename L, bool SYM>
+__device__ __forceinline__ int solve32(const Rows32<SYM> &rw, const uint8_t *p, int m, const uint8_t *t, int n, int k,
                                        Units u) {
-    nib32_set<L>(tc, p, m, true);
+    rows_pattern<L>(rw, p, m, true);
     const uint32_t M = m >= 32 ? 0xffffffffu : ((1u << m) - 1u);
     uint32_t pv = 0xffffffffu, mv = 0;
     TextScanT<L> ts;
@@ -245,10 +266,10 @@ __device__ __forceinline__ int solve32(uint32_t *tc, const uint8_t *p, int m, co
     int j = 0;
     for (; j + 4 <= n; j += 4) {
         const uint32_t w4 = ts.next4();
-        step32(pv, mv, nib32_eq(tc, w4 & 0xffu), u);
-        step32(pv, mv, nib32_eq(tc, (w4 >> 8) & 0xffu), u);
-        step32(pv, mv, nib32_eq(tc, (w4 >> 16) & 0xffu), u);
-        step32(pv, mv, nib32_eq(tc, w4 >> 24), u);
+        step32(pv, mv, rw.eq(w4 & 0xffu), u);
+        step32(pv, mv, rw.eq((w4 >> 8) & 0xffu), u);
+        step32(pv, mv, rw.eq((w4 >> 16) & 0xffu), u);
+        step32(pv, mv, rw.eq(w4 >> 24), u);
         // D[m][j+4] from the vertical deltas; the exit test is monotone in j,
         // so testing every 4th column is exact (csrc/myers.c:101-106)
         if (HASK && hopeless(j + 4 + popc32(pv & M) - popc32(mv & M), j + 3, n, k)) {
@@ -258,9 +279,9 @@ __device__ __forceinline__ int solve32(uint32_t *tc, const uint8_t *p, int m, co
     }
     if (!dead && j < n) {
         uint32_t w4 = ts.next4();
-        for (; j < n; j++, w4 >>= 8) step32(pv, mv, nib32_eq(tc, w4 & 0xffu), u);
+        for (; j < n; j++, w4 >>= 8) step32(pv, mv, rw.eq(w4 & 0xffu), u);
     }
-    nib32_set<L>(tc, p, m, false);
+    rows_pattern<L>(rw, p, m, false);
     if (dead) return k + 1;
     const int d = n + popc32(pv & M) - popc32(mv & M);
     return HASK ? cap_k(d, k) : d;
@@ -320,20 +341,24 @@ __device__ __forceinline__ void load_offs(PairOffs &o, const DevStrings &A, cons
     }
 }
 
-template <bool HASK, int NBUF, bool TRUST>
-__global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : 3)
+// alpha: the pair set's bytes (8 words; SYM builds its byte -> row map from
+// them), or null when the host chose the variant. Given to both variants,
+// the one that does not apply returns at once.
+template <bool HASK, int NBUF, bool TRUST, bool SYM>
+__global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : (SYM ? 4 : 3))
     k_pairs_tile(DevStrings A, DevStrings B, int P, int k, int dtype, void *out, LongQueue q, uint32_t *status,
-                 uint32_t unit, uint32_t wait_polls) {
+                 uint32_t unit, uint32_t wait_polls, const uint32_t *alpha) {
     extern __shared__ __align__(128) uint8_t s_raw[];
-    TileShared<NBUF> &S = *reinterpret_cast<TileShared<NBUF> *>(s_raw);
+    TileShared<NBUF, SYM> &S = *reinterpret_cast<TileShared<NBUF, SYM> *>(s_raw);
     const Units u{unit, unit + unit};
     const int tid = threadIdx.x;
+    if (alpha && (alpha_size(alpha) <= kBandSymbols) != SYM) return;   // uniform: the other variant runs the set
+    if (SYM) alpha_map(alpha, S.map);
     const int64_t n = A.n;
     const int64_t ntiles = (n + P - 1) / P;
     const int64_t G = gridDim.x;
-    uint32_t *tc = S.tab + tid;
-#pragma unroll
-    for (int r = 0; r < 32; r++) tc[r * kTileThreads] = 0;
+    const Rows32<SYM> rw{S.tab + tid, S.map};
+    rw.clear_all();
     if (tid < kTileKeys) S.hist[tid] = 0;
     if (tid == 0) {
         mbar_init(&S.bar[0], 1);
@@ -449,7 +474,7 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : 3)
                 rank = atomicAdd(&S.hist[key], 1);
                 ent = make_uint2(oa | (ob << 16), (uint32_t)lb | ((uint32_t)la << 16) | ((uint32_t)j << 22));
             } else {
-                d = solve32<HASK, GenericLoad>(tc, a, la, b, lb, k, u);   // not staged: read in place
+                d = solve32<HASK, GenericLoad>(rw, a, la, b, lb, k, u);   // not staged: read in place
             }
             S.res[j] = d;
         };
@@ -494,7 +519,7 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : 3)
             if (e < total) {
                 const uint2 E = S.ent[e];
                 const int m = (int)((E.y >> 16) & 63u), nn = (int)(E.y & 0xffffu), j = (int)(E.y >> 22);
-                S.res[j] = stage_solve32<HASK>(tc, stage, E.x & 0xffffu, m, E.x >> 16, nn, k, u);
+                S.res[j] = stage_solve32<HASK>(rw, stage, E.x & 0xffffu, m, E.x >> 16, nn, k, u);
             }
         }
         __syncthreads();
@@ -522,29 +547,48 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : 3)
 }
 
 // ------------------------------------------------------------- launcher --
-template <bool HASK, int NBUF, bool TRUST>
+template <bool HASK, int NBUF, bool TRUST, bool SYM>
 static cudaError_t launch_tile(cudaStream_t st, int sms, const DevStrings &A, const DevStrings &B, int P, int k,
-                               int dtype, void *out, const LongQueue &q, uint32_t *status, uint32_t polls) {
+                               int dtype, void *out, const LongQueue &q, uint32_t *status, uint32_t polls,
+                               const uint32_t *alpha) {
     const int64_t ntiles = (A.n + P - 1) / P;
-    const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sms * (NBUF == 2 ? 2 : 3));
-    const size_t smem = sizeof(TileShared<NBUF>);
-    cudaFuncSetAttribute(k_pairs_tile<HASK, NBUF, TRUST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_pairs_tile<HASK, NBUF, TRUST><<<grid, kTileThreads, smem, st>>>(A, B, P, k, dtype, out, q, status, 1u, polls);
+    const int per_sm = NBUF == 2 ? 2 : (SYM ? 4 : 3);
+    const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sms * per_sm);
+    const size_t smem = sizeof(TileShared<NBUF, SYM>);
+    cudaFuncSetAttribute(k_pairs_tile<HASK, NBUF, TRUST, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_pairs_tile<HASK, NBUF, TRUST, SYM><<<grid, kTileThreads, smem, st>>>(A, B, P, k, dtype, out, q, status, 1u, polls,
+                                                                          alpha);
     return cudaGetLastError();
 }
 
+// variant: 1 = one row per byte (alpha: the set's bytes), 0 = nibble rows,
+// -1 = both launch and alpha, computed on the stream before, picks.
+template <bool HASK, int NBUF, bool TRUST>
+static cudaError_t launch_tile_v(int variant, const uint32_t *alpha, cudaStream_t st, int sms, const DevStrings &A,
+                                 const DevStrings &B, int P, int k, int dtype, void *out, const LongQueue &q,
+                                 uint32_t *status, uint32_t polls) {
+    cudaError_t e = cudaSuccess;
+    if (variant != 0)
+        e = launch_tile<HASK, NBUF, TRUST, true>(st, sms, A, B, P, k, dtype, out, q, status, polls, alpha);
+    if (e == cudaSuccess && variant != 1)
+        e = launch_tile<HASK, NBUF, TRUST, false>(st, sms, A, B, P, k, dtype, out, q, status, polls,
+                                                  variant < 0 ? alpha : nullptr);
+    return e;
+}
+
 template <bool HASK, int NBUF>
-static cudaError_t launch_tile_t(bool trusted, cudaStream_t st, int sms, const DevStrings &A, const DevStrings &B,
-                                 int P, int k, int dtype, void *out, const LongQueue &q, uint32_t *status,
-                                 uint32_t polls) {
-    return trusted ? launch_tile<HASK, NBUF, true>(st, sms, A, B, P, k, dtype, out, q, status, polls)
-                   : launch_tile<HASK, NBUF, false>(st, sms, A, B, P, k, dtype, out, q, status, polls);
+static cudaError_t launch_tile_t(bool trusted, int variant, const uint32_t *alpha, cudaStream_t st, int sms,
+                                 const DevStrings &A, const DevStrings &B, int P, int k, int dtype, void *out,
+                                 const LongQueue &q, uint32_t *status, uint32_t polls) {
+    return trusted ? launch_tile_v<HASK, NBUF, true>(variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls)
+                   : launch_tile_v<HASK, NBUF, false>(variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls);
 }
 
 // trusted: the offsets were checked on the host (every pair in order).
+// variant / alpha: the row layout, as for launch_tile_v.
 cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, const DevStrings &A,
                               const DevStrings &B, int tile_pairs, int k, int dtype, void *out, const LongQueue &q,
-                              uint32_t *status, int32_t wait_polls, bool trusted) {
+                              uint32_t *status, int32_t wait_polls, bool trusted, int variant, const uint32_t *alpha) {
     if (A.n <= 0) return cudaSuccess;
     const uint32_t polls = wait_polls < 0 ? kMbarPolls : (uint32_t)wait_polls;
     int P = tile_pairs;
@@ -552,10 +596,10 @@ cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, 
     if (P < 32) P = 32;
     P &= ~3;                                                // 4-aligned tiles keep the vector stores aligned
     if (buffers == 1)
-        return hask ? launch_tile_t<true, 1>(trusted, st, sms, A, B, P, k, dtype, out, q, status, polls)
-                    : launch_tile_t<false, 1>(trusted, st, sms, A, B, P, k, dtype, out, q, status, polls);
-    return hask ? launch_tile_t<true, 2>(trusted, st, sms, A, B, P, k, dtype, out, q, status, polls)
-                : launch_tile_t<false, 2>(trusted, st, sms, A, B, P, k, dtype, out, q, status, polls);
+        return hask ? launch_tile_t<true, 1>(trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls)
+                    : launch_tile_t<false, 1>(trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls);
+    return hask ? launch_tile_t<true, 2>(trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls)
+                : launch_tile_t<false, 2>(trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls);
 }
 
 }  // namespace blg

@@ -10,7 +10,6 @@ namespace blg {
 constexpr int kPairClasses = 6;      // 0: pattern <= 64 (one thread); 1..5: 2..32 lanes
 constexpr int kCostBuckets = 256;    // counting-sort keys (log-spaced cost or predicted work)
 constexpr int kFeatures = 7;         // scheduler network inputs per record
-constexpr int kBandSymbols = 15;     // distinct bytes the banded solver's one-row-per-byte layout takes
 
 // Pairwise plan: records of non-trivial pairs per class, before (raw) and
 // after (sorted, per 1024-record segment) ordering, their keys, optional

@@ -1,10 +1,11 @@
-"""The banded pairs solver (max_dist <= 31) has two row layouts: one row per
-byte when the pair set uses at most 15 distinct bytes, nibble rows
-otherwise. A resident set picks the layout at upload from its bytes; a
-one-call run scans its bytes on the stream and launches both variants, of
-which the one that does not apply returns at once. Every alphabet size
-around the limit (1, 2, 4, 15, 16, 17, 256 bytes), with bytes spread over
-the whole 0..255 range, gives the oracle's results on both routes.
+"""The pairs kernels' pattern rows have two layouts: one row per byte when
+the pair set uses at most 15 distinct bytes, nibble rows otherwise -- in the
+banded solver (max_dist <= 31, any lengths) and in the short-pair tile
+kernel. A resident set picks the layout at upload from its bytes; a one-call
+run scans its bytes on the stream and launches both variants, of which the
+one that does not apply returns at once. Every alphabet size around the
+limit (1, 2, 4, 15, 16, 17, 256 bytes), with bytes spread over the whole
+0..255 range, gives the oracle's results on both routes.
 Reference semantics: csrc/myers.c:101-143 (max_dist exits and caps)."""
 import numpy as np
 import pytest
@@ -46,3 +47,20 @@ def test_band_alphabet_pipelined_chunks(gpu):
     a, b = W.concat(a1, a2), W.concat(b1, b2)
     want = oracle.saturate(oracle.pairs(a, b, 8, threads=16), "uint8")
     np.testing.assert_array_equal(gpu.pairwise_packed(a, b, max_dist=8, dtype="uint8"), want)
+
+
+@pytest.mark.parametrize("size", [1, 4, 15, 16, 256])
+def test_tile_alphabet_sizes(gpu, size):
+    """Short pairs (at most 32 bytes, the tile kernel), exact and thresholded."""
+    rng = np.random.default_rng(980 + size)
+    alphabet = np.sort(rng.choice(256, size, replace=False)).astype(np.uint8)
+    la = rng.integers(0, 33, 30000)
+    a = W.random_strings(rng, la, alphabet)
+    b = W.mutate(rng, a, rng.uniform(0.0, 0.2, 30000), alphabet)
+    for k, dt in ((None, "int32"), (3, "uint8")):
+        want = oracle.saturate(oracle.pairs(a, b, k, threads=8), dt)
+        np.testing.assert_array_equal(gpu.pairwise_packed(a, b, max_dist=k, dtype=dt), want,
+                                      err_msg=f"one-call, {size} bytes, k={k}")
+        batch = gpu.PairsBatch(a, b)
+        out = batch.run(batch.alloc(dt), max_dist=k)
+        np.testing.assert_array_equal(out.get(), want, err_msg=f"resident, {size} bytes, k={k}")
