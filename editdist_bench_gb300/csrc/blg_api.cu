@@ -132,11 +132,11 @@ struct blg_pairs {
     // resident runs as a CUDA graph (pairs_run_graph): the launches of one
     // run, captured once its parameters repeat, replayed while they stay
     struct GraphKey {
-        int k = 0, dtype = -1, sched = -1, learned = 0, band_ctas = 0, tile_buffers = 0;
+        int k = 0, dtype = -1, sched = -1, learned = 0, band_ctas = 0, tile_shape = 0;
         void *out = nullptr;
         bool operator==(const GraphKey &o) const {
             return k == o.k && dtype == o.dtype && sched == o.sched && learned == o.learned &&
-                   band_ctas == o.band_ctas && tile_buffers == o.tile_buffers && out == o.out;
+                   band_ctas == o.band_ctas && tile_shape == o.tile_shape && out == o.out;
         }
     };
     GraphKey g_last;              // parameters of the previous run
@@ -527,6 +527,23 @@ static PairsPlan plan_view(blg_pairs *p) {
     return pl;
 }
 
+// The bytes an uploaded set uses, scanned once (synchronises): p->nsym then
+// picks the pairs kernels' row layout for every run of the set.
+static int pairs_learn_alphabet(blg_ctx *c, blg_pairs *p) {
+    if (p->n <= 0) return BLG_OK;
+    uint32_t alpha[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (!p->d_alpha) CK(dev_alloc(c, (void **)&p->d_alpha, sizeof(alpha)), "cudaMallocAsync(alphabet)");
+    CK(cudaMemsetAsync(p->d_alpha, 0, sizeof(alpha), c->stream), "reset alphabet");
+    CK(launch(c, "byte_presence", [&] { return launch_byte_presence(c->stream, c->sms, p->a.d, p->b.d, p->d_alpha); }),
+       "byte_presence");
+    CK(cudaMemcpyAsync(alpha, p->d_alpha, sizeof(alpha), cudaMemcpyDeviceToHost, c->stream), "D2H alphabet");
+    CK(cudaStreamSynchronize(c->stream), "sync alphabet");
+    int nsym = 0;
+    for (uint32_t w : alpha) nsym += __builtin_popcount(w);
+    p->nsym = nsym;
+    return BLG_OK;
+}
+
 // The row layout of the pairs kernels for strings A, B of set p: 1 = one
 // row per byte, 0 = nibble rows, from the alphabet a resident set's upload
 // found; -1 = unknown: the bytes of A and B are scanned into p->d_alpha on
@@ -617,7 +634,7 @@ static int pairs_run_direct(blg_ctx *c, blg_pairs *p, const DevStrings &A, const
         int rc = pairs_alphabet(c, p, A, B, &variant);
         if (rc) return rc;
         CK(launch(c, "pairs_tile", [&] {
-               return launch_pairs_tile(c->stream, c->sms, c->tune.tile_buffers, hask, A, B, tile, k, dtype, d_out, q,
+               return launch_pairs_tile(c->stream, c->sms, c->tune.tile_shape, hask, A, B, tile, k, dtype, d_out, q,
                                         c->d_status, c->fault_wait_polls, p->trusted, variant, p->d_alpha);
            }), "pairs_tile");
     } else {
@@ -1759,6 +1776,7 @@ static int tune_band_pairs(blg_ctx *c) {
     int rc = pairs_upload(c, a.data(), a.off.data(), b.data(), b.off.data(), a.n(), &p);
     void *out = nullptr;
     if (!rc && dev_alloc(c, &out, (size_t)a.n()) != cudaSuccess) rc = fail(c, BLG_ERR_ALLOC, "tuning output");
+    if (!rc) rc = pairs_learn_alphabet(c, &p);
     const int sched = c->sched;
     c->sched = BLG_SCHED_AUTO;
     float best_ms = 1e30f;
@@ -1789,16 +1807,17 @@ static int tune_tile_pairs(blg_ctx *c) {
     int rc = pairs_upload(c, a.data(), a.off.data(), b.data(), b.off.data(), a.n(), &p);
     void *out = nullptr;
     if (!rc && dev_alloc(c, &out, sizeof(int32_t) * (size_t)a.n()) != cudaSuccess) rc = fail(c, BLG_ERR_ALLOC, "tuning output");
+    if (!rc) rc = pairs_learn_alphabet(c, &p);
     float best_ms = 1e30f;
-    int best = c->tune.tile_buffers;
-    for (int bufs : {1, 2}) {
+    int best = c->tune.tile_shape;
+    for (int shape : {1, 2, 3}) {
         if (rc) break;
-        c->tune.tile_buffers = bufs;
+        c->tune.tile_shape = shape;
         float ms = 0.f;
         rc = time_best(c, 5, [&] { return pairs_run(c, &p, -1, BLG_INT32, out); }, &ms);
-        if (!rc && ms < best_ms) { best_ms = ms; best = bufs; }
+        if (!rc && ms < best_ms) { best_ms = ms; best = shape; }
     }
-    c->tune.tile_buffers = best;
+    c->tune.tile_shape = best;
     dev_free(c, out);
     pairs_release(c, &p);
     return rc;
@@ -1811,7 +1830,7 @@ static std::string tuning_header(blg_ctx *c) {
     std::string name = prop.name;
     for (auto &ch : name)
         if (ch == ' ') ch = '_';
-    return "BLGTUNE5 " + name + " sm" + std::to_string(prop.major * 10 + prop.minor) + " " + std::to_string(c->sms) +
+    return "BLGTUNE6 " + name + " sm" + std::to_string(prop.major * 10 + prop.minor) + " " + std::to_string(c->sms) +
            " " + std::to_string(blg_version());
 }
 
@@ -1834,7 +1853,7 @@ static bool tuning_load(blg_ctx *c, const char *path) {
         else if (k == "lpt_job" && v >= 256 && v <= 4096) { t.lpt_job = v; fields++; }
         else if (k == "surv_round" && (v == 8 || v == 16 || v == 32)) { t.surv_round = v; fields++; }
         else if (k == "band_ctas" && v >= 1 && v <= 3) { t.band_ctas = v; fields++; }
-        else if (k == "tile_buffers" && v >= 1 && v <= 2) { t.tile_buffers = v; fields++; }
+        else if (k == "tile_shape" && v >= 1 && v <= 3) { t.tile_shape = v; fields++; }
     }
     fclose(f);
     if (!ok || fields < 13) return false;
@@ -1848,8 +1867,8 @@ static void tuning_save(blg_ctx *c, const char *path) {
     if (!f) return;
     fprintf(f, "%s\n", tuning_header(c).c_str());
     for (int w = 1; w <= 8; w++) fprintf(f, "qpb%d %d\n", w, c->tune.qpb[w]);
-    fprintf(f, "lpt_ctas %d\nlpt_job %d\nsurv_round %d\nband_ctas %d\ntile_buffers %d\n", c->tune.lpt_ctas,
-            c->tune.lpt_job, c->tune.surv_round, c->tune.band_ctas, c->tune.tile_buffers);
+    fprintf(f, "lpt_ctas %d\nlpt_job %d\nsurv_round %d\nband_ctas %d\ntile_shape %d\n", c->tune.lpt_ctas,
+            c->tune.lpt_job, c->tune.surv_round, c->tune.band_ctas, c->tune.tile_shape);
     fclose(f);
 }
 
@@ -1939,23 +1958,12 @@ int blg_pairs_upload(blg_ctx *c, const uint8_t *ba, const int64_t *oa, const uin
     blg_pairs *p = new (std::nothrow) blg_pairs();
     if (!p) return fail(c, BLG_ERR_ALLOC, "host allocation");
     int rc = pairs_upload(c, ba, oa, bb, ob, n, p);
-    // the bytes the set uses, once: they pick the banded solver's row layout
-    uint32_t alpha[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (!rc && n > 0) {
-        if (dev_alloc(c, (void **)&p->d_alpha, sizeof(alpha)) != cudaSuccess ||
-            cudaMemsetAsync(p->d_alpha, 0, sizeof(alpha), c->stream) != cudaSuccess ||
-            launch(c, "byte_presence", [&] { return launch_byte_presence(c->stream, c->sms, p->a.d, p->b.d, p->d_alpha); }) !=
-                cudaSuccess ||
-            cudaMemcpyAsync(alpha, p->d_alpha, sizeof(alpha), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
-            rc = fail(c, BLG_ERR_CUDA, "alphabet");
-    }
-    // the copies complete before the call returns: the device copy is the
-    // data the host pass checked, whatever the caller does with its buffers
+    // the bytes the set uses, once: they pick the pairs kernels' row layout.
+    // The copies complete before the call returns (the alphabet's copy back
+    // synchronises): the device copy is the data the host pass checked,
+    // whatever the caller does with its buffers.
+    if (!rc) rc = pairs_learn_alphabet(c, p);
     if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = fail(c, BLG_ERR_CUDA, "upload");
-    if (!rc && n > 0) {
-        p->nsym = 0;
-        for (uint32_t w : alpha) p->nsym += __builtin_popcount(w);
-    }
     if (rc) {
         pairs_release(c, p);
         delete p;
@@ -1986,7 +1994,7 @@ static int pairs_run_graph(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_o
     key.sched = c->sched;
     key.learned = c->sched == BLG_SCHED_LEARNED && c->model && sched_model_trained(c->model);
     key.band_ctas = c->tune.band_ctas;
-    key.tile_buffers = c->tune.tile_buffers;
+    key.tile_shape = c->tune.tile_shape;
     key.out = d_out;
     if (p->gexec && p->g_key == key) {
         CK(cudaGraphLaunch(p->gexec, c->stream), "graph launch");
@@ -2519,7 +2527,7 @@ int blg_get_tuning(blg_ctx *c, int32_t *values, int n) {
     values[9] = c->tune.lpt_job;
     values[10] = c->tune.band_ctas;
     values[11] = c->tune.tuned;
-    values[12] = c->tune.tile_buffers;
+    values[12] = c->tune.tile_shape;
     values[13] = c->tune.surv_round;
     return BLG_OK;
 }

@@ -17,7 +17,8 @@ struct blg_tuning {
     int lpt_job = 4096;                          // thresholded search: survivors per job
     int surv_round = 16;                         // thresholded search: columns per lane round (8, 16, 32)
     int band_ctas = 3;                           // banded pairs solver: CTAs per SM
-    int tile_buffers = 2;                        // short-pair tile kernel: stage buffers (1: 3 CTAs/SM)
+    int tile_shape = 2;                          // short-pair tile kernel: 1 = one stage of 512 pairs, 2 = two of 512,
+                                                 // 3 = two of 256
     int tuned = 0;
 };
 

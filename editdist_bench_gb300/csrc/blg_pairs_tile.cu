@@ -33,21 +33,29 @@ namespace blg {
 
 constexpr int kTileThreads = 256;
 constexpr int kTileMaxPairs = 512;
-constexpr int kTileCap = 16896;                  // rounded span bytes staged per side (512 pairs of <= 33)
-constexpr int kTileSide = kTileCap + 48;         // 16 bytes of slack before, 32 after
+
+// Stage of a tile of up to PM pairs: rounded span bytes per side (PM pairs
+// of at most 33 bytes), plus 16 bytes of slack before and 32 after.
+template <int PM>
+struct TileDims {
+    static constexpr int Cap = PM * 33;
+    static constexpr int Side = Cap + 48;
+};
 constexpr int kTileKeys = 64;                    // counting-sort keys: min(columns, 63)
 constexpr int32_t kNoStore = INT32_MIN;          // result slot filled by the long-pair consumer
 
-// NBUF = 2: the next tile's copy flies while this one computes (2 CTAs per
-// SM); NBUF = 1: one stage, the copy is issued when the tile is done and the
-// other CTAs of the SM (3 per SM, 4 with one row per byte) compute meanwhile.
-template <int NBUF, bool SYM>
+// NBUF = 2: the next tile's copy flies while this one computes; NBUF = 1:
+// one stage, the copy is issued when the tile is done and the other CTAs of
+// the SM compute meanwhile. Up to PM pairs per tile (512 or 256). CTAs per
+// SM: 3 (one stage, 512 pairs, nibble rows), 4 (the same with one row per
+// byte, or two stages of 256 pairs), 2 (two stages of 512).
+template <int NBUF, bool SYM, int PM>
 struct __align__(16) TileShared {
-    uint8_t stage[NBUF][2][kTileSide];            // [buffer][a|b]
+    uint8_t stage[NBUF][2][TileDims<PM>::Side];   // [buffer][a|b]
     uint32_t tab[(SYM ? 16 : 32) * kTileThreads]; // pattern rows, row r of thread t at [r*256 + t]
     uint8_t map[SYM ? 256 : 4];                   // byte -> row (SYM)
-    uint2 ent[kTileMaxPairs];                     // sorted work list
-    int32_t res[kTileMaxPairs];
+    uint2 ent[PM];                                // sorted work list
+    int32_t res[PM];
     int32_t hist[kTileKeys];
     int32_t start[kTileKeys];
     int64_t span_lo[2][2], span_hi[2][2];         // staged span [lo, hi) per buffer/side, lo < 0: none
@@ -290,7 +298,7 @@ __device__ __forceinline__ int solve32(const Rows32<SYM> &rw, const uint8_t *p, 
 // Thread 0: the rounded spans of a tile's strings, one bulk copy per side
 // into `buf`, completing on bar[buf]. (a0, a1) and (b0, b1) are the string
 // offsets bounding the tile, off[t0] and off[t0 + cnt], of each side.
-template <typename TS>
+template <int CAP, typename TS>
 __device__ __forceinline__ void tile_issue(TS &S, int buf, const DevStrings &A, const DevStrings &B,
                                            int64_t a0, int64_t a1, int64_t b0, int64_t b1) {
     auto span = [&](const DevStrings &D, int64_t o0, int64_t o1, int side) -> uint32_t {
@@ -299,7 +307,7 @@ __device__ __forceinline__ void tile_issue(TS &S, int buf, const DevStrings &A, 
         if (lo >= 0 && hi >= lo && hi <= D.bytes) {
             lo16 = lo & ~int64_t(15);
             hi16 = (hi + 15) & ~int64_t(15);     // inside the buffer's 16-byte tail slack
-            if (hi16 - lo16 > kTileCap || (reinterpret_cast<uintptr_t>(D.buf + lo16) & 15)) lo16 = hi16 = -1;
+            if (hi16 - lo16 > CAP || (reinterpret_cast<uintptr_t>(D.buf + lo16) & 15)) lo16 = hi16 = -1;
         }
         S.span_lo[buf][side] = lo16;
         S.span_hi[buf][side] = hi16;
@@ -344,12 +352,13 @@ __device__ __forceinline__ void load_offs(PairOffs &o, const DevStrings &A, cons
 // alpha: the pair set's bytes (8 words; SYM builds its byte -> row map from
 // them), or null when the host chose the variant. Given to both variants,
 // the one that does not apply returns at once.
-template <bool HASK, int NBUF, bool TRUST, bool SYM>
-__global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : (SYM ? 4 : 3))
+template <bool HASK, int NBUF, bool TRUST, bool SYM, int PM>
+__global__ void __launch_bounds__(kTileThreads, (NBUF == 1 && SYM) || PM == 256 ? 4 : (NBUF == 2 ? 2 : 3))
     k_pairs_tile(DevStrings A, DevStrings B, int P, int k, int dtype, void *out, LongQueue q, uint32_t *status,
                  uint32_t unit, uint32_t wait_polls, const uint32_t *alpha) {
     extern __shared__ __align__(128) uint8_t s_raw[];
-    TileShared<NBUF, SYM> &S = *reinterpret_cast<TileShared<NBUF, SYM> *>(s_raw);
+    TileShared<NBUF, SYM, PM> &S = *reinterpret_cast<TileShared<NBUF, SYM, PM> *>(s_raw);
+    constexpr int kSide = TileDims<PM>::Side, kCap = TileDims<PM>::Cap;
     const Units u{unit, unit + unit};
     const int tid = threadIdx.x;
     if (alpha && (alpha_size(alpha) <= kBandSymbols) != SYM) return;   // uniform: the other variant runs the set
@@ -379,7 +388,7 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : (SYM ? 4 : 3))
     if (tid == 0 && first < ntiles) {
         PairOffs bd;
         tile_bounds(first, bd);
-        tile_issue(S, 0, A, B, bd.a0, bd.a1, bd.b0, bd.b1);
+        tile_issue<kCap>(S, 0, A, B, bd.a0, bd.a1, bd.b0, bd.b1);
         if (first + G < ntiles) tile_bounds(first + G, nb);
     }
     // every thread's offsets for its (up to two) pairs of the current tile
@@ -396,7 +405,7 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : (SYM ? 4 : 3))
         const int64_t t0 = t * P;
         const int cnt = (int)(n - t0 < P ? n - t0 : P);
         if (NBUF == 2 && tid == 0 && t + G < ntiles) {    // prefetch the next tile's strings
-            tile_issue(S, buf ^ 1, A, B, nb.a0, nb.a1, nb.b0, nb.b1);
+            tile_issue<kCap>(S, buf ^ 1, A, B, nb.a0, nb.a1, nb.b0, nb.b1);
             if (t + 2 * G < ntiles) tile_bounds(t + 2 * G, nb);
         }
         const bool ok = mbar_wait(&S.bar[buf], parity, wait_polls);
@@ -431,7 +440,7 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : (SYM ? 4 : 3))
             uint32_t oa = 0, ob = 0;
             if (sa && sb) {                                 // both staged: 32-bit shared offsets
                 oa = 16 + (uint32_t)(ra - alo);
-                ob = kTileSide + 16 + (uint32_t)(rb - blo);
+                ob = kSide + 16 + (uint32_t)(rb - blo);
                 const uint32_t oa0 = oa;
                 stage_trim(stage, oa, la, ob, lb);
                 pre = oa - oa0;
@@ -439,7 +448,7 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : (SYM ? 4 : 3))
                 b = stage + ob;
             } else {
                 a = sa ? stage + 16 + (ra - alo) : ga;
-                b = sb ? stage + kTileSide + 16 + (rb - blo) : gb;
+                b = sb ? stage + kSide + 16 + (rb - blo) : gb;
                 const uint8_t *a_start = a;
                 trim_windows<GenericLoad>(a, la, b, lb);
                 pre = a - a_start;
@@ -540,53 +549,69 @@ __global__ void __launch_bounds__(kTileThreads, NBUF == 2 ? 2 : (SYM ? 4 : 3))
         if (tid < kTileKeys) S.hist[tid] = 0;
         __syncthreads();                                    // the stage buffer and lists are reused
         if (NBUF == 1 && tid == 0 && t + G < ntiles) {    // the single stage is free: next tile's copy
-            tile_issue(S, 0, A, B, nb.a0, nb.a1, nb.b0, nb.b1);
+            tile_issue<kCap>(S, 0, A, B, nb.a0, nb.a1, nb.b0, nb.b1);
             if (t + 2 * G < ntiles) tile_bounds(t + 2 * G, nb);
         }
     }
 }
 
 // ------------------------------------------------------------- launcher --
-template <bool HASK, int NBUF, bool TRUST, bool SYM>
+template <bool HASK, int NBUF, bool TRUST, bool SYM, int PM>
 static cudaError_t launch_tile(cudaStream_t st, int sms, const DevStrings &A, const DevStrings &B, int P, int k,
                                int dtype, void *out, const LongQueue &q, uint32_t *status, uint32_t polls,
                                const uint32_t *alpha) {
+    P = std::max(32, (P * PM / kTileMaxPairs) & ~3);       // the caller sized P for a 512-pair stage
     const int64_t ntiles = (A.n + P - 1) / P;
-    const int per_sm = NBUF == 2 ? 2 : (SYM ? 4 : 3);
+    const int per_sm = (NBUF == 1 && SYM) || PM == 256 ? 4 : (NBUF == 2 ? 2 : 3);
     const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sms * per_sm);
-    const size_t smem = sizeof(TileShared<NBUF, SYM>);
-    cudaFuncSetAttribute(k_pairs_tile<HASK, NBUF, TRUST, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_pairs_tile<HASK, NBUF, TRUST, SYM><<<grid, kTileThreads, smem, st>>>(A, B, P, k, dtype, out, q, status, 1u, polls,
-                                                                          alpha);
+    const size_t smem = sizeof(TileShared<NBUF, SYM, PM>);
+    cudaFuncSetAttribute(k_pairs_tile<HASK, NBUF, TRUST, SYM, PM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    k_pairs_tile<HASK, NBUF, TRUST, SYM, PM><<<grid, kTileThreads, smem, st>>>(A, B, P, k, dtype, out, q, status, 1u,
+                                                                              polls, alpha);
     return cudaGetLastError();
 }
 
 // variant: 1 = one row per byte (alpha: the set's bytes), 0 = nibble rows,
 // -1 = both launch and alpha, computed on the stream before, picks.
-template <bool HASK, int NBUF, bool TRUST>
+template <bool HASK, int NBUF, bool TRUST, int PM>
 static cudaError_t launch_tile_v(int variant, const uint32_t *alpha, cudaStream_t st, int sms, const DevStrings &A,
                                  const DevStrings &B, int P, int k, int dtype, void *out, const LongQueue &q,
                                  uint32_t *status, uint32_t polls) {
     cudaError_t e = cudaSuccess;
     if (variant != 0)
-        e = launch_tile<HASK, NBUF, TRUST, true>(st, sms, A, B, P, k, dtype, out, q, status, polls, alpha);
+        e = launch_tile<HASK, NBUF, TRUST, true, PM>(st, sms, A, B, P, k, dtype, out, q, status, polls, alpha);
     if (e == cudaSuccess && variant != 1)
-        e = launch_tile<HASK, NBUF, TRUST, false>(st, sms, A, B, P, k, dtype, out, q, status, polls,
-                                                  variant < 0 ? alpha : nullptr);
+        e = launch_tile<HASK, NBUF, TRUST, false, PM>(st, sms, A, B, P, k, dtype, out, q, status, polls,
+                                                      variant < 0 ? alpha : nullptr);
     return e;
 }
 
-template <bool HASK, int NBUF>
+template <bool HASK, int NBUF, int PM>
 static cudaError_t launch_tile_t(bool trusted, int variant, const uint32_t *alpha, cudaStream_t st, int sms,
                                  const DevStrings &A, const DevStrings &B, int P, int k, int dtype, void *out,
                                  const LongQueue &q, uint32_t *status, uint32_t polls) {
-    return trusted ? launch_tile_v<HASK, NBUF, true>(variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls)
-                   : launch_tile_v<HASK, NBUF, false>(variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls);
+    return trusted
+               ? launch_tile_v<HASK, NBUF, true, PM>(variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls)
+               : launch_tile_v<HASK, NBUF, false, PM>(variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls);
 }
 
-// trusted: the offsets were checked on the host (every pair in order).
-// variant / alpha: the row layout, as for launch_tile_v.
-cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, const DevStrings &A,
+template <bool HASK>
+static cudaError_t launch_tile_shape(int shape, bool trusted, int variant, const uint32_t *alpha, cudaStream_t st,
+                                     int sms, const DevStrings &A, const DevStrings &B, int P, int k, int dtype,
+                                     void *out, const LongQueue &q, uint32_t *status, uint32_t polls) {
+    if (shape == 1)
+        return launch_tile_t<HASK, 1, 512>(trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls);
+    if (shape == 3)
+        return launch_tile_t<HASK, 2, 256>(trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls);
+    return launch_tile_t<HASK, 2, 512>(trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls);
+}
+
+// shape: 1 = one stage of up to 512 pairs, 2 = two stages of 512, 3 = two
+// stages of 256 (the autotuner picks). trusted: the offsets were checked on
+// the host (every pair in order). variant / alpha: the row layout, as for
+// launch_tile_v.
+cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int shape, bool hask, const DevStrings &A,
                               const DevStrings &B, int tile_pairs, int k, int dtype, void *out, const LongQueue &q,
                               uint32_t *status, int32_t wait_polls, bool trusted, int variant, const uint32_t *alpha) {
     if (A.n <= 0) return cudaSuccess;
@@ -595,11 +620,10 @@ cudaError_t launch_pairs_tile(cudaStream_t st, int sms, int buffers, bool hask, 
     if (P > kTileMaxPairs) P = kTileMaxPairs;
     if (P < 32) P = 32;
     P &= ~3;                                                // 4-aligned tiles keep the vector stores aligned
-    if (buffers == 1)
-        return hask ? launch_tile_t<true, 1>(trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls)
-                    : launch_tile_t<false, 1>(trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls);
-    return hask ? launch_tile_t<true, 2>(trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls)
-                : launch_tile_t<false, 2>(trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status, polls);
+    return hask ? launch_tile_shape<true>(shape, trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status,
+                                          polls)
+                : launch_tile_shape<false>(shape, trusted, variant, alpha, st, sms, A, B, P, k, dtype, out, q, status,
+                                           polls);
 }
 
 }  // namespace blg

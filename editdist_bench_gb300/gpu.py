@@ -420,7 +420,7 @@ def tuning() -> dict:
     ctx.check(ctx.lib.blg_get_tuning(ctx.h, v, 14), "get_tuning")
     return {"search_queries_per_cta": {w + 1: int(v[w]) for w in range(8)}, "survivor_ctas_per_sm": int(v[8]),
             "survivors_per_job": int(v[9]), "survivor_round_columns": int(v[13]), "band_ctas_per_sm": int(v[10]),
-            "tile_stage_buffers": int(v[12]), "source": {0: "defaults", 1: "timed", 2: "cache"}[int(v[11])]}
+            "tile_shape": int(v[12]), "source": {0: "defaults", 1: "timed", 2: "cache"}[int(v[11])]}
 
 
 def set_schedule(name: str):

@@ -229,16 +229,17 @@ int blg_sched_load(blg_ctx *ctx, const char *path);
  * length bucket and max_dist kind and keeps the fastest for this context:
  * queries per CTA of the exact search (by query word count), CTAs per SM and
  * columns per lane round of the thresholded search's survivor kernel, CTAs
- * per SM of the banded pairs solver, stage buffers of the short-pair tile
- * kernel. With a cache path, a cache written for the same device model,
+ * per SM of the banded pairs solver, the staging shape of the short-pair
+ * tile kernel. With a cache path, a cache written for the same device model,
  * SM count and library version is loaded instead of timing, and a fresh
  * result is written there. No counterpart in the reference (fixed launch
  * geometry, bitlev/gpu.py:90-96,121-130). Results never depend on it. */
 int blg_autotune(blg_ctx *ctx, const char *cache_path);
 /* values[14]: qpb for 1..8 query words (0 = heuristic), CTAs per SM and
  * survivors per job of the thresholded search, CTAs per SM of the banded
- * solver, 0 (defaults) / 1 (timed) / 2 (loaded from a cache), the stage
- * buffers of the short-pair tile kernel, and the columns per lane round of
+ * solver, 0 (defaults) / 1 (timed) / 2 (loaded from a cache), the staging
+ * shape of the short-pair tile kernel (1: one stage of 512 pairs, 2: two
+ * stages of 512, 3: two stages of 256), and the columns per lane round of
  * the thresholded search's survivor kernel (8, 16 or 32). */
 int blg_get_tuning(blg_ctx *ctx, int32_t *values, int n);
 

@@ -17,7 +17,7 @@ def test_autotune_cache_and_exactness(gpu, tmp_path):
     assert all(q in (4, 8, 16, 32, 64) for q in t["search_queries_per_cta"].values())
     assert t["survivor_ctas_per_sm"] in (2, 3, 4) and t["survivors_per_job"] in (2048, 4096)
     assert t["survivor_round_columns"] in (8, 16, 32)
-    assert t["band_ctas_per_sm"] in (2, 3) and t["tile_stage_buffers"] in (1, 2)
+    assert t["band_ctas_per_sm"] in (2, 3) and t["tile_shape"] in (1, 2, 3)
     t2 = gpu.autotune(path)                               # same device and library: loaded, not re-timed
     assert t2["source"] == "cache"
     assert {k: v for k, v in t2.items() if k != "source"} == {k: v for k, v in t.items() if k != "source"}

@@ -99,20 +99,29 @@ def test_tile_resident_repeat(gpu):
         np.testing.assert_array_equal(out.get(), oracle.saturate(want, dt))
 
 
-def test_tile_both_stage_variants(gpu, tmp_path):
-    """The single- and double-buffered tile kernels (an autotuned choice) give
-    identical, exact results; each is forced through an edited tuning cache."""
+def test_tile_all_stage_shapes(gpu, tmp_path):
+    """The tile kernel's staging shapes (an autotuned choice: one stage of 512
+    pairs, two of 512, two of 256) give identical, exact results; each is
+    forced through an edited tuning cache, on DNA (one row per byte) and on
+    a 256-byte alphabet (nibble rows)."""
     path = tmp_path / "tune.txt"
     gpu.autotune(str(path))
     lines = path.read_text().splitlines()
     rng = np.random.default_rng(21)
     a, b = _short_pairs(rng, 30001)
     exact = oracle.pairs(a, b)
-    for bufs in (1, 2):
-        forced = tmp_path / f"tune{bufs}.txt"
-        forced.write_text("\n".join(l if not l.startswith("tile_buffers") else f"tile_buffers {bufs}"
+    full = np.arange(256, dtype=np.uint8)
+    a2 = W.random_strings(rng, rng.integers(0, 33, 20003), full)
+    b2 = W.mutate(rng, a2, 0.1, full)
+    exact2 = oracle.pairs(a2, b2)
+    for shape in (1, 2, 3):
+        forced = tmp_path / f"tune{shape}.txt"
+        forced.write_text("\n".join(l if not l.startswith("tile_shape") else f"tile_shape {shape}"
                                     for l in lines) + "\n")
-        assert gpu.autotune(str(forced))["tile_stage_buffers"] == bufs
+        assert gpu.autotune(str(forced))["tile_shape"] == shape
+        np.testing.assert_array_equal(gpu.pairwise_packed(a2, b2), exact2, err_msg=f"shape {shape}, 256 bytes")
+        batch = gpu.PairsBatch(a2, b2)
+        np.testing.assert_array_equal(batch.run(batch.alloc("int32")).get(), exact2, err_msg=f"shape {shape} resident")
         np.testing.assert_array_equal(gpu.pairwise_packed(a, b), exact)
         np.testing.assert_array_equal(gpu.pairwise_packed(a, b, 2, "uint8"),
                                       oracle.saturate(np.minimum(exact, 3), "uint8"))
