@@ -621,6 +621,83 @@ __device__ __forceinline__ int band_distance(int m, const uint8_t *t, int n, int
     return band_core(m, n, k, text, eqw, u, cols_out);
 }
 
+// The banded loop of one pair with per-thread block rows (the pairs
+// kernels): rows over a 64-position block of the pattern, bit i <->
+// position 32b - dhi + i in block b, in a [row][thread] table of stride T
+// starting at this thread's row 0 (tc). Columns 32b .. 32b+31 read their
+// 32-bit windows out of the block with one funnel shift; every 32 columns
+// the rows shift down by 32 positions and the next 32 pattern bytes enter.
+// SYM: one row per byte (map: byte -> row, kBandSymbols + 1 rows); else
+// nibble rows, Eq(c) = row[c >> 4] & row[16 + (c & 15)] (32 rows).
+// pat_at(pos) / txt_at(pos) return readers (next4()) positioned at pattern
+// / text byte pos. Caller guarantees 1 <= m, |n - m| <= k <= 31.
+template <bool SYM, int T, typename PatAt, typename TxtAt>
+__device__ __forceinline__ int band_rows_distance(uint2 *tc, const uint8_t *map, PatAt pat_at, TxtAt txt_at, int m,
+                                                  int n, int k, int *cols_out) {
+    constexpr int R = SYM ? kBandSymbols + 1 : 32;
+    auto enter = [&](uint32_t c, int bitpos) {                  // pattern byte c at block bit bitpos (0..63)
+        const uint32_t bit = 1u << (bitpos & 31);
+        if (SYM) {
+            atomicOr(reinterpret_cast<uint32_t *>(tc + map[c] * T) + (bitpos >> 5), bit);
+        } else {
+            atomicOr(reinterpret_cast<uint32_t *>(tc + (c >> 4) * T) + (bitpos >> 5), bit);
+            atomicOr(reinterpret_cast<uint32_t *>(tc + (16 + (c & 15)) * T) + (bitpos >> 5), bit);
+        }
+    };
+    auto rowbits = [&](uint32_t c) -> uint2 {
+        if (SYM) return tc[map[c] * T];
+        const uint2 h = tc[(c >> 4) * T], l = tc[(16 + (c & 15)) * T];
+        return make_uint2(h.x & l.x, h.y & l.y);
+    };
+    const BandGeom bg = band_geom(m, n, k);
+    const int dhi = bg.dhi;
+#pragma unroll
+    for (int r = 0; r < R; r++) tc[r * T] = make_uint2(0, 0);
+    // block 0: positions 0 .. min(m, 64 - dhi) - 1 at bits pos + dhi
+    const int first_end = min(m, 64 - dhi);
+    {
+        auto fs = pat_at(0);
+        for (int p = 0; p < first_end; p += 4) {
+            const uint32_t w4 = fs.next4();
+#pragma unroll
+            for (int b = 0; b < 4; b++)
+                if (p + b < first_end) enter((w4 >> (8 * b)) & 0xffu, p + b + dhi);
+        }
+    }
+    // later blocks enter the positions from 64 - dhi on, 32 at a time
+    auto ps = pat_at(first_end);
+    int next_pos = first_end;
+    auto eqw = [&](uint32_t c, int p0) -> uint32_t {
+        const int j = p0 + dhi;
+        if ((j & 31) == 0 && j > 0) {
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const uint32_t hi = tc[r * T].y;
+                tc[r * T] = make_uint2(hi, 0);
+            }
+            const int cnt = min(32, m - next_pos);
+            for (int i = 0; i < cnt; i += 4) {
+                const uint32_t w4 = ps.next4();
+#pragma unroll
+                for (int b = 0; b < 4; b++)
+                    if (i + b < cnt) enter((w4 >> (8 * b)) & 0xffu, 32 + i + b);
+            }
+            next_pos += cnt > 0 ? cnt : 0;
+        }
+        const uint2 x = rowbits(c);
+        return __funnelshift_r(x.x, x.y, (uint32_t)(j & 31));
+    };
+    auto ts = txt_at(0);
+    uint32_t w4 = 0;
+    auto text = [&](int j) -> uint32_t {
+        if ((j & 3) == 0) w4 = ts.next4();
+        const uint32_t c = w4 & 0xffu;
+        w4 >>= 8;
+        return c;
+    };
+    return band_core(m, n, k, text, eqw, Units{1u, 2u}, cols_out);
+}
+
 // Query Peq rows as 32-bit halves with zero padding (2 halves before, 4
 // after): row stride 2*NW + 6 halves. Window bits at pattern index p0:
 // halves around p0 + 64, one funnel shift.

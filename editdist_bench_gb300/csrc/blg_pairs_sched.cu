@@ -230,28 +230,12 @@ constexpr int kSymRows = kBandSymbols + 1;           // the last row stays empty
 template <bool LOG, bool SYM>
 __global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int k, int dtype, void *out,
                                                              int32_t *exit_log, const uint32_t *alpha) {
-    constexpr int R = SYM ? kSymRows : 32;
-    extern __shared__ uint2 s_rows2[];                      // [R rows][kBandThreads] 64-bit rows
+    extern __shared__ uint2 s_rows2[];                      // [rows][kBandThreads] 64-bit rows
     __shared__ uint8_t s_map[256];                          // byte -> row (SYM)
     if (alpha && (alpha_size(alpha) <= kBandSymbols) != SYM) return;   // uniform: the other variant runs the set
     if (SYM) alpha_map(alpha, s_map);
     uint2 *tc = s_rows2 + threadIdx.x;                      // row r at tc[r * kBandThreads]
     const int lane = threadIdx.x & 31;
-    // pattern byte c at window bit `bitpos` of the block (0..63)
-    auto enter = [&](uint32_t c, int bitpos) {
-        const uint32_t bit = 1u << (bitpos & 31);
-        if (SYM) {
-            atomicOr(reinterpret_cast<uint32_t *>(tc + s_map[c] * kBandThreads) + (bitpos >> 5), bit);
-        } else {
-            atomicOr(reinterpret_cast<uint32_t *>(tc + (c >> 4) * kBandThreads) + (bitpos >> 5), bit);
-            atomicOr(reinterpret_cast<uint32_t *>(tc + (16 + (c & 15)) * kBandThreads) + (bitpos >> 5), bit);
-        }
-    };
-    auto rowbits = [&](uint32_t c) -> uint2 {
-        if (SYM) return tc[s_map[c] * kBandThreads];
-        const uint2 h = tc[(c >> 4) * kBandThreads], l = tc[(16 + (c & 15)) * kBandThreads];
-        return make_uint2(h.x & l.x, h.y & l.y);
-    };
     for (int cls = kPairClasses - 1; cls >= 0; cls--) {
         const int count = min(plan.count[cls], (int)plan.cap[cls]);
         while (true) {
@@ -263,51 +247,19 @@ __global__ void __launch_bounds__(kBandThreads) k_solve_band(PairsPlan plan, int
             if (ri >= count) continue;
             const LongItem it = plan.sorted[cls][ri];
             const int m = it.m, n = it.n;
-            const uint8_t *pat = it.pat;
             int d, cols = 0;
-            if (n - m > k || m - n > k) d = k + 1;
-            else {
-                const BandGeom bg = band_geom(m, n, k);
-                const int dhi = bg.dhi;
-#pragma unroll
-                for (int r = 0; r < R; r++) tc[r * kBandThreads] = make_uint2(0, 0);
-                // block 0: positions 0 .. min(m, 64 - dhi) - 1 at bits pos + dhi
-                const int first_end = min(m, 64 - dhi);
-                {
-                    TextScan fs;
-                    fs.init(pat);
-                    for (int p = 0; p < first_end; p += 4) {
-                        const uint32_t w4 = fs.next4();
-#pragma unroll
-                        for (int b = 0; b < 4; b++)
-                            if (p + b < first_end) enter((w4 >> (8 * b)) & 0xffu, p + b + dhi);
-                    }
-                }
-                // later blocks enter the positions from 64 - dhi on, 32 at a time
-                TextScan ps;
-                if (first_end < m) ps.init(pat + first_end);
-                int next_pos = first_end;
-                auto eqw = [&](uint32_t c, int p0) -> uint32_t {
-                    const int j = p0 + dhi;
-                    if ((j & 31) == 0 && j > 0) {               // warp-uniform: lanes share j
-#pragma unroll
-                        for (int r = 0; r < R; r++) {
-                            const uint32_t hi = tc[r * kBandThreads].y;
-                            tc[r * kBandThreads] = make_uint2(hi, 0);
-                        }
-                        const int cnt = min(32, m - next_pos);
-                        for (int i = 0; i < cnt; i += 4) {
-                            const uint32_t w4 = ps.next4();
-#pragma unroll
-                            for (int b = 0; b < 4; b++)
-                                if (i + b < cnt) enter((w4 >> (8 * b)) & 0xffu, 32 + i + b);
-                        }
-                        next_pos += cnt > 0 ? cnt : 0;
-                    }
-                    const uint2 x = rowbits(c);
-                    return __funnelshift_r(x.x, x.y, (uint32_t)(j & 31));
+            if (n - m > k || m - n > k) {
+                d = k + 1;
+            } else {
+                auto at = [](const uint8_t *base) {
+                    return [base](int pos) {
+                        TextScan s;
+                        s.init(base + pos);
+                        return s;
+                    };
                 };
-                d = band_distance(m, it.txt, n, k, eqw, Units{1u, 2u}, LOG ? &cols : nullptr);
+                d = band_rows_distance<SYM, kBandThreads>(tc, s_map, at(it.pat), at(it.txt), m, n, k,
+                                                          LOG ? &cols : nullptr);
             }
             store1(out, dtype, it.idx, d);
             if (LOG) exit_log[it.idx] = cols;
