@@ -538,7 +538,9 @@ def read_profile(kernel: str, workload: str) -> dict:
     kernel launch label on a workload (profiles/<label>_<workload>.txt):
     traffic_bytes_per_launch (DRAM bytes of a full launch), inst_per_unit
     (warp instructions per pair, all launches of the label in one step),
-    alu_pipe / issue_active (ncu's pipe and issue utilisation)."""
+    time_share (the counted kernel's share of the label's time, when the
+    label is a graph of several kernels), alu_pipe / issue_active (ncu's
+    pipe and issue utilisation)."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.txt")
     out = {"path": os.path.relpath(path, ROOT)}
     try:
@@ -723,12 +725,14 @@ def roofline_block(bench, kstats, top, peak, exit_sum, dev, clock_mhz) -> dict:
     issue = None
     if prof.get("inst_per_unit") and dev.get("sms"):
         mhz = clock_mhz or dev["max_mhz"]
-        slots = dev["sms"] * 4 * mhz * 1e6 * ms / 1e3
+        share = prof.get("time_share", 1.0)   # the counted kernel's share of a label that spans several kernels
+        slots = dev["sms"] * 4 * mhz * 1e6 * ms * share / 1e3
         inst = prof["inst_per_unit"] * bench.pairs
         issue = {"frac": inst / slots, "inst_per_unit": prof["inst_per_unit"], "unit": "warp instructions per pair",
                  "clock_mhz": mhz, "alu_pipe_ncu": prof.get("alu_pipe"), "issue_active_ncu": prof.get("issue_active"),
-                 "source": prof["path"],
-                 "how": "inst_per_unit x pairs per step / (event ms x SMs x 4 issue slots per clock x SM clock)"}
+                 "time_share": share, "source": prof["path"],
+                 "how": "inst_per_unit x pairs per step / (event ms x time_share x SMs x 4 issue slots per clock "
+                        "x SM clock)"}
     # short exact pairs (config 1) are bound by moving their bytes; the rest by the integer pipe
     primary = hbm if (bench.kind == "pairwise" and bench.runs[0][0] is None) else ipart
     traffic = prof.get("traffic_bytes_per_launch")

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <array>
 #include <condition_variable>
 #include <functional>
@@ -176,6 +177,7 @@ struct blg_search {
     // and of the queries
     uint64_t *csk = nullptr, *qsk = nullptr;
     uint4 *ccnt = nullptr, *qcnt = nullptr;
+    void *sk_mem = nullptr;           // the queries' sketch block when this search owns it
     // choices in tile-transposed form (exact and unsorted runs), when the
     // padding to each tile's longest choice stays small
     bool tt = false;
@@ -763,19 +765,92 @@ static void free_classes(blg_ctx *c, blg_search *s) {
     s->cls.clear();
 }
 
-// Query classes of queries [q0, q1) by word count (bitlev/gpu.py:116-118
-// uses 1,2,4,8 and the CPU above 512; here every length has a GPU class),
-// each sorted by length; replaces the previous classes.
-static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64_t q1, blg_search *s) {
-    free_classes(c, s);
+// Length buckets of a choice set (the sorted copy of thresholded runs): a
+// stable counting sort by length on nt threads of the host pool (nt = 1
+// runs on the caller alone, so a pool task may call it). Every string of a
+// bucket has the bucket's length, so the sorted offsets follow from the
+// bucket starts. perm_at() gives the room for the permutation (pinned) once
+// the histogram is done.
+struct LengthSort {
+    int64_t mn = 0, n_len = 0, bytes = 0;
+    std::vector<int64_t> lstart;      // first sorted index per length (n_len + 1)
+    std::vector<int64_t> bstart;      // first sorted byte per length (n_len)
+};
+
+// 1: sorted; 0: the lengths spread over 2^22 or more values (no buckets);
+// -1: perm_at() gave no room.
+template <typename PermAt>
+static int length_sort(const int64_t *oc, int64_t nc, int nt, LengthSort &L, PermAt &&perm_at) {
+    HostPool &pool = HostPool::get();
+    auto lo_of = [&](int t, int parts) { return nc * t / parts; };
+    std::vector<int64_t> tmn(nt, INT64_MAX), tmx(nt, 0);
+    pool.run(nt, [&](int t) {
+        int64_t a = INT64_MAX, b = 0;
+        for (int64_t i = lo_of(t, nt), e = lo_of(t + 1, nt); i < e; i++) {
+            const int64_t l = oc[i + 1] - oc[i];
+            a = std::min(a, l);
+            b = std::max(b, l);
+        }
+        tmn[t] = a;
+        tmx[t] = b;
+    });
+    const int64_t mn = *std::min_element(tmn.begin(), tmn.end()), mx = *std::max_element(tmx.begin(), tmx.end());
+    if (mx - mn >= (1 << 22)) return 0;
+    const int64_t n_len = mx - mn + 1;
+    // per-thread histograms [thread][bucket] while they stay small
+    const int nh = n_len * nt <= (1 << 22) ? nt : 1;
+    std::vector<int64_t> hist((size_t)(n_len * nh), 0);
+    pool.run(nh, [&](int t) {
+        int64_t *h = hist.data() + (size_t)t * n_len;
+        for (int64_t i = lo_of(t, nh), e = lo_of(t + 1, nh); i < e; i++) h[oc[i + 1] - oc[i] - mn]++;
+    });
+    // bucket starts; each thread's cursor per bucket after the lower threads (stable)
+    L.lstart.assign(n_len + 1, 0);
+    L.bstart.assign(n_len, 0);
+    int64_t run = 0, bytes = 0;
+    for (int64_t b = 0; b < n_len; b++) {
+        L.lstart[b] = run;
+        L.bstart[b] = bytes;
+        for (int t = 0; t < nh; t++) {
+            const int64_t cnt = hist[(size_t)t * n_len + b];
+            hist[(size_t)t * n_len + b] = run;
+            run += cnt;
+        }
+        bytes += (run - L.lstart[b]) * (b + mn);
+    }
+    L.lstart[n_len] = run;
+    int32_t *perm = perm_at();
+    if (!perm) return -1;
+    pool.run(nh, [&](int t) {
+        int64_t *cur = hist.data() + (size_t)t * n_len;
+        for (int64_t i = lo_of(t, nh), e = lo_of(t + 1, nh); i < e; i++) perm[cur[oc[i + 1] - oc[i] - mn]++] = (int32_t)i;
+    });
+    L.mn = mn;
+    L.n_len = n_len;
+    L.bytes = bytes;
+    return 1;
+}
+
+// Queries [q0, q1) by word class (bitlev/gpu.py:116-118 uses 1,2,4,8 and the
+// CPU above 512; here every length has a GPU class): the sequential classes
+// of 1..kSeqMaxWords words, then one lane-spread class (nw = its longest
+// query's words), each sorted by length so consecutive survivor tiles share
+// choices in L2. false: a query is longer than the lane-spread limit.
+struct QueryClass {
+    bool lanes = false;
+    int nw = 0;
+    std::vector<int32_t> idx, len;
+};
+
+static bool query_classes(const int64_t *oq, int64_t q0, int64_t q1, std::vector<QueryClass> &out) {
+    out.clear();
     std::vector<std::vector<int32_t>> idx(kSeqMaxWords + 1), len(kSeqMaxWords + 1);
     int lanes_nw = 0;
     for (int64_t i = q0; i < q1; i++) {
         const int64_t m = oq[i + 1] - oq[i];
         int64_t W = (m + 63) >> 6;
         if (W < 1) W = 1;
-        if (W > kLaneMaxWords)
-            return fail(c, BLG_ERR_ARG, "query longer than 2048 bytes is not supported");
+        if (W > kLaneMaxWords) return false;
         const int slot = W <= kSeqMaxWords ? (int)W - 1 : kSeqMaxWords;
         idx[slot].push_back((int32_t)i);
         len[slot].push_back((int32_t)m);
@@ -783,18 +858,31 @@ static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64
     }
     for (int slot = 0; slot <= kSeqMaxWords; slot++) {
         if (idx[slot].empty()) continue;
-        // queries by length: consecutive survivor tiles then share choices in L2
         std::vector<size_t> ord(idx[slot].size());
         for (size_t i = 0; i < ord.size(); i++) ord[i] = i;
         std::stable_sort(ord.begin(), ord.end(), [&](size_t x, size_t y) { return len[slot][x] < len[slot][y]; });
-        std::vector<int32_t> si(ord.size()), sl(ord.size());
-        for (size_t i = 0; i < ord.size(); i++) { si[i] = idx[slot][ord[i]]; sl[i] = len[slot][ord[i]]; }
-        idx[slot].swap(si);
-        len[slot].swap(sl);
-        blg_search::Cls k{};
+        QueryClass k;
         k.lanes = slot == kSeqMaxWords;
         k.nw = k.lanes ? lanes_nw : slot + 1;
-        k.nq = (int)idx[slot].size();
+        k.idx.resize(ord.size());
+        k.len.resize(ord.size());
+        for (size_t i = 0; i < ord.size(); i++) { k.idx[i] = idx[slot][ord[i]]; k.len[i] = len[slot][ord[i]]; }
+        out.push_back(std::move(k));
+    }
+    return true;
+}
+
+// Query classes of queries [q0, q1) (query_classes), each in one device
+// block with its Peq tables; replaces the previous classes.
+static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64_t q1, blg_search *s) {
+    free_classes(c, s);
+    std::vector<QueryClass> qc;
+    if (!query_classes(oq, q0, q1, qc)) return fail(c, BLG_ERR_ARG, "query longer than 2048 bytes is not supported");
+    for (auto &q : qc) {
+        blg_search::Cls k{};
+        k.lanes = q.lanes;
+        k.nw = q.nw;
+        k.nq = (int)q.idx.size();
         // one device block per class: [qidx | qlen] (filled by one copy), lo,
         // hi, work, tile_start, peq — 256-byte aligned parts. A class joins
         // the search only once its block exists, so a failed allocation never
@@ -807,7 +895,7 @@ static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64
         CK(dev_alloc(c, &k.mem, total), "cudaMallocAsync(class)");
         s->cls.push_back(k);
         blg_search::Cls &kk = s->cls.back();
-        kk.h_qlen = len[slot];
+        kk.h_qlen = q.len;
         uint8_t *m = (uint8_t *)kk.mem;
         kk.qidx = (int32_t *)(m + o_qidx);
         kk.qlen = (int32_t *)(m + o_qlen);
@@ -817,8 +905,8 @@ static int search_build_classes(blg_ctx *c, const int64_t *oq, int64_t q0, int64
         kk.tile_start = (int64_t *)(m + o_ts);
         kk.peq = (uint64_t *)(m + o_peq);
         std::vector<int32_t> both(2 * nq);
-        std::copy(idx[slot].begin(), idx[slot].end(), both.begin());
-        std::copy(len[slot].begin(), len[slot].end(), both.begin() + nq);
+        std::copy(q.idx.begin(), q.idx.end(), both.begin());
+        std::copy(q.len.begin(), q.len.end(), both.begin() + nq);
         CK(cudaMemcpyAsync(kk.qidx, both.data(), sizeof(int32_t) * 2 * nq, cudaMemcpyHostToDevice, c->stream),
            "H2D class queries");
     }
@@ -1011,51 +1099,16 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
     // the sorted offsets follow from the bucket starts: the device computes
     // them, and only the permutation (pinned) and the bucket tables travel.
     if (nc > 0 && (need & NEED_SORTED) && nc < INT32_MAX) {
-        HostPool &pool = HostPool::get();
-        const int nt = nc >= (1 << 16) ? pool.size() : 1;
-        auto lo_of = [&](int t, int parts) { return nc * t / parts; };
-        std::vector<int64_t> tmn(nt, INT64_MAX), tmx(nt, 0);
-        pool.run(nt, [&](int t) {
-            int64_t a = INT64_MAX, b = 0;
-            for (int64_t i = lo_of(t, nt), e = lo_of(t + 1, nt); i < e; i++) {
-                const int64_t l = oc[i + 1] - oc[i];
-                a = std::min(a, l);
-                b = std::max(b, l);
-            }
-            tmn[t] = a;
-            tmx[t] = b;
+        LengthSort L;
+        const int nt = nc >= (1 << 16) ? HostPool::get().size() : 1;
+        int32_t *perm = nullptr;
+        const int sorted = length_sort(oc, nc, nt, L, [&] {
+            perm = perm_stage ? perm_stage : (int32_t *)host_stage(c, sizeof(int32_t) * (size_t)nc);
+            return perm;
         });
-        const int64_t mn = *std::min_element(tmn.begin(), tmn.end()), mx = *std::max_element(tmx.begin(), tmx.end());
-        if (mx - mn < (1 << 22)) {
-            const int64_t n_len = mx - mn + 1;
-            // per-thread histograms [thread][bucket] while they stay small
-            const int nh = n_len * nt <= (1 << 22) ? nt : 1;
-            std::vector<int64_t> hist((size_t)(n_len * nh), 0);
-            pool.run(nh, [&](int t) {
-                int64_t *h = hist.data() + (size_t)t * n_len;
-                for (int64_t i = lo_of(t, nh), e = lo_of(t + 1, nh); i < e; i++) h[oc[i + 1] - oc[i] - mn]++;
-            });
-            // bucket starts; each thread's cursor per bucket after the lower threads (stable)
-            std::vector<int64_t> lstart(n_len + 1, 0), bstart(n_len, 0);
-            int64_t run = 0, bytes = 0;
-            for (int64_t b = 0; b < n_len; b++) {
-                lstart[b] = run;
-                bstart[b] = bytes;
-                for (int t = 0; t < nh; t++) {
-                    const int64_t cnt = hist[(size_t)t * n_len + b];
-                    hist[(size_t)t * n_len + b] = run;
-                    run += cnt;
-                }
-                bytes += (run - lstart[b]) * (b + mn);
-            }
-            lstart[n_len] = run;
-            int32_t *perm = perm_stage ? perm_stage : (int32_t *)host_stage(c, sizeof(int32_t) * (size_t)nc);
-            if (!perm) return fail(c, BLG_ERR_ALLOC, "cudaHostAlloc(staging)");
-            pool.run(nh, [&](int t) {
-                int64_t *cur = hist.data() + (size_t)t * n_len;
-                for (int64_t i = lo_of(t, nh), e = lo_of(t + 1, nh); i < e; i++)
-                    perm[cur[oc[i + 1] - oc[i] - mn]++] = (int32_t)i;
-            });
+        if (sorted < 0) return fail(c, BLG_ERR_ALLOC, "cudaHostAlloc(staging)");
+        if (sorted) {
+            const int64_t mn = L.mn, n_len = L.n_len, bytes = L.bytes;
             // one device block: perm | lstart, bucket starts | sorted offsets | sketches | sorted bytes
             auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
             const size_t o_perm = 0, o_tab = up(sizeof(int32_t) * (size_t)nc),
@@ -1075,8 +1128,8 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
             uint8_t *d_buf = m + o_buf;
             CK(cudaMemcpyAsync(s->perm, perm, sizeof(int32_t) * nc, cudaMemcpyHostToDevice, c->stream), "H2D perm");
             CK(cudaEventRecord(c->stage_done, c->stream), "event");
-            std::vector<int64_t> tab(lstart);                 // lstart then the bucket starts: one copy
-            tab.insert(tab.end(), bstart.begin(), bstart.end());
+            std::vector<int64_t> tab(L.lstart);               // lstart then the bucket starts: one copy
+            tab.insert(tab.end(), L.bstart.begin(), L.bstart.end());
             CK(cudaMemcpyAsync(s->lstart, tab.data(), sizeof(int64_t) * tab.size(), cudaMemcpyHostToDevice, c->stream),
                "H2D length tables");
             CK(launch(c, "sorted_offsets", [&] {
@@ -1085,7 +1138,7 @@ static int search_upload_choices(blg_ctx *c, const uint8_t *bc, const int64_t *o
             CK(cudaMemsetAsync(d_buf, 0, kSlackBefore, c->stream), "memset slack");
             CK(cudaMemsetAsync(d_buf + kSlackBefore + bytes, 0, kSlackAfter, c->stream), "memset slack");
             OwnedStrings &cs = s->cs;                          // owned by sorted_mem
-            s->h_lstart = lstart;
+            s->h_lstart = L.lstart;
             cs.d.buf = d_buf + kSlackBefore;
             cs.d.off = d_soff;
             cs.d.n = nc;
@@ -1155,6 +1208,7 @@ static int search_upload_queries(blg_ctx *c, const uint8_t *bq, const int64_t *o
     // one block: the sketches (8 B each), then the 4-gram counts (16 B each, 16-byte aligned)
     const size_t nq1 = (size_t)std::max<int64_t>(nq, 1), o_cnt = (8 * nq1 + 15) & ~size_t(15);
     CK(dev_alloc(c, (void **)&s->qsk, o_cnt + 16 * nq1), "cudaMallocAsync(sketches)");
+    s->sk_mem = s->qsk;
     s->qcnt = (uint4 *)((uint8_t *)s->qsk + o_cnt);
     CK(launch(c, "sketch", [&] { return launch_sketch_strings(c->stream, c->sms, s->q.d, s->qsk, s->qcnt, c->d_status); }),
        "sketch");
@@ -1441,7 +1495,8 @@ static void search_release(blg_ctx *c, blg_search *s) {
     s->pfx_mem = nullptr;
     s->pfx_work = nullptr;
     s->pfx = false;
-    dev_free(c, s->qsk);
+    dev_free(c, s->sk_mem);
+    s->sk_mem = nullptr;
     s->csk = s->qsk = nullptr;
     s->ccnt = s->qcnt = nullptr;
     s->tt_words = nullptr;
@@ -1452,12 +1507,20 @@ static void search_release(blg_ctx *c, blg_search *s) {
 }
 
 // ------------------------------------------------------------ batches --
+// A batch upload lays every problem out in two device blocks: `raw` (each
+// problem's queries and choices as given, with slack) and `meta` (the rest,
+// in three regions: A the choice permutations, copied from pinned memory in
+// one copy; B the host-built tables -- length buckets, class query lists,
+// launch descriptors, the jobs -- copied from the pinned arena in one copy;
+// C what the device writes: sorted copies, offsets, sketches, Peq tables,
+// survivor plans). The per-problem searches are views into those blocks.
 struct blg_batch {
     std::vector<blg_search *> probs;
     std::vector<int> kk, dt;
     std::vector<void *> outs;
     std::vector<int> regular;         // problems outside the persistent kernel (long queries)
-    BatchJob *d_jobs = nullptr;
+    void *d_raw = nullptr, *d_meta = nullptr;
+    BatchJob *d_jobs = nullptr;       // views into d_meta
     int njobs = 0;
     int64_t *d_job_tiles = nullptr, *d_tile_base = nullptr;
     int32_t *d_work = nullptr;
@@ -1473,57 +1536,364 @@ struct blg_batch {
 static void batch_release(blg_ctx *c, blg_batch *b) {
     for (auto *s : b->probs) {
         if (!s) continue;
-        search_release(c, s);
+        search_release(c, s);         // views: nothing of its own to free
         delete s;
     }
     b->probs.clear();
-    dev_free(c, b->d_jobs);
-    dev_free(c, b->d_job_tiles);
-    dev_free(c, b->d_tile_base);
-    dev_free(c, b->d_work);
-    dev_free(c, b->d_fills);
+    dev_free(c, b->d_raw);
+    dev_free(c, b->d_meta);
+    b->d_raw = b->d_meta = nullptr;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     b->exec = nullptr;
     b->graph = nullptr;
 }
 
-static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch *b) {
+// Byte layout of a block: parts 256-byte aligned, in the order taken.
+struct BlockLayout {
+    size_t size = 0;
+    size_t take(size_t bytes) {
+        const size_t o = (size + 255) & ~size_t(255);
+        size = o + bytes;
+        return o;
+    }
+};
+
+// The pinned arena of the context, at least `bytes` (null if it cannot be had).
+static uint8_t *host_arena(blg_ctx *c, size_t bytes) {
+    if (bytes > c->arena_bytes) {
+        if (c->arena) cudaFreeHost(c->arena);
+        c->arena = nullptr;
+        c->arena_bytes = 0;
+        if (cudaHostAlloc(&c->arena, bytes, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        c->arena_bytes = bytes;
+    }
+    return (uint8_t *)c->arena;
+}
+
+// Problems are cut into up to kUploadGroups groups of similar byte counts.
+// The raw strings stream in on the upload stream group by group; the host
+// meanwhile finds each problem's length range and query classes and lays
+// out the tables, which follow the first group's strings on the same
+// stream. Each group's preparation kernels (length sort, sorted offsets,
+// gather + sketches, Peq tables) start on the context stream once its
+// strings have landed, so they overlap the next groups' copies.
+constexpr int kUploadGroups = 4;
+
+static int batch_upload_body(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch *b,
+                             std::vector<cudaEvent_t> &ev) {
     if (nprob < 0 || (nprob > 0 && !pr)) return fail(c, BLG_ERR_ARG, "bad problem list");
-    std::vector<BatchJob> jobs;
-    std::vector<BatchFill> fills;
-    // one pinned region per problem for its permutation, reserved up front
-    size_t stage_words = 0;
-    for (int i = 0; i < nprob; i++)
-        if (pr[i].nq > 0 && pr[i].nc > 0) stage_words += (size_t)pr[i].nc;
-    int32_t *stage = stage_words ? (int32_t *)host_stage(c, sizeof(int32_t) * stage_words) : nullptr;
-    if (stage_words && !stage) return fail(c, BLG_ERR_ALLOC, "cudaHostAlloc(staging)");
-    size_t stage_at = 0;
+    auto pfail = [&](int i, const char *what) { return fail(c, BLG_ERR_ARG, "problem " + std::to_string(i) + ": " + what); };
+    std::vector<char> work((size_t)nprob, 0);
     for (int i = 0; i < nprob; i++) {
         const blg_problem &p = pr[i];
-        if (!dtype_ok(p.dtype)) return fail(c, BLG_ERR_ARG, "problem " + std::to_string(i) + ": bad dtype");
-        if (p.nq < 0 || p.nc < 0) return fail(c, BLG_ERR_ARG, "problem " + std::to_string(i) + ": negative count");
-        if (p.nq > 0 && p.nc > 0 && !p.d_out)
-            return fail(c, BLG_ERR_ARG, "problem " + std::to_string(i) + ": null device output");
-        const int k = p.max_dist < 0 ? -1 : p.max_dist;
+        if (!dtype_ok(p.dtype)) return pfail(i, "bad dtype");
+        if (p.nq < 0 || p.nc < 0) return pfail(i, "negative count");
+        if (p.nq == 0 || p.nc == 0) continue;
+        if (!p.d_out) return pfail(i, "null device output");
+        int rc = check_offsets_host(c, p.off_q, p.nq);
+        if (!rc) rc = check_offsets_host(c, p.off_c, p.nc);
+        if (rc) return rc;
+        if ((p.off_q[p.nq] > p.off_q[0] && !p.buf_q) || (p.off_c[p.nc] > p.off_c[0] && !p.buf_c))
+            return pfail(i, "null buffer");
+        work[i] = 1;
+    }
+    // ---- raw strings: one block; groups of contiguous problems with about
+    // equal bytes
+    struct Raw { size_t q, qoff, c, coff; };
+    std::vector<Raw> raw((size_t)nprob);
+    BlockLayout rl;
+    for (int i = 0; i < nprob; i++) {
+        if (!work[i]) continue;
+        const blg_problem &p = pr[i];
+        raw[i].q = rl.take(kSlackBefore + (size_t)(p.off_q[p.nq] - p.off_q[0]) + kSlackAfter) + kSlackBefore;
+        raw[i].qoff = rl.take(8 * (size_t)(p.nq + 1));
+        raw[i].c = rl.take(kSlackBefore + (size_t)(p.off_c[p.nc] - p.off_c[0]) + kSlackAfter) + kSlackBefore;
+        raw[i].coff = rl.take(8 * (size_t)(p.nc + 1));
+    }
+    std::vector<int> grp((size_t)nprob, 0);
+    int G = 0;
+    {
+        size_t done = 0;
+        for (int i = 0; i < nprob; i++) {
+            if (!work[i]) continue;
+            grp[i] = std::min(kUploadGroups - 1, (int)(done * kUploadGroups / std::max<size_t>(rl.size, 1)));
+            done = raw[i].coff + 8 * (size_t)(pr[i].nc + 1);
+            G = grp[i] + 1;
+        }
+    }
+    // events: [0, G) each group's strings landed (group 0: and the tables);
+    // [G] the strings' block allocated; [G + 1] the tables' block allocated
+    for (int g = 0; g < G + 2; g++) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+        ev.push_back(e);
+    }
+    if (rl.size) CK(dev_alloc(c, &b->d_raw, rl.size), "cudaMallocAsync(batch strings)");
+    CK(cudaEventRecord(ev[G], c->stream), "event");
+    CK(cudaStreamWaitEvent(c->up, ev[G], 0), "wait");
+    uint8_t *R = (uint8_t *)b->d_raw;
+    for (int i = 0; i < nprob; i++) {
+        const blg_problem &p = pr[i];
         blg_search *s = new (std::nothrow) blg_search();
         if (!s) return fail(c, BLG_ERR_ALLOC, "host allocation");
         b->probs.push_back(s);
-        b->kk.push_back(k);
+        b->kk.push_back(p.max_dist < 0 ? -1 : p.max_dist);
         b->dt.push_back(p.dtype);
         b->outs.push_back(p.d_out);
-        if (p.nq == 0 || p.nc == 0) continue;
-        // the batch kernels read the length-sorted copy only (no tile-transposed copy)
-        int rc = search_upload(c, p.buf_q, p.off_q, p.nq, p.buf_c, p.off_c, p.nc, s, NEED_SORTED, stage + stage_at);
-        stage_at += (size_t)p.nc;
-        if (rc) return rc;
+        if (!work[i]) continue;
+        s->nq = p.nq;
+        s->nc = p.nc;
+        auto view = [&](OwnedStrings &o, size_t at, size_t off_at, const int64_t *off, int64_t n) {
+            o.d.buf = R + at;
+            o.d.off = (const int64_t *)(R + off_at);
+            o.d.n = n;
+            o.d.base = off[0];
+            o.d.bytes = off[n] - off[0];
+        };
+        view(s->q, raw[i].q, raw[i].qoff, p.off_q, p.nq);
+        view(s->c, raw[i].c, raw[i].coff, p.off_c, p.nc);
         b->pairs += p.nq * p.nc;
-        bool eligible = s->lsorted;
-        for (auto &cl : s->cls) eligible &= !cl.lanes && cl.nw <= kBatchMaxWords;
-        if (!eligible) {
-            b->regular.push_back(i);
-            continue;
+    }
+    // the strings of problems [i0, i1) on the upload stream
+    auto copy_raw = [&](int i0, int i1) -> cudaError_t {
+        for (int i = i0; i < i1; i++) {
+            if (!work[i]) continue;
+            const blg_problem &p = pr[i];
+            const blg_search *s = b->probs[i];
+            const struct { const DevStrings &d; const uint8_t *buf; const int64_t *off; } side[2] = {
+                {s->q.d, p.buf_q, p.off_q}, {s->c.d, p.buf_c, p.off_c}};
+            for (const auto &x : side) {
+                cudaError_t e = cudaSuccess;
+                if (x.d.bytes > 0)
+                    e = cudaMemcpyAsync((uint8_t *)x.d.buf, x.buf + x.off[0], (size_t)x.d.bytes, cudaMemcpyHostToDevice,
+                                        c->up);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync((int64_t *)x.d.off, x.off, 8 * (size_t)(x.d.n + 1), cudaMemcpyHostToDevice, c->up);
+                if (e != cudaSuccess) return e;
+            }
         }
+        return cudaSuccess;
+    };
+    int g0_end = 0;                           // the first problem after group 0
+    while (g0_end < nprob && (!work[g0_end] || grp[g0_end] == 0)) g0_end++;
+    CK(copy_raw(0, g0_end), "H2D batch strings");
+    // ---- host, while group 0's strings fly: each problem's length range
+    // (choices) and query classes, problems spread over the pool
+    struct Prep {
+        int64_t mn = 0, mx = 0;
+        bool ok = true, neg = false;
+        std::vector<QueryClass> cls;
+    };
+    std::vector<Prep> prep((size_t)nprob);
+    std::vector<int> order;
+    for (int i = 0; i < nprob; i++)
+        if (work[i]) order.push_back(i);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return pr[x].nc > pr[y].nc; });
+    std::atomic<size_t> next{0};
+    HostPool::get().run(HostPool::get().size(), [&](int) {
+        for (size_t t; (t = next++) < order.size();) {
+            const int i = order[t];
+            Prep &P = prep[i];
+            const int64_t *oc = pr[i].off_c, *oq = pr[i].off_q;
+            int64_t mn = INT64_MAX, mx = INT64_MIN;
+            for (int64_t x = 0; x < pr[i].nc; x++) {
+                const int64_t l = oc[x + 1] - oc[x];
+                mn = std::min(mn, l);
+                mx = std::max(mx, l);
+            }
+            for (int64_t x = 0; x < pr[i].nq; x++) P.neg |= oq[x + 1] < oq[x];
+            P.mn = mn;
+            P.mx = mx;
+            P.neg |= mn < 0;
+            P.ok = query_classes(oq, 0, pr[i].nq, P.cls);
+        }
+    });
+    for (int i = 0; i < nprob; i++) {
+        if (!work[i]) continue;
+        if (prep[i].neg) return fail(c, BLG_ERR_ARG, "corrupt offsets (not monotone or out of range)");
+        if (!prep[i].ok) return fail(c, BLG_ERR_ARG, "query longer than 2048 bytes is not supported");
+    }
+    // ---- which problems the persistent kernels take; the jobs and fills
+    std::vector<char> sorted((size_t)nprob, 0), eligible((size_t)nprob, 0);
+    int njobs = 0, nfill = 0, nclass = 0, nsorted = 0, nwork = 0;
+    for (int i = 0; i < nprob; i++) {
+        if (!work[i]) continue;
+        nwork++;
+        nclass += (int)prep[i].cls.size();
+        sorted[i] = pr[i].nc < INT32_MAX && prep[i].mx - prep[i].mn < (1 << 22);
+        nsorted += sorted[i];
+        bool e = sorted[i];
+        for (auto &q : prep[i].cls) e &= !q.lanes && q.nw <= kBatchMaxWords;
+        eligible[i] = e;
+        if (e) {
+            njobs += (int)prep[i].cls.size();
+            if (b->kk[i] >= 0) nfill++;
+        } else {
+            b->regular.push_back(i);
+        }
+    }
+    // ---- the meta block: B host-built tables, then C device-written
+    struct At {
+        size_t hist = 0, tab = 0, perm = 0, soff = 0, csk = 0, ccnt = 0, sbuf = 0, qsk = 0, qcnt = 0;
+        std::vector<size_t> both, lo, hi, wk, ts, peq;
+    };
+    std::vector<At> at((size_t)nprob);
+    BlockLayout ml;
+    const size_t b_begin = ml.take(0);
+    for (int i = 0; i < nprob; i++)
+        if (work[i])
+            for (auto &q : prep[i].cls) at[i].both.push_back(ml.take(sizeof(int32_t) * 2 * q.idx.size()));
+    const size_t b_ls = ml.take(sizeof(LenSortSet) * (size_t)nsorted),
+                 b_ls_start = ml.take(sizeof(int64_t) * (size_t)(nsorted + 1)),
+                 b_prep = ml.take(sizeof(UploadPrep) * (size_t)nwork),
+                 b_prep_start = ml.take(sizeof(int64_t) * (size_t)(nwork + 1)),
+                 b_sk = ml.take(sizeof(SketchSet) * (size_t)(nwork + nsorted)),
+                 b_sk_start = ml.take(sizeof(int64_t) * (size_t)(nwork + nsorted + 1)),
+                 b_peq = ml.take(sizeof(PeqSet) * (size_t)nclass),
+                 b_peq_start = ml.take(sizeof(int64_t) * (size_t)(nclass + 1)),
+                 b_jobs = ml.take(sizeof(BatchJob) * (size_t)njobs),
+                 b_fills = ml.take(sizeof(BatchFill) * (size_t)nfill);
+    const size_t b_end = ml.take(0);
+    const size_t c_hist = ml.take(0);         // the count arrays, contiguous: one memset clears them
+    for (int i = 0; i < nprob; i++)
+        if (work[i] && sorted[i]) at[i].hist = ml.take(8 * (size_t)(prep[i].mx - prep[i].mn + 1));
+    const size_t c_hist_end = ml.take(0);
+    for (int i = 0; i < nprob; i++) {
+        if (!work[i]) continue;
+        const blg_problem &p = pr[i];
+        if (sorted[i]) {
+            const int64_t n_len = prep[i].mx - prep[i].mn + 1;
+            at[i].tab = ml.take(sizeof(int64_t) * (size_t)(2 * n_len + 1));
+            at[i].perm = ml.take(sizeof(int32_t) * (size_t)p.nc);
+            at[i].soff = ml.take(sizeof(int64_t) * (size_t)(p.nc + 1));
+            at[i].csk = ml.take(sizeof(uint64_t) * (size_t)p.nc);
+            at[i].ccnt = ml.take(sizeof(uint4) * (size_t)p.nc);
+            at[i].sbuf = ml.take(kSlackBefore + (size_t)b->probs[i]->c.d.bytes + kSlackAfter) + kSlackBefore;
+        }
+        at[i].qsk = ml.take(sizeof(uint64_t) * (size_t)p.nq);
+        at[i].qcnt = ml.take(sizeof(uint4) * (size_t)p.nq);
+        for (auto &q : prep[i].cls) {
+            const size_t nq = q.idx.size();
+            at[i].lo.push_back(ml.take(4 * nq));
+            at[i].hi.push_back(ml.take(4 * nq));
+            at[i].wk.push_back(ml.take(256));
+            at[i].ts.push_back(ml.take(8 * (nq + 1)));
+            at[i].peq.push_back(ml.take(sizeof(uint64_t) * 256 * (size_t)q.nw * nq));
+        }
+    }
+    const size_t c_job_tiles = ml.take(sizeof(int64_t) * (size_t)std::max(njobs, 1)),
+                 c_tile_base = ml.take(sizeof(int64_t) * (size_t)(njobs + 1)), c_work = ml.take(2 * sizeof(int32_t));
+    CK(dev_alloc(c, &b->d_meta, ml.size), "cudaMallocAsync(batch tables)");
+    CK(cudaEventRecord(ev[G + 1], c->stream), "event");
+    uint8_t *M = (uint8_t *)b->d_meta;
+    // ---- the problems' views, and region B built in the pinned arena
+    const size_t b_bytes = b_end - b_begin;
+    std::vector<uint8_t> pageable;
+    uint8_t *H = host_arena(c, b_bytes);
+    if (!H) {
+        pageable.resize(b_bytes);
+        H = pageable.data();
+    }
+    auto hb = [&](size_t off) { return H + (off - b_begin); };
+    LenSortSet *lss = (LenSortSet *)hb(b_ls);
+    int64_t *lss_start = (int64_t *)hb(b_ls_start);
+    UploadPrep *ups = (UploadPrep *)hb(b_prep);
+    int64_t *ups_start = (int64_t *)hb(b_prep_start);
+    SketchSet *sks = (SketchSet *)hb(b_sk);
+    int64_t *sks_start = (int64_t *)hb(b_sk_start);
+    PeqSet *pqs = (PeqSet *)hb(b_peq);
+    int64_t *pqs_start = (int64_t *)hb(b_peq_start);
+    BatchJob *jobs = (BatchJob *)hb(b_jobs);
+    BatchFill *fills = (BatchFill *)hb(b_fills);
+    int nl = 0, nu = 0, nsk = 0, npq = 0, nj = 0, nf = 0, max_nwc = 1;
+    lss_start[0] = ups_start[0] = sks_start[0] = pqs_start[0] = 0;
+    // each group's first set of every kind
+    std::vector<int> gl((size_t)G + 1, 0), gu((size_t)G + 1, 0), gk((size_t)G + 1, 0), gq((size_t)G + 1, 0);
+    for (int i = 0; i < nprob; i++) {
+        if (!work[i]) continue;
+        const blg_problem &p = pr[i];
+        blg_search *s = b->probs[i];
+        Prep &P = prep[i];
+        for (int g = grp[i] + 1; g <= G; g++) {
+            gl[g] = nl + (sorted[i] ? 1 : 0);
+            gu[g] = nu + 1;
+            gk[g] = nsk + 1 + (sorted[i] ? 1 : 0);
+            gq[g] = npq + (int)P.cls.size();
+        }
+        s->qsk = (uint64_t *)(M + at[i].qsk);
+        s->qcnt = (uint4 *)(M + at[i].qcnt);
+        UploadPrep u{};
+        u.buf[0] = (uint8_t *)s->q.d.buf;
+        u.bytes[0] = s->q.d.bytes;
+        u.buf[1] = (uint8_t *)s->c.d.buf;
+        u.bytes[1] = s->c.d.bytes;
+        sks[nsk] = SketchSet{s->q.d, nullptr, nullptr, nullptr, s->qsk, s->qcnt, p.nq};
+        sks_start[nsk + 1] = sks_start[nsk] + p.nq;
+        nsk++;
+        if (sorted[i]) {
+            const int64_t n_len = P.mx - P.mn + 1;
+            s->perm = (int32_t *)(M + at[i].perm);
+            s->lstart = (int64_t *)(M + at[i].tab);
+            s->csk = (uint64_t *)(M + at[i].csk);
+            s->ccnt = (uint4 *)(M + at[i].ccnt);
+            s->cs.d.buf = M + at[i].sbuf;
+            s->cs.d.off = (const int64_t *)(M + at[i].soff);
+            s->cs.d.n = p.nc;
+            s->cs.d.base = 0;
+            s->cs.d.bytes = s->c.d.bytes;
+            s->min_len = P.mn;
+            s->n_len = n_len;
+            s->lsorted = true;
+            lss[nl] = LenSortSet{s->c.d.off, p.nc, P.mn, n_len, (unsigned long long *)(M + at[i].hist), s->lstart,
+                                 s->lstart + n_len + 1, s->perm};
+            lss_start[nl + 1] = lss_start[nl] + p.nc;
+            nl++;
+            u.buf[2] = M + at[i].sbuf;
+            u.bytes[2] = s->c.d.bytes;
+            u.lstart = s->lstart;
+            u.bstart = s->lstart + n_len + 1;
+            u.n_len = n_len;
+            u.min_len = P.mn;
+            u.n_sorted = p.nc;
+            u.soff = (int64_t *)(M + at[i].soff);
+            sks[nsk] = SketchSet{s->c.d, s->perm, s->cs.d.off, M + at[i].sbuf, s->csk, s->ccnt, p.nc};
+            sks_start[nsk + 1] = sks_start[nsk] + p.nc;
+            nsk++;
+        }
+        ups[nu] = u;
+        ups_start[nu + 1] = ups_start[nu] + u.n_sorted + 1;
+        nu++;
+        for (size_t x = 0; x < P.cls.size(); x++) {
+            const QueryClass &q = P.cls[x];
+            const size_t nq = q.idx.size();
+            blg_search::Cls k{};
+            k.lanes = q.lanes;
+            k.nw = q.nw;
+            k.nq = (int)nq;
+            k.qidx = (int32_t *)(M + at[i].both[x]);
+            k.qlen = k.qidx + nq;
+            k.lo = (int32_t *)(M + at[i].lo[x]);
+            k.hi = (int32_t *)(M + at[i].hi[x]);
+            k.work = (int32_t *)(M + at[i].wk[x]);
+            k.tile_start = (int64_t *)(M + at[i].ts[x]);
+            k.peq = (uint64_t *)(M + at[i].peq[x]);
+            k.mem = nullptr;
+            k.h_qlen = q.len;
+            int32_t *both = (int32_t *)hb(at[i].both[x]);
+            std::copy(q.idx.begin(), q.idx.end(), both);
+            std::copy(q.len.begin(), q.len.end(), both + nq);
+            pqs[npq] = PeqSet{s->q.d, k.qidx, k.peq, k.nw};
+            pqs_start[npq + 1] = pqs_start[npq] + (int64_t)nq;
+            npq++;
+            max_nwc = std::max(max_nwc, k.nw);
+            s->cls.push_back(std::move(k));
+        }
+        if (!eligible[i]) continue;
+        const int k = b->kk[i];
         for (auto &cl : s->cls) {
             BatchJob j{};
             j.CS = s->cs.d;
@@ -1545,34 +1915,86 @@ static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch 
             j.ccnt = s->ccnt;
             j.qcnt = s->qcnt;
             j.out = p.d_out;
-            jobs.push_back(j);
+            jobs[nj++] = j;
         }
         if (k >= 0) {
             const uint32_t v = (uint32_t)(p.dtype == BLG_UINT8 ? std::min(k + 1, 255)
                                           : p.dtype == BLG_UINT16 ? std::min(k + 1, 65535) : k + 1);
-            fills.push_back(BatchFill{p.d_out, p.nq * p.nc, p.dtype, v});
+            fills[nf++] = BatchFill{p.d_out, p.nq * p.nc, p.dtype, v};
             b->max_fill = std::max(b->max_fill, p.nq * p.nc * (int64_t)dtype_size(p.dtype));
         }
     }
     // banded jobs first (they run in their own persistent kernel)
-    std::stable_partition(jobs.begin(), jobs.end(), [](const BatchJob &j) { return j.k >= 0 && j.k <= 31; });
-    b->nbanded = (int)std::count_if(jobs.begin(), jobs.end(), [](const BatchJob &j) { return j.k >= 0 && j.k <= 31; });
-    b->njobs = (int)jobs.size();
-    b->nfill = (int)fills.size();
-    if (b->njobs > 0) {
-        CK(dev_alloc(c, (void **)&b->d_jobs, sizeof(BatchJob) * jobs.size()), "alloc jobs");
-        CK(cudaMemcpyAsync(b->d_jobs, jobs.data(), sizeof(BatchJob) * jobs.size(), cudaMemcpyHostToDevice, c->stream), "H2D jobs");
-        CK(dev_alloc(c, (void **)&b->d_job_tiles, sizeof(int64_t) * jobs.size()), "alloc job tiles");
-        CK(dev_alloc(c, (void **)&b->d_tile_base, sizeof(int64_t) * (jobs.size() + 1)), "alloc tile base");
-        CK(dev_alloc(c, (void **)&b->d_work, 2 * sizeof(int32_t)), "alloc work");
+    std::stable_partition(jobs, jobs + nj, [](const BatchJob &j) { return j.k >= 0 && j.k <= 31; });
+    b->nbanded = (int)std::count_if(jobs, jobs + nj, [](const BatchJob &j) { return j.k >= 0 && j.k <= 31; });
+    b->njobs = nj;
+    b->nfill = nf;
+    b->d_jobs = (BatchJob *)(M + b_jobs);
+    b->d_fills = (BatchFill *)(M + b_fills);
+    b->d_job_tiles = (int64_t *)(M + c_job_tiles);
+    b->d_tile_base = (int64_t *)(M + c_tile_base);
+    b->d_work = (int32_t *)(M + c_work);
+    // ---- the tables behind group 0's strings, then the other groups
+    CK(cudaStreamWaitEvent(c->up, ev[G + 1], 0), "wait");
+    CK(cudaMemcpyAsync(M + b_begin, H, b_bytes, cudaMemcpyHostToDevice, c->up), "H2D batch tables");
+    if (G > 0) CK(cudaEventRecord(ev[0], c->up), "event");
+    for (int g = 1; g < G; g++) {
+        int i0 = 0, i1 = 0;
+        while (i0 < nprob && (!work[i0] || grp[i0] < g)) i0++;
+        i1 = i0;
+        while (i1 < nprob && (!work[i1] || grp[i1] == g)) i1++;
+        CK(copy_raw(i0, i1), "H2D batch strings");
+        CK(cudaEventRecord(ev[g], c->up), "event");
     }
-    if (b->nfill > 0) {
-        CK(dev_alloc(c, (void **)&b->d_fills, sizeof(BatchFill) * fills.size()), "alloc fills");
-        CK(cudaMemcpyAsync(b->d_fills, fills.data(), sizeof(BatchFill) * fills.size(), cudaMemcpyHostToDevice, c->stream), "H2D fills");
+    if (c_hist_end > c_hist) CK(cudaMemsetAsync(M + c_hist, 0, c_hist_end - c_hist, c->stream), "memset counts");
+    for (int g = 0; g < G; g++) {
+        CK(cudaStreamWaitEvent(c->stream, ev[g], 0), "wait");
+        const int l0 = gl[g], l1 = gl[g + 1], u0 = gu[g], u1 = gu[g + 1], k0 = gk[g], k1 = gk[g + 1], q0 = gq[g],
+                  q1 = gq[g + 1];
+        CK(launch(c, "length_sort", [&] {
+               return launch_length_sort(c->stream, c->sms, (const LenSortSet *)(M + b_ls) + l0,
+                                         (const int64_t *)(M + b_ls_start) + l0, l1 - l0, lss_start[l0],
+                                         lss_start[l1] - lss_start[l0]);
+           }), "length_sort");
+        CK(launch(c, "upload_prep", [&] {
+               return launch_upload_prep(c->stream, c->sms, (const UploadPrep *)(M + b_prep) + u0,
+                                         (const int64_t *)(M + b_prep_start) + u0, u1 - u0, ups_start[u0],
+                                         ups_start[u1] - ups_start[u0]);
+           }), "upload_prep");
+        CK(launch(c, "sketch_sets", [&] {
+               return launch_sketch_sets(c->stream, c->sms, (const SketchSet *)(M + b_sk) + k0,
+                                         (const int64_t *)(M + b_sk_start) + k0, k1 - k0, sks_start[k0],
+                                         sks_start[k1] - sks_start[k0], c->d_status);
+           }), "sketch_sets");
+        CK(launch(c, "peq_sets", [&] {
+               return launch_peq_sets(c->stream, (const PeqSet *)(M + b_peq) + q0, (const int64_t *)(M + b_peq_start) + q0,
+                                      q1 - q0, pqs_start[q0], pqs_start[q1] - pqs_start[q0], max_nwc, c->d_status);
+           }), "peq_sets");
     }
     CK(batch_set_attributes(), "kernel attributes");
+    // the arena is read by the tables' copy; the context stream waited for
+    // every group's strings
     CK(cudaStreamSynchronize(c->stream), "sync upload");
+    // problems outside the persistent kernels plan their survivor jobs on
+    // the host from the length buckets
+    for (int i : b->regular) {
+        blg_search *s = b->probs[i];
+        if (!s->lsorted) continue;
+        s->h_lstart.resize((size_t)s->n_len + 1);
+        CK(cudaMemcpy(s->h_lstart.data(), s->lstart, 8 * (size_t)(s->n_len + 1), cudaMemcpyDeviceToHost),
+           "D2H length buckets");
+    }
     return BLG_OK;
+}
+
+static int batch_upload(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch *b) {
+    std::vector<cudaEvent_t> ev;
+    const int rc = batch_upload_body(c, pr, nprob, b, ev);
+    // after a failure, copies on the upload stream may still be in flight:
+    // they end before the caller frees their destination
+    cudaStreamSynchronize(c->up);
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    return rc;
 }
 
 // First run: capture the batch's launches into one CUDA graph; every run
@@ -1937,6 +2359,7 @@ void blg_destroy(blg_ctx *c) {
     if (c->t1) cudaEventDestroy(c->t1);
     if (c->stage_done) cudaEventDestroy(c->stage_done);
     if (c->stage) cudaFreeHost(c->stage);
+    if (c->arena) cudaFreeHost(c->arena);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->up) cudaStreamDestroy(c->up);
     if (c->down) cudaStreamDestroy(c->down);

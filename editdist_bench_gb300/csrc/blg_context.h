@@ -17,8 +17,8 @@ struct blg_tuning {
     int lpt_job = 4096;                          // thresholded search: survivors per job
     int surv_round = 16;                         // thresholded search: columns per lane round (8, 16, 32)
     int band_ctas = 3;                           // banded pairs solver: CTAs per SM
-    int tile_shape = 2;                          // short-pair tile kernel: 1 = one stage of 512 pairs, 2 = two of 512,
-                                                 // 3 = two of 256
+    int tile_shape = 1;                          // short-pair tile kernel: 1 = one stage of 512 pairs, 2 = two of 512,
+                                                 // 3 = two of 256 (1M pairs of 32 bytes: 61, 79, 76 us)
     int tuned = 0;
 };
 
@@ -50,6 +50,9 @@ struct blg_ctx {
     // pinned host staging for arrays the host builds and copies (grown on
     // demand; stage_done marks the end of the last copy out of it)
     void *stage = nullptr;
+    // pinned room for a batch upload's small host-built tables (HostArena)
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
     size_t stage_bytes = 0;
     cudaEvent_t stage_done = nullptr;
     std::vector<ProfRec> prof_recs;

@@ -25,7 +25,8 @@ namespace blg {
 // (one unaligned 4-byte read each, consecutive across the warp) and counts
 // them in its own 16 byte counters (4 registers); every 255 steps, before a
 // lane counter can wrap, and at the end the counters are folded into
-// saturating totals, then summed over the warp with saturating byte adds.
+// saturating totals, then summed over the warp: with plain adds when the
+// string has fewer than 256 grams, else with saturating byte adds.
 // The sketch bits are an OR over the warp. The values equal the per-thread
 // functions' (the same grams, hash and saturation at 255).
 __global__ void __launch_bounds__(256) k_sketch_strings(DevStrings S, uint64_t *sketch, uint4 *counts,
@@ -55,10 +56,15 @@ __global__ void __launch_bounds__(256) k_sketch_strings(DevStrings S, uint64_t *
 #pragma unroll
             for (int w = 0; w < 4; w++) t[w] = __vaddus4(t[w], c[w]);
         }
+        if (n <= 256) {                // fewer than 256 grams: plain adds never carry into the next byte
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1)
+            for (int w = 0; w < 4; w++) t[w] = __reduce_add_sync(kFull, t[w]);
+        } else {
 #pragma unroll
-            for (int w = 0; w < 4; w++) t[w] = __vaddus4(t[w], __shfl_xor_sync(kFull, t[w], off));
+            for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+                for (int w = 0; w < 4; w++) t[w] = __vaddus4(t[w], __shfl_xor_sync(kFull, t[w], off));
+        }
         sk_lo = __reduce_or_sync(kFull, sk_lo);
         sk_hi = __reduce_or_sync(kFull, sk_hi);
         if (lane == 0) {
