@@ -69,10 +69,11 @@ struct TransposedChoices {
 // Choices sorted lexicographically for the exact search with prefix reuse
 // (k_search_pfx). A warp's 32 lanes hold different queries and share one
 // choice at a time, so the text, its length and its restart column are the
-// same on every lane. Each warp walks a chain of kPfxChain consecutive sorted
-// choices; a choice restarts at the largest checkpoint column not above its
-// common prefix with the previous sorted choice (0 at a chain start), from
-// the column state that choice's run saved there.
+// same on every lane. Each warp walks a chain of consecutive sorted choices
+// (kPfxChain, or a divisor of it when a launch has few queries); a choice
+// restarts at the largest checkpoint column not above its common prefix with
+// the previous sorted choice (0 at a chain start), from the column state that
+// choice's run saved there.
 // Text: sorted choice p occupies words text[woff[p] ..] with two characters
 // per 32-bit word, each character stored as its shared-memory Peq row offset
 // (alphabet index x kPfxRowBytes, 16 bits), so a column's Peq address needs
@@ -80,7 +81,6 @@ struct TransposedChoices {
 // in the choices (at most kPfxMaxSymbols).
 constexpr int kPfxChain = 32;
 constexpr int kPfxWarps = 8;                         // warps per CTA; a work item = kPfxWarps chains
-constexpr int kPfxItem = kPfxChain * kPfxWarps;      // sorted choices per work item
 constexpr int kPfxCheckpoints = 2;
 constexpr int kPfxMaxSymbols = 32;
 constexpr int kPfxRowBytes = 1024;                   // one symbol's Peq entries: 32 lanes x QI x NW x 8 B

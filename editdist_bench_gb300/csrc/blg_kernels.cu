@@ -157,10 +157,13 @@ __global__ void __launch_bounds__(256) k_search_ttq(TransposedChoices T, SearchC
 // Here a warp's 32 lanes hold QI queries each (QI*32 per warp, the same block
 // of queries for the whole CTA) and share one choice at a time: the text, the
 // choice length and the restart column are warp-uniform, so a skipped column
-// is skipped by the whole warp. Each warp walks a chain of kPfxChain
-// consecutive sorted choices (PrefixChoices), saving its lanes' column states
-// at the launch's checkpoint columns in shared memory; a choice restarts from
-// the checkpoint P.restart names (computed on the host). The block's Peq rows
+// is skipped by the whole warp. Each warp walks a chain of `chain`
+// consecutive sorted choices (a divisor of kPfxChain), saving its lanes'
+// column states at the launch's checkpoint columns in shared memory; the
+// chain's first choice starts from column 0 and every other one restarts
+// from the checkpoint P.restart names (computed on the host for chains of
+// kPfxChain, whose starts are chain starts here too). Shorter chains give a
+// launch over few queries enough work items to fill the GPU. The block's Peq rows
 // are staged per alphabet symbol as [symbol][query][lane] (conflict-free
 // 64-bit loads) and the text carries each character's row offset, so a
 // column's row address is one half-word extract for QI queries. A persistent
@@ -169,7 +172,7 @@ __global__ void __launch_bounds__(256) k_search_ttq(TransposedChoices T, SearchC
 // Results leave through the sort's permutation (P.orig).
 template <int NW, int QI>
 __global__ void __launch_bounds__(256) k_search_pfx(PrefixChoices P, SearchClass cls, unsigned long long *work,
-                                                    int64_t items, int dtype, void *out, uint32_t unit) {
+                                                    int64_t items, int chain, int dtype, void *out, uint32_t unit) {
     static_assert(QI * NW * 32 * 8 == kPfxRowBytes, "one symbol's entries fill a row");
     static_assert(kPfxCheckpoints == 2, "two checkpoint columns");
     static_assert(kPfxWarps * 32 == 256, "256 threads");
@@ -180,7 +183,7 @@ __global__ void __launch_bounds__(256) k_search_pfx(PrefixChoices P, SearchClass
     const Units u{unit, unit + unit};
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t nc = P.n;
-    const int64_t segs = (nc + kPfxItem - 1) / kPfxItem;
+    const int64_t seg_len = (int64_t)kPfxWarps * chain, segs = (nc + seg_len - 1) / seg_len;
     const int ck0 = P.ck[0], ck1 = P.ck[1];                    // (no dynamic index into the parameter block)
     const uint32_t hi16 = u.one << 16;
     const char *pl = reinterpret_cast<const char *>(s_peq) + lane * NW * 8;
@@ -214,13 +217,13 @@ __global__ void __launch_bounds__(256) k_search_pfx(PrefixChoices P, SearchClass
             __syncthreads();
             cur = qb;
         }
-        const int64_t p0 = seg * kPfxItem + (int64_t)warp * kPfxChain;
+        const int64_t p0 = seg * seg_len + (int64_t)warp * chain;
 #pragma unroll 1
-        for (int r = 0; r < kPfxChain; r++) {
+        for (int r = 0; r < chain; r++) {
             const int64_t p = p0 + r;
             if (p >= nc) break;                                // warp-uniform
             const int n = __ldg(P.len + p);
-            const int b = __ldg(P.restart + p);
+            const int b = r == 0 ? 0 : __ldg(P.restart + p);
             const uint32_t *tx = P.text + __ldg(P.woff + p);
             if (b == 0) {
 #pragma unroll
@@ -755,12 +758,18 @@ cudaError_t launch_search_tt(cudaStream_t st, int nw, bool hask, const Transpose
     }
 }
 
+// Chain length: the longest (most prefix reuse) that still gives the grid
+// at least 6 waves of (query block, chain group) items; 4 at the least.
 template <int NW, int QI>
 static cudaError_t launch_pfx_nw(cudaStream_t st, int grid, const PrefixChoices &P, const SearchClass &cls,
-                                 unsigned long long *work, int64_t items, int dtype, void *out) {
+                                 unsigned long long *work, int dtype, void *out) {
     const size_t smem = (size_t)P.nsym * kPfxRowBytes + (size_t)kPfxCheckpoints * QI * NW * 4 * 256 * 4;
+    const int64_t qblocks = (cls.nq + QI * 32 - 1) / (QI * 32);
+    int chain = kPfxChain;
+    auto items_of = [&](int ch) { return qblocks * ((P.n + (int64_t)kPfxWarps * ch - 1) / ((int64_t)kPfxWarps * ch)); };
+    while (chain > 4 && items_of(chain) < 6 * (int64_t)grid) chain >>= 1;
     cudaFuncSetAttribute(k_search_pfx<NW, QI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_search_pfx<NW, QI><<<grid, 256, smem, st>>>(P, cls, work, items, dtype, out, 1u);
+    k_search_pfx<NW, QI><<<grid, 256, smem, st>>>(P, cls, work, items_of(chain), chain, dtype, out, 1u);
     return cudaGetLastError();
 }
 
@@ -771,10 +780,9 @@ cudaError_t launch_search_pfx(cudaStream_t st, int sms, int ctas_per_sm, int nw,
                               const SearchClass &cls, unsigned long long *work, int dtype, void *out) {
     if (cls.nq <= 0 || P.n <= 0) return cudaSuccess;
     if (P.nsym < 1 || P.nsym > kPfxMaxSymbols) return cudaErrorInvalidValue;
-    const int64_t segs = (P.n + kPfxItem - 1) / kPfxItem;
     const int grid = sms * std::max(1, std::min(ctas_per_sm, 8));
-    if (nw == 1) return launch_pfx_nw<1, 4>(st, grid, P, cls, work, segs * ((cls.nq + 127) / 128), dtype, out);
-    if (nw == 2) return launch_pfx_nw<2, 2>(st, grid, P, cls, work, segs * ((cls.nq + 63) / 64), dtype, out);
+    if (nw == 1) return launch_pfx_nw<1, 4>(st, grid, P, cls, work, dtype, out);
+    if (nw == 2) return launch_pfx_nw<2, 2>(st, grid, P, cls, work, dtype, out);
     return cudaErrorInvalidValue;
 }
 
