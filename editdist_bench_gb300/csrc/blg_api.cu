@@ -1575,13 +1575,14 @@ static uint8_t *host_arena(blg_ctx *c, size_t bytes) {
 }
 
 // Problems are cut into up to kUploadGroups groups of similar byte counts.
-// The raw strings stream in on the upload stream group by group; the host
-// meanwhile finds each problem's length range and query classes and lays
-// out the tables, which follow the first group's strings on the same
-// stream. Each group's preparation kernels (length sort, sorted offsets,
+// The choices stream in on the upload stream group by group (their bytes
+// and offsets, two copies per problem); the host meanwhile finds each
+// problem's length range and query classes and lays out the tables, with
+// every problem's queries packed among them, which follow the first group's
+// choices on the same stream in one copy. Each group's preparation kernels (length sort, sorted offsets,
 // gather + sketches, Peq tables) start on the context stream once its
 // strings have landed, so they overlap the next groups' copies.
-constexpr int kUploadGroups = 4;
+constexpr int kUploadGroups = 8;
 
 static int batch_upload_body(blg_ctx *c, const blg_problem *pr, int nprob, blg_batch *b,
                              std::vector<cudaEvent_t> &ev) {
@@ -1601,18 +1602,24 @@ static int batch_upload_body(blg_ctx *c, const blg_problem *pr, int nprob, blg_b
             return pfail(i, "null buffer");
         work[i] = 1;
     }
-    // ---- raw strings: one block; groups of contiguous problems with about
-    // equal bytes
-    struct Raw { size_t q, qoff, c, coff; };
+    // ---- raw choices: one block; groups of contiguous problems with about
+    // equal bytes. Queries: packed back to back (bytes at qpos, offsets at
+    // qopos) into the tables' region, 16 zero bytes before them all and 48
+    // after (a problem's neighbours are its slack).
+    struct Raw { size_t c, coff; };
     std::vector<Raw> raw((size_t)nprob);
+    std::vector<size_t> qpos((size_t)nprob, 0), qopos((size_t)nprob, 0);
+    size_t qbytes = 0, qoffs = 0;
     BlockLayout rl;
     for (int i = 0; i < nprob; i++) {
         if (!work[i]) continue;
         const blg_problem &p = pr[i];
-        raw[i].q = rl.take(kSlackBefore + (size_t)(p.off_q[p.nq] - p.off_q[0]) + kSlackAfter) + kSlackBefore;
-        raw[i].qoff = rl.take(8 * (size_t)(p.nq + 1));
         raw[i].c = rl.take(kSlackBefore + (size_t)(p.off_c[p.nc] - p.off_c[0]) + kSlackAfter) + kSlackBefore;
         raw[i].coff = rl.take(8 * (size_t)(p.nc + 1));
+        qpos[i] = qbytes;
+        qopos[i] = qoffs;
+        qbytes += (size_t)(p.off_q[p.nq] - p.off_q[0]);
+        qoffs += (size_t)p.nq + 1;
     }
     std::vector<int> grp((size_t)nprob, 0);
     int G = 0;
@@ -1654,27 +1661,21 @@ static int batch_upload_body(blg_ctx *c, const blg_problem *pr, int nprob, blg_b
             o.d.base = off[0];
             o.d.bytes = off[n] - off[0];
         };
-        view(s->q, raw[i].q, raw[i].qoff, p.off_q, p.nq);
         view(s->c, raw[i].c, raw[i].coff, p.off_c, p.nc);
         b->pairs += p.nq * p.nc;
     }
-    // the strings of problems [i0, i1) on the upload stream
+    // the choices of problems [i0, i1) on the upload stream
     auto copy_raw = [&](int i0, int i1) -> cudaError_t {
         for (int i = i0; i < i1; i++) {
             if (!work[i]) continue;
             const blg_problem &p = pr[i];
-            const blg_search *s = b->probs[i];
-            const struct { const DevStrings &d; const uint8_t *buf; const int64_t *off; } side[2] = {
-                {s->q.d, p.buf_q, p.off_q}, {s->c.d, p.buf_c, p.off_c}};
-            for (const auto &x : side) {
-                cudaError_t e = cudaSuccess;
-                if (x.d.bytes > 0)
-                    e = cudaMemcpyAsync((uint8_t *)x.d.buf, x.buf + x.off[0], (size_t)x.d.bytes, cudaMemcpyHostToDevice,
-                                        c->up);
-                if (e == cudaSuccess)
-                    e = cudaMemcpyAsync((int64_t *)x.d.off, x.off, 8 * (size_t)(x.d.n + 1), cudaMemcpyHostToDevice, c->up);
-                if (e != cudaSuccess) return e;
-            }
+            const DevStrings &d = b->probs[i]->c.d;
+            cudaError_t e = cudaSuccess;
+            if (d.bytes > 0)
+                e = cudaMemcpyAsync((uint8_t *)d.buf, p.buf_c + p.off_c[0], (size_t)d.bytes, cudaMemcpyHostToDevice, c->up);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync((int64_t *)d.off, p.off_c, 8 * (size_t)(p.nc + 1), cudaMemcpyHostToDevice, c->up);
+            if (e != cudaSuccess) return e;
         }
         return cudaSuccess;
     };
@@ -1744,6 +1745,7 @@ static int batch_upload_body(blg_ctx *c, const blg_problem *pr, int nprob, blg_b
     std::vector<At> at((size_t)nprob);
     BlockLayout ml;
     const size_t b_begin = ml.take(0);
+    const size_t b_qbytes = ml.take(kSlackBefore + qbytes + kSlackAfter), b_qoff = ml.take(8 * qoffs);
     for (int i = 0; i < nprob; i++)
         if (work[i])
             for (auto &q : prep[i].cls) at[i].both.push_back(ml.take(sizeof(int32_t) * 2 * q.idx.size()));
@@ -1799,6 +1801,22 @@ static int batch_upload_body(blg_ctx *c, const blg_problem *pr, int nprob, blg_b
         H = pageable.data();
     }
     auto hb = [&](size_t off) { return H + (off - b_begin); };
+    // the queries, packed (a problem's bytes and its offsets as given)
+    {
+        uint8_t *qb = hb(b_qbytes);
+        memset(qb, 0, kSlackBefore);
+        memset(qb + kSlackBefore + qbytes, 0, kSlackAfter);
+        std::atomic<int> nx{0};
+        HostPool::get().run(HostPool::get().size(), [&](int) {
+            for (int i; (i = nx++) < nprob;) {
+                if (!work[i]) continue;
+                const blg_problem &p = pr[i];
+                const size_t nb = (size_t)(p.off_q[p.nq] - p.off_q[0]);
+                if (nb) memcpy(qb + kSlackBefore + qpos[i], p.buf_q + p.off_q[0], nb);
+                memcpy(hb(b_qoff) + 8 * qopos[i], p.off_q, 8 * (size_t)(p.nq + 1));
+            }
+        });
+    }
     LenSortSet *lss = (LenSortSet *)hb(b_ls);
     int64_t *lss_start = (int64_t *)hb(b_ls_start);
     UploadPrep *ups = (UploadPrep *)hb(b_prep);
@@ -1824,11 +1842,14 @@ static int batch_upload_body(blg_ctx *c, const blg_problem *pr, int nprob, blg_b
             gk[g] = nsk + 1 + (sorted[i] ? 1 : 0);
             gq[g] = npq + (int)P.cls.size();
         }
+        s->q.d.buf = M + b_qbytes + kSlackBefore + qpos[i];
+        s->q.d.off = (const int64_t *)(M + b_qoff) + qopos[i];
+        s->q.d.n = p.nq;
+        s->q.d.base = p.off_q[0];
+        s->q.d.bytes = p.off_q[p.nq] - p.off_q[0];
         s->qsk = (uint64_t *)(M + at[i].qsk);
         s->qcnt = (uint4 *)(M + at[i].qcnt);
-        UploadPrep u{};
-        u.buf[0] = (uint8_t *)s->q.d.buf;
-        u.bytes[0] = s->q.d.bytes;
+        UploadPrep u{};                          // (the packed queries' slack came with the tables)
         u.buf[1] = (uint8_t *)s->c.d.buf;
         u.bytes[1] = s->c.d.bytes;
         sks[nsk] = SketchSet{s->q.d, nullptr, nullptr, nullptr, s->qsk, s->qcnt, p.nq};
