@@ -88,7 +88,8 @@ cudaError_t launch_sketch_strings(cudaStream_t st, int sms, const DevStrings &S,
                                   uint32_t *status);
 cudaError_t launch_search_band(cudaStream_t st, int sms, int ctas_per_sm, int round, int jobsz, const SurvClasses &C,
                                const DevStrings &CS, const int32_t *perm, const uint4 *ccnt, const uint4 *qcnt, int k,
-                               int dtype, void *out, int64_t nc, const SurvRows *rows, uint32_t *status);
+                               int dtype, void *out, int64_t nc, const SurvRows *rows, const ResultList *list,
+                               const FillItems *fill, uint32_t *status);
 cudaError_t launch_surv_plan(cudaStream_t st, const SurvClasses &C, const int64_t *lstart, int64_t min_len,
                              int64_t n_len, int k, int tile);
 cudaError_t launch_search_surv(cudaStream_t st, int sms, int nw, const DevStrings &CS, const int32_t *perm,
@@ -1358,28 +1359,41 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
     const bool hask = k >= 0;
     const bool surv = hask && s->lsorted && c->sched != BLG_SCHED_PLAIN;
     if (surv) {
+        // the sequential classes' survivor plans in one launch; max_dist <=
+        // 31: their survivors in one more (lanes refilled as survivors
+        // finish), which also fills the output with k+1 and defers its
+        // results to the context's list (scattered after it; an in-place
+        // repair launch runs only if the list ran full). max_dist > 31: the
+        // fill kernel, then the full-word survivor kernels.
         const uint32_t fillv = (uint32_t)(dtype == BLG_UINT8 ? std::min(k + 1, 255)
                                           : dtype == BLG_UINT16 ? std::min(k + 1, 65535) : k + 1);
-        CK(launch(c, "fill", [&] {
-               return launch_fill(c->stream, c->sms, (uint8_t *)d_out + q0 * s->nc * (int64_t)dtype_size(dtype),
-                                  (q1 - q0) * s->nc, dtype, fillv);
-           }), "fill");
-    }
-    if (surv) {
-        // the sequential classes' survivor plans in one launch; max_dist <=
-        // 31: their survivors in one more (lanes refilled as survivors finish)
+        const BatchFill whole{(uint8_t *)d_out + q0 * s->nc * (int64_t)dtype_size(dtype), (q1 - q0) * s->nc, dtype,
+                              fillv};
         const SurvClasses C = seq_classes(s);
-        const bool band = k <= 31;
+        const bool band = k <= 31 && C.n > 0;
         const int job = band ? survivor_job_size(c, s, k) : 1024;
+        if (!band)
+            CK(launch(c, "fill", [&] { return launch_fill(c->stream, c->sms, whole.out, whole.n, dtype, fillv); }),
+               "fill");
         CK(launch(c, "surv_plan", [&] {
                return launch_surv_plan(c->stream, C, s->lstart, s->min_len, s->n_len, k, job);
            }), "surv_plan");
         if (band) {
+            const ResultList L{c->rl_hdr + 2, c->rl_hdr, c->rl_cap};
+            const FillItems F{nullptr, nullptr, 0, whole, fill_items_of(whole), c->rl_hdr + 1};
+            CK(cudaMemsetAsync(c->rl_hdr, 0, 2 * sizeof(unsigned long long), c->stream), "clear list");
             CK(launch(c, "search_band", [&] {
                    return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, c->tune.surv_round, job, C, s->cs.d,
-                                             s->perm, s->ccnt,
-                                             s->qcnt, k, dtype, d_out, s->nc, nullptr, c->d_status);
+                                             s->perm, s->ccnt, s->qcnt, k, dtype, d_out, s->nc, nullptr, &L, &F,
+                                             c->d_status);
                }), "search_band");
+            CK(launch(c, "list_scatter", [&] { return launch_list_scatter(c->stream, c->sms, L, C.work[0]); }),
+               "list_scatter");
+            CK(launch(c, "search_band_repair", [&] {
+                   return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, c->tune.surv_round, job, C, s->cs.d,
+                                             s->perm, s->ccnt, s->qcnt, k, dtype, d_out, s->nc, nullptr, &L, nullptr,
+                                             c->d_status);
+               }), "search_band_repair");
         } else {
             for (int i = 0; i < C.n; i++)
                 CK(launch(c, "search_surv", [&] {
@@ -1528,6 +1542,9 @@ struct blg_batch {
     BatchFill *d_fills = nullptr;
     int nfill = 0;
     int64_t max_fill = 0, pairs = 0;
+    ResultList list{};                // the banded kernel's deferred results (list.item null: none)
+    FillItems fill{};                 // the thresholded outputs as fill items of the banded kernel
+    unsigned long long *hdr = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int64_t graph_kernels = 0;
@@ -1758,7 +1775,8 @@ static int batch_upload_body(blg_ctx *c, const blg_problem *pr, int nprob, blg_b
                  b_peq = ml.take(sizeof(PeqSet) * (size_t)nclass),
                  b_peq_start = ml.take(sizeof(int64_t) * (size_t)(nclass + 1)),
                  b_jobs = ml.take(sizeof(BatchJob) * (size_t)njobs),
-                 b_fills = ml.take(sizeof(BatchFill) * (size_t)nfill);
+                 b_fills = ml.take(sizeof(BatchFill) * (size_t)nfill),
+                 b_fstart = ml.take(sizeof(int64_t) * (size_t)(nfill + 1));
     const size_t b_end = ml.take(0);
     const size_t c_hist = ml.take(0);         // the count arrays, contiguous: one memset clears them
     for (int i = 0; i < nprob; i++)
@@ -1789,6 +1807,9 @@ static int batch_upload_body(blg_ctx *c, const blg_problem *pr, int nprob, blg_b
     }
     const size_t c_job_tiles = ml.take(sizeof(int64_t) * (size_t)std::max(njobs, 1)),
                  c_tile_base = ml.take(sizeof(int64_t) * (size_t)(njobs + 1)), c_work = ml.take(2 * sizeof(int32_t));
+    // the banded kernel's deferred results: [count, fill items claimed], entries
+    constexpr unsigned long long kBatchListCap = 1u << 20;
+    const size_t c_list = ml.take(sizeof(unsigned long long) * (2 + kBatchListCap));
     CK(dev_alloc(c, &b->d_meta, ml.size), "cudaMallocAsync(batch tables)");
     CK(cudaEventRecord(ev[G + 1], c->stream), "event");
     uint8_t *M = (uint8_t *)b->d_meta;
@@ -1955,6 +1976,12 @@ static int batch_upload_body(blg_ctx *c, const blg_problem *pr, int nprob, blg_b
     b->d_job_tiles = (int64_t *)(M + c_job_tiles);
     b->d_tile_base = (int64_t *)(M + c_tile_base);
     b->d_work = (int32_t *)(M + c_work);
+    int64_t *fstart = (int64_t *)hb(b_fstart);
+    fstart[0] = 0;
+    for (int f = 0; f < nf; f++) fstart[f + 1] = fstart[f] + fill_items_of(fills[f]);
+    b->hdr = (unsigned long long *)(M + c_list);
+    b->list = ResultList{b->hdr + 2, b->hdr, kBatchListCap};
+    b->fill = FillItems{b->d_fills, (const int64_t *)(M + b_fstart), nf, BatchFill{}, fstart[nf], b->hdr + 1};
     // ---- the tables behind group 0's strings, then the other groups
     CK(cudaStreamWaitEvent(c->up, ev[G + 1], 0), "wait");
     CK(cudaMemcpyAsync(M + b_begin, H, b_bytes, cudaMemcpyHostToDevice, c->up), "H2D batch tables");
@@ -2026,8 +2053,10 @@ static int batch_run(blg_ctx *c, blg_batch *b) {
         c->prof = false;                      // no per-launch events inside a capture
         const int64_t before = c->launches;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "begin capture");
-        BatchPlan plan{b->d_jobs, b->njobs, b->nbanded, b->d_job_tiles, b->d_tile_base, b->d_work};
-        cudaError_t e = launch_batch(c->stream, c->sms, plan, b->d_fills, b->nfill, b->max_fill, c->d_status);
+        BatchPlan plan{b->d_jobs, b->njobs, b->nbanded, b->d_job_tiles, b->d_tile_base, b->d_work, b->list,
+                       b->fill, b->hdr};
+        int nk = 0;
+        cudaError_t e = launch_batch(c->stream, c->sms, plan, b->d_fills, b->nfill, b->max_fill, c->d_status, &nk);
         int rc = e == cudaSuccess ? BLG_OK : cuda_fail(c, e, "batch launch");
         for (int i : b->regular)
             if (!rc) rc = search_run(c, b->probs[i], b->kk[i], b->dt[i], b->outs[i]);
@@ -2039,9 +2068,7 @@ static int batch_run(blg_ctx *c, blg_batch *b) {
         e = cudaGraphInstantiate(&b->exec, g, 0);
         if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_fail(c, e, "graph instantiate"); }
         b->graph = g;
-        b->graph_kernels = (b->nfill > 0 ? 1 : 0) +
-                           (b->njobs > 0 ? 2 + (b->nbanded > 0 ? 1 : 0) + (b->nbanded < b->njobs ? 1 : 0) : 0) +
-                           (c->launches - before);
+        b->graph_kernels = nk + (c->launches - before);
         c->launches = before;
     }
     CK(launch(c, "batch_graph", [&] { return cudaGraphLaunch(b->exec, c->stream); }), "graph launch");
@@ -2345,6 +2372,10 @@ int blg_init(int device, blg_ctx **out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->down, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(uint32_t));
+    // the survivor search's deferred results (8 MB): 2^20 entries, one per
+    // result <= max_dist of a launch; more run the in-place repair launch
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->rl_hdr, sizeof(unsigned long long) * (2 + (1u << 20)));
+    if (e == cudaSuccess) c->rl_cap = 1u << 20;
     if (e == cudaSuccess) e = cudaEventCreate(&c->t0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->t1);
     if (e == cudaSuccess) {
@@ -2376,6 +2407,7 @@ void blg_destroy(blg_ctx *c) {
     sched_model_free(c->model);
     c->model = nullptr;
     if (c->d_status) cudaFree(c->d_status);
+    if (c->rl_hdr) cudaFree(c->rl_hdr);
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
     if (c->stage_done) cudaEventDestroy(c->stage_done);
@@ -2583,7 +2615,7 @@ int blg_sched_train_search(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t 
     CK(launch(c, "search_band_logged", [&] {
            return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, c->tune.surv_round, job, C, s->cs.d, s->perm,
                                      s->ccnt, s->qcnt,
-                                     max_dist, BLG_UINT8, out, s->nc, &R, c->d_status);
+                                     max_dist, BLG_UINT8, out, s->nc, &R, nullptr, nullptr, c->d_status);
        }), "search_band_logged");
     int64_t rows = 0;
     CK(cudaMemcpyAsync(&rows, nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream), "D2H rows");

@@ -24,30 +24,6 @@ namespace blg {
 // kBatchMaxWords.
 constexpr int kBatchSearchSmem = 256 * kBatchMaxWords * 8;
 
-// out[0..n) = v (dtype-sized) by this thread's share (tid of stride).
-__device__ __forceinline__ void fill_share(void *out, int64_t n, int dtype, uint32_t v, int64_t tid,
-                                           int64_t stride) {
-    const int es = dtype == DT_UINT8 ? 1 : dtype == DT_UINT16 ? 2 : 4;
-    uint32_t word = v;
-    if (es == 1) word = v * 0x01010101u;
-    else if (es == 2) word = v | (v << 16);
-    const int64_t bytes = n * es;
-    uint8_t *b = reinterpret_cast<uint8_t *>(out);
-    const int64_t head = (16 - (reinterpret_cast<uintptr_t>(b) & 15)) & 15;
-    const int64_t nvec = bytes > head ? (bytes - head) / 16 : 0;
-    uint4 *vp = reinterpret_cast<uint4 *>(b + head);
-    const uint4 vv = make_uint4(word, word, word, word);
-    for (int64_t i = tid; i < nvec; i += stride) vp[i] = vv;
-    const int64_t tail0 = head + nvec * 16;
-    for (int64_t r = tid * es; r < head + (bytes - tail0); r += stride * es) {
-        const int64_t x = r < head ? r : tail0 + (r - head);
-        if (x >= bytes) break;
-        if (es == 1) b[x] = (uint8_t)v;
-        else if (es == 2) *reinterpret_cast<uint16_t *>(b + x) = (uint16_t)v;
-        else *reinterpret_cast<uint32_t *>(b + x) = v;
-    }
-}
-
 __global__ void __launch_bounds__(256) k_batch_fill(const BatchFill *fills) {
     const BatchFill f = fills[blockIdx.y];
     fill_share(f.out, f.n, f.dtype, f.value, (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
@@ -149,19 +125,30 @@ __device__ __forceinline__ void batch_tile(const BatchJob &job, const uint64_t *
 
 // Banded jobs (0 <= k <= 31): persistent warps pull (job, query, survivor
 // unit) tiles of the banded part of the tile space.
-template <int R>
-__global__ void __launch_bounds__(256) k_batch_band(BatchPlan plan, uint32_t *status) {
+// DEFER: fills every thresholded output (one fill item per unit claimed, the
+// rest once the units are gone; config 5: 0.75 ms per step against 0.92 with
+// the fill kernel first) and defers its results to plan.list; else
+// stores in place, and a launch given the list runs only if it ran full.
+template <int R, bool DEFER>
+__global__ void __launch_bounds__(256) k_batch_band(BatchPlan plan, bool repair, uint32_t *status) {
+    if (!DEFER && repair && *plan.list.count <= plan.list.cap) return;
     __shared__ __align__(16) unsigned char s_raw[8 * sizeof(SurvJob)];   // (no constructor runs on shared memory)
     SurvJob *s_job = reinterpret_cast<SurvJob *>(s_raw);
     __shared__ int32_t s_pend[8][kSurvPend];
     __shared__ uint16_t s_pgd[8][kSurvPend];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t total = plan.tile_base[plan.nbanded];
+    bool fill_on = DEFER;                          // warp-uniform
     auto next_job = [&](SurvJob &J) -> bool {
+        if (DEFER && fill_on) fill_on = fill_one(plan.fill);
         int64_t tile = 0;
         if (lane == 0) tile = atomicAdd(&plan.work[0], 1);
         tile = __shfl_sync(kFull, tile, 0);
-        if (tile >= total) return false;
+        if (tile >= total) {
+            if (DEFER)
+                while (fill_on) fill_on = fill_one(plan.fill);
+            return false;
+        }
         if (lane == 0) {
             const int j = upper_index(plan.tile_base, plan.nbanded, tile);
             const BatchJob &job = plan.jobs[j];
@@ -185,7 +172,11 @@ __global__ void __launch_bounds__(256) k_batch_band(BatchPlan plan, uint32_t *st
         }
         return true;
     };
-    survivor_warp<R>(s_job[w], next_job, s_pend[w], s_pgd[w], status, [](int64_t, int, int, int, uint32_t) {});
+    survivor_warp<R>(s_job[w], next_job, s_pend[w], s_pgd[w], status, [](int64_t, int, int, int, uint32_t) {},
+                     [&](void *o, int dt, int64_t idx, int d) {
+                         if (DEFER) list_emit(plan.list, o, dt, idx, d);
+                         else store1(o, dt, idx, d);
+                     });
 }
 
 // The other jobs (exact, or max_dist > 31): 1024-choice tiles, 4 per thread.
@@ -548,22 +539,44 @@ cudaError_t batch_set_attributes() {
 
 // The launches of one batch run, on `st` (capturable: no allocation, no
 // attribute change, no synchronisation). The queries' Peq tables were built
-// at upload.
+// at upload. With the deferred list the banded kernel fills the outputs
+// (the fill overlaps the survivor search) and the scatter follows, then
+// the in-place repair launch that runs only if the list ran full; else the
+// fill kernel runs first. *kernels: the kernels launched.
 cudaError_t launch_batch(cudaStream_t st, int sms, const BatchPlan &plan, const BatchFill *fills, int nfill,
-                         int64_t max_fill, uint32_t *status) {
-    if (nfill > 0) {
+                         int64_t max_fill, uint32_t *status, int *kernels) {
+    int nk = 0;
+    const bool defer = plan.list.item && plan.nbanded > 0;
+    if (defer) {
+        cudaError_t e = cudaMemsetAsync(plan.hdr, 0, 2 * sizeof(unsigned long long), st);
+        if (e != cudaSuccess) return e;
+    } else if (nfill > 0) {
         int64_t bx = (max_fill / 16 + 255) / 256;
         bx = bx < 1 ? 1 : (bx > 1024 ? 1024 : bx);
         k_batch_fill<<<dim3((unsigned)bx, (unsigned)nfill), 256, 0, st>>>(fills);
+        nk++;
     }
     if (plan.njobs > 0) {
         k_batch_plan<<<plan.njobs, 1024, 0, st>>>(plan);
         k_batch_scan<<<1, 1024, 0, st>>>(plan);
+        nk += 2;
         // 32 columns per round: the batch's short strings mostly end within
         // one (config 5: 1.38 ms per step, 1.70 with 16 columns, 1.72 with 8)
-        if (plan.nbanded > 0) k_batch_band<32><<<sms * 4, 256, 0, st>>>(plan, status);
-        if (plan.nbanded < plan.njobs) k_batch_search<<<sms * 3, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
+        if (defer) {
+            k_batch_band<32, true><<<sms * 4, 256, 0, st>>>(plan, false, status);
+            launch_list_scatter(st, sms, plan.list, plan.work);
+            k_batch_band<32, false><<<sms * 4, 256, 0, st>>>(plan, true, status);
+            nk += 3;
+        } else if (plan.nbanded > 0) {
+            k_batch_band<32, false><<<sms * 4, 256, 0, st>>>(plan, false, status);
+            nk++;
+        }
+        if (plan.nbanded < plan.njobs) {
+            k_batch_search<<<sms * 3, 256, kBatchSearchSmem, st>>>(plan, status, 1u);
+            nk++;
+        }
     }
+    if (kernels) *kernels = nk;
     return cudaGetLastError();
 }
 

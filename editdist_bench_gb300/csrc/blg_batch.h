@@ -28,13 +28,6 @@ struct BatchJob {
     void *out;
 };
 
-struct BatchFill {
-    void *out;
-    int64_t n;
-    int dtype;
-    uint32_t value;
-};
-
 struct BatchPlan {
     const BatchJob *jobs;      // device array; banded jobs (0 <= k <= 31) first
     int njobs;
@@ -42,6 +35,12 @@ struct BatchPlan {
     int64_t *job_tiles;        // [njobs]
     int64_t *tile_base;        // [njobs + 1]
     int32_t *work;             // persistent-kernel counters: [0] banded jobs, [1] the others
+    // with list.item: the banded kernel fills every thresholded output itself
+    // (fill items) and defers its results to the list; hdr = [list count,
+    // fill items claimed], cleared by the run
+    ResultList list;
+    FillItems fill;
+    unsigned long long *hdr;
 };
 
 // ---- batch upload: each kind of preparation runs once per group of
@@ -104,6 +103,7 @@ cudaError_t launch_peq_sets(cudaStream_t st, const PeqSet *sets, const int64_t *
 
 cudaError_t batch_set_attributes();
 cudaError_t launch_batch(cudaStream_t st, int sms, const BatchPlan &plan, const BatchFill *fills, int nfill,
-                         int64_t max_fill, uint32_t *status);
+                         int64_t max_fill, uint32_t *status, int *kernels);
+cudaError_t launch_list_scatter(cudaStream_t st, int sms, const ResultList &L, int32_t *work);
 
 }  // namespace blg

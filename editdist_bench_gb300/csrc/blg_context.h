@@ -53,6 +53,10 @@ struct blg_ctx {
     // pinned room for a batch upload's small host-built tables (HostArena)
     void *arena = nullptr;
     size_t arena_bytes = 0;
+    // the survivor search's deferred results: header [count, fill items
+    // claimed], then rl_cap entries (allocated at init)
+    unsigned long long *rl_hdr = nullptr;
+    unsigned long long rl_cap = 0;
     size_t stage_bytes = 0;
     cudaEvent_t stage_done = nullptr;
     std::vector<ProfRec> prof_recs;

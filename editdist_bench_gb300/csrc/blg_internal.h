@@ -126,4 +126,40 @@ struct SurvClasses {
     int32_t *work[kSurvClasses];               // job counters (cleared by the plan)
 };
 
+// An output array to fill with one value (dtype-sized elements).
+struct BatchFill {
+    void *out;
+    int64_t n;
+    int dtype;
+    uint32_t value;
+};
+
+// Results <= k deferred by a survivor kernel that fills its own output:
+// entries (element address << 8 | dtype << 6 | value), count (may pass cap:
+// the list ran full).
+struct ResultList {
+    unsigned long long *item;
+    unsigned long long *count;
+    unsigned long long cap;
+};
+
+// Output arrays to fill, as work items of kFillChunk bytes (whole elements).
+constexpr int64_t kFillChunk = 65536;
+
+struct FillItems {
+    const BatchFill *fills;       // the arrays (null: the one array `one`)
+    const int64_t *start;         // [nfill + 1] first item of each array
+    int nfill;
+    BatchFill one;
+    int64_t total;                // items
+    unsigned long long *ctr;      // items claimed, zero before the launch
+};
+
+// element bytes of a result dtype (0 int32, 1 uint16, 2 uint8)
+__host__ __device__ inline int elem_bytes(int dtype) { return dtype == 2 ? 1 : dtype == 1 ? 2 : 4; }
+
+__host__ __device__ inline int64_t fill_items_of(const BatchFill &f) {
+    return (f.n * elem_bytes(f.dtype) + kFillChunk - 1) / kFillChunk;
+}
+
 }  // namespace blg

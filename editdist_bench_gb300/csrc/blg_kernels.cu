@@ -522,28 +522,7 @@ __global__ void __launch_bounds__(256) k_pairs_long(LongQueue q, int k, int dtyp
 
 // out[0..n) = v (dtype-sized), 16-byte stores for the aligned middle.
 __global__ void __launch_bounds__(256) k_fill(void *out, int64_t n, int dtype, uint32_t v) {
-    const int es = dtype == DT_UINT8 ? 1 : dtype == DT_UINT16 ? 2 : 4;
-    uint32_t word = v;
-    if (es == 1) word = v * 0x01010101u;
-    else if (es == 2) word = v | (v << 16);
-    const int64_t bytes = n * es;
-    uint8_t *b = reinterpret_cast<uint8_t *>(out);
-    const int64_t head = (16 - (reinterpret_cast<uintptr_t>(b) & 15)) & 15;
-    const int64_t nvec = bytes > head ? (bytes - head) / 16 : 0;
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
-    uint4 *vp = reinterpret_cast<uint4 *>(b + head);
-    const uint4 vv = make_uint4(word, word, word, word);
-    for (int64_t i = tid; i < nvec; i += stride) vp[i] = vv;
-    // unaligned head and tail, one element at a time (out is element-aligned,
-    // so the head is a whole number of elements)
-    const int64_t tail0 = head + nvec * 16;
-    for (int64_t r = tid * es; r < head + (bytes - tail0); r += stride * es) {
-        const int64_t x = r < head ? r : tail0 + (r - head);
-        if (x >= bytes) break;
-        if (es == 1) b[x] = (uint8_t)v;
-        else if (es == 2) *reinterpret_cast<uint16_t *>(b + x) = (uint16_t)v;
-        else *reinterpret_cast<uint32_t *>(b + x) = v;
-    }
+    fill_share(out, n, dtype, v, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 // dst string i = src string perm[i]; one warp per string, byte-wise copy.

@@ -856,14 +856,77 @@ __device__ __forceinline__ int upper_index(const int64_t *pre, int n, int64_t x)
     return a;
 }
 
+// ---- deferred results and the output fill as work items
+// A survivor kernel that also fills its output with k+1 (fill items taken
+// between survivor jobs, so the HBM-bound fill overlaps the latency-bound
+// search) cannot store results in place: a fill item may reach an element
+// after its result. Its results <= k go to a list instead, one 64-bit entry
+// each (element address << 8 | dtype << 6 | value; value <= 63), and a
+// scatter kernel stores them after the kernel (ResultList). A list that ran
+// full (count > cap) is seen on the device: the search then runs again in
+// place. Fill work is FillItems: arrays cut into kFillChunk-byte items.
+__device__ __forceinline__ void list_emit(const ResultList &L, void *out, int dtype, int64_t idx, int d) {
+    const int es = dtype == DT_UINT8 ? 1 : dtype == DT_UINT16 ? 2 : 4;
+    const unsigned long long a = (unsigned long long)reinterpret_cast<uintptr_t>(out) + (unsigned long long)(idx * es);
+    const unsigned long long at = atomicAdd(L.count, 1ull);
+    if (at < L.cap) L.item[at] = (a << 8) | ((unsigned long long)dtype << 6) | (unsigned long long)d;
+}
+
+// out[0..n) = v (dtype-sized) by this thread's share (tid of stride): 16-byte
+// stores for the aligned middle, element stores for the ends (out is
+// element-aligned, so the unaligned head is whole elements).
+__device__ __forceinline__ void fill_share(void *out, int64_t n, int dtype, uint32_t v, int64_t tid,
+                                           int64_t stride) {
+    const int es = dtype == DT_UINT8 ? 1 : dtype == DT_UINT16 ? 2 : 4;
+    uint32_t word = v;
+    if (es == 1) word = v * 0x01010101u;
+    else if (es == 2) word = v | (v << 16);
+    const int64_t bytes = n * es;
+    uint8_t *b = reinterpret_cast<uint8_t *>(out);
+    const int64_t head = (16 - (reinterpret_cast<uintptr_t>(b) & 15)) & 15;
+    const int64_t nvec = bytes > head ? (bytes - head) / 16 : 0;
+    uint4 *vp = reinterpret_cast<uint4 *>(b + head);
+    const uint4 vv = make_uint4(word, word, word, word);
+    for (int64_t i = tid; i < nvec; i += stride) vp[i] = vv;
+    const int64_t tail0 = head + nvec * 16;
+    for (int64_t r = tid * es; r < head + (bytes - tail0); r += stride * es) {
+        const int64_t x = r < head ? r : tail0 + (r - head);
+        if (x >= bytes) break;
+        if (es == 1) b[x] = (uint8_t)v;
+        else if (es == 2) *reinterpret_cast<uint16_t *>(b + x) = (uint16_t)v;
+        else *reinterpret_cast<uint32_t *>(b + x) = v;
+    }
+}
+
+// The warp claims one fill item and fills it (every lane calls it); false
+// when every item was claimed.
+__device__ __forceinline__ bool fill_one(const FillItems &F) {
+    unsigned long long i = 0;
+    if ((threadIdx.x & 31) == 0) i = atomicAdd(F.ctr, 1ull);
+    i = __shfl_sync(kFull, i, 0);
+    if ((int64_t)i >= F.total) return false;
+    BatchFill f = F.one;
+    int64_t li = (int64_t)i;
+    if (F.fills) {
+        const int a = upper_index(F.start, F.nfill, li);
+        f = F.fills[a];
+        li -= F.start[a];
+    }
+    const int es = f.dtype == DT_UINT8 ? 1 : f.dtype == DT_UINT16 ? 2 : 4;
+    const int64_t per = kFillChunk / es, e0 = li * per, e1 = min(f.n, e0 + per);
+    fill_share(reinterpret_cast<uint8_t *>(f.out) + e0 * es, e1 - e0, f.dtype, f.value, threadIdx.x & 31, 32);
+    return true;
+}
+
 // Called by every lane of a warp. next_job(J) fills the warp's job (every
 // lane calls it; lane 0 writes J) and returns false when none is left.
 // s_pend: the warp's kSurvPend passer slots (sorted choice index), s_pgd
 // their 4-gram count distances. log(sidx, m, n, cols, gd) sees every
-// survivor the banded loop finished.
-template <int R, typename NextJob, typename LogFn>
+// survivor the banded loop finished; emit(out, dtype, index, d) takes every
+// result <= k (a store in place, or list_emit).
+template <int R, typename NextJob, typename LogFn, typename Emit>
 __device__ __forceinline__ void survivor_warp(SurvJob &J, NextJob next_job, int32_t *s_pend, uint16_t *s_pgd,
-                                              uint32_t *status, LogFn log) {
+                                              uint32_t *status, LogFn log, Emit emit) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     bool have_job = false, jobs_done = false;
@@ -895,7 +958,7 @@ __device__ __forceinline__ void survivor_warp(SurvJob &J, NextJob next_job, int3
                         for (int64_t x = J.s + lane; x < J.s1; x += 32) {
                             int nn;
                             string_at(J.CS, x, nn, status);
-                            store1(J.out, J.dtype, J.row * J.nc + J.perm[x], cap_k(nn, J.k));
+                            emit(J.out, J.dtype, J.row * J.nc + J.perm[x], cap_k(nn, J.k));
                         }
                         __syncwarp();
                         if (lane == 0) J.s = J.s1;
@@ -978,7 +1041,7 @@ __device__ __forceinline__ void survivor_warp(SurvJob &J, NextJob next_job, int3
             const bool exited = band_steps(k, bg, bs, min(n, bs.j + R), text, eqw);
             if (exited || bs.j == n) {
                 const int d = exited ? k + 1 : band_finish(k, bg, bs);
-                if (d <= k) store1(out, dtype, oidx, d);
+                if (d <= k) emit(out, dtype, oidx, d);
                 log((int64_t)sidx, m, n, bs.j, gd);
                 busy = false;
             }
