@@ -315,6 +315,14 @@ int sync_and_status(blg_ctx *c) {
     return status_to_rc(c, st);
 }
 
+// The tuned shapes of the banded kernels for a run's max_dist k (the max_dist
+// axis of the autotuner: small k and the rest up to 31 are tuned apart).
+static int surv_ctas(const blg_ctx *c, int k) { return k < kSurvWideK ? c->tune.lpt_ctas : c->tune.lpt_ctas_wide; }
+static int surv_round(const blg_ctx *c, int k) {
+    return k < kSurvWideK ? c->tune.surv_round : c->tune.surv_round_wide;
+}
+static int band_ctas(const blg_ctx *c, int k) { return k < kBandWideK ? c->tune.band_ctas : c->tune.band_ctas_wide; }
+
 static size_t dtype_size(int dt) { return dt == BLG_UINT8 ? 1 : dt == BLG_UINT16 ? 2 : 4; }
 
 static bool dtype_ok(int dt) { return dt == BLG_INT32 || dt == BLG_UINT16 || dt == BLG_UINT8; }
@@ -594,7 +602,7 @@ static int pairs_run_scheduled(blg_ctx *c, blg_pairs *p, const DevStrings &A, co
         rc = pairs_alphabet(c, p, A, B, &variant);
         if (rc) return rc;
         CK(launch(c, "pairs_band", [&] {
-               return launch_solve_band(c->stream, c->sms, c->tune.band_ctas, plan, k, dtype, d_out, exit_log, variant,
+               return launch_solve_band(c->stream, c->sms, band_ctas(c, k), plan, k, dtype, d_out, exit_log, variant,
                                         p->d_alpha);
            }), "pairs_band");
     } else {
@@ -1329,7 +1337,7 @@ static int survivor_job_size(blg_ctx *c, const blg_search *s, int k) {
             if (b > a) total += s->h_lstart[b] - s->h_lstart[a];
         }
     }
-    const int64_t warps = (int64_t)c->sms * c->tune.lpt_ctas * 8;
+    const int64_t warps = (int64_t)c->sms * surv_ctas(c, k) * 8;
     int job = c->tune.lpt_job;
     while (job > 1024 && total < 4 * warps * (int64_t)job) job >>= 1;
     return job;
@@ -1383,14 +1391,14 @@ static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, 
             const FillItems F{nullptr, nullptr, 0, whole, fill_items_of(whole), c->rl_hdr + 1};
             CK(cudaMemsetAsync(c->rl_hdr, 0, 2 * sizeof(unsigned long long), c->stream), "clear list");
             CK(launch(c, "search_band", [&] {
-                   return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, c->tune.surv_round, job, C, s->cs.d,
+                   return launch_search_band(c->stream, c->sms, surv_ctas(c, k), surv_round(c, k), job, C, s->cs.d,
                                              s->perm, s->ccnt, s->qcnt, k, dtype, d_out, s->nc, nullptr, &L, &F,
                                              c->d_status);
                }), "search_band");
             CK(launch(c, "list_scatter", [&] { return launch_list_scatter(c->stream, c->sms, L, C.work[0]); }),
                "list_scatter");
             CK(launch(c, "search_band_repair", [&] {
-                   return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, c->tune.surv_round, job, C, s->cs.d,
+                   return launch_search_band(c->stream, c->sms, surv_ctas(c, k), surv_round(c, k), job, C, s->cs.d,
                                              s->perm, s->ccnt, s->qcnt, k, dtype, d_out, s->nc, nullptr, &L, nullptr,
                                              c->d_status);
                }), "search_band_repair");
@@ -2186,20 +2194,25 @@ static int tune_exact_search(blg_ctx *c, int nw) {
     return rc;
 }
 
-// The survivor kernel's CTAs per SM and job size, on a search big enough
-// that the run-time job size (survivor_job_size) keeps the candidate job
-// sizes: 512 queries x 2^19 choices (about 15 M survivors at max_dist 4).
-// A smaller search had its jobs halved at run time whatever the candidate,
-// so the choice was noise, and a 1024 x 2^20 search paid for it (up to 14%).
-static int tune_threshold_search(blg_ctx *c) {
-    Rng r{0x2545F4914F6CDD1Dull};
+// The survivor kernel's CTAs per SM and columns per lane round for max_dist
+// k, on a search big enough that the run-time job size (survivor_job_size)
+// keeps the 4096-survivor jobs. k = 4 (the shapes of max_dist <= 8): 512
+// queries x 2^19 choices (about 15 M survivors). A smaller search had its
+// jobs halved at run time whatever the candidate, so the choice was noise,
+// and a 1024 x 2^20 search paid for it (up to 14%). k = 16 (max_dist 9..31):
+// 256 queries x 2^18 choices, where the wider band lets 4x more length
+// candidates through the length filter and more of them past the 4-gram
+// bound, and each passer runs longer.
+static int tune_threshold_search(blg_ctx *c, int k) {
+    Rng r{0x2545F4914F6CDD1Dull ^ (uint64_t)k};
     Packed q, ch;
     std::vector<std::vector<uint8_t>> qs;
-    for (int i = 0; i < 512; i++) {
+    const int nq = k < kSurvWideK ? 512 : 256, nc = k < kSurvWideK ? (1 << 19) : (1 << 18);
+    for (int i = 0; i < nq; i++) {
         qs.push_back(dna(r, 100 + (int)(r.next() % 157)));
         q.add(qs.back());
     }
-    for (int i = 0; i < (1 << 19); i++) {
+    for (int i = 0; i < nc; i++) {
         if (r.uni() < 0.05) ch.add(mutate(r, qs[r.next() % qs.size()], 0.05 * r.uni()));
         else ch.add(dna(r, 100 + (int)(r.next() % 157)));
     }
@@ -2210,31 +2223,36 @@ static int tune_threshold_search(blg_ctx *c) {
     // The job size stays at its maximum, 4096: on 1024 x 2^20 it measured 8%
     // faster than 2048, while a search of this size cannot tell them apart;
     // smaller searches get smaller jobs at run time (survivor_job_size).
-    // CTAs per SM x columns per lane round
+    // CTAs per SM x columns per lane round, set in the bucket k runs in
+    int &ctas_t = k < kSurvWideK ? c->tune.lpt_ctas : c->tune.lpt_ctas_wide;
+    int &round_t = k < kSurvWideK ? c->tune.surv_round : c->tune.surv_round_wide;
     float best_ms = 1e30f;
-    int best_ctas = c->tune.lpt_ctas, best_round = c->tune.surv_round;
+    int best_ctas = ctas_t, best_round = round_t;
     c->tune.lpt_job = 4096;
     for (int ctas : {2, 3, 4})
         for (int round : {8, 16, 32}) {
             if (rc) break;
-            c->tune.lpt_ctas = ctas;
-            c->tune.surv_round = round;
+            ctas_t = ctas;
+            round_t = round;
             float ms = 0.f;
-            rc = time_best(c, 5, [&] { return search_run(c, &s, 4, BLG_UINT8, out); }, &ms);
+            rc = time_best(c, 5, [&] { return search_run(c, &s, k, BLG_UINT8, out); }, &ms);
             if (!rc && ms < best_ms) {
                 best_ms = ms;
                 best_ctas = ctas;
                 best_round = round;
             }
         }
-    c->tune.lpt_ctas = best_ctas;
-    c->tune.surv_round = best_round;
+    ctas_t = best_ctas;
+    round_t = best_round;
     dev_free(c, out);
     search_release(c, &s);
     return rc;
 }
 
-static int tune_band_pairs(blg_ctx *c) {
+// CTAs per SM of the banded pairs solver for max_dist k (8: the shape of
+// max_dist <= 15; 24: max_dist 16..31), on 2^19 pairs of lengths 8..256
+// with edit rates 0..30%.
+static int tune_band_pairs(blg_ctx *c, int k) {
     Rng r{0xD1B54A32D192ED03ull};
     Packed a, b;
     for (int i = 0; i < (1 << 19); i++) {
@@ -2249,17 +2267,18 @@ static int tune_band_pairs(blg_ctx *c) {
     if (!rc) rc = pairs_learn_alphabet(c, &p);
     const int sched = c->sched;
     c->sched = BLG_SCHED_AUTO;
+    int &ctas_t = k < kBandWideK ? c->tune.band_ctas : c->tune.band_ctas_wide;
     float best_ms = 1e30f;
-    int best = c->tune.band_ctas;
+    int best = ctas_t;
     for (int ctas : {2, 3}) {
         if (rc) break;
-        c->tune.band_ctas = ctas;
+        ctas_t = ctas;
         float ms = 0.f;
-        rc = time_best(c, 3, [&] { return pairs_run(c, &p, 8, BLG_UINT8, out); }, &ms);
+        rc = time_best(c, 3, [&] { return pairs_run(c, &p, k, BLG_UINT8, out); }, &ms);
         if (!rc && ms < best_ms) { best_ms = ms; best = ctas; }
     }
     c->sched = sched;
-    c->tune.band_ctas = best;
+    ctas_t = best;
     dev_free(c, out);
     pairs_release(c, &p);
     return rc;
@@ -2300,7 +2319,7 @@ static std::string tuning_header(blg_ctx *c) {
     std::string name = prop.name;
     for (auto &ch : name)
         if (ch == ' ') ch = '_';
-    return "BLGTUNE6 " + name + " sm" + std::to_string(prop.major * 10 + prop.minor) + " " + std::to_string(c->sms) +
+    return "BLGTUNE7 " + name + " sm" + std::to_string(prop.major * 10 + prop.minor) + " " + std::to_string(c->sms) +
            " " + std::to_string(blg_version());
 }
 
@@ -2322,11 +2341,14 @@ static bool tuning_load(blg_ctx *c, const char *path) {
         } else if (k == "lpt_ctas" && v >= 1 && v <= 8) { t.lpt_ctas = v; fields++; }
         else if (k == "lpt_job" && v >= 256 && v <= 4096) { t.lpt_job = v; fields++; }
         else if (k == "surv_round" && (v == 8 || v == 16 || v == 32)) { t.surv_round = v; fields++; }
+        else if (k == "lpt_ctas_wide" && v >= 1 && v <= 8) { t.lpt_ctas_wide = v; fields++; }
+        else if (k == "surv_round_wide" && (v == 8 || v == 16 || v == 32)) { t.surv_round_wide = v; fields++; }
         else if (k == "band_ctas" && v >= 1 && v <= 3) { t.band_ctas = v; fields++; }
+        else if (k == "band_ctas_wide" && v >= 1 && v <= 3) { t.band_ctas_wide = v; fields++; }
         else if (k == "tile_shape" && v >= 1 && v <= 3) { t.tile_shape = v; fields++; }
     }
     fclose(f);
-    if (!ok || fields < 13) return false;
+    if (!ok || fields < 16) return false;
     t.tuned = 2;                                        // loaded from the cache
     c->tune = t;
     return true;
@@ -2339,6 +2361,8 @@ static void tuning_save(blg_ctx *c, const char *path) {
     for (int w = 1; w <= 8; w++) fprintf(f, "qpb%d %d\n", w, c->tune.qpb[w]);
     fprintf(f, "lpt_ctas %d\nlpt_job %d\nsurv_round %d\nband_ctas %d\ntile_shape %d\n", c->tune.lpt_ctas,
             c->tune.lpt_job, c->tune.surv_round, c->tune.band_ctas, c->tune.tile_shape);
+    fprintf(f, "lpt_ctas_wide %d\nsurv_round_wide %d\nband_ctas_wide %d\n", c->tune.lpt_ctas_wide,
+            c->tune.surv_round_wide, c->tune.band_ctas_wide);
     fclose(f);
 }
 
@@ -2469,7 +2493,7 @@ static int pairs_run_graph(blg_ctx *c, blg_pairs *p, int k, int dtype, void *d_o
     key.dtype = dtype;
     key.sched = c->sched;
     key.learned = c->sched == BLG_SCHED_LEARNED && c->model && sched_model_trained(c->model);
-    key.band_ctas = c->tune.band_ctas;
+    key.band_ctas = band_ctas(c, k);
     key.tile_shape = c->tune.tile_shape;
     key.out = d_out;
     if (p->gexec && p->g_key == key) {
@@ -2613,8 +2637,8 @@ int blg_sched_train_search(blg_ctx *c, blg_search *s, int32_t max_dist, int32_t 
            return launch_surv_plan(c->stream, C, s->lstart, s->min_len, s->n_len, max_dist, job);
        }), "surv_plan");
     CK(launch(c, "search_band_logged", [&] {
-           return launch_search_band(c->stream, c->sms, c->tune.lpt_ctas, c->tune.surv_round, job, C, s->cs.d, s->perm,
-                                     s->ccnt, s->qcnt,
+           return launch_search_band(c->stream, c->sms, surv_ctas(c, max_dist), surv_round(c, max_dist), job, C, s->cs.d,
+                                     s->perm, s->ccnt, s->qcnt,
                                      max_dist, BLG_UINT8, out, s->nc, &R, nullptr, nullptr, c->d_status);
        }), "search_band_logged");
     int64_t rows = 0;
@@ -2981,9 +3005,13 @@ int blg_autotune(blg_ctx *c, const char *cache_path) {
         // word counts not timed take the nearest timed one
         c->tune.qpb[3] = c->tune.qpb[4];
         for (int w = 5; w <= 8; w++) c->tune.qpb[w] = c->tune.qpb[4];
-        rc = tune_threshold_search(c);
+        // the max_dist axis: the survivor search at max_dist 4 and 16, the
+        // banded pairs solver at 8 and 24 (each sets its own bucket)
+        rc = tune_threshold_search(c, 4);
+        if (!rc) rc = tune_threshold_search(c, 16);
     }
-    if (!rc) rc = tune_band_pairs(c);
+    if (!rc) rc = tune_band_pairs(c, 8);
+    if (!rc) rc = tune_band_pairs(c, 24);
     if (!rc) rc = tune_tile_pairs(c);
     c->sched = sched;
     if (rc) {
@@ -2997,7 +3025,7 @@ int blg_autotune(blg_ctx *c, const char *cache_path) {
 
 int blg_get_tuning(blg_ctx *c, int32_t *values, int n) {
     ENTER(c);
-    if (!values || n < 14) return fail(c, BLG_ERR_ARG, "need 14 values");
+    if (!values || n < 14) return fail(c, BLG_ERR_ARG, "need at least 14 values");
     for (int w = 1; w <= 8; w++) values[w - 1] = c->tune.qpb[w];
     values[8] = c->tune.lpt_ctas;
     values[9] = c->tune.lpt_job;
@@ -3005,6 +3033,11 @@ int blg_get_tuning(blg_ctx *c, int32_t *values, int n) {
     values[11] = c->tune.tuned;
     values[12] = c->tune.tile_shape;
     values[13] = c->tune.surv_round;
+    if (n >= 17) {                                      // the shapes of the wide max_dist buckets
+        values[14] = c->tune.lpt_ctas_wide;
+        values[15] = c->tune.surv_round_wide;
+        values[16] = c->tune.band_ctas_wide;
+    }
     return BLG_OK;
 }
 

@@ -10,13 +10,21 @@
 struct blg_sched_model;   // the work-order scheduler network (blg_mlp.cu)
 
 // Launch shapes chosen by the autotuner (blg_autotune); the defaults are the
-// hand-picked shapes used before any tuning.
+// hand-picked shapes used before any tuning. The banded kernels' shapes have
+// a max_dist axis: one shape for small max_dist, one for the rest up to 31
+// (kSurvWideK, kBandWideK): a wider band keeps more survivors alive for
+// more columns, which moves the best occupancy / round length.
+constexpr int kSurvWideK = 9;     // thresholded search: max_dist 9..31 take the *_wide shapes (tuned at 16)
+constexpr int kBandWideK = 16;    // banded pairs solver: max_dist 16..31 take band_ctas_wide (tuned at 24)
 struct blg_tuning {
     int qpb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};   // exact search: queries per CTA by query words (0: heuristic)
-    int lpt_ctas = 4;                            // thresholded search: CTAs per SM
+    int lpt_ctas = 4;                            // thresholded search, max_dist <= 8: CTAs per SM
     int lpt_job = 4096;                          // thresholded search: survivors per job
-    int surv_round = 16;                         // thresholded search: columns per lane round (8, 16, 32)
-    int band_ctas = 3;                           // banded pairs solver: CTAs per SM
+    int surv_round = 16;                         // thresholded search, max_dist <= 8: columns per lane round (8, 16, 32)
+    int lpt_ctas_wide = 4;                       // thresholded search, max_dist 9..31: CTAs per SM
+    int surv_round_wide = 16;                    // thresholded search, max_dist 9..31: columns per lane round
+    int band_ctas = 3;                           // banded pairs solver, max_dist <= 15: CTAs per SM
+    int band_ctas_wide = 3;                      // banded pairs solver, max_dist 16..31: CTAs per SM
     int tile_shape = 1;                          // short-pair tile kernel: 1 = one stage of 512 pairs, 2 = two of 512,
                                                  // 3 = two of 256 (1M pairs of 32 bytes: 61, 79, 76 us)
     int tuned = 0;

@@ -416,11 +416,16 @@ def autotune(cache_path=None) -> dict:
 def tuning() -> dict:
     """The context's current launch shapes."""
     ctx = _lib.context()
-    v = (ctypes.c_int32 * 14)()
-    ctx.check(ctx.lib.blg_get_tuning(ctx.h, v, 14), "get_tuning")
+    v = (ctypes.c_int32 * 17)()
+    ctx.check(ctx.lib.blg_get_tuning(ctx.h, v, 17), "get_tuning")
     return {"search_queries_per_cta": {w + 1: int(v[w]) for w in range(8)}, "survivor_ctas_per_sm": int(v[8]),
             "survivors_per_job": int(v[9]), "survivor_round_columns": int(v[13]), "band_ctas_per_sm": int(v[10]),
-            "tile_shape": int(v[12]), "source": {0: "defaults", 1: "timed", 2: "cache"}[int(v[11])]}
+            "tile_shape": int(v[12]),
+            # the max_dist axis: the shapes above serve max_dist <= 8 (survivor
+            # search) and <= 15 (banded pairs); these the rest up to 31
+            "survivor_ctas_per_sm_k9_31": int(v[14]), "survivor_round_columns_k9_31": int(v[15]),
+            "band_ctas_per_sm_k16_31": int(v[16]),
+            "source": {0: "defaults", 1: "timed", 2: "cache"}[int(v[11])]}
 
 
 def set_schedule(name: str):

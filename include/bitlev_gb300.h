@@ -228,19 +228,23 @@ int blg_sched_load(blg_ctx *ctx, const char *path);
 /* Autotuner: times candidate launch shapes on synthetic inputs of each
  * length bucket and max_dist kind and keeps the fastest for this context:
  * queries per CTA of the exact search (by query word count), CTAs per SM and
- * columns per lane round of the thresholded search's survivor kernel, CTAs
- * per SM of the banded pairs solver, the staging shape of the short-pair
- * tile kernel. With a cache path, a cache written for the same device model,
+ * columns per lane round of the thresholded search's survivor kernel (one
+ * shape for max_dist <= 8, tuned at 4, one for 9..31, tuned at 16), CTAs
+ * per SM of the banded pairs solver (max_dist <= 15, tuned at 8; 16..31,
+ * tuned at 24), the staging shape of the short-pair tile kernel. With a cache path, a cache written for the same device model,
  * SM count and library version is loaded instead of timing, and a fresh
  * result is written there. No counterpart in the reference (fixed launch
  * geometry, bitlev/gpu.py:90-96,121-130). Results never depend on it. */
 int blg_autotune(blg_ctx *ctx, const char *cache_path);
-/* values[14]: qpb for 1..8 query words (0 = heuristic), CTAs per SM and
- * survivors per job of the thresholded search, CTAs per SM of the banded
- * solver, 0 (defaults) / 1 (timed) / 2 (loaded from a cache), the staging
- * shape of the short-pair tile kernel (1: one stage of 512 pairs, 2: two
- * stages of 512, 3: two stages of 256), and the columns per lane round of
- * the thresholded search's survivor kernel (8, 16 or 32). */
+/* values[n >= 14]: qpb for 1..8 query words (0 = heuristic), CTAs per SM
+ * (max_dist <= 8) and survivors per job of the thresholded search, CTAs per
+ * SM of the banded solver (max_dist <= 15), 0 (defaults) / 1 (timed) / 2
+ * (loaded from a cache), the staging shape of the short-pair tile kernel
+ * (1: one stage of 512 pairs, 2: two stages of 512, 3: two stages of 256),
+ * and the columns per lane round of the thresholded search's survivor
+ * kernel (8, 16 or 32; max_dist <= 8). With n >= 17 also the wide max_dist
+ * buckets: the survivor kernel's CTAs per SM and columns per round for
+ * max_dist 9..31 and the banded solver's CTAs per SM for 16..31. */
 int blg_get_tuning(blg_ctx *ctx, int32_t *values, int n);
 
 /* Device memory and stream helpers (the parts of CuPy bitlev.gpu used:
