@@ -129,8 +129,10 @@ __device__ __forceinline__ void batch_tile(const BatchJob &job, const uint64_t *
 // rest once the units are gone; config 5: 0.75 ms per step against 0.92 with
 // the fill kernel first) and defers its results to plan.list; else
 // stores in place, and a launch given the list runs only if it ran full.
+// At most 64 registers, so its 4-CTA-per-SM grid is resident at once (78
+// registers left free; config 5: 0.730 vs 0.747 ms per step).
 template <int R, bool DEFER>
-__global__ void __launch_bounds__(256) k_batch_band(BatchPlan plan, bool repair, uint32_t *status) {
+__global__ void __launch_bounds__(256, 4) k_batch_band(BatchPlan plan, bool repair, uint32_t *status) {
     if (!DEFER && repair && *plan.list.count <= plan.list.cap) return;
     __shared__ __align__(16) unsigned char s_raw[8 * sizeof(SurvJob)];   // (no constructor runs on shared memory)
     SurvJob *s_job = reinterpret_cast<SurvJob *>(s_raw);

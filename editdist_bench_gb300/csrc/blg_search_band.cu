@@ -81,8 +81,12 @@ __global__ void __launch_bounds__(256) k_sketch_strings(DevStrings S, uint64_t *
     }
 }
 
+// At most 64 registers (4 CTAs of 256 threads per SM, the largest tuned
+// shape): left free, the fill and deferred-result paths took the kernel to
+// 76, which fits only 3 CTAs per SM, so a 4-per-SM grid ran a quarter of
+// its CTAs as a second wave (the cap costs at most 40 bytes of spills).
 template <int R, bool LOG, bool DEFER>
-__global__ void __launch_bounds__(256) k_search_band(DevStrings CS, const int32_t *perm, const uint4 *ccnt,
+__global__ void __launch_bounds__(256, 4) k_search_band(DevStrings CS, const int32_t *perm, const uint4 *ccnt,
                                                      const uint4 *qcnt, SurvClasses C, int jobsz,
                                                      int k, int dtype, void *out, int64_t nc, SurvRows rows,
                                                      ResultList L, FillItems F, uint32_t *status) {
