@@ -2089,12 +2089,14 @@ static int batch_run(blg_ctx *c, blg_batch *b) {
 // fixed seed) and the fastest kept per device:
 //   exact search:        queries per CTA, for queries of 1, 2 and 4 words
 //                        (1024 queries x 65536 choices of the same length);
-//   thresholded search:  CTAs per SM x largest survivors per job (128 queries
-//                        x 262144 choices, lengths 100..256, 5% planted
-//                        near-copies, max_dist 4);
+//   thresholded search:  CTAs per SM x columns per lane round, for max_dist
+//                        <= 8 (1024 queries x 2^20 choices, lengths 100..256,
+//                        5% planted near-copies, max_dist 4) and for 9..31
+//                        (256 x 2^18, max_dist 16);
 //   banded pairs solver: CTAs per SM (2^19 pairs, lengths 8..256, edit rates
-//                        0..30%, max_dist 8);
-//   short-pair tiles:    one or two stage buffers (2^20 pairs of 32 bytes, 5%
+//                        0..30%), for max_dist <= 15 (timed at 8) and 16..31
+//                        (timed at 24);
+//   short-pair tiles:    the staging shape (2^20 pairs of 32 bytes, 5%
 //                        edits, exact).
 // Results never depend on a shape; only time does.
 namespace {
@@ -2121,10 +2123,16 @@ struct Packed {
     const uint8_t *data() const { return buf.empty() ? nullptr : buf.data(); }
 };
 
+// Random DNA, 16 bases per generator step.
 std::vector<uint8_t> dna(Rng &r, int len) {
     static const uint8_t A[4] = {'A', 'C', 'G', 'T'};
     std::vector<uint8_t> x(len);
-    for (auto &ch : x) ch = A[r.next() & 3];
+    uint32_t bits = 0;
+    for (int i = 0; i < len; i++) {
+        if ((i & 15) == 0) bits = r.next();
+        x[i] = A[bits & 3];
+        bits >>= 2;
+    }
     return x;
 }
 
@@ -2196,18 +2204,19 @@ static int tune_exact_search(blg_ctx *c, int nw) {
 
 // The survivor kernel's CTAs per SM and columns per lane round for max_dist
 // k, on a search big enough that the run-time job size (survivor_job_size)
-// keeps the 4096-survivor jobs. k = 4 (the shapes of max_dist <= 8): 512
-// queries x 2^19 choices (about 15 M survivors). A smaller search had its
-// jobs halved at run time whatever the candidate, so the choice was noise,
-// and a 1024 x 2^20 search paid for it (up to 14%). k = 16 (max_dist 9..31):
-// 256 queries x 2^18 choices, where the wider band lets 4x more length
-// candidates through the length filter and more of them past the 4-gram
-// bound, and each passer runs longer.
+// keeps the 4096-survivor jobs. k = 4 (the shapes of max_dist <= 8): 1024
+// queries x 2^20 choices. Smaller searches misled it: 512 x 2^19 picked 3
+// CTAs per SM in two runs of three, 7% slower at 1024 x 2^20 than the 4 it
+// picks there (the output fill and the job tail weigh differently), and a
+// still smaller one had its jobs halved at run time whatever the candidate.
+// k = 16 (max_dist 9..31): 256 queries x 2^18 choices, where the wider band
+// lets 4x more length candidates through the length filter and more of
+// them past the 4-gram bound, and each passer runs longer.
 static int tune_threshold_search(blg_ctx *c, int k) {
     Rng r{0x2545F4914F6CDD1Dull ^ (uint64_t)k};
     Packed q, ch;
     std::vector<std::vector<uint8_t>> qs;
-    const int nq = k < kSurvWideK ? 512 : 256, nc = k < kSurvWideK ? (1 << 19) : (1 << 18);
+    const int nq = k < kSurvWideK ? 1024 : 256, nc = k < kSurvWideK ? (1 << 20) : (1 << 18);
     for (int i = 0; i < nq; i++) {
         qs.push_back(dna(r, 100 + (int)(r.next() % 157)));
         q.add(qs.back());
