@@ -472,7 +472,8 @@ def matches_leg(bench, ctx, pin, flush, args):
             "e2e": {"value": bench.pairs / e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": int(n) * gpu.MATCH_DTYPE.itemsize + 8,
                     "path": "blg_cdist_matches, pinned host buffers, wall clock"},
-            "path": "blg_search_matches on the resident search: dense scratch, count, compaction; CUDA events"}
+            "path": ("blg_search_matches on the resident search: the survivor kernel's result list (no output, no "
+                     "fill), sorted into records on the host and copied to HBM; CUDA events")}
 
 
 def exit_columns(bench, sample_rows_or_n):

@@ -1500,6 +1500,90 @@ static int search_matches_rows(blg_ctx *c, blg_search *s, int k, int64_t q0, int
     return BLG_OK;
 }
 
+// LSD radix sort of list entries by their element index (entry >> 8), 8
+// bits per pass over the index bytes that vary.
+static void sort_by_index(std::vector<unsigned long long> &v) {
+    if (v.size() < 2) return;
+    unsigned long long top = 0;
+    for (auto e : v) top |= e >> 8;
+    std::vector<unsigned long long> tmp(v.size());
+    for (int shift = 8; shift < 64 && (top >> (shift - 8)) != 0; shift += 8) {
+        size_t cnt[257] = {0};
+        for (auto e : v) cnt[((e >> shift) & 0xffu) + 1]++;
+        for (int d = 0; d < 256; d++) cnt[d + 1] += cnt[d];
+        for (auto e : v) tmp[cnt[(e >> shift) & 0xffu]++] = e;
+        v.swap(tmp);
+    }
+}
+
+// Matches of a thresholded search straight from the survivor kernel's result
+// list, for runs on the survivor path with the banded loop (max_dist <= 31,
+// choices length-sorted, a schedule other than plain, every query of the
+// current classes in a sequential class). The kernel runs without an
+// output and without a fill: it lists every result <= max_dist as its dense
+// element index (base 0, one byte per element, so the listed address is
+// row * nc + choice). The listed entries <= max_dist (an empty query lists
+// min(n, max_dist + 1) for each survivor) are sorted by index on the host
+// and become the records: no dense scratch, no compaction passes. *done =
+// false, with nothing written, when the run does not qualify or the list
+// ran full; the caller then takes the dense path.
+static int search_matches_list(blg_ctx *c, blg_search *s, int k, blg_match *d_out, blg_match *host_out, int64_t cap,
+                               int64_t *total, bool *done) {
+    *done = false;
+    *total = 0;
+    if (k < 0 || k > 31 || !s->lsorted || c->sched == BLG_SCHED_PLAIN || !c->rl_hdr || c->rl_cap == 0)
+        return BLG_OK;
+    const SurvClasses C = seq_classes(s);
+    if (C.n == 0 || C.n != (int)s->cls.size()) return BLG_OK;    // a lane-spread class: the dense path
+    const int job = survivor_job_size(c, s, k);
+    CK(launch(c, "surv_plan", [&] { return launch_surv_plan(c->stream, C, s->lstart, s->min_len, s->n_len, k, job); }),
+       "surv_plan");
+    const ResultList L{c->rl_hdr + 2, c->rl_hdr, c->rl_cap};
+    const FillItems F{nullptr, nullptr, 0, BatchFill{nullptr, 0, BLG_UINT8, 0}, 0, c->rl_hdr + 1};
+    CK(cudaMemsetAsync(c->rl_hdr, 0, 2 * sizeof(unsigned long long), c->stream), "clear list");
+    CK(launch(c, "search_band_list", [&] {
+           return launch_search_band(c->stream, c->sms, surv_ctas(c, k), surv_round(c, k), job, C, s->cs.d, s->perm,
+                                     s->ccnt, s->qcnt, k, BLG_UINT8, nullptr, s->nc, nullptr, &L, &F, c->d_status);
+       }), "search_band_list");
+    unsigned long long cnt = 0;
+    CK(cudaMemcpyAsync(&cnt, c->rl_hdr, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream), "D2H list count");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    if (cnt > c->rl_cap) return BLG_OK;                            // ran full: the dense path
+    std::vector<unsigned long long> e(cnt);
+    if (cnt) {
+        CK(cudaMemcpyAsync(e.data(), c->rl_hdr + 2, sizeof(unsigned long long) * cnt, cudaMemcpyDeviceToHost,
+                           c->stream), "D2H list");
+        CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    }
+    size_t keep = 0;
+    for (auto x : e)
+        if ((int)(x & 63u) <= k) e[keep++] = x;
+    e.resize(keep);
+    sort_by_index(e);
+    const int64_t m = std::min<int64_t>((int64_t)keep, cap);
+    std::vector<blg_match> staged;
+    blg_match *rec = host_out;
+    if (!rec && m > 0) {
+        staged.resize((size_t)m);
+        rec = staged.data();
+    }
+    for (int64_t i = 0; i < m; i++) {
+        const int64_t idx = (int64_t)(e[(size_t)i] >> 8);
+        rec[i].query = idx / s->nc;
+        rec[i].choice = idx % s->nc;
+        rec[i].dist = (int32_t)(e[(size_t)i] & 63u);
+        rec[i].reserved = 0;
+    }
+    if (!host_out && m > 0) {
+        CK(cudaMemcpyAsync(d_out, staged.data(), sizeof(blg_match) * (size_t)m, cudaMemcpyHostToDevice, c->stream),
+           "H2D matches");
+        CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    }
+    *total = (int64_t)keep;
+    *done = true;
+    return BLG_OK;
+}
+
 static void search_release(blg_ctx *c, blg_search *s) {
     free_strings(c, s->q);
     free_strings(c, s->c);
@@ -2819,7 +2903,19 @@ int blg_search_matches(blg_ctx *c, blg_search *s, int32_t max_dist, blg_match *d
     if (capacity < 0 || (capacity > 0 && !d_out)) return fail(c, BLG_ERR_ARG, "bad match buffer");
     *count = 0;
     if (s->nq == 0 || s->nc == 0) return BLG_OK;
-    // query rows in chunks whose dense scratch stays within the budget
+    {   // the survivor kernel's result list, where the run qualifies
+        bool listed = false;
+        int64_t t = 0;
+        const int rc = search_matches_list(c, s, max_dist, d_out, nullptr, capacity, &t, &listed);
+        if (rc) return rc;
+        if (listed) {
+            const int rc2 = sync_and_status(c);
+            if (rc2) return rc2;
+            *count = t;
+            return BLG_OK;
+        }
+    }
+    // else query rows in chunks whose dense scratch stays within the budget
     // (1 GiB); the all-query classes are rebuilt afterwards for the
     // search's other runs
     const size_t row = dtype_size(match_dtype(max_dist)) * (size_t)s->nc;
@@ -2862,14 +2958,21 @@ int blg_cdist_matches(blg_ctx *c, const uint8_t *bq, const int64_t *oq, int64_t 
     const bool surv = c->sched != BLG_SCHED_PLAIN;
     int rc = search_upload_queries(c, bq, oq, nq, &s);
     if (!rc) rc = search_upload_choices(c, bc, oc, nc, &s, surv ? NEED_SORTED : NEED_TT);
-    // query rows in chunks whose dense scratch stays within the budget (1 GiB)
+    // the survivor kernel's result list, where the run qualifies
+    int64_t total = 0;
+    bool listed = false;
+    if (!rc && surv && max_dist <= 31) {
+        rc = search_build_classes(c, oq, 0, nq, &s);
+        if (!rc) rc = search_matches_list(c, &s, max_dist, nullptr, out, capacity, &total, &listed);
+    }
+    // else query rows in chunks whose dense scratch stays within the budget
+    // (1 GiB)
     const size_t row = dtype_size(match_dtype(max_dist)) * (size_t)nc;
     const int64_t rows = std::max<int64_t>(1, std::min<int64_t>(nq, (int64_t)(match_scratch_bytes() / row)));
     void *scratch = nullptr;
-    if (!rc && dev_alloc(c, &scratch, row * (size_t)rows) != cudaSuccess)
+    if (!rc && !listed && dev_alloc(c, &scratch, row * (size_t)rows) != cudaSuccess)
         rc = fail(c, BLG_ERR_ALLOC, "cudaMallocAsync(match scratch)");
-    int64_t total = 0;
-    for (int64_t q0 = 0; q0 < nq && !rc; q0 += rows) {
+    for (int64_t q0 = 0; q0 < nq && !rc && !listed; q0 += rows) {
         const int64_t q1 = std::min(nq, q0 + rows);
         rc = search_build_classes(c, oq, q0, q1, &s);
         int64_t t = 0;

@@ -1,7 +1,8 @@
 """Failure paths, made on the host: no test here faults, traps or hangs a GPU.
 
 * An injected allocation failure (blg_set_fault_injection) at each device
-  allocation of a one-call pairwise / cdist in turn raises MemoryError, and
+  allocation of a one-call pairwise / cdist / matches-only cdist in turn
+  raises MemoryError, and
   the next call on the same context is correct. The reference's error model
   is the same: an allocation failure returns -1 / raises MemoryError
   (csrc/myers.c:162-164, bench/cmyers.py:82-84).
@@ -84,6 +85,28 @@ def test_alloc_failure_cdist_paths(gpu):
     want = oracle.cross(W.take(w.q, rows), w.c)
     _sweep_allocations(gpu, lambda: gpu.cdist_packed(w.q, w.c),
                        lambda got: np.testing.assert_array_equal(got[rows], want))
+
+
+def test_alloc_failure_matches_paths(gpu):
+    """The matches-only search from the survivor kernel's result list (the
+    automatic schedule) and from the dense scratch (the plain one)."""
+    rng = np.random.default_rng(43)
+    q = W.random_strings(rng, rng.integers(0, 150, 30))
+    c = W.concat(W.mutate(rng, W.take(q, rng.integers(0, 30, 200)), 0.05), W.random_strings(rng, rng.integers(0, 160, 700)))
+    d = oracle.cross(q, c, 4)
+    qi, ci = np.nonzero(d <= 4)
+
+    def check(got):
+        np.testing.assert_array_equal(got[0], qi)
+        np.testing.assert_array_equal(got[1], ci)
+        np.testing.assert_array_equal(got[2], d[qi, ci])
+
+    for sched in ("auto", "plain"):
+        gpu.set_schedule(sched)
+        try:
+            _sweep_allocations(gpu, lambda: gpu.cdist_matches_packed(q, c, 4), check)
+        finally:
+            gpu.set_schedule("auto")
 
 
 def test_tile_wait_timeout_is_reported_and_recoverable(gpu):

@@ -1,8 +1,11 @@
 """Matches-only thresholded search (blg_cdist_matches / blg_search_matches):
 the records are exactly the oracle's pairs with d <= max_dist, sorted by
 (query, choice), with their distances; capacity truncation reports the full
-count; every scratch width (uint8 / uint16 / int32 by max_dist) and every
-schedule gives the same records."""
+count; both ways of finding them give the same records: the survivor
+kernel's result list (max_dist <= 31 under the survivor schedules) and the
+dense scratch compaction (max_dist > 31, the plain schedule, or a list that
+ran full), the latter with every scratch width (uint8 / uint16 / int32 by
+max_dist)."""
 import numpy as np
 import pytest
 
@@ -92,17 +95,41 @@ def test_matches_edges():
 
 
 def test_matches_in_query_chunks(monkeypatch):
-    """A small scratch budget (BLG_MATCH_SCRATCH_BYTES) makes both entry
-    points walk several query chunks; the records are the same, and the
-    resident search still runs dense afterwards (its classes are rebuilt)."""
+    """Under the plain schedule (the dense path), a small scratch budget
+    (BLG_MATCH_SCRATCH_BYTES) makes both entry points walk several query
+    chunks; the records are the same, and the resident search still runs
+    dense afterwards (its classes are rebuilt)."""
     rng = np.random.default_rng(13)
     q = W.random_strings(rng, rng.integers(0, 120, 41))
     c = W.concat(W.mutate(rng, W.take(q, rng.integers(0, 41, 500)), 0.1), W.random_strings(rng, rng.integers(0, 130, 2500)))
     nc = len(c[1]) - 1
     want = _want(q, c, 3)
     monkeypatch.setenv("BLG_MATCH_SCRATCH_BYTES", str(5 * nc))      # 5 rows of uint8 per chunk
+    gpu.set_schedule("plain")
+    try:
+        _check(gpu.cdist_matches_packed(q, c, 3), want)
+        s = gpu.SearchBatch(q, c)
+        _check(s.matches(3), want)
+        out = s.alloc("uint8")
+        np.testing.assert_array_equal(s.run(out, max_dist=3).get(), oracle.saturate(oracle.cross(q, c, 3), "uint8"))
+    finally:
+        gpu.set_schedule("auto")
+    # the same search under the survivor schedule takes the result list
     _check(gpu.cdist_matches_packed(q, c, 3), want)
+    _check(gpu.SearchBatch(q, c).matches(3), want)
+
+
+def test_matches_list_full_falls_back():
+    """More matches than the survivor kernel's result list holds (2^20
+    entries): 1100 x 1000 equal strings at max_dist 0 are 1.1 M matches, so
+    both entry points fall back to the dense path and still return every
+    record."""
+    rng = np.random.default_rng(14)
+    one = W.random_strings(rng, np.array([6]))
+    q, c = W.take(one, np.zeros(1100, dtype=np.int64)), W.take(one, np.zeros(1000, dtype=np.int64))
+    qi, ci = np.divmod(np.arange(1100 * 1000, dtype=np.int64), 1000)
+    want = (qi, ci, np.zeros(1100 * 1000, dtype=np.int64))
+    assert len(qi) > (1 << 20)
+    _check(gpu.cdist_matches_packed(q, c, 0, capacity=1100 * 1000), want)
     s = gpu.SearchBatch(q, c)
-    _check(s.matches(3), want)
-    out = s.alloc("uint8")
-    np.testing.assert_array_equal(s.run(out, max_dist=3).get(), oracle.saturate(oracle.cross(q, c, 3), "uint8"))
+    _check(s.matches(0), want)
