@@ -1359,10 +1359,22 @@ static SurvClasses seq_classes(blg_search *s) {
     return C;
 }
 
+// Queries in the search's current classes (every query of the rows they
+// were built for, empty ones included).
+static int64_t class_queries(const blg_search *s) {
+    int64_t n = 0;
+    for (auto &k_ : s->cls) n += k_.nq;
+    return n;
+}
+
 static int search_run(blg_ctx *c, blg_search *s, int k, int dtype, void *d_out, int64_t q0, int64_t q1) {
     if (!dtype_ok(dtype)) return fail(c, BLG_ERR_ARG, "dtype must be int32, uint16 or uint8");
     if (s->nq == 0 || s->nc == 0) return BLG_OK;
     if (q1 < 0) q1 = s->nq;
+    // a class rebuild that an allocation failure cut short leaves queries
+    // without a class: refuse to run rather than skip their rows
+    if (class_queries(s) != q1 - q0)
+        return fail(c, BLG_ERR_ALLOC, "the search's query classes are incomplete after an allocation failure");
     if (!d_out) return fail(c, BLG_ERR_ARG, "null output");
     const bool hask = k >= 0;
     const bool surv = hask && s->lsorted && c->sched != BLG_SCHED_PLAIN;
@@ -1535,6 +1547,7 @@ static int search_matches_list(blg_ctx *c, blg_search *s, int k, blg_match *d_ou
         return BLG_OK;
     const SurvClasses C = seq_classes(s);
     if (C.n == 0 || C.n != (int)s->cls.size()) return BLG_OK;    // a lane-spread class: the dense path
+    if (class_queries(s) != s->nq) return BLG_OK;                  // not every query's class: the dense path
     const int job = survivor_job_size(c, s, k);
     CK(launch(c, "surv_plan", [&] { return launch_surv_plan(c->stream, C, s->lstart, s->min_len, s->n_len, k, job); }),
        "surv_plan");
@@ -2935,7 +2948,10 @@ int blg_search_matches(blg_ctx *c, blg_search *s, int32_t max_dist, blg_match *d
                                           nullptr, capacity - written, &t);
         total += t;
     }
-    if (chunked && !rc) rc = search_build_classes(c, s->h_oq.data(), 0, s->nq, s);
+    if (chunked) {      // the all-query classes back for the search's other runs, after an error too
+        const int rc3 = search_build_classes(c, s->h_oq.data(), 0, s->nq, s);
+        if (!rc) rc = rc3;
+    }
     dev_free(c, scratch);
     const int rc2 = sync_and_status(c);
     if (rc) return rc;

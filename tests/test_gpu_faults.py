@@ -109,6 +109,36 @@ def test_alloc_failure_matches_paths(gpu):
             gpu.set_schedule("auto")
 
 
+def test_alloc_failure_resident_matches_keeps_search_whole(gpu, monkeypatch):
+    """A resident search whose matches call walks query chunks (the dense
+    path: plain schedule, a scratch budget of 4 rows) and fails at any of
+    its allocations still holds every query afterwards: its class set is
+    rebuilt for all rows whatever happened, so the next matches call and
+    the next dense run are exact."""
+    rng = np.random.default_rng(44)
+    q = W.random_strings(rng, rng.integers(0, 120, 23))
+    c = W.concat(W.mutate(rng, W.take(q, rng.integers(0, 23, 150)), 0.08), W.random_strings(rng, rng.integers(0, 130, 400)))
+    nc = len(c[1]) - 1
+    d = oracle.cross(q, c, 3)
+    qi, ci = np.nonzero(d <= 3)
+    dense = oracle.saturate(d, "uint8")
+    monkeypatch.setenv("BLG_MATCH_SCRATCH_BYTES", str(4 * nc))
+    gpu.set_schedule("plain")
+    try:
+        s = gpu.SearchBatch(q, c)
+        out = s.alloc("uint8")
+
+        def check(got):
+            np.testing.assert_array_equal(got[0], qi)
+            np.testing.assert_array_equal(got[1], ci)
+            np.testing.assert_array_equal(got[2], d[qi, ci])
+            np.testing.assert_array_equal(s.run(out, max_dist=3).get(), dense)
+
+        _sweep_allocations(gpu, lambda: s.matches(3), check)
+    finally:
+        gpu.set_schedule("auto")
+
+
 def test_tile_wait_timeout_is_reported_and_recoverable(gpu):
     ctx = _lib.context()
     w = W.config1(n=8192, seed=15)
