@@ -887,7 +887,7 @@ __device__ __forceinline__ void fill_share(void *out, int64_t n, int dtype, uint
     const int64_t nvec = bytes > head ? (bytes - head) / 16 : 0;
     uint4 *vp = reinterpret_cast<uint4 *>(b + head);
     const uint4 vv = make_uint4(word, word, word, word);
-    for (int64_t i = tid; i < nvec; i += stride) vp[i] = vv;
+    for (int64_t i = tid; i < nvec; i += stride) __stcs(vp + i, vv);   // streaming: no L2 residency wanted
     const int64_t tail0 = head + nvec * 16;
     for (int64_t r = tid * es; r < head + (bytes - tail0); r += stride * es) {
         const int64_t x = r < head ? r : tail0 + (r - head);
